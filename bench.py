@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Newton-iteration element throughput of the element-block hot path.
+
+Workload: the plain FP64 GPU path at scale -- a 64x64x64 mesh of 8-node
+bricks (262,144 elements, 2,097,152 Gauss points), interior nodes jittered
+U(-0.1, 0.1) h (PCG64(12345)), mm01 bilinear Mises (E = 200 GPa,
+nu = 0.3, yield 400 MPa, H' = 2 GPa, isotropic), element blocks of 128.
+Synthetic data: the state is set by one load step to 1% uniaxial strain
+(every Gauss point plastic); each timed step is one Newton iteration of
+the element work -- one tangent (tanstf) plus one strain/stress/internal
+force recovery (drive_eps_sig_internal_forces) -- on a perturbed
+increment. Inputs (~3 GB of element state per iteration) exceed the
+129 MB L2, so no flush is needed between steps.
+
+metric: elements per second per Newton iteration
+        = n_elements / (t_tangent + t_recovery).
+value:  plain FP64 form, inputs resident in HBM (device-pointer C-ABI).
+mixed:  the same iteration with the FP32 tangent (recovery stays FP64).
+e2e:    the host-array C-ABI calls a Fortran caller makes (w3g_tanstf
+        with host estiff blocks + w3g_recover with host ifv), all
+        host<->device copies inside the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton-iteration element throughput (elem/s) FP64 vs mixed @ equal residual"
+UNIT = "elem/s"
+
+# Algorithmic FP64 work per hex8 element per call (flops, FMA = 2), the
+# minimal operation counts of the computed quantities:
+#   tangent  per GP: [J] 72 FMA + inverse 30 + gradients 72 + [D] scale 21
+#            + [q] 63 + {T} 36 + [q][D][q]^T 342 + Q-bar 25 + D*B 432
+#            + B^T(D*B) 900 + {T}g 72 + G^T T G 216  = 2281 ops -> 4562 flop/GP
+#   recovery per GP: 2 x (jacob1 + tcomp1 + fcomp1 + polar) 1060,
+#            mid-step [B] and d 310, [q] rotations 135, mm01+cnst1 260,
+#            ifv 290  = 2055 ops -> 4110 flop/GP (+ 4 sqrt, atan2, sin, cos
+#            per polar decomposition, counted as executed instructions only)
+TANGENT_FLOP_PER_ELEM = 8 * 4562
+RECOVER_FLOP_PER_ELEM = 8 * 4110
+# reference's dense counts for comparison in the JSON
+TANGENT_FLOP_PER_ELEM_REFDENSE = 52992
+RECOVER_FLOP_PER_ELEM_REFDENSE = 12000
+# compulsory HBM bytes per element (FP64): tangent reads cep 21*8, coords
+# 24, rot+urcs 18*8 per GP and writes Ke 300; recovery per SURVEY 8d.
+TANGENT_BYTES_PER_ELEM = 8 * (21 * 8 + 24 + 48 + 18 * 8 + 300)
+TANGENT32_BYTES_PER_ELEM = TANGENT_BYTES_PER_ELEM - 4 * 300
+RECOVER_BYTES_PER_ELEM = 6016
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=64, help="elements per cube edge")
+    ap.add_argument("--cpu-sample-blocks", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    return ap.parse_args()
+
+
+def build_workload(n):
+    from warp3d_gb300.model import Bilinear, Model, cube_mesh
+    coords, incid = cube_mesh(n, jitter=0.1, seed=12345)
+    mat = Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0, beta=1.0)
+    model = Model(coords, incid, block_size=128, materials=[mat])
+    X = coords
+    # load step 1: homogeneous 1% tension with plastic lateral contraction
+    F1 = np.diag([1 - 0.005, 1 - 0.005, 1 + 0.01])
+    u1 = ((F1 - np.eye(3)) @ X.T).T.ravel()
+    # Newton-iteration increment of the next step: 0.1% more, perturbed
+    rng = np.random.Generator(np.random.PCG64(2024))
+    dF = np.diag([-0.0005, -0.0005, 0.001])
+    du = ((dF @ X.T).T + rng.normal(0.0, 2e-5, X.shape)).ravel()
+    return model, u1, du
+
+
+def sample_clocks():
+    try:
+        return subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+             "--format=csv,noheader,nounits", "-lms", "200"],
+            stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return None
+
+
+def finish_clocks(proc, device_index):
+    if proc is None:
+        return None
+    proc.terminate()
+    try:
+        out, _ = proc.communicate(timeout=5)
+    except subprocess.TimeoutExpired:
+        proc.kill()
+        out, _ = proc.communicate()
+    mhz, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in out.strip().splitlines():
+        f = [x.strip() for x in line.split(",")]
+        if len(f) < 9 or f[0] != str(device_index):
+            continue
+        try:
+            mhz.append(float(f[1]))
+            mx = float(f[2])
+        except ValueError:
+            continue
+        for nm, v in zip(names, f[5:9]):
+            if v.lower() == "active":
+                reasons.add(nm)
+    if not mhz:
+        return None
+    return {"sm_mhz": statistics.median(mhz), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def cpu_baseline(model_n, nblocks, threads, reps=8):
+    """Times the oracle (CPU restatement, OpenMP over blocks) on the first
+    `nblocks` element blocks of the same workload: one recovery + one
+    tangent per rep, like a Newton iteration."""
+    import oracle
+    from warp3d_gb300.model import Bilinear, Model, cube_mesh
+    coords, incid = cube_mesh(model_n, jitter=0.1, seed=12345)
+    ne = min(nblocks * 128, incid.shape[0])
+    used = np.unique(incid[:ne])
+    remap = -np.ones(coords.shape[0], dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    sub = Model(coords[used], remap[incid[:ne]], block_size=128,
+                materials=[Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)])
+    X = sub.coords
+    F1 = np.diag([1 - 0.005, 1 - 0.005, 1 + 0.01])
+    u1 = ((F1 - np.eye(3)) @ X.T).T.ravel()
+    rng = np.random.Generator(np.random.PCG64(2024))
+    du = ((np.diag([-0.0005, -0.0005, 0.001]) @ X.T).T + rng.normal(0.0, 2e-5, X.shape)).ravel()
+    ora = oracle.Oracle(sub, threads=threads, deterministic=False)
+    ifv = np.zeros(sub.nodof)
+    ora.recover(1, 1, False, sub.c, np.zeros(sub.nodof), u1, ifv)
+    ora.update()
+    est = [np.zeros((s, sub.utsz)) for s in sub.spans]
+    ora.recover(2, 1, False, sub.c, u1, du, ifv)          # warm-up
+    ora.tanstf(2, 1, sub.c, u1, du, est)
+    t_rec = t_tan = 0.0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        ora.recover(2, 1, False, sub.c, u1, du, ifv)
+        t1 = time.perf_counter()
+        ora.tanstf(2, 1, sub.c, u1, du, est)
+        t2 = time.perf_counter()
+        t_rec += t1 - t0
+        t_tan += t2 - t1
+    t_rec /= reps
+    t_tan /= reps
+    return {"value": ne / (t_rec + t_tan), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{ne} elements ({nblocks} blocks of 128) of the {model_n}^3 workload, {reps} iterations",
+            "tangent_elem_per_s": ne / t_tan, "recovery_elem_per_s": ne / t_rec}
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    threads = host_threads()
+    reps = max(1, min(args.steps, 8))
+    cb = cpu_baseline(args.n, args.cpu_sample_blocks, threads, reps=reps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": reps, "warmup": 1, "ms_per_step": 1e3 * args.cpu_sample_blocks * 128 / cb["value"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.n}^3 hex8 l3disop geonl, mm01, blocks of 128 (bounded CPU sample)",
+                   "sample": cb["sample"]},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "WARP3D itself (Fortran + Intel MKL) cannot be built here; the reference arm times the "
+                "oracle, a C++ restatement of the same routines, OpenMP over blocks on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+
+    model, u1, du = build_workload(args.n)
+    ne = model.noelem
+    eng = Engine(model, device=local)
+    ifv_h = np.zeros(model.nodof)
+    st, _ = eng.recover(1, 1, False, model.c, np.zeros(model.nodof), u1, ifv_h)
+    assert st == 0
+    eng.update()
+
+    tc = torch.from_numpy(model.c).to(dev)
+    tu = torch.from_numpy(u1).to(dev)
+    tdu = torch.from_numpy(du).to(dev)
+    tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def timed(precision):
+        eng.set_precision(precision)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), sh)
+                eng.recover_dev(2, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), sh)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps + 1)]
+        launches = 0
+        with torch.cuda.stream(stream):
+            evs[0].record(stream)
+            for k in range(args.steps):
+                eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), sh)
+                launches += eng.last_launch_count()
+                evs[2 * k + 1].record(stream)
+                eng.recover_dev(2, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), sh)
+                launches += eng.last_launch_count()
+                evs[2 * k + 2].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        t_tan = sum(evs[2 * k].elapsed_time(evs[2 * k + 1]) for k in range(args.steps)) / args.steps
+        t_rec = sum(evs[2 * k + 1].elapsed_time(evs[2 * k + 2]) for k in range(args.steps)) / args.steps
+        total = evs[0].elapsed_time(evs[-1])
+        st, info = eng.recover_info()
+        assert st == 0
+        return total / args.steps, t_tan, t_rec, launches
+
+    peak = C.c_double()
+    abi.check(eng.lib, eng.lib.w3g_measure_fp64_peak(local, C.byref(peak)))
+    fp64_peak_tflops = peak.value
+
+    clk = sample_clocks()
+    ms64, tan64, rec64, launches64 = timed(abi.TANGENT_FP64)
+    clocks = finish_clocks(clk, local)
+    mixed = None
+    if not args.no_mixed:
+        ms32, tan32, rec32, launches32 = timed(abi.TANGENT_FP32)
+        mixed = {"value": ne / (ms32 * 1e-3), "ms_per_step": ms32, "tangent_ms": tan32, "recovery_ms": rec32,
+                 "speedup_vs_fp64": ms64 / ms32, "dtype": "tangent fp32 (FMA), recovery fp64"}
+        eng.set_precision(abi.TANGENT_FP64)
+
+    # whole-job throughput: max time over ranks
+    t_step = ms64
+    if dist is not None:
+        t = torch.tensor([ms64], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = world * ne / (t_step * 1e-3)
+
+    # ---- e2e through the host-array C-ABI ----
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
+        c_h, u_h, du_h = pin(model.c), pin(u1), pin(du)
+        ifv_p = pin(np.zeros(model.nodof))
+        est_all = torch.empty(ne * model.utsz, dtype=torch.float64).pin_memory().numpy()
+        est_blocks, off = [], 0
+        for s in model.spans:
+            est_blocks.append(est_all[off:off + s * model.utsz].reshape(s, model.utsz))
+            off += s * model.utsz
+        for _ in range(2):
+            eng.tanstf(2, 1, c_h, u_h, du_h, est_blocks)
+            eng.recover(2, 1, False, c_h, u_h, du_h, ifv_p)
+        barrier()
+        reps = max(3, args.steps // 4)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            eng.tanstf(2, 1, c_h, u_h, du_h, est_blocks)
+            eng.recover(2, 1, False, c_h, u_h, du_h, ifv_p)
+        t_e2e = (time.perf_counter() - t0) / reps
+        h2d = 2 * 8 * (model.ncoord + 2 * model.nodof)
+        d2h = 8 * (ne * model.utsz + model.nodof) + C.sizeof(abi.RecoverInfo)
+        e2e = {"value": world * ne / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": 1e3 * t_e2e, "estiff_to_host": True}
+
+    # ---- roofline of the dominant kernel ----
+    traffic = load_traffic()
+    if tan64 >= rec64:
+        kname, kms, flop = "k_tangent_hex8<double>", tan64, TANGENT_FLOP_PER_ELEM
+        tr = traffic.get("tangent_fp64_bytes_per_elem")
+    else:
+        kname, kms, flop = "k_recover_hex8", rec64, RECOVER_FLOP_PER_ELEM
+        tr = traffic.get("recover_bytes_per_elem")
+    achieved = flop * ne / (kms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": kname, "achieved": achieved, "peak": fp64_peak_tflops,
+                "unit": "TFLOP/s", "frac": achieved / fp64_peak_tflops,
+                "traffic": (tr * ne) if tr else None,
+                "peak_source": "measured live: w3g_measure_fp64_peak (DFMA chains, all SMs)",
+                "algorithmic_flop_per_elem": flop,
+                "tangent": {"ms": tan64, "tflops": TANGENT_FLOP_PER_ELEM * ne / (tan64 * 1e-3) / 1e12,
+                            "tflops_refdense_count": TANGENT_FLOP_PER_ELEM_REFDENSE * ne / (tan64 * 1e-3) / 1e12,
+                            "hbm_gbs": TANGENT_BYTES_PER_ELEM * ne / (tan64 * 1e-3) / 1e9},
+                "recovery": {"ms": rec64, "tflops": RECOVER_FLOP_PER_ELEM * ne / (rec64 * 1e-3) / 1e12,
+                             "tflops_refdense_count": RECOVER_FLOP_PER_ELEM_REFDENSE * ne / (rec64 * 1e-3) / 1e12,
+                             "hbm_gbs": RECOVER_BYTES_PER_ELEM * ne / (rec64 * 1e-3) / 1e9}}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            roofline["hbm_peak_gbs_measured"] = json.load(f).get("hbm_gbs")
+    except OSError:
+        pass
+    if mixed:
+        mixed["tangent_hbm_gbs"] = TANGENT32_BYTES_PER_ELEM * ne / (mixed["tangent_ms"] * 1e-3) / 1e9
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(args.n, args.cpu_sample_blocks, host_threads())
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.n}^3 hex8 l3disop geonl (jitter 0.1h), mm01 bilinear, blocks of 128, "
+                                   f"1 Newton iteration = tangent + recovery",
+                       "elements": ne, "gauss_points": ne * 8, "l2": "inputs ~3 GB per step > L2, no flush",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "tangent_ms": tan64, "recovery_ms": rec64,
+            "mixed": mixed, "e2e": e2e, "roofline": roofline, "cpu_baseline": cb, "clocks": clocks,
+            "gpu_launches": launches64,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

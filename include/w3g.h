@@ -1,0 +1,202 @@
+/*
+ * w3g.h -- C-ABI of the GB300 element-block engine for WARP3D's
+ * tangent-stiffness and strain/stress/internal-force block loops.
+ *
+ * The entry points replace, one for one, the two OpenMP block loops that
+ * WARP3D's Newton driver calls once per iteration phase:
+ *
+ *   w3g_tanstf   <- subroutine tanstf              (src/tanstf.f:17, block
+ *                   loop at :80-88, per-block work do_nlek_block :119)
+ *   w3g_recover  <- subroutine drive_eps_sig_internal_forces
+ *                   (src/drive_eps_sig_internal_forces.f:20, block loop
+ *                   :160-180, ifv scatter :287-305)
+ *   w3g_update   <- subroutine update, block-state copy n+1 -> n
+ *                   (src/update.f:73-94)
+ *
+ * Every array keeps the layout of WARP3D's module elem_block_data
+ * (src/mod_eleblocks.f:17-150) and of the element property tables
+ * props/iprops/lprops (src/mod_main.f:47-52):
+ *
+ *   estiff   (utsz, span)        upper triangle, column packed:
+ *                                pos = j(j-1)/2 + i for row i <= col j
+ *                                (src/setup.f:265-275, :407-417)
+ *   cep      (21, span, ngp)     lower triangle of [D], row-wise
+ *                                (src/rstgp1.f:5360-5397)
+ *   history  (hist, ngp, span)   per-Gauss-point material history
+ *   urcs     (9, ngp, span)      unrotated Cauchy stress + U, Wp, ebarp
+ *   eps      (6, ngp, span)      strains
+ *   rot_n1   (9, ngp, span)      [R,n+1] column-major 3x3
+ *   einfvec  (span, totdof)      element internal forces
+ *   elem_vol (span)              element volumes at n+1
+ *   edest/cdest (totdof, span)   int32, 1-based global dof / coordinate
+ *                                index, ordered u1..un, v1..vn, w1..wn
+ *   props/iprops/lprops (43, noelem)  float32 / int32 / logical(int32)
+ *   elblks   (0:2, nelblk)       span, first element (1-based), owner
+ *
+ * Per-block arrays are passed as arrays of nelblk host pointers, exactly
+ * as a Fortran caller obtains them with c_loc(x_blocks(blk)%ptr).
+ *
+ * All functions return an int status:
+ *     0  ok
+ *     1  step cut requested: det[F] <= 0 at some Gauss point
+ *        (src/gtmat1.f:649-664 -> material_cut_step)
+ *     2  local material solve failed (material_cut_step)
+ *    <0  fatal: bad argument, unsupported element/material, CUDA error
+ *        (replaces die_abort). w3g_last_error() gives the message.
+ *
+ * Nothing in this header uses torch or CUDA types; device pointers and
+ * streams travel as void*.
+ */
+#ifndef W3G_H
+#define W3G_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define W3G_MXELPR 43
+#define W3G_MXVL 128
+
+/* Element types (iprops(1,elem)), src/elprp.f */
+#define W3G_ETYPE_Q3DISOP 1   /* 20-node hexahedron */
+#define W3G_ETYPE_L3DISOP 2   /* 8-node hexahedron  */
+#define W3G_ETYPE_TET10 6     /* 10-node tetrahedron */
+
+/* Material models (iprops(25,elem)) */
+#define W3G_MAT_BILINEAR 1    /* mm01: bilinear Mises, mixed hardening */
+#define W3G_MAT_CRYSTAL 10    /* mm10: crystal plasticity */
+
+/* Status codes */
+#define W3G_OK 0
+#define W3G_STEP_CUT 1
+#define W3G_LOCAL_FAIL 2
+#define W3G_EARG -1
+#define W3G_EUNSUPPORTED -2
+#define W3G_ECUDA -3
+#define W3G_ENOMEM -4
+#define W3G_EFATAL -5
+
+/* Precision of the tangent contraction (w3g_set_tangent_precision). */
+#define W3G_TANGENT_FP64 0    /* plain form: everything FP64            */
+#define W3G_TANGENT_FP32 1    /* Ke in FP32 (CUDA-core FP32 FMA)        */
+
+/*
+ * Model description: what WARP3D holds in elblks, props/iprops/lprops,
+ * edest_blocks and cdest_blocks after input processing.
+ */
+typedef struct w3g_model_desc {
+  int nelblk;
+  const int* elblks;            /* 3*nelblk: span, felem, owner          */
+  int noelem;
+  const float* props;           /* 43*noelem                             */
+  const int* iprops;            /* 43*noelem                             */
+  const int* lprops;            /* 43*noelem, nonzero = .true.           */
+  const int* const* edest;      /* nelblk pointers to (totdof, span)     */
+  const int* const* cdest;      /* nelblk pointers to (totdof, span)     */
+  int nodof;                    /* length of u, du, ifv                  */
+  int ncoord;                   /* length of c                           */
+  int qbar_flag;                /* consistent Q-bar term, default 1      */
+  double beta_fact;             /* plane-strain thickness factor, 1 in 3-D */
+} w3g_model_desc;
+
+/*
+ * Host copies of the blocked element state (module elem_block_data).
+ * Any member may be NULL when a call does not move that array.
+ */
+typedef struct w3g_block_state {
+  double* const* history;       /* (hist, ngp, span), state n            */
+  double* const* history1;      /* (hist, ngp, span), state n+1          */
+  double* const* urcs_n;        /* (9, ngp, span)                        */
+  double* const* urcs_n1;       /* (9, ngp, span)                        */
+  double* const* eps_n;         /* (6, ngp, span)                        */
+  double* const* eps_n1;        /* (6, ngp, span)                        */
+  double* const* rot_n1;        /* (9, ngp, span)                        */
+  double* const* cep;           /* (21, span, ngp)                       */
+  double* const* einfvec;       /* (span, totdof)                        */
+  double* const* element_vol;   /* (span)                                */
+} w3g_block_state;
+
+/* Scalars drive_eps_sig_internal_forces returns to the Newton driver
+   (src/drive_eps_sig_internal_forces.f:210-226, :276-319). */
+typedef struct w3g_recover_info {
+  double internal_energy;
+  double plastic_work;
+  double sum_ifv;               /* sum |eleifv|, addifv.f:101-106        */
+  long long num_term_ifv;       /* totdof*span summed over blocks        */
+  int material_cut_step;
+  int first_bad_element;        /* 1-based element of a det[F]<=0 GP, or 0 */
+} w3g_recover_info;
+
+typedef struct w3g_context w3g_context;
+
+/* ---- context and model -------------------------------------------- */
+
+/* Creates a context on CUDA device `device` and copies the model tables
+   to the device. Replaces the per-run setup that WARP3D does in
+   src/reopen.f cdest_init/edest_init and the block allocations in
+   src/mod_eleblocks.f. The state arrays start as WARP3D initialises
+   them: zeros, with rot_n1 = identity (src/reopen.f:1912-1915). */
+int w3g_create(int device, const w3g_model_desc* model, w3g_context** out);
+int w3g_destroy(w3g_context* ctx);
+const char* w3g_last_error(void);
+
+/* Selects the precision form of the tangent (W3G_TANGENT_*). The FP32
+   form writes Ke as float into a separate device array; w3g_tanstf then
+   widens to double only when host estiff pointers are given. */
+int w3g_set_tangent_precision(w3g_context* ctx, int precision);
+
+/* ---- state transfer (restart, fixtures, output) -------------------- */
+int w3g_state_upload(w3g_context* ctx, const w3g_block_state* host);
+int w3g_state_download(w3g_context* ctx, const w3g_block_state* host);
+
+/* ---- the hot path, host arrays ------------------------------------- */
+
+/* tanstf (src/tanstf.f:17): element tangent stiffnesses for all blocks.
+   c, u, du: global coordinate / displacement / increment vectors.
+   estiff: nelblk host pointers to (utsz, span) doubles, or NULL to keep
+   the matrices resident on the device only. */
+int w3g_tanstf(w3g_context* ctx, int step, int iter,
+               const double* c, const double* u, const double* du,
+               double* const* estiff);
+
+/* drive_eps_sig_internal_forces (src/drive_eps_sig_internal_forces.f:20):
+   strains, stresses, material update, [D] storage, element internal
+   forces and their assembly into ifv (length nodof, overwritten).
+   extrapolated_du follows main_data::extrapolated_du (mnralg.f:255-285). */
+int w3g_recover(w3g_context* ctx, int step, int iter, int extrapolated_du,
+                const double* c, const double* u, const double* du,
+                double* ifv, w3g_recover_info* info);
+
+/* update (src/update.f:73-94): history, strains, stresses n+1 -> n. */
+int w3g_update(w3g_context* ctx);
+
+/* ---- the hot path, device-resident arrays --------------------------
+   Same work as above on device pointers (c, u, du, ifv of type double*
+   on ctx's device) enqueued on `stream` (a cudaStream_t, or NULL for the
+   legacy default stream). The call returns after enqueueing; info is
+   written to a device buffer and read back by w3g_recover_info_get. */
+int w3g_tanstf_dev(w3g_context* ctx, int step, int iter,
+                   const void* d_c, const void* d_u, const void* d_du,
+                   void* stream);
+int w3g_recover_dev(w3g_context* ctx, int step, int iter,
+                    int extrapolated_du, const void* d_c, const void* d_u,
+                    const void* d_du, void* d_ifv, void* stream);
+int w3g_recover_info_get(w3g_context* ctx, w3g_recover_info* info);
+
+/* Device pointer of the resident element stiffnesses: FP64 (utsz, span)
+   blocks back to back for W3G_TANGENT_FP64, FP32 for W3G_TANGENT_FP32.
+   *count receives the number of values. */
+int w3g_estiff_device(w3g_context* ctx, void** d_estiff, long long* count);
+
+/* Number of kernels the last w3g_tanstf/w3g_recover(_dev) call launched. */
+int w3g_last_launch_count(w3g_context* ctx);
+
+/* ---- measurement helper (no WARP3D counterpart) ---------------------
+   Sustained FP64 FMA throughput of `device` in TFLOP/s (2 flops per FMA),
+   the roofline denominator of the FP64-bound element kernels. */
+int w3g_measure_fp64_peak(int device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* W3G_H */

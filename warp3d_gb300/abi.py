@@ -1,0 +1,137 @@
+"""ctypes mirror of include/w3g.h and loader of the CUDA engine.
+
+The engine is the in-tree shared library ``warp3d_gb300/_build/libw3g.so``
+(built by :mod:`warp3d_gb300.build`). There is no CPU fallback: if the
+library or a CUDA device is missing, :func:`load` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libw3g.so")
+
+MXELPR = 43
+MXVL = 128
+ETYPE_Q3DISOP = 1
+ETYPE_L3DISOP = 2
+ETYPE_TET10 = 6
+MAT_BILINEAR = 1
+MAT_CRYSTAL = 10
+
+OK = 0
+STEP_CUT = 1
+LOCAL_FAIL = 2
+EARG = -1
+EUNSUPPORTED = -2
+ECUDA = -3
+ENOMEM = -4
+
+TANGENT_FP64 = 0
+TANGENT_FP32 = 1
+
+_dpp = C.POINTER(C.POINTER(C.c_double))
+_ipp = C.POINTER(C.POINTER(C.c_int))
+
+
+class ModelDesc(C.Structure):
+    _fields_ = [
+        ("nelblk", C.c_int),
+        ("elblks", C.POINTER(C.c_int)),
+        ("noelem", C.c_int),
+        ("props", C.POINTER(C.c_float)),
+        ("iprops", C.POINTER(C.c_int)),
+        ("lprops", C.POINTER(C.c_int)),
+        ("edest", _ipp),
+        ("cdest", _ipp),
+        ("nodof", C.c_int),
+        ("ncoord", C.c_int),
+        ("qbar_flag", C.c_int),
+        ("beta_fact", C.c_double),
+    ]
+
+
+class BlockState(C.Structure):
+    _fields_ = [
+        ("history", _dpp),
+        ("history1", _dpp),
+        ("urcs_n", _dpp),
+        ("urcs_n1", _dpp),
+        ("eps_n", _dpp),
+        ("eps_n1", _dpp),
+        ("rot_n1", _dpp),
+        ("cep", _dpp),
+        ("einfvec", _dpp),
+        ("element_vol", _dpp),
+    ]
+
+
+class RecoverInfo(C.Structure):
+    _fields_ = [
+        ("internal_energy", C.c_double),
+        ("plastic_work", C.c_double),
+        ("sum_ifv", C.c_double),
+        ("num_term_ifv", C.c_longlong),
+        ("material_cut_step", C.c_int),
+        ("first_bad_element", C.c_int),
+    ]
+
+
+# exported symbols and their prototypes: (name, restype, argtypes)
+_vp = C.c_void_p
+_d = C.POINTER(C.c_double)
+PROTOTYPES = [
+    ("w3g_create", C.c_int, [C.c_int, C.POINTER(ModelDesc), C.POINTER(_vp)]),
+    ("w3g_destroy", C.c_int, [_vp]),
+    ("w3g_last_error", C.c_char_p, []),
+    ("w3g_set_tangent_precision", C.c_int, [_vp, C.c_int]),
+    ("w3g_state_upload", C.c_int, [_vp, C.POINTER(BlockState)]),
+    ("w3g_state_download", C.c_int, [_vp, C.POINTER(BlockState)]),
+    ("w3g_tanstf", C.c_int, [_vp, C.c_int, C.c_int, _d, _d, _d, C.POINTER(_d)]),
+    ("w3g_recover", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _d, _d, _d, _d, C.POINTER(RecoverInfo)]),
+    ("w3g_update", C.c_int, [_vp]),
+    ("w3g_tanstf_dev", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
+    ("w3g_recover_dev", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    ("w3g_recover_info_get", C.c_int, [_vp, C.POINTER(RecoverInfo)]),
+    ("w3g_estiff_device", C.c_int, [_vp, C.POINTER(_vp), C.POINTER(C.c_longlong)]),
+    ("w3g_last_launch_count", C.c_int, [_vp]),
+    ("w3g_measure_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+]
+
+_lib = None
+
+
+def declare(lib: C.CDLL) -> C.CDLL:
+    for name, res, args in PROTOTYPES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads libw3g.so (building it first when only the sources exist)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        from . import build as _build
+        _build.build()
+    lib = declare(C.CDLL(p))
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class W3GError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"w3g status {code}: {msg}")
+        self.code = code
+
+
+def check(lib: C.CDLL, code: int, allow=(OK,)) -> int:
+    if code not in allow:
+        raise W3GError(code, lib.w3g_last_error().decode(errors="replace"))
+    return code

@@ -1,0 +1,530 @@
+// w3g_api.cu -- the C-ABI of include/w3g.h: model registration, resident
+// device state, and the tanstf / drive_eps_sig_internal_forces / update
+// replacements. No torch types cross this boundary.
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "w3g_internal.cuh"
+#include "w3g_elem.cuh"
+
+using namespace w3g;
+
+struct w3g_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DeviceModel m;
+  DeviceState s;
+  int precision = W3G_TANGENT_FP64;
+  int ifv_parts = 0;
+  int last_launches = 0;
+  // host copies needed for state transfer
+  std::vector<BlockDesc> blocks;
+  double* h_stage = nullptr;   // pinned staging, max(estiff_total, ...) doubles
+  size_t h_stage_n = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(W3G_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+void free_all(w3g_context* c) {
+  DeviceModel& m = c->m;
+  DeviceState& s = c->s;
+  void* ptrs[] = {m.blocks, m.chunks, m.edest, m.cdest, m.mat, m.dn_hex8, m.ifv_rowptr, m.ifv_src,
+                  s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
+                  s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
+                  s.d_c, s.d_u, s.d_du, s.d_ifv};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+__global__ void k_init_rot(double* rot, long long ngp_total) {
+  long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k < ngp_total) {
+    double* r = rot + k * 9;
+    r[0] = 1.0; r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; r[4] = 1.0; r[5] = 0.0; r[6] = 0.0; r[7] = 0.0; r[8] = 1.0;
+  }
+}
+
+__global__ void k_reset_status(int* status) { status[0] = INT_MAX; }
+
+// copy n values between per-block host pointers and one device array
+int blocks_h2d(w3g_context* c, double* dev, double* const* host, int per_elem_or_gp, bool per_gp) {
+  for (int b = 0; b < c->m.nelblk; ++b) {
+    const BlockDesc& bd = c->blocks[b];
+    size_t n = (size_t)bd.span * (per_gp ? bd.ngp : 1) * per_elem_or_gp;
+    size_t off = (size_t)(per_gp ? bd.gp_off : bd.felem) * per_elem_or_gp;
+    if (!host[b]) continue;
+    CK(cudaMemcpyAsync(dev + off, host[b], n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int blocks_d2h(w3g_context* c, const double* dev, double* const* host, int per, bool per_gp) {
+  for (int b = 0; b < c->m.nelblk; ++b) {
+    const BlockDesc& bd = c->blocks[b];
+    size_t n = (size_t)bd.span * (per_gp ? bd.ngp : 1) * per;
+    size_t off = (size_t)(per_gp ? bd.gp_off : bd.felem) * per;
+    if (!host[b]) continue;
+    CK(cudaMemcpyAsync(host[b], dev + off, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, const double* d_du) {
+  TangentArgs a;
+  a.dn = c->m.dn_hex8;
+  a.blocks = c->m.blocks;
+  a.chunks = c->m.chunks;
+  a.edest = c->m.edest;
+  a.cdest = c->m.cdest;
+  a.c = d_c; a.u = d_u; a.du = d_du;
+  a.rot_n1 = c->s.rot_n1;
+  a.urcs_n1 = c->s.urcs_n1;
+  a.cep = c->s.cep;
+  a.estiff = c->precision == W3G_TANGENT_FP32 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
+  a.qbar = c->m.qbar;
+  a.beta_fact = c->m.beta_fact;
+  return a;
+}
+
+int run_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
+  TangentArgs a = tangent_args(c, d_c, d_u, d_du);
+  cudaError_t e = c->precision == W3G_TANGENT_FP32 ? launch_tangent_fp32(c->m, a, st)
+                                                   : launch_tangent_fp64(c->m, a, st);
+  if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
+  c->last_launches = 1;
+  return 0;
+}
+
+int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_c, const double* d_u,
+                const double* d_du, double* d_ifv, cudaStream_t st) {
+  k_reset_status<<<1, 1, 0, st>>>(c->s.status);
+  RecoverArgs a;
+  a.dn = c->m.dn_hex8;
+  a.blocks = c->m.blocks;
+  a.chunks = c->m.chunks;
+  a.edest = c->m.edest;
+  a.cdest = c->m.cdest;
+  a.mat = c->m.mat;
+  a.c = d_c; a.u = d_u; a.du = d_du;
+  a.hist = c->s.hist; a.hist1 = c->s.hist1;
+  a.urcs_n = c->s.urcs_n; a.urcs_n1 = c->s.urcs_n1;
+  a.eps_n = c->s.eps_n; a.eps_n1 = c->s.eps_n1;
+  a.rot_n1 = c->s.rot_n1;
+  a.cep = c->s.cep;
+  a.einf = c->s.einf;
+  a.evol = c->s.evol;
+  a.partials = c->s.partials;
+  a.status = c->s.status;
+  a.step = step; a.iter = iter;
+  a.nonlinear = (iter >= 1 || extrap) ? 1 : 0;
+  a.beta_fact = c->m.beta_fact;
+  cudaError_t e = launch_recover(c->m, a, st);
+  if (e == cudaSuccess) e = launch_assemble_ifv(c->m, c->s.einf, d_ifv, c->s.ifv_partials, c->ifv_parts, st);
+  if (e == cudaSuccess)
+    e = launch_finalize(c->m, c->s.partials, c->s.ifv_partials, c->ifv_parts, c->s.status, c->s.d_info, st);
+  if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("recover launch: ") + cudaGetErrorString(e));
+  c->last_launches = 4;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* w3g_last_error(void) { return g_err.c_str(); }
+
+int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
+  if (!md || !out) return fail(W3G_EARG, "null argument");
+  *out = nullptr;
+  if (md->nelblk <= 0 || md->noelem <= 0 || !md->elblks || !md->props || !md->iprops || !md->lprops ||
+      !md->edest || !md->cdest)
+    return fail(W3G_EARG, "incomplete model description");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return fail(W3G_ECUDA, "CUDA device " + std::to_string(device) + " not available");
+  CK(cudaSetDevice(device));
+
+  w3g_context* c = new w3g_context();
+  c->device = device;
+  DeviceModel& m = c->m;
+  m.nelblk = md->nelblk; m.noelem = md->noelem; m.nodof = md->nodof; m.ncoord = md->ncoord;
+  m.qbar = md->qbar_flag ? 1 : 0;
+  m.beta_fact = md->beta_fact;
+
+  // ---- block table (elblks, iprops, lprops) ----
+  std::vector<BlockDesc>& B = c->blocks;
+  B.resize(md->nelblk);
+  long long gp = 0, cep = 0, est = 0, einf = 0;
+  int expect_felem = 1;
+  std::vector<Chunk> chunks;
+  for (int b = 0; b < md->nelblk; ++b) {
+    BlockDesc& d = B[b];
+    d.span = md->elblks[3 * b];
+    int felem1 = md->elblks[3 * b + 1];
+    if (d.span < 1 || d.span > W3G_MXVL || felem1 < 1 || felem1 + d.span - 1 > md->noelem) {
+      delete c;
+      return fail(W3G_EARG, "block " + std::to_string(b + 1) + ": bad span/felem");
+    }
+    if (felem1 != expect_felem) {
+      delete c;
+      return fail(W3G_EARG, "blocks must cover elements 1..noelem in order");
+    }
+    expect_felem = felem1 + d.span;
+    d.felem = felem1 - 1;
+    const int* ip = md->iprops + (size_t)d.felem * W3G_MXELPR;
+    const int* lp = md->lprops + (size_t)d.felem * W3G_MXELPR;
+    d.etype = ip[0]; d.nnode = ip[1]; d.ngp = ip[5]; d.mat = ip[24];
+    d.totdof = d.nnode * ip[3];
+    d.utsz = (d.totdof * d.totdof - d.totdof) / 2 + d.totdof;
+    d.geonl = lp[17] != 0; d.bbar = lp[18] != 0;
+    if (d.etype != W3G_ETYPE_L3DISOP || d.nnode != 8 || d.ngp != 8 || ip[3] != 3 || ip[4] != 1) {
+      delete c;
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": element type not supported");
+    }
+    if (d.mat != W3G_MAT_BILINEAR) {
+      delete c;
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": material model not supported");
+    }
+    if (!d.geonl || d.bbar) {
+      delete c;
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": small-strain or b-bar not supported");
+    }
+    d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf;
+    gp += (long long)d.span * d.ngp;
+    cep += 21LL * d.span * d.ngp;
+    est += (long long)d.utsz * d.span;
+    einf += (long long)d.totdof * d.span;
+    for (int i0 = 0; i0 < d.span; i0 += kChunk) chunks.push_back(Chunk{b, i0, std::min(kChunk, d.span - i0)});
+  }
+  if (expect_felem != md->noelem + 1) {
+    delete c;
+    return fail(W3G_EARG, "blocks do not cover all elements");
+  }
+  m.ngp_total = gp; m.cep_total = cep; m.estiff_total = est; m.einf_total = einf;
+  m.nchunks = (int)chunks.size();
+
+  // ---- edest / cdest, ifv CSR ----
+  std::vector<int> ed(einf), cd(einf);
+  for (int b = 0; b < md->nelblk; ++b) {
+    size_t n = (size_t)B[b].totdof * B[b].span;
+    std::memcpy(&ed[B[b].einf_off], md->edest[b], n * sizeof(int));
+    std::memcpy(&cd[B[b].einf_off], md->cdest[b], n * sizeof(int));
+  }
+  std::vector<int> rowptr(md->nodof + 1, 0);
+  for (int b = 0; b < md->nelblk; ++b) {
+    const BlockDesc& d = B[b];
+    for (int i = 0; i < d.span; ++i)
+      for (int j = 0; j < d.totdof; ++j) {
+        int gd = ed[d.einf_off + (size_t)i * d.totdof + j];
+        int gc = cd[d.einf_off + (size_t)i * d.totdof + j];
+        if (gd < 1 || gd > md->nodof || gc < 1 || gc > md->ncoord) {
+          delete c;
+          return fail(W3G_EARG, "edest/cdest index out of range in block " + std::to_string(b + 1));
+        }
+        rowptr[gd]++;
+      }
+  }
+  for (int k = 0; k < md->nodof; ++k) rowptr[k + 1] += rowptr[k];
+  std::vector<long long> src(einf);
+  {
+    std::vector<int> fill(rowptr.begin(), rowptr.end() - 1);
+    // ascending einfvec index: block, then dof j, then element i
+    for (int b = 0; b < md->nelblk; ++b) {
+      const BlockDesc& d = B[b];
+      for (int j = 0; j < d.totdof; ++j)
+        for (int i = 0; i < d.span; ++i) {
+          int gd = ed[d.einf_off + (size_t)i * d.totdof + j] - 1;
+          src[fill[gd]++] = d.einf_off + (long long)j * d.span + i;
+        }
+    }
+  }
+  // ---- material properties (setup_mm01_rknstr) ----
+  std::vector<MatProps> mat(md->noelem);
+  for (int e = 0; e < md->noelem; ++e) {
+    const float* p = md->props + (size_t)e * W3G_MXELPR;
+    const int* lp = md->lprops + (size_t)e * W3G_MXELPR;
+    mat[e].e = p[6]; mat[e].nu = p[7]; mat[e].beta = p[13]; mat[e].h = p[14]; mat[e].yld = p[22];
+    mat[e].lnelas = lp[16] ? 1.0 : 0.0;
+  }
+  double dn[dn_table_size<Hex8>()];
+  fill_dn_table<Hex8>(dn);
+
+  DeviceState& s = c->s;
+  cudaError_t e = cudaSuccess;
+#define AL(p, n) if (e == cudaSuccess) e = dalloc(&(p), (size_t)(n))
+  AL(m.blocks, md->nelblk);
+  AL(m.chunks, m.nchunks);
+  AL(m.edest, einf);
+  AL(m.cdest, einf);
+  AL(m.mat, md->noelem);
+  AL(m.dn_hex8, dn_table_size<Hex8>());
+  AL(m.ifv_rowptr, md->nodof + 1);
+  AL(m.ifv_src, einf);
+  AL(s.hist, kHistMM01 * gp);
+  AL(s.hist1, kHistMM01 * gp);
+  AL(s.urcs_n, 9 * gp);
+  AL(s.urcs_n1, 9 * gp);
+  AL(s.eps_n, 6 * gp);
+  AL(s.eps_n1, 6 * gp);
+  AL(s.rot_n1, 9 * gp);
+  AL(s.cep, cep);
+  AL(s.estiff, est);
+  AL(s.einf, einf);
+  AL(s.evol, md->noelem);
+  AL(s.partials, 2 * m.nchunks);
+  c->ifv_parts = assemble_ifv_parts(md->nodof);
+  AL(s.ifv_partials, c->ifv_parts);
+  AL(s.status, 1);
+  AL(s.d_info, 1);
+  AL(s.d_c, md->ncoord);
+  AL(s.d_u, md->nodof);
+  AL(s.d_du, md->nodof);
+  AL(s.d_ifv, md->nodof);
+#undef AL
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    free_all(c);
+    delete c;
+    return fail(W3G_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+  }
+  cudaStream_t st = c->stream;
+#define UP(d, h, n) if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, (size_t)(n) * sizeof(*(h)), cudaMemcpyHostToDevice, st)
+  UP(m.blocks, B.data(), md->nelblk);
+  UP(m.chunks, chunks.data(), m.nchunks);
+  UP(m.edest, ed.data(), einf);
+  UP(m.cdest, cd.data(), einf);
+  UP(m.mat, mat.data(), md->noelem);
+  UP(m.dn_hex8, dn, dn_table_size<Hex8>());
+  UP(m.ifv_rowptr, rowptr.data(), md->nodof + 1);
+  UP(m.ifv_src, src.data(), einf);
+#undef UP
+  // WARP3D's initial state: zeros, rotations = identity (src/reopen.f:1912-1915)
+  double* zs[] = {s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.cep, s.estiff, s.einf, s.evol};
+  long long zn[] = {kHistMM01 * gp, kHistMM01 * gp, 9 * gp, 9 * gp, 6 * gp, 6 * gp, cep, est, einf, md->noelem};
+  for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = cudaMemsetAsync(zs[k], 0, (size_t)zn[k] * sizeof(double), st);
+  if (e == cudaSuccess) {
+    k_init_rot<<<(unsigned)((gp + 255) / 256), 256, 0, st>>>(s.rot_n1, gp);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    free_all(c);
+    delete c;
+    return fail(W3G_ECUDA, std::string("model upload: ") + cudaGetErrorString(e));
+  }
+  *out = c;
+  return 0;
+}
+
+int w3g_destroy(w3g_context* c) {
+  if (!c) return 0;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_all(c);
+  delete c;
+  return 0;
+}
+
+int w3g_set_tangent_precision(w3g_context* c, int precision) {
+  if (!c) return fail(W3G_EARG, "null context");
+  if (precision != W3G_TANGENT_FP64 && precision != W3G_TANGENT_FP32) return fail(W3G_EARG, "bad precision");
+  CK(cudaSetDevice(c->device));
+  if (precision == W3G_TANGENT_FP32 && !c->s.estiff32) {
+    CK(dalloc(&c->s.estiff32, (size_t)c->m.estiff_total));
+    CK(cudaMemsetAsync(c->s.estiff32, 0, (size_t)c->m.estiff_total * sizeof(float), c->stream));
+  }
+  c->precision = precision;
+  return 0;
+}
+
+int w3g_state_upload(w3g_context* c, const w3g_block_state* h) {
+  if (!c || !h) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  int r = 0;
+  if (h->history && (r = blocks_h2d(c, c->s.hist, h->history, kHistMM01, true))) return r;
+  if (h->history1 && (r = blocks_h2d(c, c->s.hist1, h->history1, kHistMM01, true))) return r;
+  if (h->urcs_n && (r = blocks_h2d(c, c->s.urcs_n, h->urcs_n, 9, true))) return r;
+  if (h->urcs_n1 && (r = blocks_h2d(c, c->s.urcs_n1, h->urcs_n1, 9, true))) return r;
+  if (h->eps_n && (r = blocks_h2d(c, c->s.eps_n, h->eps_n, 6, true))) return r;
+  if (h->eps_n1 && (r = blocks_h2d(c, c->s.eps_n1, h->eps_n1, 6, true))) return r;
+  if (h->rot_n1 && (r = blocks_h2d(c, c->s.rot_n1, h->rot_n1, 9, true))) return r;
+  if (h->cep && (r = blocks_h2d(c, c->s.cep, h->cep, 21, true))) return r;
+  if (h->element_vol && (r = blocks_h2d(c, c->s.evol, h->element_vol, 1, false))) return r;
+  if (h->einfvec) {
+    for (int b = 0; b < c->m.nelblk; ++b) {
+      const BlockDesc& bd = c->blocks[b];
+      if (!h->einfvec[b]) continue;
+      CK(cudaMemcpyAsync(c->s.einf + bd.einf_off, h->einfvec[b], (size_t)bd.totdof * bd.span * sizeof(double),
+                         cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return 0;
+}
+
+int w3g_state_download(w3g_context* c, const w3g_block_state* h) {
+  if (!c || !h) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  int r = 0;
+  if (h->history && (r = blocks_d2h(c, c->s.hist, h->history, kHistMM01, true))) return r;
+  if (h->history1 && (r = blocks_d2h(c, c->s.hist1, h->history1, kHistMM01, true))) return r;
+  if (h->urcs_n && (r = blocks_d2h(c, c->s.urcs_n, h->urcs_n, 9, true))) return r;
+  if (h->urcs_n1 && (r = blocks_d2h(c, c->s.urcs_n1, h->urcs_n1, 9, true))) return r;
+  if (h->eps_n && (r = blocks_d2h(c, c->s.eps_n, h->eps_n, 6, true))) return r;
+  if (h->eps_n1 && (r = blocks_d2h(c, c->s.eps_n1, h->eps_n1, 6, true))) return r;
+  if (h->rot_n1 && (r = blocks_d2h(c, c->s.rot_n1, h->rot_n1, 9, true))) return r;
+  if (h->cep && (r = blocks_d2h(c, c->s.cep, h->cep, 21, true))) return r;
+  if (h->element_vol && (r = blocks_d2h(c, c->s.evol, h->element_vol, 1, false))) return r;
+  if (h->einfvec) {
+    for (int b = 0; b < c->m.nelblk; ++b) {
+      const BlockDesc& bd = c->blocks[b];
+      if (!h->einfvec[b]) continue;
+      CK(cudaMemcpyAsync(h->einfvec[b], c->s.einf + bd.einf_off, (size_t)bd.totdof * bd.span * sizeof(double),
+                         cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return 0;
+}
+
+int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const double* hu, const double* hdu,
+               double* const* estiff) {
+  (void)step; (void)iter;
+  if (!c || !hc || !hu || !hdu) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->s.d_c, hc, (size_t)c->m.ncoord * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->s.d_u, hu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->s.d_du, hdu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
+  int r = run_tangent(c, c->s.d_c, c->s.d_u, c->s.d_du, st);
+  if (r) return r;
+  if (estiff) {
+    for (int b = 0; b < c->m.nelblk; ++b) {
+      const BlockDesc& bd = c->blocks[b];
+      if (!estiff[b]) continue;
+      size_t n = (size_t)bd.utsz * bd.span;
+      if (c->precision == W3G_TANGENT_FP64) {
+        // blocks whose host arrays follow each other in memory go in one copy
+        int e = b;
+        size_t run = n;
+        while (e + 1 < c->m.nelblk && estiff[e + 1] &&
+               estiff[e + 1] == estiff[e] + (size_t)c->blocks[e].utsz * c->blocks[e].span) {
+          ++e;
+          run += (size_t)c->blocks[e].utsz * c->blocks[e].span;
+        }
+        CK(cudaMemcpyAsync(estiff[b], c->s.estiff + bd.estiff_off, run * sizeof(double), cudaMemcpyDeviceToHost, st));
+        b = e;
+      } else {
+        // FP32 form: widen on the host
+        if (c->h_stage_n < n) {
+          if (c->h_stage) cudaFreeHost(c->h_stage);
+          c->h_stage = nullptr;
+          CK(cudaMallocHost((void**)&c->h_stage, n * sizeof(double)));
+          c->h_stage_n = n;
+        }
+        float* f = reinterpret_cast<float*>(c->h_stage);
+        CK(cudaMemcpyAsync(f, c->s.estiff32 + bd.estiff_off, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (size_t k = 0; k < n; ++k) estiff[b][k] = f[k];
+      }
+    }
+  }
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int w3g_recover(w3g_context* c, int step, int iter, int extrapolated_du, const double* hc, const double* hu,
+                const double* hdu, double* hifv, w3g_recover_info* info) {
+  if (!c || !hc || !hu || !hdu) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->s.d_c, hc, (size_t)c->m.ncoord * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->s.d_u, hu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->s.d_du, hdu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
+  int r = run_recover(c, step, iter, extrapolated_du, c->s.d_c, c->s.d_u, c->s.d_du, c->s.d_ifv, st);
+  if (r) return r;
+  w3g_recover_info hi;
+  CK(cudaMemcpyAsync(&hi, c->s.d_info, sizeof(hi), cudaMemcpyDeviceToHost, st));
+  if (hifv) CK(cudaMemcpyAsync(hifv, c->s.d_ifv, (size_t)c->m.nodof * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (info) *info = hi;
+  if (hi.material_cut_step) {
+    if (hifv) std::memset(hifv, 0, (size_t)c->m.nodof * sizeof(double));
+    return W3G_STEP_CUT;
+  }
+  return 0;
+}
+
+int w3g_update(w3g_context* c) {
+  if (!c) return fail(W3G_EARG, "null context");
+  CK(cudaSetDevice(c->device));
+  const long long gp = c->m.ngp_total;
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->s.hist, c->s.hist1, (size_t)kHistMM01 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->s.eps_n, c->s.eps_n1, (size_t)6 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->s.urcs_n, c->s.urcs_n1, (size_t)9 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int w3g_tanstf_dev(w3g_context* c, int step, int iter, const void* d_c, const void* d_u, const void* d_du,
+                   void* stream) {
+  (void)step; (void)iter;
+  if (!c || !d_c || !d_u || !d_du) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  return run_tangent(c, (const double*)d_c, (const double*)d_u, (const double*)d_du, (cudaStream_t)stream);
+}
+
+int w3g_recover_dev(w3g_context* c, int step, int iter, int extrapolated_du, const void* d_c, const void* d_u,
+                    const void* d_du, void* d_ifv, void* stream) {
+  if (!c || !d_c || !d_u || !d_du || !d_ifv) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  return run_recover(c, step, iter, extrapolated_du, (const double*)d_c, (const double*)d_u, (const double*)d_du,
+                     (double*)d_ifv, (cudaStream_t)stream);
+}
+
+int w3g_recover_info_get(w3g_context* c, w3g_recover_info* info) {
+  if (!c || !info) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpy(info, c->s.d_info, sizeof(*info), cudaMemcpyDeviceToHost));
+  return info->material_cut_step ? W3G_STEP_CUT : 0;
+}
+
+int w3g_estiff_device(w3g_context* c, void** d_estiff, long long* count) {
+  if (!c || !d_estiff || !count) return fail(W3G_EARG, "null argument");
+  *d_estiff = c->precision == W3G_TANGENT_FP32 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
+  *count = c->m.estiff_total;
+  return 0;
+}
+
+int w3g_last_launch_count(w3g_context* c) { return c ? c->last_launches : 0; }
+
+}  // extern "C"

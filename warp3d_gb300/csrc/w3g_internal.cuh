@@ -1,0 +1,146 @@
+// w3g_internal.cuh -- device-resident element-block state and the
+// launch-argument structs shared by the kernels and the C-ABI layer.
+//
+// Layout in HBM: every blocked array of WARP3D's elem_block_data is kept
+// as ONE device allocation holding all blocks back to back, block b at
+// the offset in its BlockDesc. Inside a block the reference's layout is
+// kept unchanged, so a block's slice can be copied to or from the
+// Fortran block pointer with one memcpy:
+//   (k, ngp, span) arrays (history, urcs, eps, rot): element-major, the
+//       element's ngp*k values contiguous -> global element index e,
+//       GP g: (gp_off + i*ngp + g)*k
+//   cep (21, span, ngp): GP-major inside the block
+//   estiff (utsz, span), einfvec (span, totdof)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/w3g.h"
+
+namespace w3g {
+
+constexpr int kMxvl = W3G_MXVL;
+constexpr int kHistMM01 = 11;      // mm01_set_sizes, src/mm01.f:976-979
+constexpr int kChunk = 8;          // elements per warp-sized work item
+
+struct BlockDesc {
+  int span;
+  int felem;          // 0-based first element
+  int etype, nnode, ngp, totdof, utsz, mat;
+  int geonl, bbar;
+  long long gp_off;     // sum of span*ngp over previous blocks
+  long long cep_off;    // sum of 21*span*ngp
+  long long estiff_off; // sum of utsz*span
+  long long einf_off;   // sum of totdof*span (also edest/cdest offset)
+};
+
+// one work item = up to kChunk consecutive elements of one block
+struct Chunk {
+  int blk;
+  int i0;     // first relative element
+  int n;      // number of elements (<= kChunk)
+};
+
+// per-element mm01 properties as doubles (promoted from the float32
+// props table exactly as setup_mm01_rknstr does, src/rknstr.f:1036-1054)
+struct MatProps {
+  double e, nu, beta, h, yld;
+  double lnelas;      // 1.0 = always linear elastic (lprops(17))
+};
+
+struct DeviceModel {
+  int nelblk = 0, noelem = 0, nodof = 0, ncoord = 0;
+  int qbar = 1;
+  double beta_fact = 1.0;
+  int nchunks = 0;
+  long long ngp_total = 0, cep_total = 0, estiff_total = 0, einf_total = 0;
+  BlockDesc* blocks = nullptr;     // device
+  Chunk* chunks = nullptr;         // device
+  int* edest = nullptr;            // device, concatenated (totdof, span)
+  int* cdest = nullptr;
+  MatProps* mat = nullptr;         // device, noelem
+  double* dn_hex8 = nullptr;       // device, fill_dn_table<Hex8>
+  // deterministic ifv assembly: CSR over global dofs of einfvec indices
+  int* ifv_rowptr = nullptr;       // nodof+1
+  long long* ifv_src = nullptr;    // einf_total
+};
+
+struct DeviceState {
+  double* hist = nullptr;    // 11 * ngp_total
+  double* hist1 = nullptr;
+  double* urcs_n = nullptr;  // 9 * ngp_total
+  double* urcs_n1 = nullptr;
+  double* eps_n = nullptr;   // 6 * ngp_total
+  double* eps_n1 = nullptr;
+  double* rot_n1 = nullptr;  // 9 * ngp_total
+  double* cep = nullptr;     // cep_total
+  double* estiff = nullptr;  // estiff_total (FP64 form)
+  float* estiff32 = nullptr; // estiff_total (FP32 form), lazily allocated
+  double* einf = nullptr;    // einf_total
+  double* evol = nullptr;    // noelem
+  // per-launch scratch
+  double* partials = nullptr;      // 2 * nchunks: energy, plastic work
+  double* ifv_partials = nullptr;  // per CTA of the ifv assembly
+  int* status = nullptr;           // [0]: min bad element (INT_MAX = none)
+  w3g_recover_info* d_info = nullptr;
+  // host-call staging
+  double* d_c = nullptr;
+  double* d_u = nullptr;
+  double* d_du = nullptr;
+  double* d_ifv = nullptr;
+};
+
+// ---- launch arguments --------------------------------------------------
+struct TangentArgs {
+  const double* dn;      // element table, fill_dn_table layout
+  const BlockDesc* blocks;
+  const Chunk* chunks;
+  const int* edest;
+  const int* cdest;
+  const double* c;
+  const double* u;
+  const double* du;
+  const double* rot_n1;
+  const double* urcs_n1;
+  const double* cep;
+  void* estiff;          // double* or float*
+  int qbar;
+  double beta_fact;
+};
+
+struct RecoverArgs {
+  const double* dn;
+  const BlockDesc* blocks;
+  const Chunk* chunks;
+  const int* edest;
+  const int* cdest;
+  const MatProps* mat;
+  const double* c;
+  const double* u;
+  const double* du;
+  const double* hist;
+  double* hist1;
+  const double* urcs_n;
+  double* urcs_n1;
+  const double* eps_n;
+  double* eps_n1;
+  double* rot_n1;
+  double* cep;
+  double* einf;
+  double* evol;
+  double* partials;
+  int* status;
+  int step, iter, nonlinear;
+  double beta_fact;
+};
+
+// ---- kernel launchers (defined in the .cu files) -----------------------
+cudaError_t launch_tangent_fp64(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
+cudaError_t launch_tangent_fp32(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
+cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, cudaStream_t s);
+cudaError_t launch_assemble_ifv(const DeviceModel& m, const double* einf, double* ifv, double* ifv_partials,
+                                int nparts, cudaStream_t s);
+cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const double* ifv_partials,
+                            int nparts, const int* status, w3g_recover_info* d_info, cudaStream_t s);
+int assemble_ifv_parts(int nodof);
+
+}  // namespace w3g

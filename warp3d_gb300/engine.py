@@ -1,0 +1,99 @@
+"""Host-side mirror of WARP3D's two element-block entry points on top of
+the C-ABI (include/w3g.h).
+
+``Engine.tanstf``  <- tanstf (src/tanstf.f:17)
+``Engine.recover`` <- drive_eps_sig_internal_forces
+                      (src/drive_eps_sig_internal_forces.f:20)
+``Engine.update``  <- update (src/update.f:73-94)
+
+Same argument meaning as the Fortran: ``step``/``iter`` are the load step
+and Newton iteration, ``c``, ``u``, ``du`` the global coordinate,
+displacement and displacement-increment vectors, ``ifv`` the internal
+force vector (overwritten). A step-cut request comes back as the status
+``abi.STEP_CUT`` (WARP3D's material_cut_step); fatal errors raise
+:class:`abi.W3GError`. There is no CPU fallback: without the CUDA library
+or a device, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .model import HostState, Model, block_ptrs, dptr
+
+
+class Engine:
+    def __init__(self, model: Model, device: int = 0, precision: int = abi.TANGENT_FP64):
+        self.lib = abi.load()
+        self.model = model
+        self.desc = model.desc()
+        self.ctx = C.c_void_p()
+        abi.check(self.lib, self.lib.w3g_create(device, C.byref(self.desc), C.byref(self.ctx)))
+        if precision != abi.TANGENT_FP64:
+            self.set_precision(precision)
+
+    # ---- lifecycle --------------------------------------------------------
+    def close(self):
+        if self.ctx:
+            self.lib.w3g_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_precision(self, precision: int):
+        abi.check(self.lib, self.lib.w3g_set_tangent_precision(self.ctx, precision))
+
+    # ---- state transfer ----------------------------------------------------
+    def upload(self, state: HostState, names=None):
+        s = state.struct(names)
+        abi.check(self.lib, self.lib.w3g_state_upload(self.ctx, C.byref(s)))
+
+    def download(self, state: HostState, names=None):
+        s = state.struct(names)
+        abi.check(self.lib, self.lib.w3g_state_download(self.ctx, C.byref(s)))
+
+    # ---- hot path, host arrays --------------------------------------------
+    def tanstf(self, step: int, it: int, c: np.ndarray, u: np.ndarray, du: np.ndarray, estiff_blocks=None):
+        ptrs = None
+        if estiff_blocks is not None:
+            ptrs = C.cast(block_ptrs(estiff_blocks), C.POINTER(C.POINTER(C.c_double)))
+        return abi.check(self.lib, self.lib.w3g_tanstf(self.ctx, step, it, dptr(c), dptr(u), dptr(du), ptrs))
+
+    def recover(self, step: int, it: int, extrapolated: bool, c, u, du, ifv):
+        info = abi.RecoverInfo()
+        st = self.lib.w3g_recover(self.ctx, step, it, 1 if extrapolated else 0, dptr(c), dptr(u), dptr(du),
+                                  dptr(ifv) if ifv is not None else None, C.byref(info))
+        abi.check(self.lib, st, allow=(abi.OK, abi.STEP_CUT))
+        return st, info
+
+    def update(self):
+        return abi.check(self.lib, self.lib.w3g_update(self.ctx))
+
+    # ---- hot path, device pointers (ints) ----------------------------------
+    def tanstf_dev(self, step, it, d_c: int, d_u: int, d_du: int, stream: int = 0):
+        return abi.check(self.lib, self.lib.w3g_tanstf_dev(self.ctx, step, it, d_c, d_u, d_du, stream or None))
+
+    def recover_dev(self, step, it, extrapolated, d_c: int, d_u: int, d_du: int, d_ifv: int, stream: int = 0):
+        return abi.check(self.lib, self.lib.w3g_recover_dev(self.ctx, step, it, 1 if extrapolated else 0, d_c, d_u,
+                                                            d_du, d_ifv, stream or None))
+
+    def recover_info(self):
+        info = abi.RecoverInfo()
+        st = self.lib.w3g_recover_info_get(self.ctx, C.byref(info))
+        abi.check(self.lib, st, allow=(abi.OK, abi.STEP_CUT))
+        return st, info
+
+    def estiff_device(self):
+        p = C.c_void_p()
+        n = C.c_longlong()
+        abi.check(self.lib, self.lib.w3g_estiff_device(self.ctx, C.byref(p), C.byref(n)))
+        return p.value, n.value
+
+    def last_launch_count(self) -> int:
+        return self.lib.w3g_last_launch_count(self.ctx)
