@@ -40,7 +40,7 @@ METRIC = "Newton-iteration element throughput (elem/s) FP64 vs mixed @ equal res
 UNIT = "elem/s"
 
 # Algorithmic FP64 work per hex8 element per call (flops, FMA = 2), the
-# minimal operation counts of the computed quantities (see DESIGN.md):
+# minimal operation counts of the computed quantities:
 #   tangent  per GP: [J] 72 FMA + inverse 30 + gradients 72 + [D] scale 21
 #            + [q] 63 + {T} 36 + [q][D][q]^T 342 + Q-bar 25 + D*B 432
 #            + B^T(D*B) 900 + {T}g 72 + G^T T G 216  = 2281 ops -> 4562 flop/GP
@@ -50,11 +50,14 @@ UNIT = "elem/s"
 #            per polar decomposition, counted as executed instructions only)
 TANGENT_FLOP_PER_ELEM = 8 * 4562
 RECOVER_FLOP_PER_ELEM = 8 * 4110
-# reference's dense counts for comparison in the JSON
+# the reference's dense operation counts (B as a full 6 x totdof matrix),
+# reported beside ours in the JSON
 TANGENT_FLOP_PER_ELEM_REFDENSE = 52992
 RECOVER_FLOP_PER_ELEM_REFDENSE = 12000
 # compulsory HBM bytes per element (FP64): tangent reads cep 21*8, coords
-# 24, rot+urcs 18*8 per GP and writes Ke 300; recovery per SURVEY 8d.
+# 24, rot+urcs 18*8 per GP and writes Ke 300; recovery reads coordinates,
+# u, du and the state at n (2,240 B) and writes the state at n+1, cep, R
+# and the element forces (3,776 B).
 TANGENT_BYTES_PER_ELEM = 8 * (21 * 8 + 24 + 48 + 18 * 8 + 300)
 TANGENT32_BYTES_PER_ELEM = TANGENT_BYTES_PER_ELEM - 4 * 300
 RECOVER_BYTES_PER_ELEM = 6016

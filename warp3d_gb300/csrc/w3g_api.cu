@@ -69,7 +69,7 @@ __global__ void k_init_rot(double* rot, long long ngp_total) {
   }
 }
 
-__global__ void k_reset_status(int* status) { status[0] = INT_MAX; }
+__global__ void k_reset_status(unsigned long long* status) { status[0] = ~0ull; }
 
 // copy n values between per-block host pointers and one device array
 int blocks_h2d(w3g_context* c, double* dev, double* const* host, int per_elem_or_gp, bool per_gp) {
@@ -155,6 +155,8 @@ int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_
 }
 
 }  // namespace
+
+void w3g::set_last_error(const std::string& msg) { g_err = msg; }
 
 extern "C" {
 

@@ -13,6 +13,7 @@
 //   estiff (utsz, span), einfvec (span, totdof)
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 #include "../../include/w3g.h"
 
@@ -80,7 +81,7 @@ struct DeviceState {
   // per-launch scratch
   double* partials = nullptr;      // 2 * nchunks: energy, plastic work
   double* ifv_partials = nullptr;  // per CTA of the ifv assembly
-  int* status = nullptr;           // [0]: min bad element (INT_MAX = none)
+  unsigned long long* status = nullptr;  // first det[F] <= 0 point, w3g::bad_point_key order
   w3g_recover_info* d_info = nullptr;
   // host-call staging
   double* d_c = nullptr;
@@ -128,7 +129,7 @@ struct RecoverArgs {
   double* einf;
   double* evol;
   double* partials;
-  int* status;
+  unsigned long long* status;
   int step, iter, nonlinear;
   double beta_fact;
 };
@@ -140,7 +141,20 @@ cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, cudaStrea
 cudaError_t launch_assemble_ifv(const DeviceModel& m, const double* einf, double* ifv, double* ifv_partials,
                                 int nparts, cudaStream_t s);
 cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const double* ifv_partials,
-                            int nparts, const int* status, w3g_recover_info* d_info, cudaStream_t s);
+                            int nparts, const unsigned long long* status, w3g_recover_info* d_info, cudaStream_t s);
+
+// Order in which WARP3D reports the element of a det[F] <= 0 point: the
+// block loop returns at the first Gauss point (gpn) where any element of
+// the block fails, checking F at n+1 for all elements before F at n+1/2
+// (rstgp1.f:135-145, fcomp1 in gtmat1.f:649-664), and names the first
+// failing element of that check. The smallest key is that point.
+__host__ __device__ inline unsigned long long bad_point_key(int blk, int gp, int half_step, int i) {
+  return ((unsigned long long)blk << 40) | ((unsigned long long)gp << 24) | ((unsigned long long)half_step << 20) |
+         (unsigned long long)i;
+}
 int assemble_ifv_parts(int nodof);
+
+// message returned by w3g_last_error() (defined in w3g_api.cu)
+void set_last_error(const std::string& msg);
 
 }  // namespace w3g

@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(kThreads) k_recover_hex8(RecoverArgs a) {
     double Fh[9] = {thh[0] + 1.0, thh[1], thh[2], thh[3], thh[4] + 1.0, thh[5], thh[6], thh[7], thh[8] + 1.0};
     const double dfn1 = det_ref(F1);
     const double dfh = det_ref(Fh);
-    if (dfn1 <= 1.0e-20 || dfh <= 1.0e-20) atomicMin(a.status, eg + 1);
+    if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
+    else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
     double R1[9], Rh[9], qnh[36];
     polar_rotation_ref(F1, R1);
     polar_rotation_ref(Fh, Rh);
@@ -298,8 +299,9 @@ __global__ void __launch_bounds__(kAsmThreads) k_assemble_ifv(int nodof, const i
 }
 
 __global__ void __launch_bounds__(256) k_finalize(int nchunks, const double* partials, int nparts,
-                                                  const double* ifv_partials, const int* status,
-                                                  long long num_term, w3g_recover_info* info) {
+                                                  const double* ifv_partials, const unsigned long long* status,
+                                                  const BlockDesc* blocks, long long num_term,
+                                                  w3g_recover_info* info) {
   __shared__ double s0[256], s1[256], s2[256];
   double e = 0.0, p = 0.0, f = 0.0;
   for (int k = threadIdx.x; k < nchunks; k += 256) { e += partials[2 * k]; p += partials[2 * k + 1]; }
@@ -315,13 +317,14 @@ __global__ void __launch_bounds__(256) k_finalize(int nchunks, const double* par
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const int st = status[0];
+    const unsigned long long st = status[0];
+    const bool cut = st != ~0ull;
     info->internal_energy = s0[0];
     info->plastic_work = s1[0];
     info->sum_ifv = s2[0];
     info->num_term_ifv = num_term;
-    info->material_cut_step = st != INT_MAX ? 1 : 0;
-    info->first_bad_element = st != INT_MAX ? st : 0;
+    info->material_cut_step = cut ? 1 : 0;
+    info->first_bad_element = cut ? blocks[st >> 40].felem + (int)(st & 0xFFFFFull) + 1 : 0;
   }
 }
 
@@ -343,8 +346,8 @@ cudaError_t launch_assemble_ifv(const DeviceModel& m, const double* einf, double
 }
 
 cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const double* ifv_partials, int nparts,
-                            const int* status, w3g_recover_info* d_info, cudaStream_t s) {
-  k_finalize<<<1, 256, 0, s>>>(m.nchunks, partials, nparts, ifv_partials, status, m.einf_total, d_info);
+                            const unsigned long long* status, w3g_recover_info* d_info, cudaStream_t s) {
+  k_finalize<<<1, 256, 0, s>>>(m.nchunks, partials, nparts, ifv_partials, status, m.blocks, m.einf_total, d_info);
   return cudaGetLastError();
 }
 
