@@ -191,6 +191,27 @@ int w3g_estiff_device(w3g_context* ctx, void** d_estiff, long long* count);
 /* Number of kernels the last w3g_tanstf/w3g_recover(_dev) call launched. */
 int w3g_last_launch_count(w3g_context* ctx);
 
+/* ---- internal-force assembly without device allocation --------------
+   No counterpart in the reference. For callers that cannot allocate
+   device memory -- a Fortran code whose device arrays come from a pool or
+   a framework that owns the allocator, or a run where allocation is
+   forbidden after start-up -- and so cannot create a w3g_context: given
+   element internal forces d_einfvec (all blocks back to back, each
+   (span, totdof)) and d_edest (each (totdof, span), 1-based) on the
+   current device, writes the nodal vector d_ifv (nodof, zeroed first)
+   and *d_sum_ifv = sum |einfvec| (addifv, src/addifv.f:86-124).
+   elblks (3*nelblk) and totdof (nelblk) are host arrays.
+   Allocates nothing: its scratch is a fixed static device array for at
+   most W3G_NOALLOC_MAX_BLOCKS element blocks (larger models: W3G_EARG).
+   The first call on a device sets up the array's address and must come
+   before any stream capture. Calls share the array: calls that overlap
+   on the GPU race and must be serialised. Returns after the work ends. */
+#define W3G_NOALLOC_MAX_BLOCKS 65536
+int w3g_assemble_ifv_noalloc(int nelblk, const int* elblks, const int* totdof,
+                             int nodof, const double* d_einfvec,
+                             const int* d_edest, double* d_ifv,
+                             double* d_sum_ifv, void* stream);
+
 /* ---- measurement helper (no WARP3D counterpart) ---------------------
    Sustained FP64 FMA throughput of `device` in TFLOP/s (2 flops per FMA),
    the roofline denominator of the FP64-bound element kernels. */

@@ -97,6 +97,8 @@ PROTOTYPES = [
     ("w3g_estiff_device", C.c_int, [_vp, C.POINTER(_vp), C.POINTER(C.c_longlong)]),
     ("w3g_last_launch_count", C.c_int, [_vp]),
     ("w3g_measure_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    ("w3g_assemble_ifv_noalloc", C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, _vp, _vp,
+                                           _vp, _vp, _vp]),
 ]
 
 _lib = None
