@@ -39,17 +39,21 @@ sys.path.insert(0, ROOT)
 METRIC = "Newton-iteration element throughput (elem/s) FP64 vs mixed @ equal residual"
 UNIT = "elem/s"
 
-# Algorithmic FP64 work per hex8 element per call (flops, FMA = 2), the
-# minimal operation counts of the computed quantities:
-#   tangent  per GP: [J] 72 FMA + inverse 30 + gradients 72 + [D] scale 21
-#            + [q] 63 + {T} 36 + [q][D][q]^T 342 + Q-bar 25 + D*B 432
-#            + B^T(D*B) 900 + {T}g 72 + G^T T G 216  = 2281 ops -> 4562 flop/GP
-#   recovery per GP: 2 x (jacob1 + tcomp1 + fcomp1 + polar) 1060,
-#            mid-step [B] and d 310, [q] rotations 135, mm01+cnst1 260,
-#            ifv 290  = 2055 ops -> 4110 flop/GP (+ 4 sqrt, atan2, sin, cos
-#            per polar decomposition, counted as executed instructions only)
-TANGENT_FLOP_PER_ELEM = 8 * 4562
-RECOVER_FLOP_PER_ELEM = 8 * 4110
+# Algorithmic FP64 work per hex8 element per call, in flops (FMA = 2,
+# add/mul = 1): the minimal counts of the quantities computed, per GP:
+#   tangent  [J] 144, det/inverse 50, shape gradients 120, [D] scale 21,
+#            [q] 54, {T} = [q]{t} 66, [q][D][q]^T lower triangle 627,
+#            Q-bar 30, {T}w 6, D*B_b 720, {T}g_b 120,
+#            B^T(D*B) upper triangle (900 multiply-adds) 1800, G^T T G 288
+#            = 4046 flop/GP
+#   recovery theta at n+1 and n+1/2 in reference order 360, det[F] 34,
+#            2 polar decompositions 400 (plus per decomposition: atan2,
+#            sin, cos, 5 sqrt, 1 division), d = sym(dDu/dX Fh^-1) 220,
+#            unrotation 81, mm01 + cnst1 250, energy 12, Cauchy rotation
+#            75, P = T F^-T 84, element forces 120, GP sums 21
+#            = 1657 flop/GP
+TANGENT_FLOP_PER_ELEM = 8 * 4046
+RECOVER_FLOP_PER_ELEM = 8 * 1657
 # the reference's dense operation counts (B as a full 6 x totdof matrix),
 # reported beside ours in the JSON
 TANGENT_FLOP_PER_ELEM_REFDENSE = 52992

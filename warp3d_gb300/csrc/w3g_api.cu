@@ -52,6 +52,7 @@ void free_all(w3g_context* c) {
   DeviceModel& m = c->m;
   DeviceState& s = c->s;
   void* ptrs[] = {m.blocks, m.chunks, m.edest, m.cdest, m.mat, m.dn_hex8, m.ifv_rowptr, m.ifv_src,
+                  s.geo, s.c_geo, s.geo_dirty,
                   s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
                   s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
                   s.d_c, s.d_u, s.d_du, s.d_ifv};
@@ -142,15 +143,17 @@ int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_
   a.evol = c->s.evol;
   a.partials = c->s.partials;
   a.status = c->s.status;
+  a.geo = c->s.geo;
+  a.geo_dirty = c->s.geo_dirty;
   a.step = step; a.iter = iter;
   a.nonlinear = (iter >= 1 || extrap) ? 1 : 0;
   a.beta_fact = c->m.beta_fact;
-  cudaError_t e = launch_recover(c->m, a, st);
+  cudaError_t e = launch_recover(c->m, a, c->s.c_geo, st);
   if (e == cudaSuccess) e = launch_assemble_ifv(c->m, c->s.einf, d_ifv, c->s.ifv_partials, c->ifv_parts, st);
   if (e == cudaSuccess)
     e = launch_finalize(c->m, c->s.partials, c->s.ifv_partials, c->ifv_parts, c->s.status, c->s.d_info, st);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("recover launch: ") + cudaGetErrorString(e));
-  c->last_launches = 4;
+  c->last_launches = 7;
   return 0;
 }
 
@@ -274,6 +277,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     const int* lp = md->lprops + (size_t)e * W3G_MXELPR;
     mat[e].e = p[6]; mat[e].nu = p[7]; mat[e].beta = p[13]; mat[e].h = p[14]; mat[e].yld = p[22];
     mat[e].lnelas = lp[16] ? 1.0 : 0.0;
+    fill_mat_constants(mat[e]);
   }
   double dn[dn_table_size<Hex8>()];
   fill_dn_table<Hex8>(dn);
@@ -300,6 +304,9 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(s.estiff, est);
   AL(s.einf, einf);
   AL(s.evol, md->noelem);
+  AL(s.geo, (long long)geo_values_per_gp() * gp);
+  AL(s.c_geo, md->ncoord);
+  AL(s.geo_dirty, 1);
   AL(s.partials, 2 * m.nchunks);
   c->ifv_parts = assemble_ifv_parts(md->nodof);
   AL(s.ifv_partials, c->ifv_parts);
@@ -331,6 +338,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   double* zs[] = {s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.cep, s.estiff, s.einf, s.evol};
   long long zn[] = {kHistMM01 * gp, kHistMM01 * gp, 9 * gp, 9 * gp, 6 * gp, 6 * gp, cep, est, einf, md->noelem};
   for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = cudaMemsetAsync(zs[k], 0, (size_t)zn[k] * sizeof(double), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.geo_dirty, 0xff, sizeof(int), st);   // nonzero: not built
   if (e == cudaSuccess) {
     k_init_rot<<<(unsigned)((gp + 255) / 256), 256, 0, st>>>(s.rot_n1, gp);
     e = cudaGetLastError();

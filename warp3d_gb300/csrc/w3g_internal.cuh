@@ -42,11 +42,41 @@ struct Chunk {
 };
 
 // per-element mm01 properties as doubles (promoted from the float32
-// props table exactly as setup_mm01_rknstr does, src/rknstr.f:1036-1054)
+// props table exactly as setup_mm01_rknstr does, src/rknstr.f:1036-1054),
+// plus the constants of mm01/cnst1 that depend only on them, evaluated on
+// the host with the reference's expressions (fill_mat_constants).
 struct MatProps {
   double e, nu, beta, h, yld;
   double lnelas;      // 1.0 = always linear elastic (lprops(17))
+  double inv_e;       // 1/e
+  double inv_gn;      // 1/(e/two/(one+nu))         mm01_init g_n
+  double shear;       // e/(two*(one+nu))           mm01_init, cnst1 g
+  double hbari;       // beta*h
+  double hbark;       // (one-beta)*h
+  double yld_root3;   // yld/sqrt(3)                mm01_set_history kn
+  double k3;          // three*e*nu/((one+nu)*(one-two*nu)) + two*shear
+  double c2, c3, c4;  // elastic [D] of cnst1
+  double kbulk;       // (three*l + two*g)/three   cnst1 k
+  double gamma;       // one/(one + h/(three*g))   cnst1
 };
+
+inline void fill_mat_constants(MatProps& m) {
+  const double one = 1.0, two = 2.0, three = 3.0;
+  m.inv_e = one / m.e;
+  m.inv_gn = one / (m.e / two / (one + m.nu));
+  m.shear = m.e / (two * (one + m.nu));
+  m.hbari = m.beta * m.h;
+  m.hbark = (one - m.beta) * m.h;
+  m.yld_root3 = m.yld / 1.7320508075688772;
+  m.k3 = three * m.e * m.nu / ((one + m.nu) * (one - two * m.nu)) + two * m.shear;
+  const double c1 = (m.e / ((one + m.nu) * (one - two * m.nu)));
+  m.c2 = (one - m.nu) * c1;
+  m.c3 = ((one - two * m.nu) / two) * c1;
+  m.c4 = m.nu * c1;
+  const double l = (m.e * m.nu) / ((one + m.nu) * (one - two * m.nu));
+  m.kbulk = (three * l + two * m.shear) / three;
+  m.gamma = one / (one + m.h / (three * m.shear));
+}
 
 struct DeviceModel {
   int nelblk = 0, noelem = 0, nodof = 0, ncoord = 0;
@@ -78,6 +108,11 @@ struct DeviceState {
   float* estiff32 = nullptr; // estiff_total (FP32 form), lazily allocated
   double* einf = nullptr;    // einf_total
   double* evol = nullptr;    // noelem
+  // undeformed geometry per GP (dN/dX, det[J0]) and the coordinates it
+  // was built from; geo_dirty = 1 until built
+  double* geo = nullptr;     // geo_values_per_gp() * ngp_total
+  double* c_geo = nullptr;   // ncoord
+  int* geo_dirty = nullptr;
   // per-launch scratch
   double* partials = nullptr;      // 2 * nchunks: energy, plastic work
   double* ifv_partials = nullptr;  // per CTA of the ifv assembly
@@ -130,6 +165,8 @@ struct RecoverArgs {
   double* evol;
   double* partials;
   unsigned long long* status;
+  double* geo;
+  int* geo_dirty;
   int step, iter, nonlinear;
   double beta_fact;
 };
@@ -137,7 +174,8 @@ struct RecoverArgs {
 // ---- kernel launchers (defined in the .cu files) -----------------------
 cudaError_t launch_tangent_fp64(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
 cudaError_t launch_tangent_fp32(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
-cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, cudaStream_t s);
+cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, cudaStream_t s);
+int geo_values_per_gp();
 cudaError_t launch_assemble_ifv(const DeviceModel& m, const double* einf, double* ifv, double* ifv_partials,
                                 int nparts, cudaStream_t s);
 cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const double* ifv_partials,

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include "w3g_internal.cuh"
 
 namespace w3g {
 
@@ -313,11 +314,6 @@ __device__ __forceinline__ double mm01_state_word(int s) {
   return __longlong_as_double((long long)(unsigned long long)(uint32_t)s);
 }
 
-struct MM01In {
-  double e, nu, beta, h, yld;
-  bool lnelas;
-};
-
 // One Gauss point of mm01 (src/mm01.f:24-233): mm01_set_history (step 1),
 // mm01_init, mm01_general, the elastic branch, mm01_sig_final,
 // mm01_wrapup; then cnst1 (src/mm01.f:1196-1348) for the lower triangle
@@ -325,89 +321,86 @@ struct MM01In {
 // the reference modifies its local copy. alpha11_first: history word 11
 // of the block's first element at this Gauss point, which mm01_general
 // reads for every element (src/mm01.f:843-845).
-__device__ __forceinline__ void mm01_point(const MM01In& mp, int step, double* cgn /*9, modified at step 1*/,
+//
+// Per-element constants come precomputed (MatProps, evaluated on the host
+// with the reference's expressions); the remaining divisions by
+// per-point values use one reciprocal each.
+__device__ __forceinline__ void mm01_point(const MatProps& mp, int step, double* cgn /*9, modified at step 1*/,
                                            const double* deps, double* hist /*11*/, double alpha11_first,
                                            double* cgn1 /*9*/, double* hist1 /*11*/, double* cep21) {
-  const double one = 1.0, two = 2.0, three = 3.0, half = 0.5;
-  const double root3 = 1.7320508075688772, root2 = 1.4142135623730951;
+  const double one = 1.0, two = 2.0, half = 0.5;
+  const double third = 1.0 / 3.0;
+  const double root2 = 1.4142135623730951, inv_root3 = 0.5773502691896258, inv_root2 = 0.7071067811865476;
+  const bool lnelas = mp.lnelas != 0.0;
   if (step == 1) {   // mm01_set_history
-    double kn = mp.yld / root3;
-    hist[0] = 0.0; hist[1] = kn; hist[2] = 0.0; hist[3] = mm01_state_word(3); hist[4] = mp.h;
+    hist[0] = 0.0; hist[1] = mp.yld_root3; hist[2] = 0.0; hist[3] = mm01_state_word(3); hist[4] = mp.h;
 #pragma unroll
     for (int k = 5; k < 11; ++k) hist[k] = 0.0;
     cgn[7] = 0.0; cgn[8] = 0.0;
     alpha11_first = 0.0;
   }
   // mm01_init
-  double deps_vol = deps[0] + deps[1] + deps[2];
-  double eps_mean = deps_vol / three;
-  double de1 = deps[0] - eps_mean, de2 = deps[1] - eps_mean, de3 = deps[2] - eps_mean;
-  double e_n = mp.e, nu_n = mp.nu;
-  double g_n = e_n / two / (one + nu_n);
-  double een1 = (cgn[0] - nu_n * (cgn[1] + cgn[2])) / e_n;
-  double een2 = (cgn[1] - nu_n * (cgn[0] + cgn[2])) / e_n;
-  double een3 = (cgn[2] - nu_n * (cgn[0] + cgn[1])) / e_n;
-  double een4 = cgn[3] / g_n, een5 = cgn[4] / g_n, een6 = cgn[5] / g_n;
-  double eps_vol_n1 = een1 + een2 + een3 + deps_vol;
-  double eps_mean_n = (een1 + een2 + een3) / three;
-  double ed[6];
-  ed[0] = (een1 - eps_mean_n) + de1;
-  ed[1] = (een2 - eps_mean_n) + de2;
-  ed[2] = (een3 - eps_mean_n) + de3;
-  ed[3] = een4 + deps[3]; ed[4] = een5 + deps[4]; ed[5] = een6 + deps[5];
-  double shear_mod = mp.e / (two * (one + mp.nu));
+  const double deps_vol = deps[0] + deps[1] + deps[2];
+  const double eps_mean = deps_vol * third;
+  const double een1 = (cgn[0] - mp.nu * (cgn[1] + cgn[2])) * mp.inv_e;
+  const double een2 = (cgn[1] - mp.nu * (cgn[0] + cgn[2])) * mp.inv_e;
+  const double een3 = (cgn[2] - mp.nu * (cgn[0] + cgn[1])) * mp.inv_e;
+  const double eps_vol_n1 = een1 + een2 + een3 + deps_vol;
+  const double eps_mean_n = (een1 + een2 + een3) * third;
+  const double g2 = two * mp.shear;
   double dev[6];
-  dev[0] = two * shear_mod * ed[0]; dev[1] = two * shear_mod * ed[1]; dev[2] = two * shear_mod * ed[2];
-  dev[3] = shear_mod * ed[3]; dev[4] = shear_mod * ed[4]; dev[5] = shear_mod * ed[5];
-  double hbari_np1 = mp.beta * mp.h;
-  double hbark_np1 = (one - mp.beta) * mp.h;
-  double hbark_n = (one - mp.beta) * hist[4];
-  double kbar = (mp.yld + hbari_np1 * hist[2]) / root3;
+  dev[0] = g2 * ((een1 - eps_mean_n) + (deps[0] - eps_mean));
+  dev[1] = g2 * ((een2 - eps_mean_n) + (deps[1] - eps_mean));
+  dev[2] = g2 * ((een3 - eps_mean_n) + (deps[2] - eps_mean));
+  dev[3] = mp.shear * (cgn[3] * mp.inv_gn + deps[3]);
+  dev[4] = mp.shear * (cgn[4] * mp.inv_gn + deps[4]);
+  dev[5] = mp.shear * (cgn[5] * mp.inv_gn + deps[5]);
+  const double hbark_n = (one - mp.beta) * hist[4];
+  const double kbar = (mp.yld + mp.hbari * hist[2]) * inv_root3;
   double lk = one;
-  if (fabs(hbark_n) > 0.000001) lk = hbark_np1 / hbark_n;
+  if (fabs(hbark_n) > 0.000001) lk = mp.hbark / hbark_n;
   double rtse[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) rtse[k] = dev[k] - hist[5 + k] * lk;
   double mrts = sqrt(rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
                      two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]));
-  double yf = mrts - root2 * kbar;
+  const double yf = mrts - root2 * kbar;
 #pragma unroll
   for (int k = 0; k < 6; ++k) rtse[k] = dev[k] - hist[5 + k];
-  mrts = sqrt(rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
-              two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]));
-  bool yield = false;
-  int instat = 3;
-  if (!mp.lnelas && yf >= 0.0000001 * root2 * kbar) { yield = true; instat = 1; }
+  const double mrtsq = rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
+                       two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]);
+  mrts = sqrt(mrtsq);
+  const bool yield = !lnelas && yf >= 0.0000001 * root2 * kbar;
+  const int instat = yield ? 1 : 3;
 
   double devn1[6];
   if (yield) {   // mm01_general
     const double root2c = 1.414213562373095, twthrd = 0.666666666666667, root23 = 0.816496580927,
                  root2o3 = 0.4714045207910;
-    double a = (two * shear_mod + twthrd * hbark_np1) / mrts;
-    double b = one - lk;
-    double d = root2o3 * hbari_np1;
-    double vbar = mrts * mrts;
-    double wbar = hist[5] * hist[5] + hist[6] * hist[6] + hist[7] * hist[7] +
-                  two * (hist[8] * hist[8] + hist[9] * hist[9] + alpha11_first * alpha11_first);
-    double vwbar = rtse[0] * hist[5] + rtse[1] * hist[6] + rtse[2] * hist[7] +
-                   two * (rtse[3] * hist[8] + rtse[4] * hist[9] + rtse[5] * hist[10]);
-    double t1 = a * a * vbar - two * d * d;
-    double t2 = -4.0 * d * kbar - two * a * vbar - two * a * b * vwbar;
-    double t3 = b * b * wbar + two * b * vwbar + vbar - two * kbar * kbar;
-    double discr = t2 * t2 - 4.0 * t1 * t3;
+    const double rmrts = one / mrts;
+    const double a = (g2 + twthrd * mp.hbark) * rmrts;
+    const double b = one - lk;
+    const double d = root2o3 * mp.hbari;
+    const double vbar = mrts * mrts;
+    const double wbar = hist[5] * hist[5] + hist[6] * hist[6] + hist[7] * hist[7] +
+                        two * (hist[8] * hist[8] + hist[9] * hist[9] + alpha11_first * alpha11_first);
+    const double vwbar = rtse[0] * hist[5] + rtse[1] * hist[6] + rtse[2] * hist[7] +
+                         two * (rtse[3] * hist[8] + rtse[4] * hist[9] + rtse[5] * hist[10]);
+    const double t1 = a * a * vbar - two * d * d;
+    const double t2 = -4.0 * d * kbar - two * a * vbar - two * a * b * vwbar;
+    const double t3 = b * b * wbar + two * b * vwbar + vbar - two * kbar * kbar;
+    const double discr = t2 * t2 - 4.0 * t1 * t3;
     double lambda_deltat = 0.0;
     if (!(discr < 0.0)) {
-      double sd = sqrt(discr);
-      double qroot1 = (-t2 + sd) / (two * t1);
-      double qroot2 = (-t2 - sd) / (two * t1);
-      lambda_deltat = fmin(qroot1, qroot2);
+      const double sd = sqrt(discr), r2t1 = half / t1;
+      lambda_deltat = fmin((-t2 + sd) * r2t1, (-t2 - sd) * r2t1);
     }
     hist1[0] = lambda_deltat;
-    hist1[1] = kbar + (root2c / three) * hbari_np1 * lambda_deltat;
+    hist1[1] = kbar + (root2c / 3.0) * mp.hbari * lambda_deltat;
     hist1[2] = hist[2] + lambda_deltat * root23;
     hist1[4] = mp.h;
-    double const1 = twthrd * hbark_np1 * lambda_deltat / mrts;
-    double const2 = one - lambda_deltat * (twthrd * hbark_np1 + two * shear_mod) / mrts;
+    const double const1 = twthrd * mp.hbark * lambda_deltat * rmrts;
+    const double const2 = one - lambda_deltat * (twthrd * mp.hbark + g2) * rmrts;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
       hist1[5 + k] = lk * hist[5 + k] + const1 * rtse[k];
@@ -415,7 +408,7 @@ __device__ __forceinline__ void mm01_point(const MM01In& mp, int step, double* c
     }
   } else {
     hist1[0] = 0.0;
-    hist1[1] = mp.lnelas ? 0.0 : kbar;
+    hist1[1] = lnelas ? 0.0 : kbar;
     hist1[2] = hist[2];
     hist1[4] = mp.h;
 #pragma unroll
@@ -425,8 +418,7 @@ __device__ __forceinline__ void mm01_point(const MM01In& mp, int step, double* c
     }
   }
   // mm01_sig_final
-  double ym = mp.e, nu = mp.nu;
-  double sig_mean_np1 = eps_vol_n1 * (three * ym * nu / ((one + nu) * (one - two * nu)) + two * shear_mod) / three;
+  const double sig_mean_np1 = eps_vol_n1 * mp.k3 * third;
   cgn1[0] = devn1[0] + sig_mean_np1;
   cgn1[1] = devn1[1] + sig_mean_np1;
   cgn1[2] = devn1[2] + sig_mean_np1;
@@ -440,64 +432,94 @@ __device__ __forceinline__ void mm01_point(const MM01In& mp, int step, double* c
   cgn1[8] = cgn[8];
   if (yield) {
     const double six = 6.0;
-    double sbar_n = sqrt((cgn[0] - cgn[1]) * (cgn[0] - cgn[1]) + (cgn[1] - cgn[2]) * (cgn[1] - cgn[2]) +
-                         (cgn[0] - cgn[2]) * (cgn[0] - cgn[2]) +
-                         six * (cgn[3] * cgn[3] + cgn[4] * cgn[4] + cgn[5] * cgn[5])) / root2;
-    double sbar_n1 = sqrt((cgn1[0] - cgn1[1]) * (cgn1[0] - cgn1[1]) + (cgn1[1] - cgn1[2]) * (cgn1[1] - cgn1[2]) +
-                          (cgn1[0] - cgn1[2]) * (cgn1[0] - cgn1[2]) +
-                          six * (cgn1[3] * cgn1[3] + cgn1[4] * cgn1[4] + cgn1[5] * cgn1[5])) / root2;
-    double depbar = hist1[2] - hist[2];
+    const double sbar_n = sqrt((cgn[0] - cgn[1]) * (cgn[0] - cgn[1]) + (cgn[1] - cgn[2]) * (cgn[1] - cgn[2]) +
+                               (cgn[0] - cgn[2]) * (cgn[0] - cgn[2]) +
+                               six * (cgn[3] * cgn[3] + cgn[4] * cgn[4] + cgn[5] * cgn[5])) * inv_root2;
+    const double sbar_n1 = sqrt((cgn1[0] - cgn1[1]) * (cgn1[0] - cgn1[1]) + (cgn1[1] - cgn1[2]) * (cgn1[1] - cgn1[2]) +
+                                (cgn1[0] - cgn1[2]) * (cgn1[0] - cgn1[2]) +
+                                six * (cgn1[3] * cgn1[3] + cgn1[4] * cgn1[4] + cgn1[5] * cgn1[5])) * inv_root2;
+    const double depbar = hist1[2] - hist[2];
     cgn1[7] = cgn[7] + half * (sbar_n1 + sbar_n) * depbar;
     cgn1[8] = cgn[8] + depbar;
   }
   // cnst1: lower triangle, order (1,1) (2,1) (2,2) (3,1) (3,2) (3,3) (4,1)..(6,6)
   if (!yield) {
-    double c1 = (mp.e / ((one + mp.nu) * (one - two * mp.nu)));
-    double c2 = (one - mp.nu) * c1;
-    double c3 = ((one - two * mp.nu) / two) * c1;
-    double c4 = mp.nu * c1;
-    cep21[0] = c2; cep21[1] = c4; cep21[2] = c2; cep21[3] = c4; cep21[4] = c4; cep21[5] = c2;
+    cep21[0] = mp.c2; cep21[1] = mp.c4; cep21[2] = mp.c2; cep21[3] = mp.c4; cep21[4] = mp.c4; cep21[5] = mp.c2;
 #pragma unroll
     for (int k = 6; k < 21; ++k) cep21[k] = 0.0;
-    cep21[9] = c3; cep21[14] = c3; cep21[20] = c3;
+    cep21[9] = mp.c3; cep21[14] = mp.c3; cep21[20] = mp.c3;
   } else {
     const double root2t = 1.414213562;   // cnst1 uses a truncated sqrt(2)
-    double kn1 = hist1[1], hprime = hist1[4], ldt = hist1[0];
-    double g = mp.e / (two * (one + mp.nu));
-    double l = (mp.e * mp.nu) / ((one + mp.nu) * (one - two * mp.nu));
-    double k = (three * l + two * g) / three;
-    double mrtsq = rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
-                   two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]);
-    double bb = (root2t * kn1 + (two / three) * (one - mp.beta) * hprime * ldt) / sqrt(mrtsq);
-    double gamma = one / (one + hprime / (three * g));
-    double gambar = gamma - one + bb;
-    double gbar = g * bb;
-    double albar = k - two * gbar / three;
-    double thbar = two * g * gambar;
-    double rm = thbar / mrtsq;
+    const double kn1 = hist1[1], ldt = hist1[0];
+    const double rm = one / mrtsq;
+    const double bb = (root2t * kn1 + (two / 3.0) * (one - mp.beta) * mp.h * ldt) / mrts;
+    const double gambar = mp.gamma - one + bb;
+    const double gbar = mp.shear * bb;
+    const double albar = mp.kbulk - two * gbar * third;
+    const double thbar = two * mp.shear * gambar * rm;
     const double* r = rtse;
-    cep21[0] = albar + two * gbar - rm * (r[0] * r[0]);
-    cep21[1] = albar - rm * r[0] * r[1];
-    cep21[2] = albar + two * gbar - rm * (r[1] * r[1]);
-    cep21[3] = albar - rm * r[0] * r[2];
-    cep21[4] = albar - rm * r[2] * r[1];
-    cep21[5] = albar + two * gbar - rm * (r[2] * r[2]);
-    cep21[6] = -(rm * r[0] * r[3]);
-    cep21[7] = -(rm * r[1] * r[3]);
-    cep21[8] = -(rm * r[2] * r[3]);
-    cep21[9] = gbar - rm * (r[3] * r[3]);
-    cep21[10] = -(rm * r[0] * r[4]);
-    cep21[11] = -(rm * r[1] * r[4]);
-    cep21[12] = -(rm * r[2] * r[4]);
-    cep21[13] = -(rm * r[3] * r[4]);
-    cep21[14] = gbar - rm * (r[4] * r[4]);
-    cep21[15] = -(rm * r[0] * r[5]);
-    cep21[16] = -(rm * r[1] * r[5]);
-    cep21[17] = -(rm * r[2] * r[5]);
-    cep21[18] = -(rm * r[3] * r[5]);
-    cep21[19] = -(rm * r[4] * r[5]);
-    cep21[20] = gbar - rm * (r[5] * r[5]);
+    const double a2g = albar + two * gbar;
+    cep21[0] = a2g - thbar * (r[0] * r[0]);
+    cep21[1] = albar - thbar * r[0] * r[1];
+    cep21[2] = a2g - thbar * (r[1] * r[1]);
+    cep21[3] = albar - thbar * r[0] * r[2];
+    cep21[4] = albar - thbar * r[2] * r[1];
+    cep21[5] = a2g - thbar * (r[2] * r[2]);
+    cep21[6] = -(thbar * r[0] * r[3]);
+    cep21[7] = -(thbar * r[1] * r[3]);
+    cep21[8] = -(thbar * r[2] * r[3]);
+    cep21[9] = gbar - thbar * (r[3] * r[3]);
+    cep21[10] = -(thbar * r[0] * r[4]);
+    cep21[11] = -(thbar * r[1] * r[4]);
+    cep21[12] = -(thbar * r[2] * r[4]);
+    cep21[13] = -(thbar * r[3] * r[4]);
+    cep21[14] = gbar - thbar * (r[4] * r[4]);
+    cep21[15] = -(thbar * r[0] * r[5]);
+    cep21[16] = -(thbar * r[1] * r[5]);
+    cep21[17] = -(thbar * r[2] * r[5]);
+    cep21[18] = -(thbar * r[3] * r[5]);
+    cep21[19] = -(thbar * r[4] * r[5]);
+    cep21[20] = gbar - thbar * (r[5] * r[5]);
   }
+}
+
+// {t} = [R]{T}[R]^T-type rotations of a symmetric tensor in Voigt form
+// (xx, yy, zz, xy, yz, xz). rotate_to_spatial: S = R s R^T (getrm1 opt 2 +
+// qmply1, src/gtmat1.f:803-846); rotate_to_unrotated for a rate of
+// deformation with engineering shears: d = R^T D R (getrm1 opt 1).
+__device__ __forceinline__ void rotate_to_spatial(const double* R, const double* s, double* S) {
+  // A = R s (3x3), S = A R^T, symmetric tensor s
+  const double t[9] = {s[0], s[3], s[5], s[3], s[1], s[4], s[5], s[4], s[2]};   // column-major
+  double A[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) A[r + 3 * c] = R[r] * t[3 * c] + R[r + 3] * t[1 + 3 * c] + R[r + 6] * t[2 + 3 * c];
+  // S_ij = sum_k A_ik R_jk
+  S[0] = A[0] * R[0] + A[3] * R[3] + A[6] * R[6];
+  S[1] = A[1] * R[1] + A[4] * R[4] + A[7] * R[7];
+  S[2] = A[2] * R[2] + A[5] * R[5] + A[8] * R[8];
+  S[3] = A[0] * R[1] + A[3] * R[4] + A[6] * R[7];
+  S[4] = A[1] * R[2] + A[4] * R[5] + A[7] * R[8];
+  S[5] = A[0] * R[2] + A[3] * R[5] + A[6] * R[8];
+}
+
+__device__ __forceinline__ void rotate_to_unrotated(const double* R, const double* d, double* u) {
+  // tensor D with half shears; A = R^T D, u = A R
+  const double t[9] = {d[0], 0.5 * d[3], 0.5 * d[5], 0.5 * d[3], d[1], 0.5 * d[4], 0.5 * d[5], 0.5 * d[4], d[2]};
+  double A[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      A[r + 3 * c] = R[3 * r] * t[3 * c] + R[1 + 3 * r] * t[1 + 3 * c] + R[2 + 3 * r] * t[2 + 3 * c];
+  // u_ij = sum_k A_ik R_kj
+  u[0] = A[0] * R[0] + A[3] * R[1] + A[6] * R[2];
+  u[1] = A[1] * R[3] + A[4] * R[4] + A[7] * R[5];
+  u[2] = A[2] * R[6] + A[5] * R[7] + A[8] * R[8];
+  u[3] = 2.0 * (A[0] * R[3] + A[3] * R[4] + A[6] * R[5]);
+  u[4] = 2.0 * (A[1] * R[6] + A[4] * R[7] + A[7] * R[8]);
+  u[5] = 2.0 * (A[0] * R[6] + A[3] * R[7] + A[6] * R[8]);
 }
 
 }  // namespace w3g

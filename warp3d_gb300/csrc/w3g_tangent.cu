@@ -13,9 +13,9 @@
 //            w det[J] {T} to shared memory
 //   phase 2  per GP: lane t forms [D*][B_a] and {T}g_a for nodes 2t, 2t+1
 //            (shared memory), then accumulates 9 of the 36 node-pair
-//            3x3 blocks of Ke = sum_gp B^T D* B + G^T T G in registers.
-//            The 36 pairs (a <= b) are dealt round-robin, so every lane
-//            does the same work.
+//            3x3 blocks of Ke = sum_gp B^T D* B + G^T T G in registers
+//            with fused multiply-add chains. Each lane owns 2 diagonal
+//            and 7 off-diagonal pairs, so every lane does the same work.
 //   store    Ke is assembled in shared memory in WARP3D's column-packed
 //            upper triangle and written with coalesced stores; the chunk's
 //            elements are contiguous in estiff (utsz, span).
@@ -65,12 +65,19 @@ __global__ void __launch_bounds__(32) k_tangent_hex8(TangentArgs a) {
   const int i = ch.i0 + ge;      // relative element in block
 
   for (int k = lane; k < kDnSize; k += 32) sdn[k] = (T)a.dn[k];
-  if (lane < 8) {
-    // lexicographic (a <= b) pairs
-    int k = 0;
+  if (lane == 0) {
+    // node pairs (a <= b) of the 3x3 blocks of Ke, dealt to the 4 lanes of
+    // an element: lane t takes slot p = 4p' + t. Slots 0-7 are the
+    // diagonal pairs (t,t) and (t+4,t+4); the 28 off-diagonal pairs follow
+    // in lexicographic order, 7 per lane.
+    for (int t = 0; t < 4; ++t) {
+      pa[t] = pb[t] = (unsigned char)t;
+      pa[4 + t] = pb[4 + t] = (unsigned char)(t + 4);
+    }
+    int k = 8;
     for (int x = 0; x < NN; ++x)
-      for (int y = x; y < NN; ++y) {
-        if ((k & 7) == lane) { pa[k] = (unsigned char)x; pb[k] = (unsigned char)y; }
+      for (int y = x + 1; y < NN; ++y) {
+        pa[k] = (unsigned char)x; pb[k] = (unsigned char)y;
         ++k;
       }
   }
@@ -238,11 +245,17 @@ __global__ void __launch_bounds__(32) k_tangent_hex8(TangentArgs a) {
           const int na = pa[k], nb = pb[k];
           const T ax = g[3 * na], ay = g[3 * na + 1], az = g[3 * na + 2];
           const T* db = sDB + nb * 18;
+          // K_ab(i,k) += B_a(:,i) . (D* B_b)(:,k): rows of B_a column x are
+          // (xx, xy, xz) = (gx, gy, gz), column y (yy, xy, yz) = (gy, gx, gz),
+          // column z (zz, yz, xz) = (gz, gy, gx). Diagonal pairs (p < 2)
+          // need only i <= k.
 #pragma unroll
           for (int kk = 0; kk < 3; ++kk) {
-            acc[p][0 * 3 + kk] += ax * db[0 * 3 + kk] + ay * db[3 * 3 + kk] + az * db[5 * 3 + kk];
-            acc[p][1 * 3 + kk] += ay * db[1 * 3 + kk] + ax * db[3 * 3 + kk] + az * db[4 * 3 + kk];
-            acc[p][2 * 3 + kk] += az * db[2 * 3 + kk] + ay * db[4 * 3 + kk] + ax * db[5 * 3 + kk];
+            acc[p][0 * 3 + kk] = fma(ax, db[0 * 3 + kk], fma(ay, db[3 * 3 + kk], fma(az, db[5 * 3 + kk], acc[p][0 * 3 + kk])));
+            if (p >= 2 || kk >= 1)
+              acc[p][1 * 3 + kk] = fma(ay, db[1 * 3 + kk], fma(ax, db[3 * 3 + kk], fma(az, db[4 * 3 + kk], acc[p][1 * 3 + kk])));
+            if (p >= 2 || kk >= 2)
+              acc[p][2 * 3 + kk] = fma(az, db[2 * 3 + kk], fma(ay, db[4 * 3 + kk], fma(ax, db[5 * 3 + kk], acc[p][2 * 3 + kk])));
           }
           if (bd.geonl) {   // kgstiff (src/kg1.f:16-110)
             const T* tg = sTg + nb * 3;
@@ -268,7 +281,7 @@ __global__ void __launch_bounds__(32) k_tangent_hex8(TangentArgs a) {
       for (int ii = 0; ii < 3; ++ii)
 #pragma unroll
         for (int kk = 0; kk < 3; ++kk) {
-          if (na == nb && ii > kk) continue;
+          if (p < 2 && ii > kk) continue;
           int r = ii * NN + na, c = kk * NN + nb;
           if (r > c) { int tt = r; r = c; c = tt; }
           ke[c * (c + 1) / 2 + r] = acc[p][ii * 3 + kk] * bf;
