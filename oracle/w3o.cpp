@@ -92,9 +92,123 @@ void deriv2(double xi, double eta, double zeta, double* nxi, double* neta, doubl
   nxi[7] = ep * zp * one25;    neta[7] = xp * zp * one25;    nzeta[7] = xp * ep * one25;
 }
 
+// quad1, src/getgpts.f:177-420: 27-point rule (order 1) of the 20-node
+// brick; eta fastest, then xi, then zeta; weights by the number of zero
+// coordinates (w1..w4).
+bool quad1(int order, int gpn, double& xi, double& eta, double& zeta, double& w) {
+  if (order != 1 || gpn < 1 || gpn > 27) return false;
+  const double l1 = 0.774596669241483, l2 = 0.0;
+  const double w1 = 0.1714677640603571, w2 = 0.2743484224965712, w3 = 0.4389574759945135,
+               w4 = 0.7023319615912210;
+  const double v[3] = {-l1, l2, l1};
+  int g = gpn - 1;
+  int ie = g % 3, ix = (g / 3) % 3, iz = g / 9;
+  xi = v[ix]; eta = v[ie]; zeta = v[iz];
+  int zeros = (ix == 1) + (ie == 1) + (iz == 1);
+  const double ws[4] = {w1, w2, w3, w4};
+  w = ws[zeros];
+  return true;
+}
+
+// deriv1, src/derivs.f:182-281: 20-node brick
+void deriv1(double r, double s, double t, double* nr, double* ns, double* nt) {
+  const double one = 1.0, half = 0.5, fourth = 0.25, eighth = 0.125;
+  double rp1 = one + r, rm1 = one - r, sp1 = one + s, sm1 = one - s, tp1 = one + t, tm1 = one - t;
+  double rps = r + s, rms = r - s, spt = s + t, smt = s - t;
+  nr[0] = sm1 * (rp1 + rps - t) * tp1 * eighth;
+  nr[1] = sm1 * (rp1 + rps + t) * tm1 * eighth;
+  nr[2] = sp1 * (rp1 + rms + t) * tm1 * eighth;
+  nr[3] = sp1 * (rp1 + rms - t) * tp1 * eighth;
+  nr[4] = -sm1 * (rm1 - rms - t) * tp1 * eighth;
+  nr[5] = -sm1 * (rm1 - rms + t) * tm1 * eighth;
+  nr[6] = -sp1 * (rm1 - rps + t) * tm1 * eighth;
+  nr[7] = -sp1 * (rm1 - rps - t) * tp1 * eighth;
+  nr[8] = -sm1 * tm1 * tp1 * fourth;
+  nr[9] = -sm1 * sp1 * tm1 * fourth;
+  nr[10] = -sp1 * tm1 * tp1 * fourth;
+  nr[11] = -sm1 * sp1 * tp1 * fourth;
+  nr[12] = sm1 * tm1 * tp1 * fourth;
+  nr[13] = sm1 * sp1 * tm1 * fourth;
+  nr[14] = sp1 * tm1 * tp1 * fourth;
+  nr[15] = sm1 * sp1 * tp1 * fourth;
+  nr[16] = -r * sm1 * tp1 * half;
+  nr[17] = -r * sm1 * tm1 * half;
+  nr[18] = -r * sp1 * tm1 * half;
+  nr[19] = -r * sp1 * tp1 * half;
+  ns[0] = rm1 * (rp1 + s + smt) * tp1 * eighth;
+  ns[1] = rm1 * (rp1 + s + spt) * tm1 * eighth;
+  ns[2] = -rm1 * (rp1 - s - smt) * tm1 * eighth;
+  ns[3] = -rm1 * (rp1 - s - spt) * tp1 * eighth;
+  ns[4] = rp1 * (rm1 + s + smt) * tp1 * eighth;
+  ns[5] = rp1 * (rm1 + s + spt) * tm1 * eighth;
+  ns[6] = -rp1 * (rm1 - s - smt) * tm1 * eighth;
+  ns[7] = -rp1 * (rm1 - s - spt) * tp1 * eighth;
+  ns[8] = -rm1 * tm1 * tp1 * fourth;
+  ns[9] = -rm1 * s * tm1 * half;
+  ns[10] = rm1 * tm1 * tp1 * fourth;
+  ns[11] = -rm1 * s * tp1 * half;
+  ns[12] = -rp1 * tm1 * tp1 * fourth;
+  ns[13] = -rp1 * s * tm1 * half;
+  ns[14] = rp1 * tm1 * tp1 * fourth;
+  ns[15] = -rp1 * s * tp1 * half;
+  ns[16] = -rm1 * rp1 * tp1 * fourth;
+  ns[17] = -rm1 * rp1 * tm1 * fourth;
+  ns[18] = rm1 * rp1 * tm1 * fourth;
+  ns[19] = rm1 * rp1 * tp1 * fourth;
+  nt[0] = -rm1 * sm1 * (rp1 + smt - t) * eighth;
+  nt[1] = rm1 * sm1 * (rp1 + spt + t) * eighth;
+  nt[2] = rm1 * sp1 * (rp1 - smt + t) * eighth;
+  nt[3] = -rm1 * sp1 * (rp1 - spt - t) * eighth;
+  nt[4] = -rp1 * sm1 * (rm1 + smt - t) * eighth;
+  nt[5] = rp1 * sm1 * (rm1 + spt + t) * eighth;
+  nt[6] = rp1 * sp1 * (rm1 - smt + t) * eighth;
+  nt[7] = -rp1 * sp1 * (rm1 - spt - t) * eighth;
+  nt[8] = -rm1 * sm1 * t * half;
+  nt[9] = -rm1 * sm1 * sp1 * fourth;
+  nt[10] = -rm1 * sp1 * t * half;
+  nt[11] = rm1 * sm1 * sp1 * fourth;
+  nt[12] = -rp1 * sm1 * t * half;
+  nt[13] = -rp1 * sm1 * sp1 * fourth;
+  nt[14] = -rp1 * sp1 * t * half;
+  nt[15] = rp1 * sm1 * sp1 * fourth;
+  nt[16] = rm1 * rp1 * sm1 * fourth;
+  nt[17] = -rm1 * rp1 * sm1 * fourth;
+  nt[18] = -rm1 * rp1 * sp1 * fourth;
+  nt[19] = rm1 * rp1 * sp1 * fourth;
+}
+
+// quad6, src/getgpts.f:771-850: 4-point rule (order 4) of the tetrahedra;
+// returns (s2, s3, s4) as (xi, eta, zeta).
+bool quad6(int order, int gpn, double& xi, double& eta, double& zeta, double& w) {
+  if (order != 4 || gpn < 1 || gpn > 4) return false;
+  const double a = 0.58541020, b = 0.13819660;
+  w = 0.25;
+  xi = gpn == 2 ? a : b;
+  eta = gpn == 3 ? a : b;
+  zeta = gpn == 4 ? a : b;
+  return true;
+}
+
+// deriv6, src/derivs.f:606-662: 10-node tetrahedron
+void deriv6(double s2, double s3, double s4, double* qs2, double* qs3, double* qs4) {
+  const double zero = 0.0, one = 1.0, four = 4.0;
+  double s1 = one - s2 - s3 - s4;
+  qs2[0] = one - four * s1; qs2[1] = four * s2 - one; qs2[2] = zero; qs2[3] = zero;
+  qs2[4] = four * (s1 - s2); qs2[5] = four * s3; qs2[6] = -four * s3; qs2[7] = -four * s4;
+  qs2[8] = four * s4; qs2[9] = zero;
+  qs3[0] = one - four * s1; qs3[1] = zero; qs3[2] = four * s3 - one; qs3[3] = zero;
+  qs3[4] = -four * s2; qs3[5] = four * s2; qs3[6] = four * (s1 - s3); qs3[7] = -four * s4;
+  qs3[8] = zero; qs3[9] = four * s4;
+  qs4[0] = one - four * s1; qs4[1] = zero; qs4[2] = zero; qs4[3] = four * s4 - one;
+  qs4[4] = -four * s2; qs4[5] = zero; qs4[6] = -four * s3; qs4[7] = four * (s1 - s4);
+  qs4[8] = four * s2; qs4[9] = four * s3;
+}
+
 bool getgpts(int etype, int order, int gpn, double& xi, double& eta, double& zeta, double& w) {
   switch (etype) {
     case W3G_ETYPE_L3DISOP: return quad2(order, gpn, xi, eta, zeta, w);
+    case W3G_ETYPE_Q3DISOP: return quad1(order, gpn, xi, eta, zeta, w);
+    case W3G_ETYPE_TET10: return quad6(order, gpn, xi, eta, zeta, w);
     default: return false;
   }
 }
@@ -102,9 +216,15 @@ bool getgpts(int etype, int order, int gpn, double& xi, double& eta, double& zet
 bool derivs(int etype, double xi, double eta, double zeta, double* nxi, double* neta, double* nzeta) {
   switch (etype) {
     case W3G_ETYPE_L3DISOP: deriv2(xi, eta, zeta, nxi, neta, nzeta); return true;
+    case W3G_ETYPE_Q3DISOP: deriv1(xi, eta, zeta, nxi, neta, nzeta); return true;
+    case W3G_ETYPE_TET10: deriv6(xi, eta, zeta, nxi, neta, nzeta); return true;
     default: return false;
   }
 }
+
+// adjust_scalar_weights, src/initst.f:888-930: tetrahedra integrate with
+// weights summing to 1 over the unit parametric tet of volume 1/6
+double adjust_scalar(int etype) { return etype == W3G_ETYPE_TET10 ? 1.0 / 6.0 : 1.0; }
 
 // ---------------------------------------------------------------------
 // block description
@@ -126,7 +246,10 @@ bool block_info(const w3g_model_desc* m, int blk, Blk& b) {
   b.totdof = b.nnode * b.ndof;
   b.utsz = (b.totdof * b.totdof - b.totdof) / 2 + b.totdof;   // tanstf.f:185
   b.geonl = flog(lp[17]); b.bbar = flog(lp[18]);
-  return b.span >= 1 && b.span <= MXVL && b.etype == W3G_ETYPE_L3DISOP;
+  const bool known = (b.etype == W3G_ETYPE_L3DISOP && b.nnode == 8 && b.ngp == 8) ||
+                     (b.etype == W3G_ETYPE_Q3DISOP && b.nnode == 20 && b.ngp == 27) ||
+                     (b.etype == W3G_ETYPE_TET10 && b.nnode == 10 && b.ngp == 4);
+  return b.span >= 1 && b.span <= MXVL && known && b.ndof == 3;
 }
 
 // column-major helpers for (span, k) and (span, k, l) work arrays
@@ -882,7 +1005,7 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
   for (int g = 0; g < ngp; ++g)
     jacob1(span, nnode, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], cen1, det_j[g].data(), gama[g]);
   for (int g = 0; g < ngp; ++g) {
-    double w = weights[g];
+    double w = weights[g] * adjust_scalar(B.etype);   // gpifv1.f:43-47
     b.zero();
     blcmp1(span, b, totdof, gama[g], &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], nnode);
     const double* dj = det_j[g].data();
@@ -1051,6 +1174,14 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
         }
       }
 #undef Q
+    }
+    // adjust_cnst (src/gpmas1.f:399-430): tetrahedra scale [D] by 1/6
+    // after ctran1; the geometric stiffness below is not scaled
+    // (gptns1.f:222-225 then :278-288)
+    if (B.etype == W3G_ETYPE_TET10) {
+      const double scalar = adjust_scalar(B.etype);
+      for (int k = 0; k < 36; ++k)
+        for (int i = 0; i < span; ++i) cep(i, k) = scalar * cep(i, k);
     }
     // bdbtgen (src/gptns1.f:1628-1718)
 #define BB(i, j, k) b(i, (j) + totdof * (k))

@@ -15,8 +15,11 @@ of the reference arrays:
   einfvec (totdof, span)      == Fortran (span, totdof)
   edest   (span, totdof)      == Fortran (totdof, span)
 
-The synthetic meshes stand in for WARP3D input decks: structured cubes of
-8-node bricks (element type l3disop) with optional seeded nodal jitter.
+A model is a list of parts, each one element type (8-node brick
+``l3disop``, 20-node brick ``q3disop``, 10-node tetrahedron) cut into
+blocks of at most 128 elements, as WARP3D's blocking does. The synthetic
+meshes stand in for input decks: structured cubes with optional seeded
+nodal jitter.
 """
 from __future__ import annotations
 
@@ -31,12 +34,27 @@ HIST_MM01 = 11
 NSTR = 6
 NSTRS = 9
 
+# element type -> (nodes, Gauss points, integration order) as elprp1,
+# elprp2 and the tet10 routines set iprops(2), (6), (5)
+ELEMENT_TYPES = {
+    abi.ETYPE_L3DISOP: (8, 8, 1),
+    abi.ETYPE_Q3DISOP: (20, 27, 1),
+    abi.ETYPE_TET10: (10, 4, 4),
+}
+
 # WARP3D 8-node brick node order in parent coordinates (xi, eta, zeta),
-# src/derivs.f:302-325
+# src/derivs.f:302-325; the 20-node brick adds the mid-edge nodes 9-20 in
+# the order of deriv1 (src/derivs.f:182-281)
 HEX8_NODES = np.array(
     [[-1, -1, 1], [-1, -1, -1], [-1, 1, -1], [-1, 1, 1], [1, -1, 1], [1, -1, -1], [1, 1, -1], [1, 1, 1]],
     dtype=np.int64,
 )
+HEX20_NODES = np.concatenate([HEX8_NODES, np.array(
+    [[-1, -1, 0], [-1, 0, -1], [-1, 1, 0], [-1, 0, 1], [1, -1, 0], [1, 0, -1], [1, 1, 0], [1, 0, 1],
+     [0, -1, 1], [0, -1, -1], [0, 1, -1], [0, 1, 1]], dtype=np.int64)])
+# 10-node tetrahedron: corners 1-4 then mid-edge nodes of edges
+# (1,2) (2,3) (1,3) (1,4) (2,4) (3,4) (deriv6, src/derivs.f:606-662)
+TET10_EDGES = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
 
 
 @dataclass
@@ -65,109 +83,231 @@ class Bilinear:
         return {7: e, 8: np.float32(self.nu), 14: np.float32(self.beta), 15: h, 23: np.float32(self.yld)}
 
 
-def cube_mesh(n: int, h: float = 1.0, jitter: float = 0.0, seed: int = 12345, n_xyz=None):
-    """Structured brick mesh: nodes (i, j, k) at (i h, j h, k h); interior
-    nodes moved by U(-jitter, jitter)*h per coordinate (numpy PCG64(seed)).
-    Returns (coords[nnode,3], incid[noelem,8]) with 0-based node ids in
-    WARP3D's hex8 node order."""
-    nx, ny, nz = (n, n, n) if n_xyz is None else n_xyz
-    ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
-    # node id = i + (nx+1)*(j + (ny+1)*k)
-    coords = np.zeros(((nx + 1) * (ny + 1) * (nz + 1), 3))
-    nid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
-    ids = nid(ii, jj, kk).ravel()
-    coords[ids, 0] = ii.ravel() * h
-    coords[ids, 1] = jj.ravel() * h
-    coords[ids, 2] = kk.ravel() * h
+def _lattice(nx, ny, nz, h, jitter, seed, level=1):
+    """Nodes (i, j, k) of a lattice with `level` points per element edge
+    (1: corners, 2: corners + mid-edge); interior corner nodes moved by
+    U(-jitter, jitter)*h per coordinate, mid nodes placed at the centre of
+    their (jittered) corners. Returns (positions of every lattice point,
+    id function)."""
+    mx, my, mz = level * nx, level * ny, level * nz
+    ii, jj, kk = np.meshgrid(np.arange(mx + 1), np.arange(my + 1), np.arange(mz + 1), indexing="ij")
+    P = np.stack([ii, jj, kk], axis=-1).astype(np.float64) * (h / level)
     if jitter > 0.0:
         rng = np.random.Generator(np.random.PCG64(seed))
-        pert = rng.uniform(-jitter, jitter, size=coords.shape) * h
-        interior = (
-            (ii > 0) & (ii < nx) & (jj > 0) & (jj < ny) & (kk > 0) & (kk < nz)
-        ).ravel()
-        mask = np.zeros(len(coords), dtype=bool)
-        mask[ids[interior]] = True
-        coords[mask] += pert[mask]
-    ex, ey, ez = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
-    # element id = ex + nx*(ey + ny*ez)
-    order = np.argsort((ex + nx * (ey + ny * ez)).ravel())
-    ex, ey, ez = ex.ravel()[order], ey.ravel()[order], ez.ravel()[order]
+        pert = rng.uniform(-jitter, jitter, size=(nx + 1, ny + 1, nz + 1, 3)) * h
+        ci, cj, ck = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+        interior = (ci > 0) & (ci < nx) & (cj > 0) & (cj < ny) & (ck > 0) & (ck < nz)
+        pert[~interior] = 0.0
+        corner = P[::level, ::level, ::level] + pert
+        if level == 1:
+            P = corner
+        else:
+            # mid points: average of the lattice corners that bracket them
+            def lerp(arr, axis):
+                sl0 = [slice(None)] * 4
+                sl1 = [slice(None)] * 4
+                sl0[axis] = slice(0, -1)
+                sl1[axis] = slice(1, None)
+                mid = 0.5 * (arr[tuple(sl0)] + arr[tuple(sl1)])
+                shape = list(arr.shape)
+                shape[axis] = 2 * shape[axis] - 1
+                out = np.empty(shape)
+                so = [slice(None)] * 4
+                so[axis] = slice(0, None, 2)
+                out[tuple(so)] = arr
+                so[axis] = slice(1, None, 2)
+                out[tuple(so)] = mid
+                return out
+            P = lerp(lerp(lerp(corner, 0), 1), 2)
+    return P
+
+
+def cube_mesh(n: int, h: float = 1.0, jitter: float = 0.0, seed: int = 12345, n_xyz=None):
+    """Structured brick mesh of 8-node bricks: nodes (i, j, k) at
+    (i h, j h, k h); interior nodes moved by U(-jitter, jitter)*h per
+    coordinate (numpy PCG64(seed)). Returns (coords[nnode,3],
+    incid[noelem,8]) with 0-based node ids in WARP3D's hex8 node order."""
+    nx, ny, nz = (n, n, n) if n_xyz is None else n_xyz
+    P = _lattice(nx, ny, nz, h, jitter, seed, 1)
+    nid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
+    ii, jj, kk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    coords = np.zeros(((nx + 1) * (ny + 1) * (nz + 1), 3))
+    coords[nid(ii, jj, kk).ravel()] = P.reshape(-1, 3)
+    ex, ey, ez = _cells(nx, ny, nz)
     incid = np.empty((nx * ny * nz, 8), dtype=np.int64)
     for a, (sx, sy, sz) in enumerate(HEX8_NODES):
         incid[:, a] = nid(ex + (sx > 0), ey + (sy > 0), ez + (sz > 0))
     return coords, incid
 
 
+def _cells(nx, ny, nz):
+    ex, ey, ez = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    order = np.argsort((ex + nx * (ey + ny * ez)).ravel())
+    return ex.ravel()[order], ey.ravel()[order], ez.ravel()[order]
+
+
+def cube_mesh_hex20(n: int, h: float = 1.0, jitter: float = 0.0, seed: int = 12345, n_xyz=None):
+    """Structured mesh of 20-node bricks (q3disop): corner lattice as in
+    cube_mesh, mid-edge nodes at the centres of their corners. Node ids are
+    numbered over the half-step lattice points that are corners or edge
+    mid-points."""
+    nx, ny, nz = (n, n, n) if n_xyz is None else n_xyz
+    P = _lattice(nx, ny, nz, h, jitter, seed, 2)
+    ii, jj, kk = np.meshgrid(np.arange(2 * nx + 1), np.arange(2 * ny + 1), np.arange(2 * nz + 1), indexing="ij")
+    odd = (ii % 2) + (jj % 2) + (kk % 2)
+    keep = odd <= 1
+    ids = -np.ones(ii.shape, dtype=np.int64)
+    ids[keep] = np.arange(int(keep.sum()))
+    coords = P[keep]
+    ex, ey, ez = _cells(nx, ny, nz)
+    incid = np.empty((nx * ny * nz, 20), dtype=np.int64)
+    for a, (sx, sy, sz) in enumerate(HEX20_NODES):
+        incid[:, a] = ids[2 * ex + 1 + sx, 2 * ey + 1 + sy, 2 * ez + 1 + sz]
+    assert (incid >= 0).all()
+    return coords, incid
+
+
+def cube_mesh_tet10(n: int, h: float = 1.0, jitter: float = 0.0, seed: int = 12345, n_xyz=None):
+    """Structured mesh of 10-node tetrahedra: every cell of the corner
+    lattice split into 6 tetrahedra around its main diagonal, oriented so
+    that det[J] > 0, mid-edge nodes at the centres of their corners."""
+    nx, ny, nz = (n, n, n) if n_xyz is None else n_xyz
+    P = _lattice(nx, ny, nz, h, jitter, seed, 2)
+    ii, jj, kk = np.meshgrid(np.arange(2 * nx + 1), np.arange(2 * ny + 1), np.arange(2 * nz + 1), indexing="ij")
+    # corners and every point that is the centre of a lattice edge used by
+    # the tetrahedra (cell edges, face diagonals, the main diagonal)
+    ex, ey, ez = _cells(nx, ny, nz)
+    corners = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+    # Kuhn split around the diagonal 0-6
+    tets = [(0, 1, 2, 6), (0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 4, 5, 6), (0, 5, 1, 6)]
+    ne = nx * ny * nz * 6
+    half = np.zeros((ne, 10, 3), dtype=np.int64)   # half-step lattice index of each node
+    k = 0
+    for t in tets:
+        c = np.stack([2 * np.stack([ex, ey, ez], -1) + 2 * corners[v] for v in t], axis=1)   # (ncell, 4, 3)
+        sl = slice(k, ne, 6)
+        half[sl, :4] = c
+        for m, (a, b) in enumerate(TET10_EDGES):
+            half[sl, 4 + m] = (c[:, a] + c[:, b]) // 2
+        k += 1
+    used = np.unique(half.reshape(-1, 3), axis=0)
+    ids = -np.ones(ii.shape, dtype=np.int64)
+    ids[used[:, 0], used[:, 1], used[:, 2]] = np.arange(len(used))
+    coords = P[used[:, 0], used[:, 1], used[:, 2]]
+    incid = ids[half[..., 0], half[..., 1], half[..., 2]]
+    # straight edges: every mid node at the centre of its two corners (the
+    # Kuhn split uses the same face diagonals in neighbouring cells)
+    for m, (a, b) in enumerate(TET10_EDGES):
+        coords[incid[:, 4 + m]] = 0.5 * (coords[incid[:, a]] + coords[incid[:, b]])
+    # orientation: (x2-x1, x3-x1, x4-x1) right-handed, else swap corners 3,4
+    X = coords[incid[:, :4]]
+    vol = np.einsum("ij,ij->i", np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]), X[:, 3] - X[:, 0])
+    neg = vol < 0
+    if neg.any():
+        sw = incid[neg].copy()
+        # swap corners 3 and 4; edges (1,2)(2,3)(1,3)(1,4)(2,4)(3,4) then
+        # read (1,2)(2,4)(1,4)(1,3)(2,3)(4,3) of the old numbering
+        perm = [0, 1, 3, 2, 4, 8, 7, 6, 5, 9]
+        incid[neg] = sw[:, perm]
+    return coords, incid
+
+
 @dataclass
+class Part:
+    """One element type of a model: incidences and its blocking."""
+
+    etype: int
+    incid: np.ndarray                      # (n, nnode) 0-based node ids
+    spans: list | None = None              # block sizes (default: block_size chunks)
+    materials: list | None = None          # one Bilinear per block, or one for all
+
+
 class Model:
-    """A WARP3D model restricted to what the element-block path reads."""
+    """A WARP3D model restricted to what the element-block path reads.
 
-    coords: np.ndarray            # (nnode, 3)
-    incid: np.ndarray             # (noelem, nnode_per_elem), 0-based
-    block_size: int = 128
-    etype: int = abi.ETYPE_L3DISOP
-    geonl: bool = True
-    bbar: bool = False
-    qbar: bool = True
-    materials: list = field(default_factory=list)   # one Bilinear per block or one for all
-    block_spans: list | None = None
+    ``Model(coords, incid)`` is a single-part model of 8-node bricks;
+    ``Model(coords, parts=[Part(...), ...])`` mixes element types (blocks
+    never mix types, as in WARP3D)."""
 
-    def __post_init__(self):
-        self.nnode_el = self.incid.shape[1]
-        self.ngp = 8
-        self.totdof = 3 * self.nnode_el
-        self.utsz = self.totdof * (self.totdof + 1) // 2
-        self.noelem = self.incid.shape[0]
+    def __init__(self, coords, incid=None, *, parts=None, block_size=128, etype=abi.ETYPE_L3DISOP, geonl=True,
+                 bbar=False, qbar=True, materials=None, block_spans=None):
+        if parts is None:
+            parts = [Part(etype, np.asarray(incid), block_spans, materials)]
+        self.coords = np.asarray(coords, dtype=np.float64)
+        self.parts = parts
+        self.block_size = block_size
+        self.geonl, self.bbar, self.qbar = geonl, bbar, qbar
         self.nnode = self.coords.shape[0]
         self.nodof = 3 * self.nnode
         self.ncoord = 3 * self.nnode
         # crdmap/dstmap: node n -> 3n (0-based)
         self.c = np.ascontiguousarray(self.coords.reshape(-1))
-        spans = self.block_spans
-        if spans is None:
-            spans = [self.block_size] * (self.noelem // self.block_size)
-            if self.noelem % self.block_size:
-                spans.append(self.noelem % self.block_size)
-        assert sum(spans) == self.noelem and all(1 <= s <= abi.MXVL for s in spans)
-        self.spans = list(spans)
+        spans, btype, bmat, bincid = [], [], [], []
+        for p in parts:
+            ne = p.incid.shape[0]
+            sp = p.spans
+            if sp is None:
+                sp = [block_size] * (ne // block_size) + ([ne % block_size] if ne % block_size else [])
+            assert sum(sp) == ne and all(1 <= s <= abi.MXVL for s in sp)
+            mats = p.materials or [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)]
+            off = 0
+            for b, s in enumerate(sp):
+                spans.append(s)
+                btype.append(p.etype)
+                bmat.append(mats[b] if len(mats) == len(sp) else mats[0])
+                bincid.append(p.incid[off:off + s])
+                off += s
+        self.spans = spans
+        self.block_etype = btype
+        self.block_material = bmat
         self.nelblk = len(spans)
+        self.noelem = int(sum(spans))
         self.felem = np.concatenate([[0], np.cumsum(spans)[:-1]]).astype(np.int64)
         self.elblks = np.zeros((self.nelblk, 3), dtype=np.int32)
         self.elblks[:, 0] = spans
         self.elblks[:, 1] = self.felem + 1
+        self.block_nnode = [ELEMENT_TYPES[t][0] for t in btype]
+        self.block_ngp = [ELEMENT_TYPES[t][1] for t in btype]
+        self.block_totdof = [3 * n for n in self.block_nnode]
+        self.block_utsz = [d * (d + 1) // 2 for d in self.block_totdof]
+        self._block_incid = bincid
+        self.uniform = len(set(btype)) == 1
+        # single-type conveniences
+        t0 = btype[0]
+        self.etype = t0
+        self.nnode_el, self.ngp = ELEMENT_TYPES[t0][0], ELEMENT_TYPES[t0][1]
+        self.totdof = 3 * self.nnode_el
+        self.utsz = self.totdof * (self.totdof + 1) // 2
+        self.incid = np.concatenate(bincid) if self.uniform else None
         self._tables()
 
-    # -- property tables (src/elprp.f elprp2, src/mod_main.f:47-52) ----
+    # -- property tables (src/elprp.f elprp1/elprp2, src/mod_main.f:47-52) --
     def _tables(self):
         ne = self.noelem
         self.props = np.zeros((ne, abi.MXELPR), dtype=np.float32)
         self.iprops = np.zeros((ne, abi.MXELPR), dtype=np.int32)
         self.lprops = np.zeros((ne, abi.MXELPR), dtype=np.int32)
-        self.iprops[:, 0] = self.etype
-        self.iprops[:, 1] = self.nnode_el
-        self.iprops[:, 2] = 24 * 65536 + 6
-        self.iprops[:, 3] = 3
-        self.iprops[:, 4] = 1          # 2x2x2 for l3disop
-        self.iprops[:, 5] = self.ngp
-        self.iprops[:, 24] = abi.MAT_BILINEAR
-        self.iprops[:, 37] = 1
-        self.lprops[:, 17] = 1 if self.geonl else 0
-        self.lprops[:, 18] = 1 if self.bbar else 0
-        mats = self.materials or [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)]
-        for b in range(self.nelblk):
-            m = mats[b] if len(mats) == self.nelblk else mats[0]
-            f, s = self.felem[b], self.spans[b]
-            for k, v in m.props_values().items():
-                self.props[f:f + s, k - 1] = v
-        # edest/cdest per block: (span, totdof) with u1..un, v1..vn, w1..wn
-        nn = self.nnode_el
         self.edest = []
         for b in range(self.nelblk):
-            f, s = self.felem[b], self.spans[b]
-            nodes = self.incid[f:f + s]                       # (span, nn)
+            f, s, t = self.felem[b], self.spans[b], self.block_etype[b]
+            nn, ngp, order = ELEMENT_TYPES[t]
+            rows = slice(f, f + s)
+            self.iprops[rows, 0] = t
+            self.iprops[rows, 1] = nn
+            self.iprops[rows, 2] = 3 * nn * 65536 + 6
+            self.iprops[rows, 3] = 3
+            self.iprops[rows, 4] = order
+            self.iprops[rows, 5] = ngp
+            self.iprops[rows, 24] = abi.MAT_BILINEAR
+            self.iprops[rows, 37] = 1
+            self.lprops[rows, 17] = 1 if self.geonl else 0
+            self.lprops[rows, 18] = 1 if self.bbar else 0
+            for k, v in self.block_material[b].props_values().items():
+                self.props[rows, k - 1] = v
+            nodes = self._block_incid[b]                     # (span, nn)
             d = np.empty((s, 3 * nn), dtype=np.int32)
             for k in range(3):
-                d[:, k * nn:(k + 1) * nn] = 3 * nodes + k + 1   # 1-based
+                d[:, k * nn:(k + 1) * nn] = 3 * nodes + k + 1   # 1-based, u1..un, v1..vn, w1..wn
             self.edest.append(np.ascontiguousarray(d))
         self.cdest = [e.copy() for e in self.edest]
 
@@ -196,7 +336,7 @@ class Model:
         return HostState(self)
 
     def estiff_blocks(self):
-        return [np.zeros((s, self.utsz)) for s in self.spans]
+        return [np.zeros((s, u)) for s, u in zip(self.spans, self.block_utsz)]
 
 
 def _ptrs(arrs):
@@ -212,21 +352,20 @@ class HostState:
 
     def __init__(self, model: Model):
         self.model = model
-        ng = model.ngp
-        sp = model.spans
-        self.history = [np.zeros((s, ng, HIST_MM01)) for s in sp]
-        self.history1 = [np.zeros((s, ng, HIST_MM01)) for s in sp]
-        self.urcs_n = [np.zeros((s, ng, NSTRS)) for s in sp]
-        self.urcs_n1 = [np.zeros((s, ng, NSTRS)) for s in sp]
-        self.eps_n = [np.zeros((s, ng, NSTR)) for s in sp]
-        self.eps_n1 = [np.zeros((s, ng, NSTR)) for s in sp]
+        sp, ng, td = model.spans, model.block_ngp, model.block_totdof
+        self.history = [np.zeros((s, g, HIST_MM01)) for s, g in zip(sp, ng)]
+        self.history1 = [np.zeros((s, g, HIST_MM01)) for s, g in zip(sp, ng)]
+        self.urcs_n = [np.zeros((s, g, NSTRS)) for s, g in zip(sp, ng)]
+        self.urcs_n1 = [np.zeros((s, g, NSTRS)) for s, g in zip(sp, ng)]
+        self.eps_n = [np.zeros((s, g, NSTR)) for s, g in zip(sp, ng)]
+        self.eps_n1 = [np.zeros((s, g, NSTR)) for s, g in zip(sp, ng)]
         self.rot_n1 = []
-        for s in sp:
-            r = np.zeros((s, ng, 9))
+        for s, g in zip(sp, ng):
+            r = np.zeros((s, g, 9))
             r[:, :, 0] = r[:, :, 4] = r[:, :, 8] = 1.0
             self.rot_n1.append(r)
-        self.cep = [np.zeros((ng, s, 21)) for s in sp]
-        self.einfvec = [np.zeros((model.totdof, s)) for s in sp]
+        self.cep = [np.zeros((g, s, 21)) for s, g in zip(sp, ng)]
+        self.einfvec = [np.zeros((d, s)) for s, d in zip(sp, td)]
         self.element_vol = [np.zeros(s) for s in sp]
 
     def copy(self) -> "HostState":
@@ -248,13 +387,16 @@ class HostState:
         return s
 
     def concat(self, name: str) -> np.ndarray:
-        """All blocks of one array, element-major (cep/einfvec per element)."""
+        """All blocks of one array, element-major (cep/einfvec per element);
+        for mixed element types, the flattened per-element values."""
         arrs = getattr(self, name)
         if name == "cep":
-            return np.concatenate([a.transpose(1, 0, 2) for a in arrs])      # (noelem, ngp, 21)
-        if name == "einfvec":
-            return np.concatenate([a.T for a in arrs])                        # (noelem, totdof)
-        return np.concatenate(arrs)
+            arrs = [a.transpose(1, 0, 2) for a in arrs]                        # (span, ngp, 21)
+        elif name == "einfvec":
+            arrs = [a.T for a in arrs]                                          # (span, totdof)
+        if self.model.uniform:
+            return np.concatenate(arrs)
+        return np.concatenate([a.reshape(-1) for a in arrs])
 
 
 def dptr(a: np.ndarray):

@@ -37,24 +37,29 @@ class Assembler:
 
     def __init__(self, model):
         self.model = model
-        r, c = upper_pairs(model.totdof)
-        ed = np.concatenate(model.edest).astype(np.int64) - 1          # (noelem, totdof)
-        gi = ed[:, r]
-        gj = ed[:, c]
-        off = r != c
-        self.I = np.concatenate([gi.ravel(), gj[:, off].ravel()])
-        self.J = np.concatenate([gj.ravel(), gi[:, off].ravel()])
-        self.off = off
-        n = model.nodof
-        coo = sp.coo_matrix((np.ones(len(self.I)), (self.I, self.J)), shape=(n, n)).tocsr()
-        coo.sum_duplicates()
-        self.pattern = coo
+        I, J, self.off = [], [], []
+        pairs = {}
+        for b in range(model.nelblk):
+            td = model.block_totdof[b]
+            if td not in pairs:
+                pairs[td] = upper_pairs(td)
+            r, c = pairs[td]
+            ed = model.edest[b].astype(np.int64) - 1          # (span, totdof)
+            gi, gj = ed[:, r], ed[:, c]
+            off = r != c
+            I += [gi.ravel(), gj[:, off].ravel()]
+            J += [gj.ravel(), gi[:, off].ravel()]
+            self.off.append(off)
+        self.I = np.concatenate(I)
+        self.J = np.concatenate(J)
 
-    def assemble(self, estiff_elem: np.ndarray) -> sp.csr_matrix:
-        """estiff_elem: (noelem, utsz) element matrices."""
-        v = np.concatenate([estiff_elem.ravel(), estiff_elem[:, self.off].ravel()])
+    def assemble(self, estiff_blocks) -> sp.csr_matrix:
+        """estiff_blocks: per block (span, utsz) element matrices."""
+        v = []
+        for est, off in zip(estiff_blocks, self.off):
+            v += [est.ravel(), est[:, off].ravel()]
         n = self.model.nodof
-        K = sp.coo_matrix((v, (self.I, self.J)), shape=(n, n)).tocsr()
+        K = sp.coo_matrix((np.concatenate(v), (self.I, self.J)), shape=(n, n)).tocsr()
         K.sum_duplicates()
         return K
 
@@ -78,7 +83,7 @@ class NewtonDriver:
 
     def _tangent(self, step, it, du):
         self.engine.tanstf(step, it, self.model.c, self.u, du, self.estiff)
-        return self.asm.assemble(np.concatenate(self.estiff))
+        return self.asm.assemble(self.estiff)
 
     def step(self, step: int, imposed: np.ndarray):
         """imposed: full-length vector; its values on fixed dofs are the
@@ -117,15 +122,19 @@ class NewtonDriver:
 
 def uniaxial_bcs(model, n_xyz, h: float = 1.0):
     """Bottom face (z = 0) fixed in z, top face (z = nz h) loaded in z;
-    minimal in-plane supports: node (0,0,0) fixed in x and y, node
-    (nx,0,0) fixed in y. Returns (fixed dofs, top-face z dofs)."""
+    minimal in-plane supports: the node at (0,0,0) fixed in x and y, the
+    node at (nx h, 0, 0) fixed in y. Faces are found from the (unjittered)
+    boundary coordinates, so any element type works. Returns (fixed dofs,
+    top-face z dofs)."""
     nx, ny, nz = n_xyz
-    nid = lambda i, j, k: i + (nx + 1) * (j + (ny + 1) * k)
-    ii, jj = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), indexing="ij")
-    bottom = nid(ii, jj, 0).ravel()
-    top = nid(ii, jj, nz).ravel()
+    X = model.coords
+    tol = 1e-9 * h
+    bottom = np.nonzero(np.abs(X[:, 2]) < tol)[0]
+    top = np.nonzero(np.abs(X[:, 2] - nz * h) < tol)[0]
+    o = np.nonzero(np.linalg.norm(X - np.array([0.0, 0.0, 0.0]), axis=1) < tol)[0][0]
+    xe = np.nonzero(np.linalg.norm(X - np.array([nx * h, 0.0, 0.0]), axis=1) < tol)[0][0]
     fixed = set((3 * bottom + 2).tolist())
-    fixed.update([3 * nid(0, 0, 0), 3 * nid(0, 0, 0) + 1, 3 * nid(nx, 0, 0) + 1])
+    fixed.update([3 * o, 3 * o + 1, 3 * xe + 1])
     top_z = 3 * top + 2
     fixed.update(top_z.tolist())
     return np.array(sorted(fixed)), top_z
