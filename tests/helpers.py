@@ -8,25 +8,29 @@ from __future__ import annotations
 
 import numpy as np
 
-from warp3d_gb300.model import Bilinear, Model, cube_mesh
+from warp3d_gb300 import abi
+from warp3d_gb300.model import Bilinear, Model, cube_mesh, cube_mesh_hex20, cube_mesh_tet10
 from warp3d_gb300.newton import NewtonDriver, uniaxial_bcs
 
+MESHES = {abi.ETYPE_L3DISOP: cube_mesh, abi.ETYPE_Q3DISOP: cube_mesh_hex20, abi.ETYPE_TET10: cube_mesh_tet10}
 
-def make_model(n=6, jitter=0.1, seed=12345, block_size=128, spans=None, beta=1.0, n_xyz=None, materials=None):
+
+def make_model(n=6, jitter=0.1, seed=12345, block_size=128, spans=None, beta=1.0, n_xyz=None, materials=None,
+               etype=abi.ETYPE_L3DISOP):
     nxyz = (n, n, n) if n_xyz is None else n_xyz
-    coords, incid = cube_mesh(n, jitter=jitter, seed=seed, n_xyz=nxyz)
+    coords, incid = MESHES[etype](n, jitter=jitter, seed=seed, n_xyz=nxyz)
     mats = materials or [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0, beta=beta)]
-    return Model(coords, incid, block_size=block_size, block_spans=spans, materials=mats), nxyz
+    return Model(coords, incid, block_size=block_size, block_spans=spans, materials=mats, etype=etype), nxyz
 
 
 def loaded_state(model, nxyz, engine_cls, steps=3, strain_per_step=0.0015, shear_per_step=0.0,
-                 tol=1e-8, seed=7):
+                 tol=1e-8, seed=7, origins=None):
     """Runs `steps` converged load steps (uniaxial z plus optional x-shear
     of the top face) with an engine built by engine_cls(model), then
     returns (engine, driver, du_trial): du_trial is a perturbed increment
     for the next step, i.e. a mid-iteration state."""
     eng = engine_cls(model)
-    fixed, topz = uniaxial_bcs(model, nxyz)
+    fixed, topz = uniaxial_bcs(model, nxyz, origins=origins)
     top = (topz - 2) // 3
     fixed = np.union1d(fixed, 3 * top) if shear_per_step else fixed
     drv = NewtonDriver(model, eng, fixed, tol=tol)

@@ -51,7 +51,8 @@ cudaError_t dalloc(T** p, size_t n) {
 void free_all(w3g_context* c) {
   DeviceModel& m = c->m;
   DeviceState& s = c->s;
-  void* ptrs[] = {m.blocks, m.chunks, m.edest, m.cdest, m.mat, m.dn_hex8, m.ifv_rowptr, m.ifv_src,
+  void* ptrs[] = {m.blocks, m.chunks, m.edest, m.cdest, m.mat, m.dn_hex8, m.dn_hex20, m.dn_tet10,
+                  m.ifv_rowptr, m.ifv_src,
                   s.geo, s.c_geo, s.geo_dirty,
                   s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
                   s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
@@ -97,11 +98,19 @@ int blocks_d2h(w3g_context* c, const double* dev, double* const* host, int per, 
   return 0;
 }
 
+// one element kernel per element type present
+int type_launches(const DeviceModel& m) {
+  int n = 0;
+  for (int t = 0; t < kNumTypes; ++t) n += m.type_chunks[t] > 0 ? 1 : 0;
+  return n;
+}
+
 TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, const double* d_du) {
   TangentArgs a;
   a.dn = c->m.dn_hex8;
   a.blocks = c->m.blocks;
   a.chunks = c->m.chunks;
+  a.chunk0 = 0;
   a.edest = c->m.edest;
   a.cdest = c->m.cdest;
   a.c = d_c; a.u = d_u; a.du = d_du;
@@ -119,7 +128,7 @@ int run_tangent(w3g_context* c, const double* d_c, const double* d_u, const doub
   cudaError_t e = c->precision == W3G_TANGENT_FP32 ? launch_tangent_fp32(c->m, a, st)
                                                    : launch_tangent_fp64(c->m, a, st);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
-  c->last_launches = 1;
+  c->last_launches = type_launches(c->m);
   return 0;
 }
 
@@ -130,6 +139,7 @@ int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_
   a.dn = c->m.dn_hex8;
   a.blocks = c->m.blocks;
   a.chunks = c->m.chunks;
+  a.chunk0 = 0;
   a.edest = c->m.edest;
   a.cdest = c->m.cdest;
   a.mat = c->m.mat;
@@ -153,7 +163,8 @@ int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_
   if (e == cudaSuccess)
     e = launch_finalize(c->m, c->s.partials, c->s.ifv_partials, c->ifv_parts, c->s.status, c->s.d_info, st);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("recover launch: ") + cudaGetErrorString(e));
-  c->last_launches = 7;
+  // status reset, coordinate check/commit/clear, ifv assembly, finalize
+  c->last_launches = 6 + type_launches(c->m);
   return 0;
 }
 
@@ -186,9 +197,9 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   // ---- block table (elblks, iprops, lprops) ----
   std::vector<BlockDesc>& B = c->blocks;
   B.resize(md->nelblk);
-  long long gp = 0, cep = 0, est = 0, einf = 0;
+  long long gp = 0, cep = 0, est = 0, einf = 0, geo = 0;
   int expect_felem = 1;
-  std::vector<Chunk> chunks;
+  std::vector<Chunk> type_chunks[kNumTypes];
   for (int b = 0; b < md->nelblk; ++b) {
     BlockDesc& d = B[b];
     d.span = md->elblks[3 * b];
@@ -209,7 +220,12 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     d.totdof = d.nnode * ip[3];
     d.utsz = (d.totdof * d.totdof - d.totdof) / 2 + d.totdof;
     d.geonl = lp[17] != 0; d.bbar = lp[18] != 0;
-    if (d.etype != W3G_ETYPE_L3DISOP || d.nnode != 8 || d.ngp != 8 || ip[3] != 3 || ip[4] != 1) {
+    // (etype, nnode, ngp, integration order) with a GPU path
+    const bool ok_type = ip[3] == 3 &&
+                         ((d.etype == W3G_ETYPE_L3DISOP && d.nnode == 8 && d.ngp == 8 && ip[4] == 1) ||
+                          (d.etype == W3G_ETYPE_Q3DISOP && d.nnode == 20 && d.ngp == 27 && ip[4] == 1) ||
+                          (d.etype == W3G_ETYPE_TET10 && d.nnode == 10 && d.ngp == 4 && ip[4] == 4));
+    if (!ok_type) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": element type not supported");
     }
@@ -221,18 +237,27 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": small-strain or b-bar not supported");
     }
-    d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf;
+    d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf; d.geo_off = geo;
     gp += (long long)d.span * d.ngp;
     cep += 21LL * d.span * d.ngp;
     est += (long long)d.utsz * d.span;
     einf += (long long)d.totdof * d.span;
-    for (int i0 = 0; i0 < d.span; i0 += kChunk) chunks.push_back(Chunk{b, i0, std::min(kChunk, d.span - i0)});
+    geo += (long long)(3 * d.nnode + 1) * d.span * d.ngp;
+    const int ts = type_slot(d.etype);
+    const int per = kTypeChunk[ts];
+    for (int i0 = 0; i0 < d.span; i0 += per) type_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0)});
+  }
+  std::vector<Chunk> chunks;
+  for (int t = 0; t < kNumTypes; ++t) {
+    m.type_chunk0[t] = (int)chunks.size();
+    m.type_chunks[t] = (int)type_chunks[t].size();
+    chunks.insert(chunks.end(), type_chunks[t].begin(), type_chunks[t].end());
   }
   if (expect_felem != md->noelem + 1) {
     delete c;
     return fail(W3G_EARG, "blocks do not cover all elements");
   }
-  m.ngp_total = gp; m.cep_total = cep; m.estiff_total = est; m.einf_total = einf;
+  m.ngp_total = gp; m.cep_total = cep; m.estiff_total = est; m.einf_total = einf; m.geo_total = geo;
   m.nchunks = (int)chunks.size();
 
   // ---- edest / cdest, ifv CSR ----
@@ -279,8 +304,10 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     mat[e].lnelas = lp[16] ? 1.0 : 0.0;
     fill_mat_constants(mat[e]);
   }
-  double dn[dn_table_size<Hex8>()];
-  fill_dn_table<Hex8>(dn);
+  std::vector<double> dn8(dn_table_size<Hex8>()), dn20(dn_table_size<Hex20>()), dn10(dn_table_size<Tet10>());
+  fill_dn_table<Hex8>(dn8.data());
+  fill_dn_table<Hex20>(dn20.data());
+  fill_dn_table<Tet10>(dn10.data());
 
   DeviceState& s = c->s;
   cudaError_t e = cudaSuccess;
@@ -290,7 +317,9 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(m.edest, einf);
   AL(m.cdest, einf);
   AL(m.mat, md->noelem);
-  AL(m.dn_hex8, dn_table_size<Hex8>());
+  AL(m.dn_hex8, dn8.size());
+  AL(m.dn_hex20, dn20.size());
+  AL(m.dn_tet10, dn10.size());
   AL(m.ifv_rowptr, md->nodof + 1);
   AL(m.ifv_src, einf);
   AL(s.hist, kHistMM01 * gp);
@@ -304,7 +333,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(s.estiff, est);
   AL(s.einf, einf);
   AL(s.evol, md->noelem);
-  AL(s.geo, (long long)geo_values_per_gp() * gp);
+  AL(s.geo, geo);
   AL(s.c_geo, md->ncoord);
   AL(s.geo_dirty, 1);
   AL(s.partials, 2 * m.nchunks);
@@ -330,7 +359,9 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   UP(m.edest, ed.data(), einf);
   UP(m.cdest, cd.data(), einf);
   UP(m.mat, mat.data(), md->noelem);
-  UP(m.dn_hex8, dn, dn_table_size<Hex8>());
+  UP(m.dn_hex8, dn8.data(), dn8.size());
+  UP(m.dn_hex20, dn20.data(), dn20.size());
+  UP(m.dn_tet10, dn10.data(), dn10.size());
   UP(m.ifv_rowptr, rowptr.data(), md->nodof + 1);
   UP(m.ifv_src, src.data(), einf);
 #undef UP

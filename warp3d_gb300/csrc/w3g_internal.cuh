@@ -21,7 +21,15 @@ namespace w3g {
 
 constexpr int kMxvl = W3G_MXVL;
 constexpr int kHistMM01 = 11;      // mm01_set_sizes, src/mm01.f:976-979
-constexpr int kChunk = 8;          // elements per warp-sized work item
+constexpr int kChunk = 8;          // elements per work item (largest of the types)
+// element types with a GPU path; work items are grouped by type in this
+// order: 0 = 8-node brick (l3disop), 1 = 20-node brick (q3disop),
+// 2 = 10-node tetrahedron (tet10)
+constexpr int kNumTypes = 3;
+__host__ __device__ constexpr int type_slot(int etype) {
+  return etype == W3G_ETYPE_L3DISOP ? 0 : etype == W3G_ETYPE_Q3DISOP ? 1 : etype == W3G_ETYPE_TET10 ? 2 : -1;
+}
+constexpr int kTypeChunk[kNumTypes] = {8, 2, 8};   // elements per work item
 
 struct BlockDesc {
   int span;
@@ -32,9 +40,10 @@ struct BlockDesc {
   long long cep_off;    // sum of 21*span*ngp
   long long estiff_off; // sum of utsz*span
   long long einf_off;   // sum of totdof*span (also edest/cdest offset)
+  long long geo_off;    // sum of (3*nnode+1)*span*ngp (undeformed-geometry cache)
 };
 
-// one work item = up to kChunk consecutive elements of one block
+// one work item = up to kTypeChunk[type] consecutive elements of one block
 struct Chunk {
   int blk;
   int i0;     // first relative element
@@ -83,13 +92,17 @@ struct DeviceModel {
   int qbar = 1;
   double beta_fact = 1.0;
   int nchunks = 0;
-  long long ngp_total = 0, cep_total = 0, estiff_total = 0, einf_total = 0;
+  int type_chunk0[kNumTypes] = {0, 0, 0};   // first work item of each type
+  int type_chunks[kNumTypes] = {0, 0, 0};   // work items of each type
+  long long ngp_total = 0, cep_total = 0, estiff_total = 0, einf_total = 0, geo_total = 0;
   BlockDesc* blocks = nullptr;     // device
   Chunk* chunks = nullptr;         // device
   int* edest = nullptr;            // device, concatenated (totdof, span)
   int* cdest = nullptr;
   MatProps* mat = nullptr;         // device, noelem
   double* dn_hex8 = nullptr;       // device, fill_dn_table<Hex8>
+  double* dn_hex20 = nullptr;      // device, fill_dn_table<Hex20>
+  double* dn_tet10 = nullptr;      // device, fill_dn_table<Tet10>
   // deterministic ifv assembly: CSR over global dofs of einfvec indices
   int* ifv_rowptr = nullptr;       // nodof+1
   long long* ifv_src = nullptr;    // einf_total
@@ -110,7 +123,7 @@ struct DeviceState {
   double* evol = nullptr;    // noelem
   // undeformed geometry per GP (dN/dX, det[J0]) and the coordinates it
   // was built from; geo_dirty = 1 until built
-  double* geo = nullptr;     // geo_values_per_gp() * ngp_total
+  double* geo = nullptr;     // geo_total: (3*nnode+1) per GP, block b at geo_off
   double* c_geo = nullptr;   // ncoord
   int* geo_dirty = nullptr;
   // per-launch scratch
@@ -130,6 +143,7 @@ struct TangentArgs {
   const double* dn;      // element table, fill_dn_table layout
   const BlockDesc* blocks;
   const Chunk* chunks;
+  int chunk0;            // work item of blockIdx.x == 0
   const int* edest;
   const int* cdest;
   const double* c;
@@ -147,6 +161,7 @@ struct RecoverArgs {
   const double* dn;
   const BlockDesc* blocks;
   const Chunk* chunks;
+  int chunk0;
   const int* edest;
   const int* cdest;
   const MatProps* mat;
@@ -175,7 +190,9 @@ struct RecoverArgs {
 cudaError_t launch_tangent_fp64(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
 cudaError_t launch_tangent_fp32(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, cudaStream_t s);
-int geo_values_per_gp();
+// the 20-node brick and 10-node tetrahedron work items (w3g_generic.cu)
+cudaError_t launch_tangent_other(const DeviceModel& m, TangentArgs a, bool fp32, cudaStream_t s);
+cudaError_t launch_recover_other(const DeviceModel& m, RecoverArgs a, cudaStream_t s);
 cudaError_t launch_assemble_ifv(const DeviceModel& m, const double* einf, double* ifv, double* ifv_partials,
                                 int nparts, cudaStream_t s);
 cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const double* ifv_partials,

@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(kThreads) k_recover_hex8(RecoverArgs a) {
   const int tid = threadIdx.x;
   const int ge = tid >> 3;
   const int g = tid & 7;
-  const Chunk ch = a.chunks[blockIdx.x];
+  const int cidx = a.chunk0 + blockIdx.x;
+  const Chunk ch = a.chunks[cidx];
   const BlockDesc bd = a.blocks[ch.blk];
   const bool active = ge < ch.n;
   const int i = ch.i0 + ge;
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(kThreads) k_recover_hex8(RecoverArgs a) {
     // the analysis: computed in reference order on the first call after
     // the coordinates change, then read back.
     double tg0[3 * NN], dj0;
-    double* geo = a.geo + gpi * kGeo;
+    double* geo = a.geo + bd.geo_off + ((long long)i * NG + g) * kGeo;
     if (dirty) {
       const double* dnx = sdn + (g * 3 + 0) * NN;
       const double* dne = sdn + (g * 3 + 1) * NN;
@@ -290,8 +291,8 @@ __global__ void __launch_bounds__(kThreads) k_recover_hex8(RecoverArgs a) {
   if ((tid & 31) == 0) { sred[tid >> 5][0] = en; sred[tid >> 5][1] = pw; }
   __syncthreads();
   if (tid == 0) {
-    a.partials[2 * blockIdx.x + 0] = sred[0][0] + sred[1][0];
-    a.partials[2 * blockIdx.x + 1] = sred[0][1] + sred[1][1];
+    a.partials[2 * cidx + 0] = sred[0][0] + sred[1][0];
+    a.partials[2 * cidx + 1] = sred[0][1] + sred[1][1];
   }
 }
 
@@ -372,13 +373,18 @@ __global__ void __launch_bounds__(256) k_finalize(int nchunks, const double* par
 
 int assemble_ifv_parts(int nodof) { return (nodof + kAsmThreads - 1) / kAsmThreads; }
 
-int geo_values_per_gp() { return kGeo; }
-
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, cudaStream_t s) {
   if (m.nchunks == 0) return cudaSuccess;
   const int nb = (m.ncoord + 255) / 256;
   k_check_coords<<<nb, 256, 0, s>>>(a.c, c_geo, m.ncoord, a.geo_dirty);
-  k_recover_hex8<<<m.nchunks, kThreads, 0, s>>>(a);
+  if (m.type_chunks[0] > 0) {
+    RecoverArgs h = a;
+    h.dn = m.dn_hex8;
+    h.chunk0 = m.type_chunk0[0];
+    k_recover_hex8<<<m.type_chunks[0], kThreads, 0, s>>>(h);
+  }
+  cudaError_t e = launch_recover_other(m, a, s);
+  if (e != cudaSuccess) return e;
   k_commit_coords<<<nb, 256, 0, s>>>(a.c, c_geo, m.ncoord, a.geo_dirty);
   k_clear_dirty<<<1, 1, 0, s>>>(a.geo_dirty);
   return cudaGetLastError();

@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(32) k_tangent_hex8(TangentArgs a) {
   const int lane = threadIdx.x;
   const int ge = lane >> 2;      // element within chunk
   const int t = lane & 3;
-  const Chunk ch = a.chunks[blockIdx.x];
+  const Chunk ch = a.chunks[a.chunk0 + blockIdx.x];
   const BlockDesc bd = a.blocks[ch.blk];
   const bool active = ge < ch.n;
   const int i = ch.i0 + ge;      // relative element in block
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(32, 12) k_tangent32_hex8(TangentArgs a) {
   const int lane = threadIdx.x;
   const int ge = lane >> 2;
   const int t = lane & 3;
-  const Chunk ch = a.chunks[blockIdx.x];
+  const Chunk ch = a.chunks[a.chunk0 + blockIdx.x];
   const BlockDesc bd = a.blocks[ch.blk];
   const bool active = ge < ch.n;
   const int i = ch.i0 + ge;
@@ -533,27 +533,38 @@ __global__ void __launch_bounds__(32, 12) k_tangent32_hex8(TangentArgs a) {
 
 template <class T, class KOut, bool kRel>
 cudaError_t launch_hex8(const DeviceModel& m, const TangentArgs& a, cudaStream_t s) {
-  if (m.nchunks == 0) return cudaSuccess;
+  if (m.type_chunks[0] == 0) return cudaSuccess;
   size_t smem = sizeof(T) * (size_t)(kDnSize + kChunk * kPerElem);
   auto kern = k_tangent_hex8<T, KOut, kRel>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  kern<<<m.nchunks, 32, smem, s>>>(a);
+  kern<<<m.type_chunks[0], 32, smem, s>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_tangent_fp64(const DeviceModel& m, const TangentArgs& a, cudaStream_t s) {
-  return launch_hex8<double, double, false>(m, a, s);
+  TangentArgs h = a;
+  h.dn = m.dn_hex8;
+  h.chunk0 = m.type_chunk0[0];
+  cudaError_t e = launch_hex8<double, double, false>(m, h, s);
+  if (e != cudaSuccess) return e;
+  return launch_tangent_other(m, a, false, s);
 }
 
 cudaError_t launch_tangent_fp32(const DeviceModel& m, const TangentArgs& a, cudaStream_t s) {
-  if (m.nchunks == 0) return cudaSuccess;
-  k_tangent32_hex8<<<m.nchunks, 32, 0, s>>>(a);
-  return cudaGetLastError();
+  if (m.type_chunks[0] > 0) {
+    TangentArgs h = a;
+    h.dn = m.dn_hex8;
+    h.chunk0 = m.type_chunk0[0];
+    k_tangent32_hex8<<<m.type_chunks[0], 32, 0, s>>>(h);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return launch_tangent_other(m, a, true, s);
 }
 
 }  // namespace w3g

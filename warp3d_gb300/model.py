@@ -212,6 +212,42 @@ def cube_mesh_tet10(n: int, h: float = 1.0, jitter: float = 0.0, seed: int = 123
     return coords, incid
 
 
+MESHES = {abi.ETYPE_L3DISOP: cube_mesh, abi.ETYPE_Q3DISOP: cube_mesh_hex20, abi.ETYPE_TET10: cube_mesh_tet10}
+
+
+def mixed_mesh(parts_nx, ny: int, nz: int, h: float = 1.0, jitter: float = 0.0, seed: int = 12345,
+               gap: int = 1):
+    """Several structured bars side by side along x, one per element type:
+    ``parts_nx`` is a list of (etype, nx); bar k is an nx x ny x nz cube
+    mesh of that type (jittered with seed + k) shifted in x past the
+    previous bars plus ``gap`` element lengths. The bars share no nodes.
+    Returns (coords, [(etype, incid), ...], [(x0, nx), ...])."""
+    coords, parts, origins = [], [], []
+    x0, node0 = 0.0, 0
+    for k, (etype, nx) in enumerate(parts_nx):
+        c, inc = MESHES[etype](nx, h=h, jitter=jitter, seed=seed + k, n_xyz=(nx, ny, nz))
+        c = c.copy()
+        c[:, 0] += x0
+        coords.append(c)
+        parts.append((etype, inc + node0))
+        origins.append((x0, nx))
+        node0 += c.shape[0]
+        x0 += (nx + gap) * h
+    return np.concatenate(coords), parts, origins
+
+
+def random_spans(ne: int, rng: np.random.Generator, lo: int = 16, hi: int = 128):
+    """Block sizes uniform in [lo, hi] covering ne elements (the last block
+    takes the remainder)."""
+    spans, left = [], ne
+    while left > 0:
+        s = int(rng.integers(lo, hi + 1))
+        s = min(s, left)
+        spans.append(s)
+        left -= s
+    return spans
+
+
 @dataclass
 class Part:
     """One element type of a model: incidences and its blocking."""

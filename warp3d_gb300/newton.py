@@ -120,21 +120,23 @@ class NewtonDriver:
         return res_hist
 
 
-def uniaxial_bcs(model, n_xyz, h: float = 1.0):
+def uniaxial_bcs(model, n_xyz, h: float = 1.0, origins=None):
     """Bottom face (z = 0) fixed in z, top face (z = nz h) loaded in z;
     minimal in-plane supports: the node at (0,0,0) fixed in x and y, the
     node at (nx h, 0, 0) fixed in y. Faces are found from the (unjittered)
-    boundary coordinates, so any element type works. Returns (fixed dofs,
-    top-face z dofs)."""
+    boundary coordinates, so any element type works. ``origins`` lists
+    (x0, nx) per bar of a several-bar model (mixed_mesh), each bar getting
+    its own in-plane supports. Returns (fixed dofs, top-face z dofs)."""
     nx, ny, nz = n_xyz
     X = model.coords
     tol = 1e-9 * h
     bottom = np.nonzero(np.abs(X[:, 2]) < tol)[0]
     top = np.nonzero(np.abs(X[:, 2] - nz * h) < tol)[0]
-    o = np.nonzero(np.linalg.norm(X - np.array([0.0, 0.0, 0.0]), axis=1) < tol)[0][0]
-    xe = np.nonzero(np.linalg.norm(X - np.array([nx * h, 0.0, 0.0]), axis=1) < tol)[0][0]
     fixed = set((3 * bottom + 2).tolist())
-    fixed.update([3 * o, 3 * o + 1, 3 * xe + 1])
+    for x0, bnx in (origins or [(0.0, nx)]):
+        o = np.nonzero(np.linalg.norm(X - np.array([x0, 0.0, 0.0]), axis=1) < tol)[0][0]
+        xe = np.nonzero(np.linalg.norm(X - np.array([x0 + bnx * h, 0.0, 0.0]), axis=1) < tol)[0][0]
+        fixed.update([3 * o, 3 * o + 1, 3 * xe + 1])
     top_z = 3 * top + 2
     fixed.update(top_z.tolist())
     return np.array(sorted(fixed)), top_z
