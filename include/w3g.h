@@ -188,8 +188,60 @@ int w3g_recover_info_get(w3g_context* ctx, w3g_recover_info* info);
    *count receives the number of values. */
 int w3g_estiff_device(w3g_context* ctx, void** d_estiff, long long* count);
 
-/* Number of kernels the last w3g_tanstf/w3g_recover(_dev) call launched. */
+/* Number of kernels the last w3g_tanstf/w3g_recover(_dev)/w3g_iteration_dev
+   call launched (kernels inside a replayed graph included). */
 int w3g_last_launch_count(w3g_context* ctx);
+
+/* ---- batching form (no single WARP3D counterpart) ------------------
+   WARP3D runs one element block per OpenMP thread (tanstf.f:80-88,
+   drive_eps_sig_internal_forces.f:160-180). Here the work items of all
+   blocks, of every element type and size, are either launched per element
+   type (W3G_SCHED_PER_TYPE) or taken from a device work queue by one
+   persistent launch per phase (W3G_SCHED_PERSISTENT): CTAs resident on
+   every SM pull the next items with an atomic counter, heaviest element
+   type first (W3G_ORDER_HEAVY_FIRST) or in block order. The schedule
+   changes only the order in which element results are produced, never
+   their values. */
+#define W3G_SCHED_PER_TYPE 0
+#define W3G_SCHED_PERSISTENT 1
+#define W3G_ORDER_BLOCKS 0
+#define W3G_ORDER_HEAVY_FIRST 1
+
+typedef struct w3g_schedule {
+  int mode;                  /* W3G_SCHED_*                                */
+  int recover_ctas_per_sm;   /* persistent recovery CTAs per SM, 0 = max  */
+  int tangent_ctas_per_sm;   /* persistent tangent CTAs per SM, 0 = max   */
+  int recover_grain;         /* queue entries taken per fetch (>= 1)       */
+  int tangent_grain;
+  int order;                 /* W3G_ORDER_*                                */
+} w3g_schedule;
+
+int w3g_set_schedule(w3g_context* ctx, const w3g_schedule* sched);
+int w3g_get_schedule(w3g_context* ctx, w3g_schedule* sched);
+
+/* One Newton iteration's element work on device pointers: recovery
+   (what & W3G_ITER_RECOVER, as w3g_recover_dev) then the tangent
+   (what & W3G_ITER_TANGENT, as w3g_tanstf_dev), replayed as one CUDA
+   graph. The graph is captured on the first call and again whenever the
+   pointers, `what`, the precision or the schedule change; afterwards a
+   call costs one small launch (the step/iteration scalars) plus one
+   graph launch. */
+#define W3G_ITER_RECOVER 1
+#define W3G_ITER_TANGENT 2
+int w3g_iteration_dev(w3g_context* ctx, int step, int iter, int extrapolated_du, int what,
+                      const void* d_c, const void* d_u, const void* d_du, void* d_ifv,
+                      void* stream);
+
+/* Autotuner: times candidate schedules (launch mode, persistent CTAs per
+   SM, queue grain, item order) on this model with the given inputs,
+   recovery and tangent separately, `reps` timed runs each, and keeps the
+   fastest. Runs the iteration's element work several times; afterwards
+   the element state is that of one w3g_iteration_dev call with these
+   arguments. *best (may be NULL) receives the chosen schedule,
+   *best_ms (may be NULL) its recovery + tangent time. */
+int w3g_autotune(w3g_context* ctx, int step, int iter, int extrapolated_du,
+                 const void* d_c, const void* d_u, const void* d_du, void* d_ifv,
+                 void* stream, int reps, w3g_schedule* best, double* best_ms);
 
 /* ---- internal-force assembly without device allocation --------------
    No counterpart in the reference. For callers that cannot allocate

@@ -31,6 +31,13 @@ ENOMEM = -4
 TANGENT_FP64 = 0
 TANGENT_FP32 = 1
 
+SCHED_PER_TYPE = 0
+SCHED_PERSISTENT = 1
+ORDER_BLOCKS = 0
+ORDER_HEAVY_FIRST = 1
+ITER_RECOVER = 1
+ITER_TANGENT = 2
+
 _dpp = C.POINTER(C.POINTER(C.c_double))
 _ipp = C.POINTER(C.POINTER(C.c_int))
 
@@ -78,6 +85,20 @@ class RecoverInfo(C.Structure):
     ]
 
 
+class Schedule(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int),
+        ("recover_ctas_per_sm", C.c_int),
+        ("tangent_ctas_per_sm", C.c_int),
+        ("recover_grain", C.c_int),
+        ("tangent_grain", C.c_int),
+        ("order", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # exported symbols and their prototypes: (name, restype, argtypes)
 _vp = C.c_void_p
 _d = C.POINTER(C.c_double)
@@ -99,6 +120,11 @@ PROTOTYPES = [
     ("w3g_measure_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     ("w3g_assemble_ifv_noalloc", C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, _vp, _vp,
                                            _vp, _vp, _vp]),
+    ("w3g_set_schedule", C.c_int, [_vp, C.POINTER(Schedule)]),
+    ("w3g_get_schedule", C.c_int, [_vp, C.POINTER(Schedule)]),
+    ("w3g_iteration_dev", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    ("w3g_autotune", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int,
+                               C.POINTER(Schedule), C.POINTER(C.c_double)]),
 ]
 
 _lib = None

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libw3g.so")
-SOURCES = ["w3g_api.cu", "w3g_tangent.cu", "w3g_recover.cu", "w3g_generic.cu", "w3g_peak.cu", "w3g_noalloc.cu"]
+SOURCES = ["w3g_api.cu", "w3g_tangent.cu", "w3g_recover.cu", "w3g_peak.cu", "w3g_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

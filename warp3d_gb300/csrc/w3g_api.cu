@@ -12,12 +12,23 @@
 
 using namespace w3g;
 
+// one captured iteration (w3g_iteration_dev) and what it was captured for
+struct IterationGraph {
+  cudaGraphExec_t exec = nullptr;
+  int what = 0, precision = -1;
+  const void *c = nullptr, *u = nullptr, *du = nullptr, *ifv = nullptr;
+  Schedule sched{};
+  int launches = 0;
+};
+
 struct w3g_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   DeviceModel m;
   DeviceState s;
   int precision = W3G_TANGENT_FP64;
+  Schedule sched{W3G_SCHED_PER_TYPE, 0, 0, 1, 1, W3G_ORDER_HEAVY_FIRST};
+  IterationGraph graph;
   int ifv_parts = 0;
   int last_launches = 0;
   // host copies needed for state transfer
@@ -51,8 +62,10 @@ cudaError_t dalloc(T** p, size_t n) {
 void free_all(w3g_context* c) {
   DeviceModel& m = c->m;
   DeviceState& s = c->s;
-  void* ptrs[] = {m.blocks, m.chunks, m.edest, m.cdest, m.mat, m.dn_hex8, m.dn_hex20, m.dn_tet10,
-                  m.ifv_rowptr, m.ifv_src,
+  if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
+  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
+                  m.cdest, m.mat, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
+                  m.ifv_rowptr, m.ifv_src, s.params, s.counters,
                   s.geo, s.c_geo, s.geo_dirty,
                   s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
                   s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
@@ -70,8 +83,6 @@ __global__ void k_init_rot(double* rot, long long ngp_total) {
     r[0] = 1.0; r[1] = 0.0; r[2] = 0.0; r[3] = 0.0; r[4] = 1.0; r[5] = 0.0; r[6] = 0.0; r[7] = 0.0; r[8] = 1.0;
   }
 }
-
-__global__ void k_reset_status(unsigned long long* status) { status[0] = ~0ull; }
 
 // copy n values between per-block host pointers and one device array
 int blocks_h2d(w3g_context* c, double* dev, double* const* host, int per_elem_or_gp, bool per_gp) {
@@ -98,18 +109,11 @@ int blocks_d2h(w3g_context* c, const double* dev, double* const* host, int per, 
   return 0;
 }
 
-// one element kernel per element type present
-int type_launches(const DeviceModel& m) {
-  int n = 0;
-  for (int t = 0; t < kNumTypes; ++t) n += m.type_chunks[t] > 0 ? 1 : 0;
-  return n;
-}
-
 TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, const double* d_du) {
   TangentArgs a;
-  a.dn = c->m.dn_hex8;
+  for (int t = 0; t < kNumTypes; ++t) { a.dn[t] = c->m.dn[t]; a.dn32[t] = c->m.dn32[t]; }
   a.blocks = c->m.blocks;
-  a.chunks = c->m.chunks;
+  a.chunks = c->m.tchunks;
   a.chunk0 = 0;
   a.edest = c->m.edest;
   a.cdest = c->m.cdest;
@@ -123,20 +127,29 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
   return a;
 }
 
-int run_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
+// enqueues the tangent kernels; returns the number of kernel launches or
+// a negative status
+int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
   TangentArgs a = tangent_args(c, d_c, d_u, d_du);
-  cudaError_t e = c->precision == W3G_TANGENT_FP32 ? launch_tangent_fp32(c->m, a, st)
-                                                   : launch_tangent_fp64(c->m, a, st);
+  cudaError_t e = launch_tangent(c->m, a, c->precision == W3G_TANGENT_FP32, c->sched, c->s.counters + 1, st);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
-  c->last_launches = type_launches(c->m);
+  return tangent_kernel_launches(c->m, c->sched);
+}
+
+int run_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
+  const int n = enqueue_tangent(c, d_c, d_u, d_du, st);
+  if (n < 0) return n;
+  c->last_launches = n;
   return 0;
 }
 
-int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_c, const double* d_u,
-                const double* d_du, double* d_ifv, cudaStream_t st) {
-  k_reset_status<<<1, 1, 0, st>>>(c->s.status);
+// enqueues recovery after the iteration scalars are in place (everything
+// but k_begin_recover, so that it can be captured); returns the number of
+// kernel launches or a negative status
+int enqueue_recover(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, double* d_ifv,
+                    cudaStream_t st) {
   RecoverArgs a;
-  a.dn = c->m.dn_hex8;
+  for (int t = 0; t < kNumTypes; ++t) a.dn[t] = c->m.dn[t];
   a.blocks = c->m.blocks;
   a.chunks = c->m.chunks;
   a.chunk0 = 0;
@@ -155,16 +168,30 @@ int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_
   a.status = c->s.status;
   a.geo = c->s.geo;
   a.geo_dirty = c->s.geo_dirty;
-  a.step = step; a.iter = iter;
-  a.nonlinear = (iter >= 1 || extrap) ? 1 : 0;
+  a.params = c->s.params;
   a.beta_fact = c->m.beta_fact;
-  cudaError_t e = launch_recover(c->m, a, c->s.c_geo, st);
+  cudaError_t e = launch_recover(c->m, a, c->s.c_geo, c->sched, c->s.counters, st);
   if (e == cudaSuccess) e = launch_assemble_ifv(c->m, c->s.einf, d_ifv, c->s.ifv_partials, c->ifv_parts, st);
   if (e == cudaSuccess)
     e = launch_finalize(c->m, c->s.partials, c->s.ifv_partials, c->ifv_parts, c->s.status, c->s.d_info, st);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("recover launch: ") + cudaGetErrorString(e));
-  // status reset, coordinate check/commit/clear, ifv assembly, finalize
-  c->last_launches = 6 + type_launches(c->m);
+  // coordinate check/commit/clear, element kernels, ifv assembly, finalize
+  return 5 + recover_kernel_launches(c->m, c->sched);
+}
+
+int begin_recover(w3g_context* c, int step, int iter, int extrap, cudaStream_t st) {
+  cudaError_t e = launch_begin_recover(c->s.params, c->s.status, step, iter, (iter >= 1 || extrap) ? 1 : 0, st);
+  if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("recover launch: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_c, const double* d_u,
+                const double* d_du, double* d_ifv, cudaStream_t st) {
+  int r = begin_recover(c, step, iter, extrap, st);
+  if (r) return r;
+  const int n = enqueue_recover(c, d_c, d_u, d_du, d_ifv, st);
+  if (n < 0) return n;
+  c->last_launches = 1 + n;
   return 0;
 }
 
@@ -199,7 +226,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   B.resize(md->nelblk);
   long long gp = 0, cep = 0, est = 0, einf = 0, geo = 0;
   int expect_felem = 1;
-  std::vector<Chunk> type_chunks[kNumTypes];
+  std::vector<Chunk> type_chunks[kNumTypes], ttype_chunks[kNumTypes];
   for (int b = 0; b < md->nelblk; ++b) {
     BlockDesc& d = B[b];
     d.span = md->elblks[3 * b];
@@ -244,15 +271,37 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     einf += (long long)d.totdof * d.span;
     geo += (long long)(3 * d.nnode + 1) * d.span * d.ngp;
     const int ts = type_slot(d.etype);
-    const int per = kTypeChunk[ts];
-    for (int i0 = 0; i0 < d.span; i0 += per) type_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0)});
+    for (int i0 = 0, per = kRecoverChunk[ts]; i0 < d.span; i0 += per)
+      type_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0), ts});
+    for (int i0 = 0, per = kTangentChunk[ts]; i0 < d.span; i0 += per)
+      ttype_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0), ts});
   }
-  std::vector<Chunk> chunks;
+  std::vector<Chunk> chunks, tchunks;
   for (int t = 0; t < kNumTypes; ++t) {
     m.type_chunk0[t] = (int)chunks.size();
     m.type_chunks[t] = (int)type_chunks[t].size();
     chunks.insert(chunks.end(), type_chunks[t].begin(), type_chunks[t].end());
+    m.ttype_chunk0[t] = (int)tchunks.size();
+    m.ttype_chunks[t] = (int)ttype_chunks[t].size();
+    tchunks.insert(tchunks.end(), ttype_chunks[t].begin(), ttype_chunks[t].end());
   }
+  m.ntchunks = (int)tchunks.size();
+  // schedule orders: block order, and heaviest item type first (estimated
+  // work per item: recovery ~ elements x Gauss points x (30 + nodes),
+  // tangent ~ elements x Gauss points x node pairs)
+  auto orders = [&](const std::vector<Chunk>& ch, const int* per, bool tangent, std::vector<int>* out) {
+    out[0].resize(ch.size());
+    for (size_t k = 0; k < ch.size(); ++k) out[0][k] = (int)k;
+    const int nn[kNumTypes] = {8, 20, 10}, ng[kNumTypes] = {8, 27, 4};
+    double cost[kNumTypes];
+    for (int t = 0; t < kNumTypes; ++t)
+      cost[t] = (double)per[t] * ng[t] * (tangent ? nn[t] * (nn[t] + 1) / 2 : 30 + nn[t]);
+    out[1] = out[0];
+    std::stable_sort(out[1].begin(), out[1].end(), [&](int x, int y) { return cost[ch[x].type] > cost[ch[y].type]; });
+  };
+  std::vector<int> rord[2], tord[2];
+  orders(chunks, kRecoverChunk, false, rord);
+  orders(tchunks, kTangentChunk, true, tord);
   if (expect_felem != md->noelem + 1) {
     delete c;
     return fail(W3G_EARG, "blocks do not cover all elements");
@@ -304,22 +353,39 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     mat[e].lnelas = lp[16] ? 1.0 : 0.0;
     fill_mat_constants(mat[e]);
   }
-  std::vector<double> dn8(dn_table_size<Hex8>()), dn20(dn_table_size<Hex20>()), dn10(dn_table_size<Tet10>());
-  fill_dn_table<Hex8>(dn8.data());
-  fill_dn_table<Hex20>(dn20.data());
-  fill_dn_table<Tet10>(dn10.data());
+  std::vector<double> dnt[kNumTypes] = {std::vector<double>(dn_table_size<Hex8>()),
+                                        std::vector<double>(dn_table_size<Hex20>()),
+                                        std::vector<double>(dn_table_size<Tet10>())};
+  fill_dn_table<Hex8>(dnt[0].data());
+  fill_dn_table<Hex20>(dnt[1].data());
+  fill_dn_table<Tet10>(dnt[2].data());
+  std::vector<float> dnt32[kNumTypes];
+  for (int t = 0; t < kNumTypes; ++t) dnt32[t].assign(dnt[t].begin(), dnt[t].end());
+  {
+    int dev_sms = 0;
+    CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device));
+    m.nsm = dev_sms;
+  }
 
   DeviceState& s = c->s;
   cudaError_t e = cudaSuccess;
 #define AL(p, n) if (e == cudaSuccess) e = dalloc(&(p), (size_t)(n))
   AL(m.blocks, md->nelblk);
   AL(m.chunks, m.nchunks);
+  AL(m.tchunks, m.ntchunks);
+  for (int k = 0; k < 2; ++k) {
+    AL(m.rorder[k], m.nchunks);
+    AL(m.torder[k], m.ntchunks);
+  }
+  AL(s.params, 1);
+  AL(s.counters, 2);
   AL(m.edest, einf);
   AL(m.cdest, einf);
   AL(m.mat, md->noelem);
-  AL(m.dn_hex8, dn8.size());
-  AL(m.dn_hex20, dn20.size());
-  AL(m.dn_tet10, dn10.size());
+  for (int t = 0; t < kNumTypes; ++t) {
+    AL(m.dn[t], dnt[t].size());
+    AL(m.dn32[t], dnt32[t].size());
+  }
   AL(m.ifv_rowptr, md->nodof + 1);
   AL(m.ifv_src, einf);
   AL(s.hist, kHistMM01 * gp);
@@ -356,12 +422,18 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
 #define UP(d, h, n) if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, (size_t)(n) * sizeof(*(h)), cudaMemcpyHostToDevice, st)
   UP(m.blocks, B.data(), md->nelblk);
   UP(m.chunks, chunks.data(), m.nchunks);
+  UP(m.tchunks, tchunks.data(), m.ntchunks);
+  for (int k = 0; k < 2; ++k) {
+    UP(m.rorder[k], rord[k].data(), m.nchunks);
+    UP(m.torder[k], tord[k].data(), m.ntchunks);
+  }
   UP(m.edest, ed.data(), einf);
   UP(m.cdest, cd.data(), einf);
   UP(m.mat, mat.data(), md->noelem);
-  UP(m.dn_hex8, dn8.data(), dn8.size());
-  UP(m.dn_hex20, dn20.data(), dn20.size());
-  UP(m.dn_tet10, dn10.data(), dn10.size());
+  for (int t = 0; t < kNumTypes; ++t) {
+    UP(m.dn[t], dnt[t].data(), dnt[t].size());
+    UP(m.dn32[t], dnt32[t].data(), dnt32[t].size());
+  }
   UP(m.ifv_rowptr, rowptr.data(), md->nodof + 1);
   UP(m.ifv_src, src.data(), einf);
 #undef UP
@@ -370,6 +442,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   long long zn[] = {kHistMM01 * gp, kHistMM01 * gp, 9 * gp, 9 * gp, 6 * gp, 6 * gp, cep, est, einf, md->noelem};
   for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = cudaMemsetAsync(zs[k], 0, (size_t)zn[k] * sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.geo_dirty, 0xff, sizeof(int), st);   // nonzero: not built
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.counters, 0, 2 * sizeof(int), st);
+  if (e == cudaSuccess) e = init_kernels();
   if (e == cudaSuccess) {
     k_init_rot<<<(unsigned)((gp + 255) / 256), 256, 0, st>>>(s.rot_n1, gp);
     e = cudaGetLastError();
@@ -550,6 +624,227 @@ int w3g_recover_dev(w3g_context* c, int step, int iter, int extrapolated_du, con
   CK(cudaSetDevice(c->device));
   return run_recover(c, step, iter, extrapolated_du, (const double*)d_c, (const double*)d_u, (const double*)d_du,
                      (double*)d_ifv, (cudaStream_t)stream);
+}
+
+namespace {
+
+bool valid_schedule(const Schedule& sc) {
+  return (sc.mode == W3G_SCHED_PER_TYPE || sc.mode == W3G_SCHED_PERSISTENT) && sc.recover_ctas_per_sm >= 0 &&
+         sc.tangent_ctas_per_sm >= 0 && sc.recover_grain >= 1 && sc.tangent_grain >= 1 &&
+         (sc.order == W3G_ORDER_BLOCKS || sc.order == W3G_ORDER_HEAVY_FIRST);
+}
+
+bool same_schedule(const Schedule& x, const Schedule& y) {
+  return x.mode == y.mode && x.recover_ctas_per_sm == y.recover_ctas_per_sm &&
+         x.tangent_ctas_per_sm == y.tangent_ctas_per_sm && x.recover_grain == y.recover_grain &&
+         x.tangent_grain == y.tangent_grain && x.order == y.order;
+}
+
+Schedule from_abi(const w3g_schedule& s) {
+  return Schedule{s.mode, s.recover_ctas_per_sm, s.tangent_ctas_per_sm, s.recover_grain, s.tangent_grain, s.order};
+}
+
+w3g_schedule to_abi(const Schedule& s) {
+  return w3g_schedule{s.mode, s.recover_ctas_per_sm, s.tangent_ctas_per_sm, s.recover_grain, s.tangent_grain, s.order};
+}
+
+// enqueues the capturable part of one iteration (after k_begin_recover);
+// returns the number of kernel launches or a negative status
+int enqueue_iteration(w3g_context* c, int what, const double* d_c, const double* d_u, const double* d_du,
+                      double* d_ifv, cudaStream_t st) {
+  int n = 0;
+  if (what & W3G_ITER_RECOVER) {
+    const int r = enqueue_recover(c, d_c, d_u, d_du, d_ifv, st);
+    if (r < 0) return r;
+    n += r;
+  }
+  if (what & W3G_ITER_TANGENT) {
+    const int r = enqueue_tangent(c, d_c, d_u, d_du, st);
+    if (r < 0) return r;
+    n += r;
+  }
+  return n;
+}
+
+// (re)captures the iteration graph when what, pointers, precision or the
+// schedule differ from the cached one
+int ensure_graph(w3g_context* c, int what, const void* d_c, const void* d_u, const void* d_du, void* d_ifv) {
+  IterationGraph& g = c->graph;
+  if (g.exec && g.what == what && g.precision == c->precision && g.c == d_c && g.u == d_u && g.du == d_du &&
+      g.ifv == d_ifv && same_schedule(g.sched, c->sched))
+    return 0;
+  if (g.exec) {
+    CK(cudaGraphExecDestroy(g.exec));
+    g.exec = nullptr;
+  }
+  cudaStream_t cs = c->stream;
+  CK(cudaStreamSynchronize(cs));
+  CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  const int n = enqueue_iteration(c, what, (const double*)d_c, (const double*)d_u, (const double*)d_du,
+                                  (double*)d_ifv, cs);
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(cs, &graph);
+  if (n < 0) {
+    if (graph) cudaGraphDestroy(graph);
+    return n;
+  }
+  if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("iteration capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    g.exec = nullptr;
+    return fail(W3G_ECUDA, std::string("iteration graph: ") + cudaGetErrorString(e));
+  }
+  g.what = what;
+  g.precision = c->precision;
+  g.c = d_c; g.u = d_u; g.du = d_du; g.ifv = d_ifv;
+  g.sched = c->sched;
+  g.launches = n;
+  return 0;
+}
+
+// runs `what` once under schedule sc (directly, not as a graph) and
+// returns its device time in ms, or a negative value on error
+double time_once(w3g_context* c, const Schedule& sc, int what, int step, int iter, int extrap, const double* d_c,
+                 const double* d_u, const double* d_du, double* d_ifv, cudaStream_t st, cudaEvent_t e0,
+                 cudaEvent_t e1) {
+  const Schedule keep = c->sched;
+  c->sched = sc;
+  float ms = -1.f;
+  int r = 0;
+  if (what & W3G_ITER_RECOVER) r = begin_recover(c, step, iter, extrap, st);
+  if (!r && cudaEventRecord(e0, st) == cudaSuccess) {
+    const int n = enqueue_iteration(c, what, d_c, d_u, d_du, d_ifv, st);
+    if (n >= 0 && cudaEventRecord(e1, st) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess)
+      cudaEventElapsedTime(&ms, e0, e1);
+  }
+  c->sched = keep;
+  return ms;
+}
+
+}  // namespace
+
+int w3g_set_schedule(w3g_context* c, const w3g_schedule* sched) {
+  if (!c || !sched) return fail(W3G_EARG, "null argument");
+  const Schedule sc = from_abi(*sched);
+  if (!valid_schedule(sc)) return fail(W3G_EARG, "bad schedule");
+  c->sched = sc;
+  return 0;
+}
+
+int w3g_get_schedule(w3g_context* c, w3g_schedule* sched) {
+  if (!c || !sched) return fail(W3G_EARG, "null argument");
+  *sched = to_abi(c->sched);
+  return 0;
+}
+
+int w3g_iteration_dev(w3g_context* c, int step, int iter, int extrapolated_du, int what, const void* d_c,
+                      const void* d_u, const void* d_du, void* d_ifv, void* stream) {
+  if (!c || !d_c || !d_u || !d_du) return fail(W3G_EARG, "null argument");
+  if (what <= 0 || what > (W3G_ITER_RECOVER | W3G_ITER_TANGENT)) return fail(W3G_EARG, "bad what");
+  if ((what & W3G_ITER_RECOVER) && !d_ifv) return fail(W3G_EARG, "null ifv");
+  CK(cudaSetDevice(c->device));
+  int r = ensure_graph(c, what, d_c, d_u, d_du, d_ifv);
+  if (r) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  int n = 0;
+  if (what & W3G_ITER_RECOVER) {
+    if ((r = begin_recover(c, step, iter, extrapolated_du, st))) return r;
+    n = 1;
+  }
+  CK(cudaGraphLaunch(c->graph.exec, st));
+  c->last_launches = n + c->graph.launches;
+  return 0;
+}
+
+int w3g_autotune(w3g_context* c, int step, int iter, int extrapolated_du, const void* d_c, const void* d_u,
+                 const void* d_du, void* d_ifv, void* stream, int reps, w3g_schedule* best, double* best_ms) {
+  if (!c || !d_c || !d_u || !d_du || !d_ifv) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  reps = std::max(1, reps);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const double* pc = (const double*)d_c;
+  const double* pu = (const double*)d_u;
+  const double* pdu = (const double*)d_du;
+  double* pifv = (double*)d_ifv;
+  auto measure = [&](const Schedule& sc, int what) {
+    double t = time_once(c, sc, what, step, iter, extrapolated_du, pc, pu, pdu, pifv, st, e0, e1);   // warm-up
+    if (t < 0) return -1.0;
+    double best_t = 1e300;
+    for (int k = 0; k < reps; ++k) {
+      t = time_once(c, sc, what, step, iter, extrapolated_du, pc, pu, pdu, pifv, st, e0, e1);
+      if (t < 0) return -1.0;
+      best_t = std::min(best_t, t);
+    }
+    return best_t;
+  };
+  // candidates: per-type launches, or the persistent kernels with each
+  // CTAs-per-SM count up to occupancy, queue grain 1 or 4, either order
+  const int occ_r = persistent_recover_occupancy();
+  const int occ_t = persistent_tangent_occupancy(c->precision == W3G_TANGENT_FP32);
+  double total_best = 1e300;
+  Schedule chosen = c->sched;
+  int status = 0;
+  for (int order = 0; order < 2 && !status; ++order) {
+    for (int mode = 0; mode < 2 && !status; ++mode) {
+      if (mode == W3G_SCHED_PER_TYPE && order == W3G_ORDER_BLOCKS) continue;   // order unused per type
+      Schedule base{mode, 0, 0, 1, 1, order};
+      double tr = 1e300, tt = 1e300;
+      Schedule br = base, bt = base;
+      std::vector<int> rc = {0}, tc = {0}, grains = {1};
+      if (mode == W3G_SCHED_PERSISTENT) {
+        rc.clear(); tc.clear();
+        for (int k = 1; k <= occ_r; ++k) rc.push_back(k);
+        for (int k = std::max(1, occ_t / 4); k <= occ_t; k += std::max(1, occ_t / 4)) tc.push_back(k);
+        grains = {1, 4};
+      }
+      for (int g : grains)
+        for (int k : rc) {
+          Schedule sc = base;
+          sc.recover_ctas_per_sm = k;
+          sc.recover_grain = g;
+          const double t = measure(sc, W3G_ITER_RECOVER);
+          if (t < 0) { status = fail(W3G_ECUDA, "autotune: recovery run failed"); break; }
+          if (t < tr) { tr = t; br = sc; }
+        }
+      for (int g : grains)
+        for (int k : tc) {
+          if (status) break;
+          Schedule sc = base;
+          sc.tangent_ctas_per_sm = k;
+          sc.tangent_grain = g;
+          const double t = measure(sc, W3G_ITER_TANGENT);
+          if (t < 0) { status = fail(W3G_ECUDA, "autotune: tangent run failed"); break; }
+          if (t < tt) { tt = t; bt = sc; }
+        }
+      if (!status && tr + tt < total_best) {
+        total_best = tr + tt;
+        chosen = base;
+        chosen.recover_ctas_per_sm = br.recover_ctas_per_sm;
+        chosen.recover_grain = br.recover_grain;
+        chosen.tangent_ctas_per_sm = bt.tangent_ctas_per_sm;
+        chosen.tangent_grain = bt.tangent_grain;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status) return status;
+  c->sched = chosen;
+  // leave the state of one iteration with these arguments
+  int r = begin_recover(c, step, iter, extrapolated_du, st);
+  if (!r) {
+    const int n = enqueue_iteration(c, W3G_ITER_RECOVER | W3G_ITER_TANGENT, pc, pu, pdu, pifv, st);
+    if (n < 0) r = n;
+  }
+  if (r) return r;
+  CK(cudaStreamSynchronize(st));
+  if (best) *best = to_abi(chosen);
+  if (best_ms) *best_ms = total_best;
+  return 0;
 }
 
 int w3g_recover_info_get(w3g_context* c, w3g_recover_info* info) {

@@ -12,6 +12,7 @@ namespace w3g {
 // 1(-,-,+) 2(-,-,-) 3(-,+,-) 4(-,+,+) 5(+,-,+) 6(+,-,-) 7(+,+,-) 8(+,+,+);
 // GP order: eta fastest, then xi, then zeta.
 struct Hex8 {
+  static constexpr int SLOT = 0;   // type_slot
   static constexpr int NN = 8;
   static constexpr int NG = 8;
   static constexpr int TOTDOF = 24;
@@ -44,6 +45,7 @@ struct Hex8 {
 // (src/getgpts.f:177-420) and deriv1 (src/derivs.f:182-281). Corner nodes
 // as the 8-node brick; mid-edge nodes 9-20.
 struct Hex20 {
+  static constexpr int SLOT = 1;   // type_slot
   static constexpr int NN = 20;
   static constexpr int NG = 27;
   static constexpr int TOTDOF = 60;
@@ -100,6 +102,7 @@ struct Hex20 {
 // internal-force weights carry 1/6 (adjust_scalar_weights,
 // src/initst.f:888-930).
 struct Tet10 {
+  static constexpr int SLOT = 2;   // type_slot
   static constexpr int NN = 10;
   static constexpr int NG = 4;
   static constexpr int TOTDOF = 30;

@@ -29,7 +29,14 @@ constexpr int kNumTypes = 3;
 __host__ __device__ constexpr int type_slot(int etype) {
   return etype == W3G_ETYPE_L3DISOP ? 0 : etype == W3G_ETYPE_Q3DISOP ? 1 : etype == W3G_ETYPE_TET10 ? 2 : -1;
 }
-constexpr int kTypeChunk[kNumTypes] = {8, 2, 8};   // elements per work item
+// elements per work item: recovery items run on 64 threads (one per
+// Gauss point, 32 lanes for the 27-point brick, 4 per tetrahedron),
+// tangent items on one warp (4 lanes per 8-node brick, 32 per 20-node
+// brick, 8 per tetrahedron)
+constexpr int kRecoverChunk[kNumTypes] = {8, 2, 16};
+constexpr int kTangentChunk[kNumTypes] = {8, 1, 4};
+constexpr int kRecoverThreads = 64;
+constexpr int kTangentThreads = 32;
 
 struct BlockDesc {
   int span;
@@ -43,11 +50,39 @@ struct BlockDesc {
   long long geo_off;    // sum of (3*nnode+1)*span*ngp (undeformed-geometry cache)
 };
 
-// one work item = up to kTypeChunk[type] consecutive elements of one block
+// one work item = up to kRecoverChunk / kTangentChunk [type] consecutive
+// elements of one block
 struct Chunk {
   int blk;
   int i0;     // first relative element
-  int n;      // number of elements (<= kChunk)
+  int n;      // number of elements
+  int type;   // type_slot of the block's element type
+};
+
+// per-call scalars of recovery, read by the kernels from device memory so
+// that a captured launch sequence can be replayed with new values
+struct IterParams {
+  int step, iter, nonlinear, pad;
+};
+
+// device work queue of a persistent launch: CTAs take `grain` consecutive
+// entries of `items` (work-item indices, in schedule order) at a time
+// from `counter`, which is zero when the launch starts
+struct WorkQueue {
+  const int* items;
+  int nitems;
+  int grain;
+  int* counter;
+};
+
+// how the element work of a call is launched
+struct Schedule {
+  int mode;                 // W3G_SCHED_PER_TYPE or W3G_SCHED_PERSISTENT
+  int recover_ctas_per_sm;  // persistent grid = SMs x this (0: occupancy limit)
+  int tangent_ctas_per_sm;
+  int recover_grain;
+  int tangent_grain;
+  int order;                // W3G_ORDER_BLOCKS or W3G_ORDER_HEAVY_FIRST
 };
 
 // per-element mm01 properties as doubles (promoted from the float32
@@ -91,18 +126,25 @@ struct DeviceModel {
   int nelblk = 0, noelem = 0, nodof = 0, ncoord = 0;
   int qbar = 1;
   double beta_fact = 1.0;
-  int nchunks = 0;
-  int type_chunk0[kNumTypes] = {0, 0, 0};   // first work item of each type
-  int type_chunks[kNumTypes] = {0, 0, 0};   // work items of each type
+  int nsm = 0;
+  int nchunks = 0;                          // recovery work items
+  int type_chunk0[kNumTypes] = {0, 0, 0};   // first recovery item of each type
+  int type_chunks[kNumTypes] = {0, 0, 0};   // recovery items of each type
+  int ntchunks = 0;                         // tangent work items
+  int ttype_chunk0[kNumTypes] = {0, 0, 0};
+  int ttype_chunks[kNumTypes] = {0, 0, 0};
   long long ngp_total = 0, cep_total = 0, estiff_total = 0, einf_total = 0, geo_total = 0;
   BlockDesc* blocks = nullptr;     // device
-  Chunk* chunks = nullptr;         // device
+  Chunk* chunks = nullptr;         // device, recovery items grouped by type
+  Chunk* tchunks = nullptr;        // device, tangent items grouped by type
+  // schedule orders of the work items (W3G_ORDER_BLOCKS, _HEAVY_FIRST)
+  int* rorder[2] = {nullptr, nullptr};
+  int* torder[2] = {nullptr, nullptr};
   int* edest = nullptr;            // device, concatenated (totdof, span)
   int* cdest = nullptr;
   MatProps* mat = nullptr;         // device, noelem
-  double* dn_hex8 = nullptr;       // device, fill_dn_table<Hex8>
-  double* dn_hex20 = nullptr;      // device, fill_dn_table<Hex20>
-  double* dn_tet10 = nullptr;      // device, fill_dn_table<Tet10>
+  double* dn[kNumTypes] = {nullptr, nullptr, nullptr};   // device, fill_dn_table per type
+  float* dn32[kNumTypes] = {nullptr, nullptr, nullptr};  // device, the same in float
   // deterministic ifv assembly: CSR over global dofs of einfvec indices
   int* ifv_rowptr = nullptr;       // nodof+1
   long long* ifv_src = nullptr;    // einf_total
@@ -130,6 +172,8 @@ struct DeviceState {
   double* partials = nullptr;      // 2 * nchunks: energy, plastic work
   double* ifv_partials = nullptr;  // per CTA of the ifv assembly
   unsigned long long* status = nullptr;  // first det[F] <= 0 point, w3g::bad_point_key order
+  IterParams* params = nullptr;
+  int* counters = nullptr;         // work-queue heads: recovery, tangent
   w3g_recover_info* d_info = nullptr;
   // host-call staging
   double* d_c = nullptr;
@@ -140,7 +184,8 @@ struct DeviceState {
 
 // ---- launch arguments --------------------------------------------------
 struct TangentArgs {
-  const double* dn;      // element table, fill_dn_table layout
+  const double* dn[kNumTypes];   // fill_dn_table per element type
+  const float* dn32[kNumTypes];  // the same tables rounded to float
   const BlockDesc* blocks;
   const Chunk* chunks;
   int chunk0;            // work item of blockIdx.x == 0
@@ -158,7 +203,7 @@ struct TangentArgs {
 };
 
 struct RecoverArgs {
-  const double* dn;
+  const double* dn[kNumTypes];
   const BlockDesc* blocks;
   const Chunk* chunks;
   int chunk0;
@@ -182,17 +227,34 @@ struct RecoverArgs {
   unsigned long long* status;
   double* geo;
   int* geo_dirty;
-  int step, iter, nonlinear;
+  const IterParams* params;
   double beta_fact;
 };
 
 // ---- kernel launchers (defined in the .cu files) -----------------------
-cudaError_t launch_tangent_fp64(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
-cudaError_t launch_tangent_fp32(const DeviceModel& m, const TangentArgs& a, cudaStream_t s);
-cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, cudaStream_t s);
-// the 20-node brick and 10-node tetrahedron work items (w3g_generic.cu)
-cudaError_t launch_tangent_other(const DeviceModel& m, TangentArgs a, bool fp32, cudaStream_t s);
-cudaError_t launch_recover_other(const DeviceModel& m, RecoverArgs a, cudaStream_t s);
+// element kernels of one call: per-type launches or one persistent launch
+// (queue counters are reset inside)
+cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc,
+                           int* counter, cudaStream_t s);
+cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, const Schedule& sc,
+                           int* counter, cudaStream_t s);
+// launches of the element kernels under a schedule
+int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc);
+int recover_kernel_launches(const DeviceModel& m, const Schedule& sc);
+// one-time kernel attributes (shared-memory opt-in) and occupancies;
+// called at context creation, before any capture
+cudaError_t init_tangent_kernels();
+cudaError_t init_recover_kernels();
+inline cudaError_t init_kernels() {
+  cudaError_t e = init_tangent_kernels();
+  return e == cudaSuccess ? init_recover_kernels() : e;
+}
+// resident CTAs per SM of the persistent kernels
+int persistent_tangent_occupancy(bool fp32);
+int persistent_recover_occupancy();
+// writes the iteration scalars and resets the step-cut status
+cudaError_t launch_begin_recover(IterParams* params, unsigned long long* status, int step, int iter, int nonlinear,
+                                 cudaStream_t s);
 cudaError_t launch_assemble_ifv(const DeviceModel& m, const double* einf, double* ifv, double* ifv_partials,
                                 int nparts, cudaStream_t s);
 cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const double* ifv_partials,

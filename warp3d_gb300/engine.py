@@ -75,6 +75,32 @@ class Engine:
     def update(self):
         return abi.check(self.lib, self.lib.w3g_update(self.ctx))
 
+    # ---- batching form ------------------------------------------------------
+    def set_schedule(self, mode=abi.SCHED_PERSISTENT, recover_ctas_per_sm=0, tangent_ctas_per_sm=0,
+                     recover_grain=1, tangent_grain=1, order=abi.ORDER_HEAVY_FIRST):
+        sc = abi.Schedule(mode, recover_ctas_per_sm, tangent_ctas_per_sm, recover_grain, tangent_grain, order)
+        abi.check(self.lib, self.lib.w3g_set_schedule(self.ctx, C.byref(sc)))
+
+    def schedule(self) -> dict:
+        sc = abi.Schedule()
+        abi.check(self.lib, self.lib.w3g_get_schedule(self.ctx, C.byref(sc)))
+        return sc.as_dict()
+
+    def iteration_dev(self, step, it, extrapolated, what, d_c: int, d_u: int, d_du: int, d_ifv: int,
+                      stream: int = 0):
+        """One Newton iteration's element work (recovery and/or tangent),
+        replayed as a CUDA graph."""
+        return abi.check(self.lib, self.lib.w3g_iteration_dev(self.ctx, step, it, 1 if extrapolated else 0, what,
+                                                              d_c, d_u, d_du, d_ifv or None, stream or None))
+
+    def autotune(self, step, it, extrapolated, d_c: int, d_u: int, d_du: int, d_ifv: int, stream: int = 0,
+                 reps: int = 3):
+        sc = abi.Schedule()
+        ms = C.c_double()
+        abi.check(self.lib, self.lib.w3g_autotune(self.ctx, step, it, 1 if extrapolated else 0, d_c, d_u, d_du,
+                                                  d_ifv, stream or None, reps, C.byref(sc), C.byref(ms)))
+        return sc.as_dict(), ms.value
+
     # ---- hot path, device pointers (ints) ----------------------------------
     def tanstf_dev(self, step, it, d_c: int, d_u: int, d_du: int, stream: int = 0):
         return abi.check(self.lib, self.lib.w3g_tanstf_dev(self.ctx, step, it, d_c, d_u, d_du, stream or None))
