@@ -19,6 +19,14 @@ mixed:  the same iteration with the FP32 tangent (recovery stays FP64).
 e2e:    the host-array C-ABI calls a Fortran caller makes (w3g_tanstf
         with host estiff blocks + w3g_recover with host ifv), all
         host<->device copies inside the timed region.
+batched: the batching-form workload -- about 1M elements in blocks of
+        random size uniform in [16, 128] (PCG64), 60% 8-node bricks, 25%
+        20-node bricks, 15% 10-node tetrahedra (three bars of one type
+        each, 64 x 64 cells in cross-section, jitter U(-0.05, 0.05) h),
+        mm01 with yield per block U(250, 550) MPa; one Newton iteration
+        per step through w3g_iteration_dev (graph replay), FP64 and with
+        the FP32 tangent, each under the schedule w3g_autotune picks, next
+        to the per-type launches without a graph.
 """
 from __future__ import annotations
 
@@ -78,6 +86,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-elems", type=int, default=1_000_000, help="target elements of the batched workload")
     return ap.parse_args()
 
 
@@ -95,6 +105,119 @@ def build_workload(n):
     dF = np.diag([-0.0005, -0.0005, 0.001])
     du = ((dF @ X.T).T + rng.normal(0.0, 2e-5, X.shape)).ravel()
     return model, u1, du
+
+
+def build_batched_workload(target, seed=2025, ny=64, nz=64):
+    """Mixed-type workload: bars of 8-node bricks, 20-node bricks and
+    10-node tetrahedra (60/25/15% of `target` elements), random block
+    sizes in [16, 128] and per-block yield stresses."""
+    from warp3d_gb300 import abi
+    from warp3d_gb300.model import Bilinear, Model, Part, mixed_mesh, random_spans
+    a = ny * nz
+    nx = (max(1, round(0.60 * target / a)), max(1, round(0.25 * target / a)), max(1, round(0.15 * target / (6 * a))))
+    coords, parts, _ = mixed_mesh([(abi.ETYPE_L3DISOP, nx[0]), (abi.ETYPE_Q3DISOP, nx[1]), (abi.ETYPE_TET10, nx[2])],
+                                  ny, nz, jitter=0.05, seed=seed)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    plist = []
+    for etype, inc in parts:
+        spans = random_spans(inc.shape[0], rng, 16, 128)
+        mats = [Bilinear.from_hprime(200000.0, 0.3, float(rng.uniform(250.0, 550.0)), 2000.0) for _ in spans]
+        plist.append(Part(etype, inc, spans, mats))
+    model = Model(coords, parts=plist)
+    X = coords
+    F1 = np.diag([1 - 0.005, 1 - 0.005, 1 + 0.01])
+    u1 = ((F1 - np.eye(3)) @ X.T).T.ravel()
+    r2 = np.random.Generator(np.random.PCG64(seed + 1))
+    dF = np.diag([-0.0005, -0.0005, 0.001])
+    du = ((dF @ X.T).T + r2.normal(0.0, 2e-5, X.shape)).ravel()
+    return model, u1, du, nx
+
+
+def bench_batched(args, dev, local):
+    """Batching-form line: autotuned schedule + graph replay, FP64 and FP32
+    tangent, next to per-type launches."""
+    import torch
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+    t0 = time.perf_counter()
+    model, u1, du, nx = build_batched_workload(args.batched_elems)
+    t_build = time.perf_counter() - t0
+    ne = model.noelem
+    counts = {}
+    for t, sp in zip(model.block_etype, model.spans):
+        counts[t] = counts.get(t, 0) + sp
+    eng = Engine(model, device=local)
+    tc = torch.from_numpy(model.c).to(dev)
+    tz = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+    tu = torch.from_numpy(u1).to(dev)
+    tdu = torch.from_numpy(du).to(dev)
+    tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    p = (tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr())
+    both = abi.ITER_RECOVER | abi.ITER_TANGENT
+    with torch.cuda.stream(stream):   # load step 1 to 1% strain, then the state at n
+        eng.recover_dev(1, 1, False, tc.data_ptr(), tz.data_ptr(), tu.data_ptr(), tifv.data_ptr(), sh)
+    torch.cuda.synchronize()
+    assert eng.recover_info()[0] == 0
+    eng.update()
+
+    def time_graph():
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                eng.iteration_dev(2, 1, False, both, *p, sh)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches = 0
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.steps):
+                eng.iteration_dev(2, 1, False, both, *p, sh)
+                launches += eng.last_launch_count()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        assert eng.recover_info()[0] == 0
+        return e0.elapsed_time(e1) / args.steps, launches
+
+    def time_direct():
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                eng.recover_dev(2, 1, False, *p, sh)
+                eng.tanstf_dev(2, 1, *p[:3], sh)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.steps):
+                eng.recover_dev(2, 1, False, *p, sh)
+                eng.tanstf_dev(2, 1, *p[:3], sh)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    out = {}
+    for name, prec in (("plain_fp64", abi.TANGENT_FP64), ("mixed", abi.TANGENT_FP32)):
+        eng.set_precision(prec)
+        eng.set_schedule(mode=abi.SCHED_PER_TYPE)
+        ms_pt = time_direct()
+        t1 = time.perf_counter()
+        sched, tuned_ms = eng.autotune(2, 1, False, *p, sh, reps=2)
+        t_tune = time.perf_counter() - t1
+        ms, launches = time_graph()
+        out[name] = {"value": ne / (ms * 1e-3), "ms_per_step": ms, "schedule": sched,
+                     "autotune_best_ms": tuned_ms, "autotune_s": t_tune,
+                     "per_type_direct": {"value": ne / (ms_pt * 1e-3), "ms_per_step": ms_pt},
+                     "gpu_launches": launches}
+    out["mixed"]["speedup_vs_plain"] = out["plain_fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    names = {abi.ETYPE_L3DISOP: "hex8", abi.ETYPE_Q3DISOP: "hex20", abi.ETYPE_TET10: "tet10"}
+    res = {"workload": "mixed hex8/hex20/tet10 bars 64x64 cells in section, random blocks [16,128], "
+                       "per-block yield U(250,550) MPa, jitter 0.05h, 1 Newton iteration = recovery + tangent",
+           "elements": ne, "elements_by_type": {names[k]: v for k, v in counts.items()},
+           "bars_nx": {"hex8": nx[0], "hex20": nx[1], "tet10": nx[2]}, "blocks": model.nelblk,
+           "gauss_points": int(sum(s * g for s, g in zip(model.spans, model.block_ngp))),
+           "model_build_s": t_build, **out}
+    eng.close()
+    return res
 
 
 def sample_clocks():
@@ -361,6 +484,13 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.n, args.cpu_sample_blocks, host_threads())
 
+    batched = None
+    if not args.no_batched:
+        eng.close()
+        del tc, tu, tdu, tifv
+        torch.cuda.empty_cache()
+        batched = bench_batched(args, dev, local)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -372,7 +502,7 @@ def main():
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "tangent_ms": tan64, "recovery_ms": rec64,
             "mixed": mixed, "e2e": e2e, "roofline": roofline, "cpu_baseline": cb, "clocks": clocks,
-            "gpu_launches": launches64,
+            "gpu_launches": launches64, "batched": batched,
         }
         print(json.dumps(line), flush=True)
     eng.close()
