@@ -81,6 +81,28 @@ extern "C" {
 #define W3G_TANGENT_FP32 1    /* Ke in FP32 (CUDA-core FP32 FMA)        */
 
 /*
+ * One crystal definition of mm10 crystal plasticity: c_array(cnum) of
+ * module crystal_data (src/mod_crystals.f:140-230) as the crystal input
+ * sets it (src/incrystal.f). Supported: slip_type 1 (fcc, 12 systems),
+ * elastic_type 1 (isotropic), h_type 1 (Voce, one hardening variable),
+ * one crystal per Gauss point, the default Newton solver.
+ */
+typedef struct w3g_crystal {
+  int slip_type;                /* 1 = fcc                               */
+  int elastic_type;             /* 1 = isotropic                         */
+  int h_type;                   /* 1 = Voce                              */
+  int miter;                    /* local Newton iteration limit (30)     */
+  double e, nu;                 /* elastic constants                     */
+  double harden_n;              /* slip-rate exponent n                  */
+  double tau_y, tau_v;          /* Voce initial and saturation strength  */
+  double theta_o;               /* Voce hardening modulus theta_0        */
+  double voche_m;               /* Voce exponent m (1)                   */
+  double iD_v;                  /* diffusion rate coefficient (0)        */
+  double k_o, b;                /* geometric hardening k_0 and Burgers   */
+  double atol, atol1, rtol, rtol1;  /* local tolerances (1e-5, 1e-5, 5e-5, 1e-5) */
+} w3g_crystal;
+
+/*
  * Model description: what WARP3D holds in elblks, props/iprops/lprops,
  * edest_blocks and cdest_blocks after input processing.
  */
@@ -97,6 +119,12 @@ typedef struct w3g_model_desc {
   int ncoord;                   /* length of c                           */
   int qbar_flag;                /* consistent Q-bar term, default 1      */
   double beta_fact;             /* plane-strain thickness factor, 1 in 3-D */
+  /* mm10 elements (iprops(25) = 10) only; NULL/0 otherwise */
+  const w3g_crystal* crystals;  /* crystal definitions                   */
+  int ncrystals;
+  const int* elem_crystal;      /* noelem: 0-based crystal of the element */
+  const double* elem_angles;    /* 3*noelem: Euler angles, degrees, Kocks */
+  double dt;                    /* time increment of the load step       */
 } w3g_model_desc;
 
 /*

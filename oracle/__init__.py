@@ -23,9 +23,8 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "w3o.cpp")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "w3o.h"))):
+    srcs = [os.path.join(HERE, f) for f in ("w3o.cpp", "w3o.h", "w3o_mm10.cpp", "w3o_mm10.h")]
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
         subprocess.run(["sh", os.path.join(HERE, "build.sh")], check=True)
     return LIB_PATH
 
@@ -47,6 +46,7 @@ def load() -> C.CDLL:
         lib.w3o_gauss_point.argtypes = [C.c_int, C.c_int, C.c_int, _d]
         lib.w3o_shape_derivs.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _d, _d, _d]
         lib.w3o_mm01_point.argtypes = [C.c_int, C.c_int] + [_d] * 11
+        lib.w3o_mm10_point.argtypes = [C.POINTER(abi.Crystal), _d, C.c_int, C.c_int, C.c_int, C.c_double] + [_d] * 6
         _lib = lib
     return _lib
 

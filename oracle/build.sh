@@ -7,4 +7,4 @@ set -e
 here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/_build"
 ${CXX:-g++} -O3 -fopenmp -ffp-contract=off -fPIC -shared -std=c++17 \
-    -o "$here/_build/libw3o.so" "$here/w3o.cpp"
+    -o "$here/_build/libw3o.so" "$here/w3o.cpp" "$here/w3o_mm10.cpp"

@@ -19,6 +19,7 @@
 // Build: oracle/build.sh (g++ -O2 -fopenmp -ffp-contract=off).
 
 #include "w3o.h"
+#include "w3o_mm10.h"
 
 #include <cmath>
 #include <cstdint>
@@ -36,6 +37,8 @@ constexpr int MXELPR = W3G_MXELPR;
 constexpr int NSTR = 6;
 constexpr int NSTRS = 9;
 constexpr int MM01_HIST = 11;   // mm01_set_sizes, src/mm01.f:976-979
+constexpr int MM10_HIST = w3o::MM10_HIST;
+inline int hist_size(int mat_type) { return mat_type == W3G_MAT_CRYSTAL ? MM10_HIST : MM01_HIST; }
 
 int g_threads = 0;
 int g_deterministic = 1;
@@ -797,7 +800,8 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
   const int span = B.span, nnode = B.nnode, ngp = B.ngp, totdof = B.totdof;
   const int* edest = m->edest[B.blk];
   const int* cdest = m->cdest[B.blk];
-  const int hist = MM01_HIST;
+  const int hist = hist_size(B.mat_type);
+  const bool crystal = B.mat_type == W3G_MAT_CRYSTAL;
 
   // dupstr: element displacements (src/drive_eps_sig_internal_forces.f:560)
   A2 ue(totdof), due(totdof);
@@ -938,7 +942,23 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
     double* cgn[9]; double* cgn1[9]; double* dep[6];
     for (int k = 0; k < 9; ++k) { cgn[k] = urcs_n[g].col(k); cgn1[k] = urcs_n1[g].col(k); }
     for (int k = 0; k < 6; ++k) dep[k] = uddt.col(k);
-    if (nonlinear_update) {
+    if (crystal) {
+      // drive_10_update (src/rstgp1.f:4327-4510): mm10 per element; the
+      // consistent [D] goes to history(1:36), cep_blocks is not written
+      for (int i = 0; i < span; ++i) {
+        w3o::CrystalProps cp;
+        const int e = B.felem - 1 + i;
+        w3o::mm10_element_props(m->crystals[m->elem_crystal[e]], m->elem_angles + 3 * (size_t)e, cp);
+        double hn[MM10_HIST], hn1[MM10_HIST], un[9], un1[9], dd[6], rr[9];
+        for (int k = 0; k < MM10_HIST; ++k) { hn[k] = ehist[g](i, k); hn1[k] = ehist1[g](i, k); }
+        for (int k = 0; k < 9; ++k) { un[k] = urcs_n[g](i, k); un1[k] = zero; rr[k] = rot[g](i, k); }
+        for (int k = 0; k < 6; ++k) dd[k] = uddt(i, k);
+        int st = w3o::mm10_point(cp, step, iter, extrapolated_du, m->dt, e + 1, g + 1, hn, hn1, un, un1, dd, rr);
+        if (st != 0) { out.status = W3G_LOCAL_FAIL; out.bad_elem = e + 1; return out; }
+        for (int k = 0; k < MM10_HIST; ++k) ehist1[g](i, k) = hn1[k];
+        for (int k = 0; k < 9; ++k) urcs_n1[g](i, k) = un1[k];
+      }
+    } else if (nonlinear_update) {
       mm01(span, step, mv, cgn, cgn1, dep, ehist[g], ehist1[g], rtse[g]);
       cnst1(span, cep, rtse[g], mv, ehist1[g].col(1), ehist1[g].col(4), ehist1[g].col(0), ehist1[g].col(3));
     } else {
@@ -962,7 +982,7 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
             cgn1[k][i] = cgn1[k][i] + cep(i, mm + 6 * k) * dep[mm][i];
     }
     // rstgp1_store_cep (src/rstgp1.f:5360-5397): (21, span, ngp)
-    {
+    if (!crystal) {
       double* gc = s->cep[B.blk];
       for (int i = 0; i < span; ++i)
         for (int k = 0; k < 21; ++k)
@@ -991,7 +1011,7 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
         double* rp = s->rot_n1[B.blk] + ((size_t)i * ngp + g) * 9;
         for (int k = 0; k < 9; ++k) rp[k] = rot[g](i, k);
       }
-      if (iter > 0) {
+      if (iter > 0 || crystal) {   // rplstr: mm10 history at every iteration
         double* hp = s->history1[B.blk] + ((size_t)i * ngp + g) * hist;
         for (int k = 0; k < hist; ++k) hp[k] = ehist1[g](i, k);
       }
@@ -1114,9 +1134,16 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
       qmply1(span, qn1, m1, m2);
     }
     blcmp1(span, b, totdof, gama[g], &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], nnode);
-    // drive_01_cnst -> extract_D_symmetric (src/gptns1.f:1174-1266)
+    // drive_01_cnst -> extract_D_symmetric (src/gptns1.f:1174-1266), or
+    // drive_10_cnst (:1371-1455): [D] = w det[J] history1(1:36)
     A2 cep(36);
-    {
+    if (B.mat_type == W3G_MAT_CRYSTAL) {
+      for (int i = 0; i < span; ++i) {
+        double f = weight * dj[g][i];
+        const double* h1 = s->history1[B.blk] + ((size_t)i * ngp + g) * MM10_HIST;
+        for (int k = 0; k < 36; ++k) cep(i, k) = h1[k] * f;
+      }
+    } else {
       const double* gc = s->cep[B.blk];
       for (int i = 0; i < span; ++i) {
         double f = weight * dj[g][i];
@@ -1298,7 +1325,9 @@ int w3o_recover(const w3g_model_desc* m, const w3g_block_state* s, int step, int
   for (int blk = 0; blk < m->nelblk; ++blk) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
-    if (B.mat_type != W3G_MAT_BILINEAR || !B.geonl) return W3G_EUNSUPPORTED;
+    if ((B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL) || !B.geonl) return W3G_EUNSUPPORTED;
+    if (B.mat_type == W3G_MAT_CRYSTAL && (!m->crystals || !m->elem_crystal || !m->elem_angles))
+      return W3G_EARG;
   }
 #ifdef _OPENMP
   if (g_threads > 0) omp_set_num_threads(g_threads);
@@ -1313,17 +1342,21 @@ int w3o_recover(const w3g_model_desc* m, const w3g_block_state* s, int step, int
   }
   // serial reductions (src/drive_eps_sig_internal_forces.f:210-226)
   w3g_recover_info r{};
+  int cut_status = 0;
   for (int blk = 0; blk < m->nelblk; ++blk) {
-    if (outs[blk].status == W3G_STEP_CUT) {
+    if (outs[blk].status == W3G_STEP_CUT || outs[blk].status == W3G_LOCAL_FAIL) {
       r.material_cut_step = 1;
-      if (r.first_bad_element == 0 || outs[blk].bad_elem < r.first_bad_element) r.first_bad_element = outs[blk].bad_elem;
+      if (r.first_bad_element == 0 || outs[blk].bad_elem < r.first_bad_element) {
+        r.first_bad_element = outs[blk].bad_elem;
+        cut_status = outs[blk].status;
+      }
     }
     r.internal_energy = r.internal_energy + outs[blk].energy;
     r.plastic_work = r.plastic_work + outs[blk].plastic;
   }
   if (info) *info = r;
   for (int k = 0; k < m->nodof; ++k) ifv[k] = zero;
-  if (r.material_cut_step) return W3G_STEP_CUT;
+  if (r.material_cut_step) return cut_status;
   // addifv_standard (src/addifv.f:86-124)
   double sum_ifv = 0.0;
   long long nterm = 0;
@@ -1365,7 +1398,7 @@ int w3o_update(const w3g_model_desc* m, const w3g_block_state* s) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
     size_t n = (size_t)B.span * B.ngp;
-    std::memcpy(s->history[blk], s->history1[blk], n * MM01_HIST * sizeof(double));
+    std::memcpy(s->history[blk], s->history1[blk], n * hist_size(B.mat_type) * sizeof(double));
     std::memcpy(s->eps_n[blk], s->eps_n1[blk], n * NSTR * sizeof(double));
     std::memcpy(s->urcs_n[blk], s->urcs_n1[blk], n * NSTRS * sizeof(double));
   }
@@ -1401,3 +1434,12 @@ int w3o_mm01_point(int span, int step, const double* e, const double* nu, const 
 }
 
 }  // extern "C"
+
+extern "C" int w3o_mm10_point(const w3g_crystal* crystal, const double* angles, int step, int iter,
+                              int extrapolated_du, double dt, double* hist_n, double* hist_n1,
+                              const double* urcs_n, double* urcs_n1, const double* uddt, const double* rot_n1) {
+  w3o::CrystalProps cp;
+  w3o::mm10_element_props(*crystal, angles, cp);
+  return w3o::mm10_point(cp, step, iter, extrapolated_du != 0, dt, 1, 1, hist_n, hist_n1, urcs_n, urcs_n1, uddt,
+                         rot_n1);
+}

@@ -46,6 +46,14 @@ int w3o_mm01_point(int span, int step, const double* e, const double* nu,
                    const double* deps, double* history, double* history1,
                    double* cep /* (span,6,6) */);
 
+/* Hook for the single-point crystal tests: one mm10 update of one Gauss
+   point (one crystal) as drive_10_update calls it. hist_n, hist_n1: 158
+   values; urcs_n, urcs_n1: 9; uddt: 6; rot_n1: 9 (column-major). */
+int w3o_mm10_point(const w3g_crystal* crystal, const double* angles, int step, int iter,
+                   int extrapolated_du, double dt, double* hist_n, double* hist_n1,
+                   const double* urcs_n, double* urcs_n1, const double* uddt,
+                   const double* rot_n1);
+
 #ifdef __cplusplus
 }
 #endif

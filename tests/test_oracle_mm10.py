@@ -1,0 +1,158 @@
+"""Known answers for the oracle's mm10 crystal plasticity (CPU).
+
+mm10's linear algebra is MKL in the reference and no execution of it is
+available, so these pins are physical and structural: the elastic limit,
+objectivity under a rotation of crystal and loading together, the cubic
+symmetry of the fcc slip systems, the symmetry of the stored tangent, and
+an equilibrium Newton solution of a small polycrystal.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from warp3d_gb300.model import Crystal, Model, cube_mesh, random_orientations
+from warp3d_gb300.newton import NewtonDriver, uniaxial_bcs
+
+H = 158
+TT = 87 + 42     # tau_tilde in the history vector
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _point(angles, steps, crystal=None, it=1, R=None):
+    """Runs mm10 at one point through `steps` (list of uddt), returns the
+    last (stress 9, history 158) and the history/stress before the last."""
+    lib = oracle.load()
+    cr = (crystal or Crystal()).struct()
+    ang = np.asarray(angles, dtype=np.float64)
+    Rm = np.eye(3).ravel(order="F").copy() if R is None else np.asarray(R, dtype=np.float64).ravel(order="F").copy()
+    hn, un = np.zeros(H), np.zeros(9)
+    for s, dd in enumerate(steps, start=1):
+        hc, hn1, un1 = hn.copy(), np.zeros(H), np.zeros(9)
+        st = lib.w3o_mm10_point(C.byref(cr), _dp(ang), s, it, 0, 1.0, _dp(hc), _dp(hn1), _dp(un), _dp(un1),
+                                _dp(np.asarray(dd, dtype=np.float64)), _dp(Rm))
+        assert st == 0
+        hn, un = hn1, un1
+    return un, hn
+
+
+def _iso(e=200000.0, nu=0.3):
+    lam = e * nu / ((1 + nu) * (1 - 2 * nu))
+    mu = e / (2 * (1 + nu))
+    Cm = np.zeros((6, 6))
+    Cm[:3, :3] = lam
+    Cm[np.arange(3), np.arange(3)] = lam + 2 * mu
+    Cm[np.arange(3, 6), np.arange(3, 6)] = mu
+    return Cm
+
+
+def test_elastic_limit_stress_and_tangent():
+    d = np.array([2.0, -1.0, 0.5, 1.0, -0.5, 0.25]) * 1e-7
+    s, h = _point([20.0, 70.0, 110.0], [d, d])
+    Ce = _iso()
+    # two increments of d from zero stress: resolved shears ~1e-2 MPa,
+    # slip (tau/tau_y)^20 negligible
+    assert np.allclose(s[:6], Ce @ (2 * d), rtol=1e-9, atol=1e-12)
+    D = h[:36].reshape(6, 6, order="F")
+    assert np.abs(D - Ce).max() / Ce.max() < 1e-9
+
+
+def test_tangent_is_symmetric_and_plastic():
+    d = np.array([-0.0005, -0.0005, 0.001, 0.0002, 0.0, 0.0001])
+    s, h = _point([30.0, 40.0, 50.0], [d, d, d])
+    D = h[:36].reshape(6, 6, order="F")
+    assert np.array_equal(D, D.T)
+    assert D[2, 2] < 0.9 * _iso()[2, 2]          # plastic flow softens the axial stiffness
+    assert h[TT] > 90.0                           # hardening
+
+
+def _kocks(angles):
+    a, b, c = np.radians(angles)
+    psi, theta, phi = a, b, c
+    r = np.empty((3, 3))
+    r[0, 0] = -np.sin(psi) * np.sin(phi) - np.cos(psi) * np.cos(phi) * np.cos(theta)
+    r[0, 1] = np.cos(psi) * np.sin(phi) - np.sin(psi) * np.cos(phi) * np.cos(theta)
+    r[0, 2] = np.cos(phi) * np.sin(theta)
+    r[1, 0] = np.sin(psi) * np.cos(phi) - np.cos(psi) * np.sin(phi) * np.cos(theta)
+    r[1, 1] = -np.cos(psi) * np.cos(phi) - np.sin(psi) * np.sin(phi) * np.cos(theta)
+    r[1, 2] = np.sin(phi) * np.sin(theta)
+    r[2, 0] = np.cos(psi) * np.sin(theta)
+    r[2, 1] = np.sin(psi) * np.sin(theta)
+    r[2, 2] = np.cos(theta)
+    return r
+
+
+def _angles_of(r):
+    psi = np.degrees(np.arctan2(r[2, 1], r[2, 0])) % 360.0
+    phi = np.degrees(np.arctan2(r[1, 2], r[0, 2])) % 360.0
+    theta = np.degrees(np.arccos(np.clip(r[2, 2], -1.0, 1.0)))
+    return np.array([psi, theta, phi])
+
+
+def _voigt_rot(Q, v, strain):
+    """Q t Q^T for a Voigt vector (xx, yy, zz, xy, yz, xz); engineering
+    shears when strain."""
+    f = 0.5 if strain else 1.0
+    t = np.array([[v[0], f * v[3], f * v[5]], [f * v[3], v[1], f * v[4]], [f * v[5], f * v[4], v[2]]])
+    r = Q @ t @ Q.T
+    g = 2.0 if strain else 1.0
+    return np.array([r[0, 0], r[1, 1], r[2, 2], g * r[0, 1], g * r[1, 2], g * r[0, 2]])
+
+
+def test_objectivity_rotating_crystal_and_loading():
+    """Rotating the lattice (g -> g Q^T) and the strain increment together
+    rotates the stress: exactly in the elastic range. In plastic flow the
+    plastic-spin term 2 sym(sigma W_p) is not exactly objective in the
+    reference -- mm10_symsw and mm10_iw do not match the (W23, W13, W12)
+    skew-vector convention of mm10_wt2wv -- and the oracle restates it as
+    is: the rotated result then differs by ~1e-4 of the stress."""
+    ang = np.array([35.0, 50.0, 120.0])
+    g = _kocks(ang)
+    th = 0.7
+    Q = np.array([[np.cos(th), -np.sin(th), 0.0], [np.sin(th), np.cos(th), 0.0], [0.0, 0.0, 1.0]])
+    Q = Q @ np.array([[1, 0, 0], [0, np.cos(0.4), -np.sin(0.4)], [0, np.sin(0.4), np.cos(0.4)]])
+    ang2 = _angles_of(g @ Q.T)
+    assert np.allclose(_kocks(ang2), g @ Q.T, atol=1e-12)
+    base = np.array([-0.4, -0.6, 1.0, 0.3, -0.1, 0.2])
+    for scale, tol in ((1e-6, 1e-13), (1e-4, 1e-13), (1e-3, 1e-3)):
+        d = base * scale
+        s1, _ = _point(ang, [d, d])
+        d2 = _voigt_rot(Q, d, strain=True)
+        s2, _ = _point(ang2, [d2, d2])
+        err = np.abs(s2[:6] - _voigt_rot(Q, s1[:6], strain=False)).max() / np.abs(s1[:6]).max()
+        assert err < tol, (scale, err)
+        assert abs(s2[6] - s1[6]) < 1e3 * tol * abs(s1[6])   # work density is invariant
+
+
+def test_cube_orientation_uniaxial_symmetry():
+    # identity lattice (psi = 90, theta = 0, phi = 90 gives g = I in Kocks):
+    # [001] tension activates 8 systems symmetrically -> sxx = syy, no shear
+    g = _kocks([90.0, 0.0, 90.0])
+    assert np.allclose(np.abs(g), np.eye(3), atol=1e-15)
+    d = np.array([-0.0005, -0.0005, 0.001, 0.0, 0.0, 0.0])
+    s, h = _point([90.0, 0.0, 90.0], [d] * 6)
+    assert abs(s[0] - s[1]) < 1e-9 * abs(s[2])
+    assert np.abs(s[3:6]).max() < 1e-9 * abs(s[2])
+    # resolved shear on the 8 active systems = szz-sxx times the Schmid factor 1/sqrt(6)
+    tau = (s[2] - s[0]) / np.sqrt(6.0)
+    assert 0.85 * h[TT] < tau < 1.0 * h[TT]
+
+
+def test_polycrystal_newton_equilibrium():
+    n = 2
+    coords, incid = cube_mesh(n, jitter=0.05)
+    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(n ** 3, 7))
+    ora = oracle.Oracle(model)
+    fixed, topz = uniaxial_bcs(model, (n, n, n))
+    drv = NewtonDriver(model, ora, fixed, tol=1e-8, maxit=40, extrapolate=True)
+    for s in range(1, 4):
+        imp = np.zeros(model.nodof)
+        imp[topz] = 0.0005 * n
+        res = drv.step(s, imp)
+        assert res[-1] <= 1e-8
+    szz = np.concatenate(ora.state.urcs_n)[:, :, 2]
+    assert 150.0 < szz.mean() < 400.0

@@ -28,6 +28,9 @@ EUNSUPPORTED = -2
 ECUDA = -3
 ENOMEM = -4
 
+HIST_MM01 = 11
+HIST_MM10 = 158       # one fcc crystal, one hardening variable
+
 TANGENT_FP64 = 0
 TANGENT_FP32 = 1
 
@@ -40,6 +43,30 @@ ITER_TANGENT = 2
 
 _dpp = C.POINTER(C.POINTER(C.c_double))
 _ipp = C.POINTER(C.POINTER(C.c_int))
+
+
+class Crystal(C.Structure):
+    """w3g_crystal: one mm10 crystal definition."""
+    _fields_ = [
+        ("slip_type", C.c_int),
+        ("elastic_type", C.c_int),
+        ("h_type", C.c_int),
+        ("miter", C.c_int),
+        ("e", C.c_double),
+        ("nu", C.c_double),
+        ("harden_n", C.c_double),
+        ("tau_y", C.c_double),
+        ("tau_v", C.c_double),
+        ("theta_o", C.c_double),
+        ("voche_m", C.c_double),
+        ("iD_v", C.c_double),
+        ("k_o", C.c_double),
+        ("b", C.c_double),
+        ("atol", C.c_double),
+        ("atol1", C.c_double),
+        ("rtol", C.c_double),
+        ("rtol1", C.c_double),
+    ]
 
 
 class ModelDesc(C.Structure):
@@ -56,6 +83,11 @@ class ModelDesc(C.Structure):
         ("ncoord", C.c_int),
         ("qbar_flag", C.c_int),
         ("beta_fact", C.c_double),
+        ("crystals", C.POINTER(Crystal)),
+        ("ncrystals", C.c_int),
+        ("elem_crystal", C.POINTER(C.c_int)),
+        ("elem_angles", C.POINTER(C.c_double)),
+        ("dt", C.c_double),
     ]
 
 

@@ -30,7 +30,8 @@ import numpy as np
 
 from . import abi
 
-HIST_MM01 = 11
+HIST_MM01 = abi.HIST_MM01
+HIST_MM10 = abi.HIST_MM10
 NSTR = 6
 NSTRS = 9
 
@@ -81,6 +82,49 @@ class Bilinear:
         with np.errstate(all="ignore"):
             h = np.float32(np.float32(e * et) / np.float32(e - et))
         return {7: e, 8: np.float32(self.nu), 14: np.float32(self.beta), 15: h, 23: np.float32(self.yld)}
+
+
+@dataclass
+class Crystal:
+    """mm10 crystal plasticity, WARP3D's crystal input (src/incrystal.f,
+    defaults of src/mod_crystals.f:250-416): fcc slip systems, isotropic
+    elasticity, Voce hardening tau_tilde' = theta_0 sum |1 - (tau_tilde -
+    tau_y)/tau_v|^m |gamma_dot|, slip rate gamma = dg/tau |tau_s/tau|^(n-1)
+    tau_s. One crystal per Gauss point."""
+
+    e: float = 200000.0
+    nu: float = 0.3
+    harden_n: float = 20.0
+    tau_y: float = 90.0
+    tau_v: float = 200.0
+    theta_o: float = 500.0
+    voche_m: float = 1.0
+    iD_v: float = 0.0
+    k_o: float = 0.0
+    b: float = 2.87e-7
+    atol: float = 1.0e-5
+    atol1: float = 1.0e-5
+    rtol: float = 5.0e-5
+    rtol1: float = 1.0e-5
+    miter: int = 30
+
+    def struct(self) -> abi.Crystal:
+        c = abi.Crystal()
+        c.slip_type, c.elastic_type, c.h_type, c.miter = 1, 1, 1, self.miter
+        for k in ("e", "nu", "harden_n", "tau_y", "tau_v", "theta_o", "voche_m", "iD_v", "k_o", "b", "atol",
+                  "atol1", "rtol", "rtol1"):
+            setattr(c, k, float(getattr(self, k)))
+        return c
+
+
+def random_orientations(n: int, seed: int = 4242) -> np.ndarray:
+    """Euler angles (degrees, Kocks convention psi, theta, phi) uniform on
+    SO(3): psi, phi uniform in [0, 360), cos(theta) uniform in [-1, 1]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    psi = rng.uniform(0.0, 360.0, n)
+    phi = rng.uniform(0.0, 360.0, n)
+    theta = np.degrees(np.arccos(rng.uniform(-1.0, 1.0, n)))
+    return np.ascontiguousarray(np.stack([psi, theta, phi], axis=1))
 
 
 def _lattice(nx, ny, nz, h, jitter, seed, level=1):
@@ -266,7 +310,7 @@ class Model:
     never mix types, as in WARP3D)."""
 
     def __init__(self, coords, incid=None, *, parts=None, block_size=128, etype=abi.ETYPE_L3DISOP, geonl=True,
-                 bbar=False, qbar=True, materials=None, block_spans=None):
+                 bbar=False, qbar=True, materials=None, block_spans=None, angles=None, dt=1.0):
         if parts is None:
             parts = [Part(etype, np.asarray(incid), block_spans, materials)]
         self.coords = np.asarray(coords, dtype=np.float64)
@@ -307,6 +351,19 @@ class Model:
         self.block_totdof = [3 * n for n in self.block_nnode]
         self.block_utsz = [d * (d + 1) // 2 for d in self.block_totdof]
         self._block_incid = bincid
+        self.block_crystal = [isinstance(m, Crystal) for m in bmat]
+        self.block_hist = [HIST_MM10 if cr else HIST_MM01 for cr in self.block_crystal]
+        self.dt = float(dt)
+        self.crystals = []
+        self.elem_crystal = np.full(self.noelem, -1, dtype=np.int32)
+        for b, m in enumerate(bmat):
+            if isinstance(m, Crystal):
+                if m not in self.crystals:
+                    self.crystals.append(m)
+                f = int(self.felem[b])
+                self.elem_crystal[f:f + spans[b]] = self.crystals.index(m)
+        self.elem_angles = (np.zeros((self.noelem, 3)) if angles is None
+                            else np.ascontiguousarray(np.asarray(angles, dtype=np.float64).reshape(self.noelem, 3)))
         self.uniform = len(set(btype)) == 1
         # single-type conveniences
         t0 = btype[0]
@@ -334,12 +391,17 @@ class Model:
             self.iprops[rows, 3] = 3
             self.iprops[rows, 4] = order
             self.iprops[rows, 5] = ngp
-            self.iprops[rows, 24] = abi.MAT_BILINEAR
+            mat = self.block_material[b]
+            self.iprops[rows, 24] = abi.MAT_CRYSTAL if isinstance(mat, Crystal) else abi.MAT_BILINEAR
             self.iprops[rows, 37] = 1
             self.lprops[rows, 17] = 1 if self.geonl else 0
             self.lprops[rows, 18] = 1 if self.bbar else 0
-            for k, v in self.block_material[b].props_values().items():
-                self.props[rows, k - 1] = v
+            if isinstance(mat, Crystal):
+                self.props[rows, 6] = np.float32(mat.e)
+                self.props[rows, 7] = np.float32(mat.nu)
+            else:
+                for k, v in mat.props_values().items():
+                    self.props[rows, k - 1] = v
             nodes = self._block_incid[b]                     # (span, nn)
             d = np.empty((s, 3 * nn), dtype=np.int32)
             for k in range(3):
@@ -366,6 +428,13 @@ class Model:
         d.ncoord = self.ncoord
         d.qbar_flag = 1 if self.qbar else 0
         d.beta_fact = 1.0
+        if self.crystals:
+            self._crys = (abi.Crystal * len(self.crystals))(*[c.struct() for c in self.crystals])
+            d.crystals = C.cast(self._crys, C.POINTER(abi.Crystal))
+            d.ncrystals = len(self.crystals)
+            d.elem_crystal = self.elem_crystal.ctypes.data_as(C.POINTER(C.c_int))
+            d.elem_angles = self.elem_angles.ctypes.data_as(C.POINTER(C.c_double))
+        d.dt = self.dt
         return d
 
     def new_state(self) -> "HostState":
@@ -388,9 +457,9 @@ class HostState:
 
     def __init__(self, model: Model):
         self.model = model
-        sp, ng, td = model.spans, model.block_ngp, model.block_totdof
-        self.history = [np.zeros((s, g, HIST_MM01)) for s, g in zip(sp, ng)]
-        self.history1 = [np.zeros((s, g, HIST_MM01)) for s, g in zip(sp, ng)]
+        sp, ng, td, hs = model.spans, model.block_ngp, model.block_totdof, model.block_hist
+        self.history = [np.zeros((s, g, h)) for s, g, h in zip(sp, ng, hs)]
+        self.history1 = [np.zeros((s, g, h)) for s, g, h in zip(sp, ng, hs)]
         self.urcs_n = [np.zeros((s, g, NSTRS)) for s, g in zip(sp, ng)]
         self.urcs_n1 = [np.zeros((s, g, NSTRS)) for s, g in zip(sp, ng)]
         self.eps_n = [np.zeros((s, g, NSTR)) for s, g in zip(sp, ng)]
