@@ -14,9 +14,16 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libw3g.so")
-SOURCES = ["w3g_api.cu", "w3g_tangent.cu", "w3g_recover.cu", "w3g_peak.cu", "w3g_noalloc.cu"]
+SOURCES = ["w3g_api.cu", "w3g_tangent.cu", "w3g_recover.cu", "w3g_mm10.cu", "w3g_peak.cu", "w3g_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# host code without multiply-add contraction (aarch64 g++ contracts by
+# default): the host-built tables follow the same operation order as the
+# oracle
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr"]
+# the mm10 local Newton solve evaluates residuals and Jacobians in the
+# reference's operation order (no fused multiply-add)
+EXTRA_FLAGS = {"w3g_mm10.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -26,7 +33,7 @@ def nvcc() -> str:
 
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS.get(src, []), "-c", os.path.join(CSRC, src), "-o", obj]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -65,7 +65,8 @@ void free_all(w3g_context* c) {
   if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
   void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
                   m.cdest, m.mat, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
-                  m.ifv_rowptr, m.ifv_src, s.params, s.counters,
+                  m.ifv_rowptr, m.ifv_src, s.params, s.counters, m.xtal, m.xtype, m.mm10_gp, s.mm10_scr,
+                  s.mm10_iters, s.mm10_order, s.mm10_bins,
                   s.geo, s.c_geo, s.geo_dirty,
                   s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
                   s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
@@ -109,6 +110,29 @@ int blocks_d2h(w3g_context* c, const double* dev, double* const* host, int per, 
   return 0;
 }
 
+// history blocks: (hist, ngp, span) each, hist per block
+int hist_h2d(w3g_context* c, double* dev, double* const* host) {
+  for (int b = 0; b < c->m.nelblk; ++b) {
+    const BlockDesc& bd = c->blocks[b];
+    if (!host[b]) continue;
+    CK(cudaMemcpyAsync(dev + bd.hist_off, host[b], (size_t)bd.hist * bd.ngp * bd.span * sizeof(double),
+                       cudaMemcpyHostToDevice, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int hist_d2h(w3g_context* c, const double* dev, double* const* host) {
+  for (int b = 0; b < c->m.nelblk; ++b) {
+    const BlockDesc& bd = c->blocks[b];
+    if (!host[b]) continue;
+    CK(cudaMemcpyAsync(host[b], dev + bd.hist_off, (size_t)bd.hist * bd.ngp * bd.span * sizeof(double),
+                       cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
 TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, const double* d_du) {
   TangentArgs a;
   for (int t = 0; t < kNumTypes; ++t) { a.dn[t] = c->m.dn[t]; a.dn32[t] = c->m.dn32[t]; }
@@ -121,6 +145,7 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
   a.rot_n1 = c->s.rot_n1;
   a.urcs_n1 = c->s.urcs_n1;
   a.cep = c->s.cep;
+  a.hist1 = c->s.hist1;
   a.estiff = c->precision == W3G_TANGENT_FP32 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
   a.qbar = c->m.qbar;
   a.beta_fact = c->m.beta_fact;
@@ -170,6 +195,15 @@ int enqueue_recover(w3g_context* c, const double* d_c, const double* d_u, const 
   a.geo_dirty = c->s.geo_dirty;
   a.params = c->s.params;
   a.beta_fact = c->m.beta_fact;
+  a.xtal = c->m.xtal;
+  a.xtype = c->m.xtype;
+  a.mm10_scr = c->s.mm10_scr;
+  a.mm10_gp = c->m.mm10_gp;
+  a.mm10_iters = c->s.mm10_iters;
+  a.mm10_order = c->s.mm10_order;
+  a.mm10_bins = c->s.mm10_bins;
+  a.mm10_counter = c->s.counters + 2;
+  a.dt = c->m.dt;
   cudaError_t e = launch_recover(c->m, a, c->s.c_geo, c->sched, c->s.counters, st);
   if (e == cudaSuccess) e = launch_assemble_ifv(c->m, c->s.einf, d_ifv, c->s.ifv_partials, c->ifv_parts, st);
   if (e == cudaSuccess)
@@ -224,9 +258,10 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   // ---- block table (elblks, iprops, lprops) ----
   std::vector<BlockDesc>& B = c->blocks;
   B.resize(md->nelblk);
-  long long gp = 0, cep = 0, est = 0, einf = 0, geo = 0;
-  int expect_felem = 1;
-  std::vector<Chunk> type_chunks[kNumTypes], ttype_chunks[kNumTypes];
+  long long gp = 0, cep = 0, est = 0, einf = 0, geo = 0, hist = 0;
+  int expect_felem = 1, n_mm10_gp = 0;
+  std::vector<Chunk> type_chunks[kNumTypes], ttype_chunks[kNumTypes], mm10_chunks;
+  std::vector<int> mm10_gp;
   for (int b = 0; b < md->nelblk; ++b) {
     BlockDesc& d = B[b];
     d.span = md->elblks[3 * b];
@@ -256,23 +291,59 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": element type not supported");
     }
-    if (d.mat != W3G_MAT_BILINEAR) {
+    if (d.mat != W3G_MAT_BILINEAR && d.mat != W3G_MAT_CRYSTAL) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": material model not supported");
+    }
+    if (d.mat == W3G_MAT_CRYSTAL) {
+      if (d.etype != W3G_ETYPE_L3DISOP) {
+        delete c;
+        return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": mm10 needs 8-node bricks");
+      }
+      if (!md->crystals || md->ncrystals <= 0 || !md->elem_crystal || !md->elem_angles || !(md->dt > 0.0)) {
+        delete c;
+        return fail(W3G_EARG, "block " + std::to_string(b + 1) + ": mm10 without crystal data or dt");
+      }
+      for (int i = 0; i < d.span; ++i) {
+        const int cn = md->elem_crystal[d.felem + i];
+        if (cn < 0 || cn >= md->ncrystals) {
+          delete c;
+          return fail(W3G_EARG, "element " + std::to_string(d.felem + i + 1) + ": bad crystal index");
+        }
+        const w3g_crystal& cr = md->crystals[cn];
+        if (cr.slip_type != 1 || cr.elastic_type != 1 || cr.h_type != 1) {
+          delete c;
+          return fail(W3G_EUNSUPPORTED, "crystal " + std::to_string(cn) +
+                                            ": only fcc slip, isotropic elasticity, Voce hardening");
+        }
+      }
     }
     if (!d.geonl || d.bbar) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": small-strain or b-bar not supported");
     }
     d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf; d.geo_off = geo;
+    d.hist = d.mat == W3G_MAT_CRYSTAL ? kHistMM10 : kHistMM01;
+    d.hist_off = hist;
+    d.mm10_off = d.mat == W3G_MAT_CRYSTAL ? n_mm10_gp : -1;
+    hist += (long long)d.hist * d.span * d.ngp;
+    if (d.mat == W3G_MAT_CRYSTAL) {
+      for (int i = 0; i < d.span; ++i)
+        for (int g = 0; g < d.ngp; ++g) mm10_gp.push_back((b << 12) | (i << 3) | g);
+      n_mm10_gp += d.span * d.ngp;
+    }
     gp += (long long)d.span * d.ngp;
     cep += 21LL * d.span * d.ngp;
     est += (long long)d.utsz * d.span;
     einf += (long long)d.totdof * d.span;
     geo += (long long)(3 * d.nnode + 1) * d.span * d.ngp;
     const int ts = type_slot(d.etype);
-    for (int i0 = 0, per = kRecoverChunk[ts]; i0 < d.span; i0 += per)
-      type_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0), ts});
+    if (d.mat == W3G_MAT_CRYSTAL) {   // recovered by the mm10 kernels
+      for (int i0 = 0; i0 < d.span; i0 += kChunk) mm10_chunks.push_back(Chunk{b, i0, std::min(kChunk, d.span - i0), 3});
+    } else {
+      for (int i0 = 0, per = kRecoverChunk[ts]; i0 < d.span; i0 += per)
+        type_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0), ts});
+    }
     for (int i0 = 0, per = kTangentChunk[ts]; i0 < d.span; i0 += per)
       ttype_chunks[ts].push_back(Chunk{b, i0, std::min(per, d.span - i0), ts});
   }
@@ -286,6 +357,10 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     tchunks.insert(tchunks.end(), ttype_chunks[t].begin(), ttype_chunks[t].end());
   }
   m.ntchunks = (int)tchunks.size();
+  m.nrchunks = (int)chunks.size();
+  m.mm10_chunk0 = (int)chunks.size();
+  m.mm10_chunks = (int)mm10_chunks.size();
+  m.n_mm10_gp = n_mm10_gp;
   // schedule orders: block order, and heaviest item type first (estimated
   // work per item: recovery ~ elements x Gauss points x (30 + nodes),
   // tangent ~ elements x Gauss points x node pairs)
@@ -300,13 +375,15 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     std::stable_sort(out[1].begin(), out[1].end(), [&](int x, int y) { return cost[ch[x].type] > cost[ch[y].type]; });
   };
   std::vector<int> rord[2], tord[2];
-  orders(chunks, kRecoverChunk, false, rord);
+  orders(chunks, kRecoverChunk, false, rord);   // the three element types only
   orders(tchunks, kTangentChunk, true, tord);
+  chunks.insert(chunks.end(), mm10_chunks.begin(), mm10_chunks.end());
   if (expect_felem != md->noelem + 1) {
     delete c;
     return fail(W3G_EARG, "blocks do not cover all elements");
   }
   m.ngp_total = gp; m.cep_total = cep; m.estiff_total = est; m.einf_total = einf; m.geo_total = geo;
+  m.hist_total = hist;
   m.nchunks = (int)chunks.size();
 
   // ---- edest / cdest, ifv CSR ----
@@ -353,6 +430,32 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     mat[e].lnelas = lp[16] ? 1.0 : 0.0;
     fill_mat_constants(mat[e]);
   }
+  // mm10: per-element crystal data (setup_mm10_rknstr) and definitions
+  std::vector<CrystalElem> xtal;
+  std::vector<CrystalType> xtype;
+  if (n_mm10_gp > 0) {
+    xtal.resize(md->noelem);
+    std::memset(xtal.data(), 0, xtal.size() * sizeof(CrystalElem));
+    for (int b = 0; b < md->nelblk; ++b) {
+      const BlockDesc& d = B[b];
+      if (d.mat != W3G_MAT_CRYSTAL) continue;
+      for (int i = 0; i < d.span; ++i) {
+        const int e = d.felem + i;
+        const int cn = md->elem_crystal[e];
+        build_crystal_elem(md->crystals[cn], cn, md->elem_angles + 3 * (size_t)e, xtal[e]);
+      }
+    }
+    xtype.resize(md->ncrystals);
+    for (int k = 0; k < md->ncrystals; ++k) {
+      const w3g_crystal& cr = md->crystals[k];
+      CrystalType& t = xtype[k];
+      t.rate_n = cr.harden_n; t.tau_y = cr.tau_y; t.tau_v = cr.tau_v; t.theta_0 = cr.theta_o;
+      t.voche_m = cr.voche_m; t.iD_v = cr.iD_v; t.k_0 = cr.k_o; t.burgers = cr.b;
+      t.atol = cr.atol; t.atol1 = cr.atol1; t.rtol = cr.rtol; t.rtol1 = cr.rtol1;
+      t.miter = cr.miter; t.pad = 0;
+    }
+    m.dt = md->dt;
+  }
   std::vector<double> dnt[kNumTypes] = {std::vector<double>(dn_table_size<Hex8>()),
                                         std::vector<double>(dn_table_size<Hex20>()),
                                         std::vector<double>(dn_table_size<Tet10>())};
@@ -374,11 +477,20 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(m.chunks, m.nchunks);
   AL(m.tchunks, m.ntchunks);
   for (int k = 0; k < 2; ++k) {
-    AL(m.rorder[k], m.nchunks);
+    AL(m.rorder[k], m.nrchunks);
     AL(m.torder[k], m.ntchunks);
   }
   AL(s.params, 1);
-  AL(s.counters, 2);
+  AL(s.counters, 3);
+  if (n_mm10_gp > 0) {
+    AL(m.xtal, md->noelem);
+    AL(m.xtype, md->ncrystals);
+    AL(m.mm10_gp, n_mm10_gp);
+    AL(s.mm10_scr, (long long)kMm10Scratch * n_mm10_gp);
+    AL(s.mm10_iters, n_mm10_gp);
+    AL(s.mm10_order, n_mm10_gp);
+    AL(s.mm10_bins, 128);
+  }
   AL(m.edest, einf);
   AL(m.cdest, einf);
   AL(m.mat, md->noelem);
@@ -388,8 +500,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   }
   AL(m.ifv_rowptr, md->nodof + 1);
   AL(m.ifv_src, einf);
-  AL(s.hist, kHistMM01 * gp);
-  AL(s.hist1, kHistMM01 * gp);
+  AL(s.hist, hist);
+  AL(s.hist1, hist);
   AL(s.urcs_n, 9 * gp);
   AL(s.urcs_n1, 9 * gp);
   AL(s.eps_n, 6 * gp);
@@ -424,12 +536,17 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   UP(m.chunks, chunks.data(), m.nchunks);
   UP(m.tchunks, tchunks.data(), m.ntchunks);
   for (int k = 0; k < 2; ++k) {
-    UP(m.rorder[k], rord[k].data(), m.nchunks);
+    UP(m.rorder[k], rord[k].data(), m.nrchunks);
     UP(m.torder[k], tord[k].data(), m.ntchunks);
   }
   UP(m.edest, ed.data(), einf);
   UP(m.cdest, cd.data(), einf);
   UP(m.mat, mat.data(), md->noelem);
+  if (n_mm10_gp > 0) {
+    UP(m.xtal, xtal.data(), md->noelem);
+    UP(m.xtype, xtype.data(), md->ncrystals);
+    UP(m.mm10_gp, mm10_gp.data(), n_mm10_gp);
+  }
   for (int t = 0; t < kNumTypes; ++t) {
     UP(m.dn[t], dnt[t].data(), dnt[t].size());
     UP(m.dn32[t], dnt32[t].data(), dnt32[t].size());
@@ -439,10 +556,11 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
 #undef UP
   // WARP3D's initial state: zeros, rotations = identity (src/reopen.f:1912-1915)
   double* zs[] = {s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.cep, s.estiff, s.einf, s.evol};
-  long long zn[] = {kHistMM01 * gp, kHistMM01 * gp, 9 * gp, 9 * gp, 6 * gp, 6 * gp, cep, est, einf, md->noelem};
+  long long zn[] = {hist, hist, 9 * gp, 9 * gp, 6 * gp, 6 * gp, cep, est, einf, md->noelem};
   for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = cudaMemsetAsync(zs[k], 0, (size_t)zn[k] * sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.geo_dirty, 0xff, sizeof(int), st);   // nonzero: not built
-  if (e == cudaSuccess) e = cudaMemsetAsync(s.counters, 0, 2 * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.counters, 0, 3 * sizeof(int), st);
+  if (e == cudaSuccess && n_mm10_gp > 0) e = cudaMemsetAsync(s.mm10_iters, 0, (size_t)n_mm10_gp * sizeof(int), st);
   if (e == cudaSuccess) e = init_kernels();
   if (e == cudaSuccess) {
     k_init_rot<<<(unsigned)((gp + 255) / 256), 256, 0, st>>>(s.rot_n1, gp);
@@ -483,8 +601,8 @@ int w3g_state_upload(w3g_context* c, const w3g_block_state* h) {
   if (!c || !h) return fail(W3G_EARG, "null argument");
   CK(cudaSetDevice(c->device));
   int r = 0;
-  if (h->history && (r = blocks_h2d(c, c->s.hist, h->history, kHistMM01, true))) return r;
-  if (h->history1 && (r = blocks_h2d(c, c->s.hist1, h->history1, kHistMM01, true))) return r;
+  if (h->history && (r = hist_h2d(c, c->s.hist, h->history))) return r;
+  if (h->history1 && (r = hist_h2d(c, c->s.hist1, h->history1))) return r;
   if (h->urcs_n && (r = blocks_h2d(c, c->s.urcs_n, h->urcs_n, 9, true))) return r;
   if (h->urcs_n1 && (r = blocks_h2d(c, c->s.urcs_n1, h->urcs_n1, 9, true))) return r;
   if (h->eps_n && (r = blocks_h2d(c, c->s.eps_n, h->eps_n, 6, true))) return r;
@@ -509,8 +627,8 @@ int w3g_state_download(w3g_context* c, const w3g_block_state* h) {
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->stream));
   int r = 0;
-  if (h->history && (r = blocks_d2h(c, c->s.hist, h->history, kHistMM01, true))) return r;
-  if (h->history1 && (r = blocks_d2h(c, c->s.hist1, h->history1, kHistMM01, true))) return r;
+  if (h->history && (r = hist_d2h(c, c->s.hist, h->history))) return r;
+  if (h->history1 && (r = hist_d2h(c, c->s.hist1, h->history1))) return r;
   if (h->urcs_n && (r = blocks_d2h(c, c->s.urcs_n, h->urcs_n, 9, true))) return r;
   if (h->urcs_n1 && (r = blocks_d2h(c, c->s.urcs_n1, h->urcs_n1, 9, true))) return r;
   if (h->eps_n && (r = blocks_d2h(c, c->s.eps_n, h->eps_n, 6, true))) return r;
@@ -593,7 +711,7 @@ int w3g_recover(w3g_context* c, int step, int iter, int extrapolated_du, const d
   if (info) *info = hi;
   if (hi.material_cut_step) {
     if (hifv) std::memset(hifv, 0, (size_t)c->m.nodof * sizeof(double));
-    return W3G_STEP_CUT;
+    return hi.material_cut_step;   // W3G_STEP_CUT or W3G_LOCAL_FAIL
   }
   return 0;
 }
@@ -603,7 +721,7 @@ int w3g_update(w3g_context* c) {
   CK(cudaSetDevice(c->device));
   const long long gp = c->m.ngp_total;
   cudaStream_t st = c->stream;
-  CK(cudaMemcpyAsync(c->s.hist, c->s.hist1, (size_t)kHistMM01 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(c->s.hist, c->s.hist1, (size_t)c->m.hist_total * sizeof(double), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(c->s.eps_n, c->s.eps_n1, (size_t)6 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(c->s.urcs_n, c->s.urcs_n1, (size_t)9 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
   CK(cudaStreamSynchronize(st));
@@ -851,7 +969,7 @@ int w3g_recover_info_get(w3g_context* c, w3g_recover_info* info) {
   if (!c || !info) return fail(W3G_EARG, "null argument");
   CK(cudaSetDevice(c->device));
   CK(cudaMemcpy(info, c->s.d_info, sizeof(*info), cudaMemcpyDeviceToHost));
-  return info->material_cut_step ? W3G_STEP_CUT : 0;
+  return info->material_cut_step;
 }
 
 int w3g_estiff_device(w3g_context* c, void** d_estiff, long long* count) {

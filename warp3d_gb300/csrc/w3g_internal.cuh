@@ -48,6 +48,9 @@ struct BlockDesc {
   long long estiff_off; // sum of utsz*span
   long long einf_off;   // sum of totdof*span (also edest/cdest offset)
   long long geo_off;    // sum of (3*nnode+1)*span*ngp (undeformed-geometry cache)
+  long long hist_off;   // sum of hist*span*ngp (material history)
+  int hist;             // history words per Gauss point (11 mm01, 158 mm10)
+  int mm10_off;         // first mm10 Gauss point of the block (-1: not mm10)
 };
 
 // one work item = up to kRecoverChunk / kTangentChunk [type] consecutive
@@ -58,6 +61,28 @@ struct Chunk {
   int n;      // number of elements
   int type;   // type_slot of the block's element type
 };
+
+// ---- mm10 crystal plasticity (w3g_mm10.cu) -----------------------------
+constexpr int kHistMM10 = 158;     // one fcc crystal, one hardening variable
+constexpr int kSlip = 12;          // fcc slip systems
+constexpr int kMm10Scratch = 25;   // per GP: uddt 6, R(n+1) 9, F(n+1) 9, det F(n+1)
+// per-element crystal data, built on the host at model creation exactly as
+// setup_mm10_rknstr does (src/rknstr.f:1568-2027)
+struct CrystalElem {
+  double C[36];           // elastic stiffness rotated to the reference frame, column-major
+  double ms[kSlip][6];    // sym(b x n) of each slip system, Voigt
+  double qs[kSlip][3];    // skew(b x n) as (w23, w13, w12)
+  double g[9];            // lattice -> reference rotation (rotation_g)
+  double angles[3];       // initial Euler angles, degrees (Kocks)
+  int type;               // crystal definition
+  int pad;
+};
+struct CrystalType {      // scalars of a crystal definition
+  double rate_n, tau_y, tau_v, theta_0, voche_m, iD_v, k_0, burgers;
+  double atol, atol1, rtol, rtol1;
+  int miter, pad;
+};
+void build_crystal_elem(const w3g_crystal& c, int type, const double* angles, CrystalElem& x);
 
 // per-call scalars of recovery, read by the kernels from device memory so
 // that a captured launch sequence can be replayed with new values
@@ -127,13 +152,22 @@ struct DeviceModel {
   int qbar = 1;
   double beta_fact = 1.0;
   int nsm = 0;
-  int nchunks = 0;                          // recovery work items
+  int nchunks = 0;                          // recovery work items (partials)
+  int nrchunks = 0;                         // of these, items of the three element types
   int type_chunk0[kNumTypes] = {0, 0, 0};   // first recovery item of each type
   int type_chunks[kNumTypes] = {0, 0, 0};   // recovery items of each type
   int ntchunks = 0;                         // tangent work items
   int ttype_chunk0[kNumTypes] = {0, 0, 0};
   int ttype_chunks[kNumTypes] = {0, 0, 0};
-  long long ngp_total = 0, cep_total = 0, estiff_total = 0, einf_total = 0, geo_total = 0;
+  long long ngp_total = 0, cep_total = 0, estiff_total = 0, einf_total = 0, geo_total = 0, hist_total = 0;
+  // mm10: recovery items of 8-node bricks with crystal plasticity
+  // (type slot 3 in the recovery chunk list), Gauss points, crystal data
+  int mm10_chunk0 = 0, mm10_chunks = 0;
+  int n_mm10_gp = 0;
+  CrystalElem* xtal = nullptr;
+  CrystalType* xtype = nullptr;
+  int* mm10_gp = nullptr;
+  double dt = 1.0;
   BlockDesc* blocks = nullptr;     // device
   Chunk* chunks = nullptr;         // device, recovery items grouped by type
   Chunk* tchunks = nullptr;        // device, tangent items grouped by type
@@ -173,7 +207,12 @@ struct DeviceState {
   double* ifv_partials = nullptr;  // per CTA of the ifv assembly
   unsigned long long* status = nullptr;  // first det[F] <= 0 point, w3g::bad_point_key order
   IterParams* params = nullptr;
-  int* counters = nullptr;         // work-queue heads: recovery, tangent
+  int* counters = nullptr;         // work-queue heads: recovery, tangent, mm10
+  // mm10 per-GP scratch and scheduling
+  double* mm10_scr = nullptr;      // kMm10Scratch * n_mm10_gp
+  int* mm10_iters = nullptr;       // n_mm10_gp
+  int* mm10_order = nullptr;       // n_mm10_gp, GPs sorted by last iteration count
+  int* mm10_bins = nullptr;        // counting-sort bins
   w3g_recover_info* d_info = nullptr;
   // host-call staging
   double* d_c = nullptr;
@@ -186,6 +225,7 @@ struct DeviceState {
 struct TangentArgs {
   const double* dn[kNumTypes];   // fill_dn_table per element type
   const float* dn32[kNumTypes];  // the same tables rounded to float
+  const double* hist1;           // mm10 blocks take [D] from history1(1:36)
   const BlockDesc* blocks;
   const Chunk* chunks;
   int chunk0;            // work item of blockIdx.x == 0
@@ -229,6 +269,16 @@ struct RecoverArgs {
   int* geo_dirty;
   const IterParams* params;
   double beta_fact;
+  // mm10 blocks
+  const CrystalElem* xtal;   // noelem entries (mm10 elements)
+  const CrystalType* xtype;
+  double* mm10_scr;          // kMm10Scratch per mm10 GP
+  const int* mm10_gp;        // mm10 GP -> (block << 12) | (element << 3) | gp
+  int* mm10_iters;           // local Newton iterations of the last update, per mm10 GP
+  int* mm10_order;           // work-queue order (device counting sort)
+  int* mm10_bins;
+  int* mm10_counter;
+  double dt;
 };
 
 // ---- kernel launchers (defined in the .cu files) -----------------------
@@ -241,13 +291,19 @@ cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c
 // launches of the element kernels under a schedule
 int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc);
 int recover_kernel_launches(const DeviceModel& m, const Schedule& sc);
+// mm10 recovery of the crystal-plasticity items (kinematics, local
+// solves from a work queue sorted by the last iteration counts, forces)
+cudaError_t launch_mm10(const DeviceModel& m, const RecoverArgs& a, cudaStream_t s);
+int mm10_kernel_launches(const DeviceModel& m);
 // one-time kernel attributes (shared-memory opt-in) and occupancies;
 // called at context creation, before any capture
 cudaError_t init_tangent_kernels();
 cudaError_t init_recover_kernels();
+cudaError_t init_mm10_kernels();
 inline cudaError_t init_kernels() {
   cudaError_t e = init_tangent_kernels();
-  return e == cudaSuccess ? init_recover_kernels() : e;
+  if (e == cudaSuccess) e = init_recover_kernels();
+  return e == cudaSuccess ? init_mm10_kernels() : e;
 }
 // resident CTAs per SM of the persistent kernels
 int persistent_tangent_occupancy(bool fp32);
@@ -265,6 +321,8 @@ cudaError_t launch_finalize(const DeviceModel& m, const double* partials, const 
 // the block fails, checking F at n+1 for all elements before F at n+1/2
 // (rstgp1.f:135-145, fcomp1 in gtmat1.f:649-664), and names the first
 // failing element of that check. The smallest key is that point.
+// kind (half_step): 0 det F(n+1) <= 0, 1 det F(n+1/2) <= 0, 2 mm10 local
+// solve failed
 __host__ __device__ inline unsigned long long bad_point_key(int blk, int gp, int half_step, int i) {
   return ((unsigned long long)blk << 40) | ((unsigned long long)gp << 24) | ((unsigned long long)half_step << 20) |
          (unsigned long long)i;

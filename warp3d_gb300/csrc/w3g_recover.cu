@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256) k_finalize(int nchunks, const double* par
     info->plastic_work = s1[0];
     info->sum_ifv = s2[0];
     info->num_term_ifv = num_term;
-    info->material_cut_step = cut ? 1 : 0;
+    info->material_cut_step = cut ? (((st >> 20) & 0xFull) == 2 ? W3G_LOCAL_FAIL : W3G_STEP_CUT) : 0;
     info->first_bad_element = cut ? blocks[st >> 40].felem + (int)(st & 0xFFFFFull) + 1 : 0;
   }
 }
@@ -172,8 +172,8 @@ cudaError_t init_recover_kernels() {
 int persistent_recover_occupancy() { return std::max(1, g_occ); }
 
 int recover_kernel_launches(const DeviceModel& m, const Schedule& sc) {
-  if (sc.mode == W3G_SCHED_PERSISTENT) return m.nchunks > 0 ? 1 : 0;
-  int n = 0;
+  int n = mm10_kernel_launches(m);
+  if (sc.mode == W3G_SCHED_PERSISTENT) return n + (m.nrchunks > 0 ? 1 : 0);
   for (int t = 0; t < kNumTypes; ++t) n += m.type_chunks[t] > 0 ? 1 : 0;
   return n;
 }
@@ -191,15 +191,17 @@ cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c
   k_check_coords<<<nb, 256, 0, s>>>(a.c, c_geo, m.ncoord, a.geo_dirty);
   cudaError_t e = cudaSuccess;
   if (sc.mode == W3G_SCHED_PERSISTENT) {
-    const int occ = persistent_recover_occupancy();
-    const int per_sm = sc.recover_ctas_per_sm > 0 ? std::min(sc.recover_ctas_per_sm, occ) : occ;
-    const int grain = std::max(1, sc.recover_grain);
-    const int need = (m.nchunks + grain - 1) / grain;
-    const int grid = std::max(1, std::min(m.nsm * per_sm, need));
-    WorkQueue q{m.rorder[sc.order == W3G_ORDER_HEAVY_FIRST ? 1 : 0], m.nchunks, grain, counter};
-    e = cudaMemsetAsync(counter, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    k_recover_persistent<<<grid, kRecoverThreads, kRecoverSmem, s>>>(a, q);
+    if (m.nrchunks > 0) {
+      const int occ = persistent_recover_occupancy();
+      const int per_sm = sc.recover_ctas_per_sm > 0 ? std::min(sc.recover_ctas_per_sm, occ) : occ;
+      const int grain = std::max(1, sc.recover_grain);
+      const int need = (m.nrchunks + grain - 1) / grain;
+      const int grid = std::max(1, std::min(m.nsm * per_sm, need));
+      WorkQueue q{m.rorder[sc.order == W3G_ORDER_HEAVY_FIRST ? 1 : 0], m.nrchunks, grain, counter};
+      e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+      if (e != cudaSuccess) return e;
+      k_recover_persistent<<<grid, kRecoverThreads, kRecoverSmem, s>>>(a, q);
+    }
   } else {
     const size_t s8 = sizeof(RecoverSmem<Hex8, 8>), s20 = sizeof(RecoverSmem<Hex20, 2>),
                  s10 = sizeof(RecoverSmem<Tet10, 16>);
@@ -219,6 +221,7 @@ cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c
       k_recover_type<Tet10, 4, 16><<<m.type_chunks[2], kRecoverThreads, s10, s>>>(h);
     }
   }
+  if ((e = launch_mm10(m, a, s)) != cudaSuccess) return e;
   k_commit_coords<<<nb, 256, 0, s>>>(a.c, c_geo, m.ncoord, a.geo_dirty);
   k_clear_dirty<<<1, 1, 0, s>>>(a.geo_dirty);
   return cudaGetLastError();

@@ -103,6 +103,7 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
     const double* du = &sdu[ge][0];
     const bool update_coords = bd.geonl && !(p.step == 1 && p.iter == 0);
     const long long gpi = bd.gp_off + (long long)i * NG + g;
+    const long long hoff = bd.hist_off + ((long long)i * NG + g) * kHistMM01;
 
     // ---- undeformed geometry: dN/dX and det[J] at t = 0 (jacob1 on the
     // initial coordinates inside gtmat1, src/gtmat1.f:59-63). Constant over
@@ -197,12 +198,12 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
 #pragma unroll
     for (int k = 0; k < 6; ++k) eps1[k] = a.eps_n[gpi * 6 + k] + uddt[k];
 #pragma unroll
-    for (int k = 0; k < 11; ++k) hist[k] = a.hist[gpi * kHistMM01 + k];
+    for (int k = 0; k < 11; ++k) hist[k] = a.hist[hoff + k];
 
     // ---- drive_01_update (src/rstgp1.f:614-1034) ----
     if (p.nonlinear) {
-      const long long gpf = bd.gp_off + g;   // block's first element, this GP
-      const double alpha11_first = a.hist[gpf * kHistMM01 + 10];
+      // block's first element, this GP
+      const double alpha11_first = a.hist[bd.hist_off + (long long)g * kHistMM01 + 10];
       mm01_point(mp, p.step, cgn, uddt, hist, alpha11_first, cgn1, hist1, cep21);
     } else {   // drive_01_update_a/_b: linear-elastic [D], sigma = sigma_n + D uddt
 #pragma unroll
@@ -238,7 +239,7 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
         for (int k = 0; k < 9; ++k) a.rot_n1[gpi * 9 + k] = R1[k];
       }
 #pragma unroll
-      for (int k = 0; k < 11; ++k) a.hist1[gpi * kHistMM01 + k] = hist1[k];
+      for (int k = 0; k < 11; ++k) a.hist1[hoff + k] = hist1[k];
     }
 
     // ---- rknifv_std + gpifv1 (src/rknifv.f:141-217, src/gpifv1.f:16-154):
@@ -369,6 +370,7 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
     const double* du = &sdu[ge][0];
     const bool update_coords = bd.geonl && !(p.step == 1 && p.iter == 0);
     const long long gpi = bd.gp_off + (long long)i * NG + g;
+    const long long hoff = bd.hist_off + ((long long)i * NG + g) * kHistMM01;
 
     // undeformed geometry (jacob1 on the initial coordinates), cached
     double* geo = a.geo + bd.geo_off + ((long long)i * NG + g) * GEO;
@@ -449,9 +451,9 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
 #pragma unroll
     for (int k = 0; k < 6; ++k) eps1[k] = a.eps_n[gpi * 6 + k] + uddt[k];
 #pragma unroll
-    for (int k = 0; k < 11; ++k) hist[k] = a.hist[gpi * kHistMM01 + k];
+    for (int k = 0; k < 11; ++k) hist[k] = a.hist[hoff + k];
     if (p.nonlinear) {
-      const double alpha11_first = a.hist[(bd.gp_off + g) * kHistMM01 + 10];
+      const double alpha11_first = a.hist[bd.hist_off + (long long)g * kHistMM01 + 10];
       mm01_point(mp, p.step, cgn, uddt, hist, alpha11_first, cgn1, hist1, cep21);
     } else {
 #pragma unroll
@@ -484,7 +486,7 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
         for (int k = 0; k < 9; ++k) a.rot_n1[gpi * 9 + k] = R1[k];
       }
 #pragma unroll
-      for (int k = 0; k < 11; ++k) a.hist1[gpi * kHistMM01 + k] = hist1[k];
+      for (int k = 0; k < 11; ++k) a.hist1[hoff + k] = hist1[k];
     }
 
     // element forces f_a = P dN_a/dX, P = wf det[J_{n+1}] [T] F1^-T

@@ -44,6 +44,25 @@ __host__ __device__ __forceinline__ constexpr int low(int r, int c) {
   return r >= c ? r * (r + 1) / 2 + c : c * (c + 1) / 2 + r;
 }
 
+// w det[J] [D] of Gauss point gp of element i, lower triangle row-wise:
+// from cep_blocks (extract_D_symmetric, gptns1.f:1174-1266) or, for mm10,
+// from history1(1:36) (drive_10_cnst, gptns1.f:1371-1455; symmetric)
+template <class T, int NG>
+__device__ __forceinline__ void load_D21(const TangentArgs& a, const BlockDesc& bd, int i, int gp, T f, T* C) {
+  if (bd.mat == W3G_MAT_CRYSTAL) {
+    const double* h1 = a.hist1 + bd.hist_off + ((long long)i * NG + gp) * kHistMM10;
+    int k = 0;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c <= r; ++c) C[k++] = f * (T)h1[r + 6 * c];
+  } else {
+    const double* cp = a.cep + bd.cep_off + ((long long)gp * bd.span + i) * 21;
+#pragma unroll
+    for (int k = 0; k < 21; ++k) C[k] = f * (T)cp[k];
+  }
+}
+
 namespace hex8t {
 constexpr int NN = Hex8::NN;
 constexpr int NG = Hex8::NG;
@@ -165,9 +184,7 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
         shape_gradient<T>(gama, dnx[n], dne[n], dnz[n], g[3 * n], g[3 * n + 1], g[3 * n + 2]);
       const T f = w * dj;
       T C[21];
-      const double* cp = a.cep + bd.cep_off + ((long long)gp * bd.span + i) * 21;
-#pragma unroll
-      for (int k = 0; k < 21; ++k) C[k] = f * (T)cp[k];
+      load_D21<T, NG>(a, bd, i, gp, f, C);
       T* D = sD + t * 21;
       T* Tw = sT + t * 6;
       if (bd.geonl) {
@@ -408,9 +425,7 @@ __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cid
         shape_gradient<float>(gama, dnx[n], dne[n], dnz[n], g[3 * n], g[3 * n + 1], g[3 * n + 2]);
       const float f = w * dj;
       float C[21];
-      const double* cp = a.cep + bd.cep_off + ((long long)gp * bd.span + i) * 21;
-#pragma unroll
-      for (int k = 0; k < 21; ++k) C[k] = f * (float)cp[k];
+      load_D21<float, NG>(a, bd, i, gp, f, C);
       float* D = sD + t * 21;
       float* Tw = sT + t * 6;
       if (bd.geonl) {

@@ -69,7 +69,7 @@ class Engine:
         info = abi.RecoverInfo()
         st = self.lib.w3g_recover(self.ctx, step, it, 1 if extrapolated else 0, dptr(c), dptr(u), dptr(du),
                                   dptr(ifv) if ifv is not None else None, C.byref(info))
-        abi.check(self.lib, st, allow=(abi.OK, abi.STEP_CUT))
+        abi.check(self.lib, st, allow=(abi.OK, abi.STEP_CUT, abi.LOCAL_FAIL))
         return st, info
 
     def update(self):
@@ -112,7 +112,7 @@ class Engine:
     def recover_info(self):
         info = abi.RecoverInfo()
         st = self.lib.w3g_recover_info_get(self.ctx, C.byref(info))
-        abi.check(self.lib, st, allow=(abi.OK, abi.STEP_CUT))
+        abi.check(self.lib, st, allow=(abi.OK, abi.STEP_CUT, abi.LOCAL_FAIL))
         return st, info
 
     def estiff_device(self):
