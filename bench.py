@@ -27,6 +27,15 @@ batched: the batching-form workload -- about 1M elements in blocks of
         per step through w3g_iteration_dev (graph replay), FP64 and with
         the FP32 tangent, each under the schedule w3g_autotune picks, next
         to the per-type launches without a graph.
+crystal: mm10 crystal plasticity -- 32^3 8-node bricks (32,768 elements,
+        262,144 Gauss points), one fcc crystal per Gauss point with Euler
+        angles uniform on SO(3) (PCG64), Voce hardening (tau_y 90, tau_v
+        200, theta_0 500 MPa, rate exponent 20); the state after 1%
+        homogeneous tension in 10 steps; one Newton iteration of element
+        work per step (graph replay), FP64 and with the FP32 tangent, the
+        local Newton iteration counts per Gauss point, the work queue
+        sorted by the previous counts vs in natural order, and the oracle
+        on a bounded sample of the same blocks.
 """
 from __future__ import annotations
 
@@ -88,6 +97,8 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-elems", type=int, default=1_000_000, help="target elements of the batched workload")
+    ap.add_argument("--no-crystal", action="store_true")
+    ap.add_argument("--crystal-n", type=int, default=32, help="elements per cube edge of the mm10 workload")
     return ap.parse_args()
 
 
@@ -218,6 +229,118 @@ def bench_batched(args, dev, local):
            "model_build_s": t_build, **out}
     eng.close()
     return res
+
+
+def bench_crystal(args, dev, local, with_cpu):
+    """mm10 line: 1% tension in 10 homogeneous steps, then timed iterations."""
+    import torch
+    import oracle
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+    from warp3d_gb300.model import Crystal, Model, cube_mesh, random_orientations
+    n = args.crystal_n
+    coords, incid = cube_mesh(n)
+    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(n ** 3, 4242), dt=1.0)
+    ne = model.noelem
+    X = coords
+    strain = lambda k: ((np.diag([-0.0005 * k, -0.0005 * k, 0.001 * k])) @ X.T).T.ravel()   # k x 0.1%
+    eng = Engine(model, device=local)
+    tc = torch.from_numpy(model.c).to(dev)
+    tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+    # 1% tension in steps of 0.1%; a step whose local solves fail at some
+    # Gauss point (status W3G_LOCAL_FAIL) is cut in half and retried, as
+    # WARP3D's adaptive step control does with material_cut_step
+    t0 = time.perf_counter()
+    level, h, step, cuts = 0.0, 1.0, 0, 0
+    while level < 10.0 - 1e-9:
+        h = min(h, 10.0 - level)
+        tu = torch.from_numpy(strain(level)).to(dev)
+        tdu = torch.from_numpy(strain(level + h) - strain(level)).to(dev)
+        with torch.cuda.stream(stream):
+            eng.recover_dev(step + 1, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), sh)
+        torch.cuda.synchronize()
+        st, _ = eng.recover_info()
+        if st != 0:
+            h *= 0.5
+            cuts += 1
+            if h < 1e-3:
+                eng.close()
+                return {"error": f"load level {level}: status {st} after {cuts} cuts"}
+            continue
+        eng.update()
+        step += 1
+        level += h
+        h = min(1.0, 2.0 * h)
+    t_load = time.perf_counter() - t0
+    rng = np.random.Generator(np.random.PCG64(11))
+    u = strain(level)
+    h_last = 0.25
+    du = strain(level + h_last) - strain(level) + rng.normal(0.0, 1e-7, model.nodof)
+    tu = torch.from_numpy(u).to(dev)
+    tdu = torch.from_numpy(du).to(dev)
+    p = (tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr())
+    both = abi.ITER_RECOVER | abi.ITER_TANGENT
+
+    def timed(what, steps):
+        with torch.cuda.stream(stream):
+            for _ in range(max(2, args.warmup)):
+                eng.iteration_dev(step + 1, 1, False, what, *p, sh)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches = 0
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                eng.iteration_dev(step + 1, 1, False, what, *p, sh)
+                launches += eng.last_launch_count()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        assert eng.recover_info()[0] == 0
+        return e0.elapsed_time(e1) / steps, launches
+
+    steps = max(3, args.steps // 2)
+    out = {}
+    for order in (abi.ORDER_BLOCKS, abi.ORDER_HEAVY_FIRST):
+        eng.set_schedule(mode=abi.SCHED_PER_TYPE, order=order)
+        ms_rec, _ = timed(abi.ITER_RECOVER, steps)
+        out["recovery_ms_" + ("natural_order" if order == abi.ORDER_BLOCKS else "sorted_queue")] = ms_rec
+    its = eng.local_iterations()
+    for name, prec in (("plain_fp64", abi.TANGENT_FP64), ("mixed", abi.TANGENT_FP32)):
+        eng.set_precision(prec)
+        ms, launches = timed(both, steps)
+        out[name] = {"value": ne / (ms * 1e-3), "ms_per_step": ms, "gpu_launches": launches}
+    out["mixed"]["speedup_vs_plain"] = out["plain_fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    hist = np.bincount(its, minlength=1)
+    out["local_newton_iterations"] = {"min": int(its.min()), "mean": float(its.mean()), "max": int(its.max()),
+                                      "p99": float(np.percentile(its, 99)),
+                                      "histogram": {int(k): int(v) for k, v in enumerate(hist) if v}}
+    if with_cpu:
+        # the oracle on the first 16 blocks (2,048 elements) of the same state
+        st = model.new_state()
+        eng.download(st)
+        nb = min(16, model.nelblk)
+        sub = Model(coords, model.incid[:nb * 128], materials=[Crystal()], angles=model.elem_angles[:nb * 128], dt=1.0)
+        sst = sub.new_state()
+        for name in sst.NAMES:
+            setattr(sst, name, [a.copy() for a in getattr(st, name)[:nb]])
+        ora = oracle.Oracle(sub, state=sst, threads=host_threads())
+        ifv = np.zeros(model.nodof)
+        est = sub.estiff_blocks()
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            ora.recover(step + 1, 1, False, model.c, u, du, ifv)
+            ora.tanstf(step + 1, 1, model.c, u, du, est)
+        t_cpu = (time.perf_counter() - t0) / reps
+        out["cpu_baseline"] = {"value": sub.noelem / t_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
+                               "sample": f"{sub.noelem} elements ({nb} blocks of 128) of the same state, {reps} iterations"}
+    eng.close()
+    return {"workload": f"{n}^3 hex8 l3disop geonl, mm10 fcc Voce (tau_y 90, tau_v 200, theta_0 500 MPa, n 20), "
+                        "random orientations, state after 1% tension in 10 steps",
+            "elements": ne, "gauss_points": ne * 8, "load_s": t_load, "load_steps": step, "step_cuts": cuts,
+            "timed_increment": f"{0.1 * h_last:.3f}% axial strain (+ noise 1e-7)", **out}
 
 
 def sample_clocks():
@@ -484,6 +607,12 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.n, args.cpu_sample_blocks, host_threads())
 
+    crystal = None
+    if not args.no_crystal:
+        eng.close()
+        torch.cuda.empty_cache()
+        crystal = bench_crystal(args, dev, local, rank == 0 and not args.no_cpu_baseline)
+
     batched = None
     if not args.no_batched:
         eng.close()
@@ -502,7 +631,7 @@ def main():
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "tangent_ms": tan64, "recovery_ms": rec64,
             "mixed": mixed, "e2e": e2e, "roofline": roofline, "cpu_baseline": cb, "clocks": clocks,
-            "gpu_launches": launches64, "batched": batched,
+            "gpu_launches": launches64, "batched": batched, "crystal": crystal,
         }
         print(json.dumps(line), flush=True)
     eng.close()

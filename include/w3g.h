@@ -260,6 +260,12 @@ int w3g_iteration_dev(w3g_context* ctx, int step, int iter, int extrapolated_du,
                       const void* d_c, const void* d_u, const void* d_du, void* d_ifv,
                       void* stream);
 
+/* mm10 Gauss points: local Newton iterations of the last recovery, in
+   block / element / Gauss-point order (n = number of mm10 Gauss points).
+   The persistent mm10 kernel orders its work queue by these counts
+   (W3G_ORDER_HEAVY_FIRST) so that a warp's lanes get similar counts. */
+int w3g_local_iterations(w3g_context* ctx, int* counts, int n);
+
 /* Autotuner: times candidate schedules (launch mode, persistent CTAs per
    SM, queue grain, item order) on this model with the given inputs,
    recovery and tangent separately, `reps` timed runs each, and keeps the

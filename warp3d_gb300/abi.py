@@ -153,6 +153,7 @@ PROTOTYPES = [
     ("w3g_assemble_ifv_noalloc", C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, _vp, _vp,
                                            _vp, _vp, _vp]),
     ("w3g_set_schedule", C.c_int, [_vp, C.POINTER(Schedule)]),
+    ("w3g_local_iterations", C.c_int, [_vp, C.POINTER(C.c_int), C.c_int]),
     ("w3g_get_schedule", C.c_int, [_vp, C.POINTER(Schedule)]),
     ("w3g_iteration_dev", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("w3g_autotune", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int,

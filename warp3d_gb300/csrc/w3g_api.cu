@@ -66,7 +66,7 @@ void free_all(w3g_context* c) {
   void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
                   m.cdest, m.mat, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
                   m.ifv_rowptr, m.ifv_src, s.params, s.counters, m.xtal, m.xtype, m.mm10_gp, s.mm10_scr,
-                  s.mm10_iters, s.mm10_order, s.mm10_bins,
+                  s.mm10_iters, s.mm10_order, s.mm10_ident, s.mm10_bins,
                   s.geo, s.c_geo, s.geo_dirty,
                   s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
                   s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
@@ -201,6 +201,8 @@ int enqueue_recover(w3g_context* c, const double* d_c, const double* d_u, const 
   a.mm10_gp = c->m.mm10_gp;
   a.mm10_iters = c->s.mm10_iters;
   a.mm10_order = c->s.mm10_order;
+  a.mm10_ident = c->s.mm10_ident;
+  a.mm10_sorted = c->sched.order == W3G_ORDER_HEAVY_FIRST ? 1 : 0;
   a.mm10_bins = c->s.mm10_bins;
   a.mm10_counter = c->s.counters + 2;
   a.dt = c->m.dt;
@@ -489,6 +491,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     AL(s.mm10_scr, (long long)kMm10Scratch * n_mm10_gp);
     AL(s.mm10_iters, n_mm10_gp);
     AL(s.mm10_order, n_mm10_gp);
+    AL(s.mm10_ident, n_mm10_gp);
     AL(s.mm10_bins, 128);
   }
   AL(m.edest, einf);
@@ -546,6 +549,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     UP(m.xtal, xtal.data(), md->noelem);
     UP(m.xtype, xtype.data(), md->ncrystals);
     UP(m.mm10_gp, mm10_gp.data(), n_mm10_gp);
+    for (int k = 0; k < n_mm10_gp; ++k) mm10_gp[k] = k;   // reused as the natural order
+    UP(s.mm10_ident, mm10_gp.data(), n_mm10_gp);
   }
   for (int t = 0; t < kNumTypes; ++t) {
     UP(m.dn[t], dnt[t].data(), dnt[t].size());
@@ -962,6 +967,16 @@ int w3g_autotune(w3g_context* c, int step, int iter, int extrapolated_du, const 
   CK(cudaStreamSynchronize(st));
   if (best) *best = to_abi(chosen);
   if (best_ms) *best_ms = total_best;
+  return 0;
+}
+
+int w3g_local_iterations(w3g_context* c, int* counts, int n) {
+  if (!c || (!counts && n > 0)) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  if (n != c->m.n_mm10_gp) return fail(W3G_EARG, "count array length must equal the mm10 Gauss points");
+  if (n == 0) return 0;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy(counts, c->s.mm10_iters, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost));
   return 0;
 }
 

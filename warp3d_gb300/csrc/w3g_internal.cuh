@@ -212,6 +212,7 @@ struct DeviceState {
   double* mm10_scr = nullptr;      // kMm10Scratch * n_mm10_gp
   int* mm10_iters = nullptr;       // n_mm10_gp
   int* mm10_order = nullptr;       // n_mm10_gp, GPs sorted by last iteration count
+  int* mm10_ident = nullptr;       // n_mm10_gp, natural order
   int* mm10_bins = nullptr;        // counting-sort bins
   w3g_recover_info* d_info = nullptr;
   // host-call staging
@@ -276,6 +277,8 @@ struct RecoverArgs {
   const int* mm10_gp;        // mm10 GP -> (block << 12) | (element << 3) | gp
   int* mm10_iters;           // local Newton iterations of the last update, per mm10 GP
   int* mm10_order;           // work-queue order (device counting sort)
+  const int* mm10_ident;     // natural order (W3G_ORDER_BLOCKS)
+  int mm10_sorted;           // 1: sort by last iteration count
   int* mm10_bins;
   int* mm10_counter;
   double dt;
@@ -294,7 +297,7 @@ int recover_kernel_launches(const DeviceModel& m, const Schedule& sc);
 // mm10 recovery of the crystal-plasticity items (kinematics, local
 // solves from a work queue sorted by the last iteration counts, forces)
 cudaError_t launch_mm10(const DeviceModel& m, const RecoverArgs& a, cudaStream_t s);
-int mm10_kernel_launches(const DeviceModel& m);
+int mm10_kernel_launches(const DeviceModel& m, bool sorted);
 // one-time kernel attributes (shared-memory opt-in) and occupancies;
 // called at context creation, before any capture
 cudaError_t init_tangent_kernels();

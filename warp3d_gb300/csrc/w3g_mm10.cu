@@ -168,21 +168,19 @@ struct Nstate {   // crystal state n (mm10_copy_cc_hist)
   double R[9], Rp[9], D[6], stress[6], tt, tt_rate;
 };
 
-struct Pt {       // state of a solve (np1 or curr): rotated tensors and rates
+// lattice tensors of the current solve (mm10_setup): Schmid tensors and
+// spins rotated by the plastic rotation at n and R(n+1); shared by the
+// full-step state and the sub-step states (same R, same n)
+struct Geo {
   double ms[NS][6];
   double qc[NS][3];
-  double D[6];
-  double dg, tinc, tt_rate, mu_harden;
 };
 
-__device__ __forceinline__ double rs_of(const Pt& q, const double* s, int i) {
-  return s[0] * q.ms[i][0] + s[1] * q.ms[i][1] + s[2] * q.ms[i][2] + s[3] * q.ms[i][3] + s[4] * q.ms[i][4] +
-         s[5] * q.ms[i][5];
-}
-__device__ __forceinline__ double slipinc_of(const CrystalType& t, const Pt& q, const double* s, double tt, int i) {
-  const double rs = rs_of(q, s, i);
-  return q.dg / tt * pow(fabs(rs / tt), t.rate_n - 1.0) * rs;
-}
+// strain increment and rates of a solve (np1 or a sub-step)
+struct Rate {
+  double D[6];
+  double dg, tinc, tt_rate;
+};
 
 __device__ void symsw(const double* s, const double* w, double* sw) {
   sw[0] = s[3] * w[2] - s[5] * w[1];
@@ -200,140 +198,149 @@ __device__ __forceinline__ void cmul(const double* C, const double* c, double* a
     for (int r = 0; r < 6; ++r) a[r] = a[r] + C[r + 6 * j] * c[j];
 }
 
-// spin w_p in the current configuration (mm10_form_wp)
-__device__ void form_wp(const CrystalType& t, const Pt& q, const double* s, double tt, double* w) {
-  w[0] = 0.0; w[1] = 0.0; w[2] = 0.0;
+// resolved shears and slip increments of all systems (mm10_rs,
+// mm10_slipinc): computed once per evaluation point and reused by every
+// term that the reference evaluates at that point
+__device__ __forceinline__ void slip_terms(const CrystalType& t, const Geo& G, const Rate& q, const double* s,
+                                           double tt, double* rs, double* sl) {
   for (int i = 0; i < NS; ++i) {
-    const double sl = slipinc_of(t, q, s, tt, i);
-    for (int k = 0; k < 3; ++k) w[k] = w[k] + sl * q.qc[i][k];
-    const double rs = rs_of(q, s, i);
-    for (int k = 0; k < 3; ++k) w[k] = w[k] + rs * q.tinc * t.iD_v * q.qc[i][k];
+    rs[i] = s[0] * G.ms[i][0] + s[1] * G.ms[i][1] + s[2] * G.ms[i][2] + s[3] * G.ms[i][3] + s[4] * G.ms[i][4] +
+            s[5] * G.ms[i][5];
+    sl[i] = q.dg / tt * pow(fabs(rs[i] / tt), t.rate_n - 1.0) * rs[i];
   }
 }
 
-// R1 (mm10_formR1 with mm10_form_dbarp / mm10_form_wp)
-__device__ void formR1(const CrystalElem& x, const CrystalType& t, const Pt& q, const Nstate& n, const double* s,
-                       double tt, double* R1) {
+// spin w_p in the current configuration (mm10_form_wp)
+__device__ __forceinline__ void form_wp(const CrystalType& t, const Geo& G, const Rate& q, const double* rs,
+                                        const double* sl, double* w) {
+  w[0] = 0.0; w[1] = 0.0; w[2] = 0.0;
+  for (int i = 0; i < NS; ++i) {
+    for (int k = 0; k < 3; ++k) w[k] = w[k] + sl[i] * G.qc[i][k];
+    for (int k = 0; k < 3; ++k) w[k] = w[k] + rs[i] * q.tinc * t.iD_v * G.qc[i][k];
+  }
+}
+
+// R1 (mm10_formR1 with mm10_form_dbarp / mm10_form_wp) from slip terms
+__device__ void formR1(const CrystalElem& x, const CrystalType& t, const Geo& G, const Rate& q, const Nstate& n,
+                       const double* s, const double* rs, const double* sl, double* R1) {
   double dbarp[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, wp[3], symTW[6], wv1[6], wv2[6];
   for (int i = 0; i < NS; ++i) {
-    const double sl = slipinc_of(t, q, s, tt, i);
-    const double rs = rs_of(q, s, i);
-    const double f = rs * q.tinc * t.iD_v + sl;
-    for (int k = 0; k < 6; ++k) dbarp[k] = dbarp[k] + f * q.ms[i][k];
+    const double f = rs[i] * q.tinc * t.iD_v + sl[i];
+    for (int k = 0; k < 6; ++k) dbarp[k] = dbarp[k] + f * G.ms[i][k];
   }
-  form_wp(t, q, s, tt, wp);
+  form_wp(t, G, q, rs, sl, wp);
   symsw(s, wp, symTW);
   for (int k = 0; k < 6; ++k) wv1[k] = q.D[k] - dbarp[k];
   cmul(x.C, wv1, wv2);
   for (int k = 0; k < 6; ++k) R1[k] = s[k] - n.stress[k] - wv2[k] + 2.0 * symTW[k];
 }
 
-// R2 (mm10_formR2 with mm10_h_voche); sets q.tt_rate
-__device__ double formR2(const CrystalType& t, Pt& q, const Nstate& n, const double* s, double tt) {
+// R2 (mm10_formR2 with mm10_h_voche); sets q.tt_rate. The hardening term
+// h_term = 1 - (tt - tau_y)/tau_v + tau_l/(tt - tau_y) is the same for all
+// systems (tau_l = 0: no lattice-curvature data in this scope)
+__device__ double formR2(const CrystalType& t, Rate& q, const Nstate& n, const double* sl, double tt) {
+  const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
+  const double ph = pow(fabs(h_term), t.voche_m) * sgn1(h_term);
   double h = 0.0;
-  for (int i = 0; i < NS; ++i) {
-    const double sl = slipinc_of(t, q, s, tt, i);
-    const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
-    h = h + pow(fabs(h_term), t.voche_m) * sgn1(h_term) * fabs(sl);
-  }
+  for (int i = 0; i < NS; ++i) h = h + ph * fabs(sl[i]);
   h = n.tt + t.theta_0 * h;
   q.tt_rate = (h - n.tt) / q.tinc;
   return tt - h;
 }
 
-__device__ void symtq_i(const double* s, const double* w, double* sw) { symsw(s, w, sw); }
+// residual of the predictor (R1 only) and of the coupled update (R1, R2)
+__device__ __noinline__ void eval_R1(const CrystalElem& x, const CrystalType& t, const Geo& G, const Rate& q,
+                                        const Nstate& n, const double* s, double tt, double* R1) {
+  double rs[NS], sl[NS];
+  slip_terms(t, G, q, s, tt, rs, sl);
+  formR1(x, t, G, q, n, s, rs, sl, R1);
+}
+__device__ __noinline__ void eval_R(const CrystalElem& x, const CrystalType& t, const Geo& G, Rate& q,
+                                       const Nstate& n, const double* xv, double* R) {
+  double rs[NS], sl[NS];
+  slip_terms(t, G, q, xv, xv[6], rs, sl);
+  formR1(x, t, G, q, n, xv, rs, sl, R);
+  R[6] = formR2(t, q, n, sl, xv[6]);
+}
 
-// J11 (mm10_formJ11 with mm10_dgdt_voche, mm10_iw)
-__device__ void formJ11(const CrystalElem& x, const CrystalType& t, const Pt& q, const double* s, double tt,
-                        double* J11) {
-  for (int k = 0; k < 36; ++k) J11[k] = 0.0;
+// J11 (mm10_formJ11 with mm10_dgdt_voche and mm10_iw), optionally with
+// J12, J21, J22 of mm10_formJ into the 7x7 J (the reference's J22 keeps
+// its sign(one, slipinc) factor in the rate term); ld = 6 or 7
+template <bool kFull>
+__device__ __noinline__ void formJ(const CrystalElem& x, const CrystalType& t, const Geo& G, const Rate& q, const double* s,
+                      double tt, double* J) {
+  constexpr int ld = kFull ? 7 : 6;
+  double rs[NS], sl[NS];
+  slip_terms(t, G, q, s, tt, rs, sl);
+  for (int c = 0; c < 6; ++c)
+    for (int r = 0; r < 6; ++r) J[r + ld * c] = 0.0;
+  const double A = q.dg * t.rate_n / pow(tt, t.rate_n);
+  const double B = -t.rate_n / tt;
+  double J12[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = 0; i < NS; ++i) {
     double sw[6], wv[6];
-    symtq_i(s, q.qc[i], sw);
-    const double rs = rs_of(q, s, i);
-    double d = pow(fabs(rs), t.rate_n - 1.0);
-    d = q.dg * t.rate_n / pow(tt, t.rate_n) * d;
+    symsw(s, G.qc[i], sw);
+    double d = pow(fabs(rs[i]), t.rate_n - 1.0);
+    d = A * d;
     d = d + q.tinc * t.iD_v;
     for (int r = 0; r < 6; ++r) wv[r] = 2.0 * sw[r];
     for (int j = 0; j < 6; ++j)
-      for (int r = 0; r < 6; ++r) wv[r] = wv[r] + x.C[r + 6 * j] * q.ms[i][j];
+      for (int r = 0; r < 6; ++r) wv[r] = wv[r] + x.C[r + 6 * j] * G.ms[i][j];
     for (int c = 0; c < 6; ++c) {
-      const double temp = d * q.ms[i][c];
+      const double temp = d * G.ms[i][c];
       if (temp != 0.0)
-        for (int r = 0; r < 6; ++r) J11[r + 6 * c] = J11[r + 6 * c] + wv[r] * temp;
+        for (int r = 0; r < 6; ++r) J[r + ld * c] = J[r + ld * c] + wv[r] * temp;
+    }
+    if (kFull) {
+      const double temp = 1.0 * (B * sl[i]);
+      if (temp != 0.0)
+        for (int r = 0; r < 6; ++r) J12[r] = J12[r] + wv[r] * temp;
     }
   }
   double w[3];
-  form_wp(t, q, s, tt, w);
-  // mm10_iw
-  J11[0 + 6 * 3] = J11[0 + 6 * 3] + 2.0 * w[2];
-  J11[0 + 6 * 5] = J11[0 + 6 * 5] + (-2.0 * w[1]);
-  J11[1 + 6 * 3] = J11[1 + 6 * 3] + 2.0 * w[2];
-  J11[1 + 6 * 4] = J11[1 + 6 * 4] + (-2.0 * w[0]);
-  J11[2 + 6 * 4] = J11[2 + 6 * 4] + 2.0 * w[0];
-  J11[2 + 6 * 5] = J11[2 + 6 * 5] + 2.0 * w[1];
-  J11[3 + 6 * 0] = J11[3 + 6 * 0] + w[2];
-  J11[3 + 6 * 1] = J11[3 + 6 * 1] + (-w[2]);
-  J11[3 + 6 * 4] = J11[3 + 6 * 4] + (-w[1]);
-  J11[3 + 6 * 5] = J11[3 + 6 * 5] + w[0];
-  J11[4 + 6 * 1] = J11[4 + 6 * 1] + w[0];
-  J11[4 + 6 * 2] = J11[4 + 6 * 2] + (-w[0]);
-  J11[4 + 6 * 3] = J11[4 + 6 * 3] + w[1];
-  J11[4 + 6 * 5] = J11[4 + 6 * 5] + w[2];
-  J11[5 + 6 * 0] = J11[5 + 6 * 0] + w[1];
-  J11[5 + 6 * 2] = J11[5 + 6 * 2] + (-w[1]);
-  J11[5 + 6 * 3] = J11[5 + 6 * 3] + w[0];
-  J11[5 + 6 * 4] = J11[5 + 6 * 4] + (-w[2]);
-  for (int k = 0; k < 6; ++k) J11[k + 6 * k] = J11[k + 6 * k] + 1.0;
-}
-
-// the full 7x7 Jacobian (mm10_formJ): J11, J12 (dgdh_voche), J21
-// (-estress_voche), J22 (ehard_voche, with the reference's
-// sign(one, slipinc) factor in its rate term)
-__device__ void formJ(const CrystalElem& x, const CrystalType& t, const Pt& q, const double* xv, double* J) {
-  const double tt = xv[6];
-  double J11[36];
-  formJ11(x, t, q, xv, tt, J11);
-  for (int c = 0; c < 6; ++c)
-    for (int r = 0; r < 6; ++r) J[r + 7 * c] = J11[r + 6 * c];
-  double J12[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int i = 0; i < NS; ++i) {
-    double sw[6], tm[6];
-    symtq_i(xv, q.qc[i], sw);
-    const double dgam = slipinc_of(t, q, xv, tt, i);
-    const double dgdtt = -t.rate_n / tt * dgam;
-    for (int r = 0; r < 6; ++r) tm[r] = 2.0 * sw[r];
-    for (int j = 0; j < 6; ++j)
-      for (int r = 0; r < 6; ++r) tm[r] = tm[r] + x.C[r + 6 * j] * q.ms[i][j];
-    const double temp = 1.0 * dgdtt;
-    if (temp != 0.0)
-      for (int r = 0; r < 6; ++r) J12[r] = J12[r] + tm[r] * temp;
-  }
+  form_wp(t, G, q, rs, sl, w);
+  J[0 + ld * 3] = J[0 + ld * 3] + 2.0 * w[2];
+  J[0 + ld * 5] = J[0 + ld * 5] + (-2.0 * w[1]);
+  J[1 + ld * 3] = J[1 + ld * 3] + 2.0 * w[2];
+  J[1 + ld * 4] = J[1 + ld * 4] + (-2.0 * w[0]);
+  J[2 + ld * 4] = J[2 + ld * 4] + 2.0 * w[0];
+  J[2 + ld * 5] = J[2 + ld * 5] + 2.0 * w[1];
+  J[3 + ld * 0] = J[3 + ld * 0] + w[2];
+  J[3 + ld * 1] = J[3 + ld * 1] + (-w[2]);
+  J[3 + ld * 4] = J[3 + ld * 4] + (-w[1]);
+  J[3 + ld * 5] = J[3 + ld * 5] + w[0];
+  J[4 + ld * 1] = J[4 + ld * 1] + w[0];
+  J[4 + ld * 2] = J[4 + ld * 2] + (-w[0]);
+  J[4 + ld * 3] = J[4 + ld * 3] + w[1];
+  J[4 + ld * 5] = J[4 + ld * 5] + w[2];
+  J[5 + ld * 0] = J[5 + ld * 0] + w[1];
+  J[5 + ld * 2] = J[5 + ld * 2] + (-w[1]);
+  J[5 + ld * 3] = J[5 + ld * 3] + w[0];
+  J[5 + ld * 4] = J[5 + ld * 4] + (-w[2]);
+  for (int k = 0; k < 6; ++k) J[k + ld * k] = J[k + ld * k] + 1.0;
+  if (!kFull) return;
   for (int r = 0; r < 6; ++r) J[r + 7 * 6] = J12[r];
+  const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
+  const double phm = pow(fabs(h_term), t.voche_m);
+  const double ph = phm * sgn1(h_term);
   double et[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = 0; i < NS; ++i) {
-    const double rs = rs_of(q, xv, i);
-    const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
-    const double f = pow(fabs(h_term), t.voche_m) * sgn1(h_term) * pow(fabs(rs), t.rate_n - 2.0) * rs;
-    for (int k = 0; k < 6; ++k) et[k] = et[k] + f * q.ms[i][k];
+    const double f = ph * pow(fabs(rs[i]), t.rate_n - 2.0) * rs[i];
+    for (int k = 0; k < 6; ++k) et[k] = et[k] + f * G.ms[i][k];
   }
   const double fe = t.theta_0 * q.dg * t.rate_n / pow(tt, t.rate_n);
   for (int c = 0; c < 6; ++c) J[6 + 7 * c] = -(fe * et[c]);
+  const double dd = tt - t.tau_y;
+  const double dh = t.voche_m * (-1.0 / t.tau_v - 0.0 / (dd * dd));
   double etau = 0.0;
-  for (int i = 0; i < NS; ++i) {
-    const double sl = slipinc_of(t, q, xv, tt, i);
-    const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
-    const double d = tt - t.tau_y;
-    etau = etau + (t.voche_m * (-1.0 / t.tau_v - 0.0 / (d * d)) * fabs(sl) / fabs(h_term) -
-                   fabs(sl) * t.rate_n / tt * sgn1(h_term) * sgn1(sl)) *
-                      pow(fabs(h_term), t.voche_m);
-  }
+  for (int i = 0; i < NS; ++i)
+    etau = etau + (dh * fabs(sl[i]) / fabs(h_term) - fabs(sl[i]) * t.rate_n / tt * sgn1(h_term) * sgn1(sl[i])) * phm;
   etau = t.theta_0 * etau;
   J[6 + 7 * 6] = 1.0 - etau;
 }
 
 // partial-pivot LU solve (the oracle's DGESV restatement), n <= 7
-__device__ void lu_solve(int n, double* a, double* b, int nrhs) {
+__device__ __noinline__ void lu_solve(int n, double* a, double* b, int nrhs) {
   int ipiv[7];
   for (int j = 0; j < n; ++j) {
     int jp = j;
@@ -414,15 +421,8 @@ __device__ __forceinline__ void m3vec(const double* b, const double* c, double* 
   for (int r = 0; r < 3; ++r) a[r] = b[r] * c[0] + b[r + 3] * c[1] + b[r + 6] * c[2];
 }
 
-// mm10_setup_np1 + mm10_setup for a solve with strain increment D
-__device__ void setup(const CrystalElem& x, const CrystalType& t, const Nstate& n, const double* R,
-                      const double* D, double tinc, Pt& q) {
-  for (int k = 0; k < 6; ++k) q.D[k] = D[k];
-  q.tinc = tinc;
-  q.tt_rate = 0.0;
-  const double t1 = q.D[0] * q.D[0] + q.D[1] * q.D[1] + q.D[2] * q.D[2];
-  const double t2 = q.D[3] * q.D[3] + q.D[4] * q.D[4] + q.D[5] * q.D[5];
-  q.dg = sqrt((2.0 / 3.0) * (t1 + 0.5 * t2));
+// mm10_setup: lattice tensors for R(n+1) and the plastic rotation at n
+__device__ void setup_geo(const CrystalElem& x, const Nstate& n, const double* R, Geo& G) {
   double tr[9], RE[36], RWC[9], work[9];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) tr[i + 3 * j] = n.Rp[j + 3 * i];
@@ -430,17 +430,26 @@ __device__ void setup(const CrystalElem& x, const CrystalType& t, const Nstate& 
   m3mul(R, tr, work);
   rt2rvw(work, RWC);
   for (int i = 0; i < NS; ++i) {
-    cmul(RE, x.ms[i], q.ms[i]);
-    m3vec(RWC, x.qs[i], q.qc[i]);
+    cmul(RE, x.ms[i], G.ms[i]);
+    m3vec(RWC, x.qs[i], G.qc[i]);
   }
-  q.mu_harden = x.C[5 + 6 * 5];
+}
+
+// mm10_setup_np1 + the effective strain increment of mm10_setup
+__device__ __forceinline__ void setup_rate(const double* D, double tinc, Rate& q) {
+  for (int k = 0; k < 6; ++k) q.D[k] = D[k];
+  q.tinc = tinc;
+  q.tt_rate = 0.0;
+  const double t1 = q.D[0] * q.D[0] + q.D[1] * q.D[1] + q.D[2] * q.D[2];
+  const double t2 = q.D[3] * q.D[3] + q.D[4] * q.D[4] + q.D[5] * q.D[5];
+  q.dg = sqrt((2.0 / 3.0) * (t1 + 0.5 * t2));
 }
 
 // mm10_solve: predictor (stress with extrapolated hardening) then the
 // coupled Newton with line search; J gets the last Jacobian. Returns
 // false on failure; *iters accumulates the Newton iterations.
-__device__ bool solve(const CrystalElem& x, const CrystalType& t, Pt& q, const Nstate& n, double* stress,
-                      double& tt, double dtinc, double* J, int* iters) {
+__device__ __noinline__ bool solve(const CrystalElem& x, const CrystalType& t, const Geo& G, Rate& q, const Nstate& n,
+                      double* stress, double& tt, double dtinc, double* J, int* iters) {
   const double c = 1.0e-4, red = 0.5;
   const int mls = 10, mmin = 1;
   double xv[7];
@@ -469,12 +478,12 @@ __device__ bool solve(const CrystalElem& x, const CrystalType& t, Pt& q, const N
     t2 = d1[3] * d2[3] + d1[4] * d2[4] + d1[5] * d2[5];
     const double cos_ang = fmax(t1 + t2, 0.0);
     const double x2 = xv[6] + cos_ang * n.tt_rate * dtinc;
-    formR1(x, t, q, n, x1, x2, R1);
+    eval_R1(x, t, G, q, n, x1, x2, R1);
     double nR1 = sqrt(R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2] + R1[3] * R1[3] + R1[4] * R1[4] + R1[5] * R1[5]);
     inR1 = nR1;
     while (nR1 > t.atol1 && nR1 / inR1 > t.rtol1) {
       double J11[36], mJ[36], dx1[6], wv[6], xn[6];
-      formJ11(x, t, q, x1, x2, J11);
+      formJ<false>(x, t, G, q, x1, x2, J11);
       for (int k = 0; k < 6; ++k) dx1[k] = R1[k];
       for (int k = 0; k < 36; ++k) mJ[k] = -J11[k];
       lu_solve(6, mJ, dx1, 1);
@@ -490,7 +499,7 @@ __device__ bool solve(const CrystalElem& x, const CrystalType& t, Pt& q, const N
       for (;;) {
         const double nlsx = ls1 + ls2 * alpha;
         for (int k = 0; k < 6; ++k) xn[k] = x1[k] + alpha * dx1[k];
-        formR1(x, t, q, n, xn, x2, R1);
+        eval_R1(x, t, G, q, n, xn, x2, R1);
         dotR1 = R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2] + R1[3] * R1[3] + R1[4] * R1[4] + R1[5] * R1[5];
         nR1 = sqrt(dotR1);
         const double nRs = 0.5 * dotR1;
@@ -513,15 +522,14 @@ __device__ bool solve(const CrystalElem& x, const CrystalType& t, Pt& q, const N
   {
     int iter = 0;
     double R[7], dx[7], mJ[49], xn[7], wv[7];
-    formR1(x, t, q, n, xv, xv[6], R);
-    R[6] = formR2(t, q, n, xv, xv[6]);
+    eval_R(x, t, G, q, n, xv, R);
     double dotR = 0.0;
     for (int k = 0; k < 7; ++k) dotR = dotR + R[k] * R[k];
     double nR = sqrt(dotR);
     double inR = nR;
     if (inR == 0.0) inR = inR1;
     while ((nR > t.atol && nR / inR > t.rtol) || iter < mmin) {
-      formJ(x, t, q, xv, J);
+      formJ<true>(x, t, G, q, xv, xv[6], J);
       for (int k = 0; k < 7; ++k) dx[k] = R[k];
       for (int k = 0; k < 49; ++k) mJ[k] = -J[k];
       lu_solve(7, mJ, dx, 1);
@@ -541,8 +549,7 @@ __device__ bool solve(const CrystalElem& x, const CrystalType& t, Pt& q, const N
       for (;;) {
         const double nlsx = ls1 + ls2 * alpha;
         for (int k = 0; k < 7; ++k) xn[k] = xv[k] + alpha * dx[k];
-        formR1(x, t, q, n, xn, xn[6], R);
-        R[6] = formR2(t, q, n, xn, xn[6]);
+        eval_R(x, t, G, q, n, xn, R);
         dotR = 0.0;
         for (int k = 0; k < 7; ++k) dotR = dotR + R[k] * R[k];
         nR = sqrt(dotR);
@@ -621,8 +628,10 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
   }
   const double dt = a.dt;
   // mm10_solve_strup
-  Pt q;
-  setup(x, t, n, R1, uddt, dt, q);
+  Geo G;
+  setup_geo(x, n, R1, G);
+  Rate q;
+  setup_rate(uddt, dt, q);
   double stress[6], ostress[6], tt = n.tt, ott = n.tt;
   for (int k = 0; k < 6; ++k) { stress[k] = n.stress[k]; ostress[k] = stress[k]; }
   const double temp1 = q.D[0] * q.D[0] + q.D[1] * q.D[1] + q.D[2] * q.D[2] + q.D[3] * q.D[3] + q.D[4] * q.D[4] +
@@ -637,20 +646,20 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
   if (iter0off || no_load) {
     if (!no_load) {
       double R1v[6];
-      formR1(x, t, q, n, stress, tt, R1v);
+      eval_R1(x, t, G, q, n, stress, tt, R1v);
       for (int k = 0; k < 6; ++k) stress[k] = stress[k] - R1v[k];
     }
   } else {
     double frac = 0.0, step = 1.0;
     int cuts = 0;
     bool fail = false;
-    Pt cq;
+    Rate cq;
     while (frac < 1.0) {
       double Dw[6];
       for (int k = 0; k < 6; ++k) Dw[k] = uddt[k] * (step + frac);
-      setup(x, t, n, R1, Dw, dt * (step + frac), cq);
+      setup_rate(Dw, dt * (step + frac), cq);
       tt = n.tt;
-      fail = !solve(x, t, cq, n, stress, tt, dt * step, J, &iters);
+      fail = !solve(x, t, G, cq, n, stress, tt, dt * step, J, &iters);
       if (fail) {
         for (int k = 0; k < 6; ++k) stress[k] = ostress[k];
         tt = ott;
@@ -704,14 +713,14 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
     for (int ii = 0; ii < 3; ++ii)
       for (int jj = 0; jj < 3; ++jj) tr[ii + 3 * jj] = n.Rp[jj + 3 * ii];
     rt2rvw(tr, RW);
+    double rsc[NS], slc[NS];   // slip terms at the converged state
+    slip_terms(t, G, q, stress, tt, rsc, slc);
     double wb[3] = {0.0, 0.0, 0.0};
     for (int s = 0; s < NS; ++s) {
       double qs[3];
       m3vec(RW, x.qs[s], qs);
-      const double sl = slipinc_of(t, q, stress, tt, s);
-      for (int k = 0; k < 3; ++k) wb[k] = wb[k] + sl * qs[k];
-      const double rs = rs_of(q, stress, s);
-      for (int k = 0; k < 3; ++k) wb[k] = wb[k] + rs * q.tinc * t.iD_v * qs[k];
+      for (int k = 0; k < 3; ++k) wb[k] = wb[k] + slc[s] * qs[k];
+      for (int k = 0; k < 3; ++k) wb[k] = wb[k] + rsc[s] * q.tinc * t.iD_v * qs[k];
     }
     double wt[9], ex[9];
     wt[0] = 0.0; wt[3] = wb[2]; wt[6] = wb[1];
@@ -735,7 +744,7 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
     ex[0] = ex[0] + 1.0; ex[4] = ex[4] + 1.0; ex[8] = ex[8] + 1.0;
     m3mul(ex, n.Rp, Rp1);
     // mm10_output
-    for (int s = 0; s < NS; ++s) slip_incs[s] = slipinc_of(t, q, stress, tt, s);
+    for (int s = 0; s < NS; ++s) slip_incs[s] = slc[s];
     {
       double w1[9], fr[9];
       for (int ii = 0; ii < 3; ++ii)
@@ -752,9 +761,9 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
       euler[2] = c180 * phiK;
     }
     double dif[NS], ed[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, t1, t2;
-    for (int s = 0; s < NS; ++s) dif[s] = rs_of(q, stress, s) * q.tinc * t.iD_v;
+    for (int s = 0; s < NS; ++s) dif[s] = rsc[s] * q.tinc * t.iD_v;
     for (int s = 0; s < NS; ++s)
-      for (int k = 0; k < 6; ++k) ed[k] = ed[k] + dif[s] * q.ms[s][k];
+      for (int k = 0; k < 6; ++k) ed[k] = ed[k] + dif[s] * G.ms[s][k];
     for (int k = 0; k < 6; ++k) ed6[k] = ed[k] / q.tinc;
     t1 = ed[0] * ed[0] + ed[1] * ed[1] + ed[2] * ed[2];
     t2 = ed[3] * ed[3] + ed[4] * ed[4] + ed[5] * ed[5];
@@ -801,8 +810,8 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
     cmul(erot, eu, ee);
     double dbarp[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, wp[3], ewwe[6], ep[6];
     for (int s = 0; s < NS; ++s)
-      for (int k = 0; k < 6; ++k) dbarp[k] = dbarp[k] + slip_incs[s] * q.ms[s][k];
-    form_wp(t, q, stress, tt, wp);
+      for (int k = 0; k < 6; ++k) dbarp[k] = dbarp[k] + slip_incs[s] * G.ms[s][k];
+    form_wp(t, G, q, rsc, slc, wp);
     symsw(ee, wp, ewwe);
     for (int k = 0; k < 6; ++k) ep[k] = dbarp[k] + ewwe[k];
     for (int k = 0; k < 6; ++k) ep6[k] = ep[k] / q.tinc;
@@ -824,12 +833,12 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
       for (int k = 0; k < 6; ++k) ep[k] = ep[k] / q.tinc;
       n_eff = 0.0;
       for (int s = 0; s < NS; ++s) {
-        const double rs = rs_of(q, stress, s);
+        const double rs = rsc[s];
         double d = pow(fabs(rs), t.rate_n - 1.0);
         d = q.dg * t.rate_n / pow(tt, t.rate_n) * d;
         d = d + q.tinc * t.iD_v;
-        t1 = q.ms[s][0] * ep[0] + q.ms[s][1] * ep[1] + q.ms[s][2] * ep[2];
-        t2 = q.ms[s][3] * ep[3] + q.ms[s][4] * ep[4] + q.ms[s][5] * ep[5];
+        t1 = G.ms[s][0] * ep[0] + G.ms[s][1] * ep[1] + G.ms[s][2] * ep[2];
+        t2 = G.ms[s][3] * ep[3] + G.ms[s][4] * ep[4] + G.ms[s][5] * ep[5];
         const double ec_slip = t1 + 0.5 * t2;
         t1 = rs * d / ec_dot;
         t2 = ec_slip / ec_dot / q.tinc;
@@ -1036,7 +1045,9 @@ cudaError_t init_mm10_kernels() {
   return cudaSuccess;
 }
 
-int mm10_kernel_launches(const DeviceModel& m) { return m.mm10_chunks > 0 ? 7 : 0; }
+int mm10_kernel_launches(const DeviceModel& m, bool sorted) {
+  return m.mm10_chunks > 0 ? (sorted ? 7 : 3) : 0;
+}
 
 cudaError_t launch_mm10(const DeviceModel& m, const RecoverArgs& a, cudaStream_t s) {
   int* counter = a.mm10_counter;
@@ -1046,15 +1057,17 @@ cudaError_t launch_mm10(const DeviceModel& m, const RecoverArgs& a, cudaStream_t
   k_mm10_kin<<<m.mm10_chunks, kRecoverThreads, 0, s>>>(a, m.mm10_chunk0);
   const int n = m.n_mm10_gp;
   const int nb = (n + 255) / 256;
-  k_mm10_bins_zero<<<1, 2 * kBins, 0, s>>>(bins);
-  k_mm10_hist<<<nb, 256, 0, s>>>(a.mm10_iters, n, bins);
-  k_mm10_scan<<<1, 32, 0, s>>>(bins);
-  k_mm10_scatter<<<nb, 256, 0, s>>>(a.mm10_iters, n, bins, order);
+  if (a.mm10_sorted) {
+    k_mm10_bins_zero<<<1, 2 * kBins, 0, s>>>(bins);
+    k_mm10_hist<<<nb, 256, 0, s>>>(a.mm10_iters, n, bins);
+    k_mm10_scan<<<1, 32, 0, s>>>(bins);
+    k_mm10_scatter<<<nb, 256, 0, s>>>(a.mm10_iters, n, bins, order);
+  }
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   const int warps = (n + 31) / 32;
   const int grid = std::max(1, std::min(m.nsm * g_occ, (warps + 3) / 4));
-  WorkQueue q{order, n, 32, counter};
+  WorkQueue q{a.mm10_sorted ? order : a.mm10_ident, n, 32, counter};
   k_mm10_update<<<grid, 128, 0, s>>>(a, q);
   k_mm10_forces<<<m.mm10_chunks, kRecoverThreads, 0, s>>>(a, m.mm10_chunk0);
   return cudaGetLastError();

@@ -172,7 +172,7 @@ cudaError_t init_recover_kernels() {
 int persistent_recover_occupancy() { return std::max(1, g_occ); }
 
 int recover_kernel_launches(const DeviceModel& m, const Schedule& sc) {
-  int n = mm10_kernel_launches(m);
+  int n = mm10_kernel_launches(m, sc.order == W3G_ORDER_HEAVY_FIRST);
   if (sc.mode == W3G_SCHED_PERSISTENT) return n + (m.nrchunks > 0 ? 1 : 0);
   for (int t = 0; t < kNumTypes; ++t) n += m.type_chunks[t] > 0 ? 1 : 0;
   return n;

@@ -81,6 +81,13 @@ class Engine:
         sc = abi.Schedule(mode, recover_ctas_per_sm, tangent_ctas_per_sm, recover_grain, tangent_grain, order)
         abi.check(self.lib, self.lib.w3g_set_schedule(self.ctx, C.byref(sc)))
 
+    def local_iterations(self) -> np.ndarray:
+        """Local Newton iterations of the last recovery per mm10 Gauss point."""
+        n = int(sum(s * g for s, g, cr in zip(self.model.spans, self.model.block_ngp, self.model.block_crystal) if cr))
+        out = np.zeros(n, dtype=np.int32)
+        abi.check(self.lib, self.lib.w3g_local_iterations(self.ctx, out.ctypes.data_as(C.POINTER(C.c_int)), n))
+        return out
+
     def schedule(self) -> dict:
         sc = abi.Schedule()
         abi.check(self.lib, self.lib.w3g_get_schedule(self.ctx, C.byref(sc)))
