@@ -79,6 +79,10 @@ extern "C" {
 /* Precision of the tangent contraction (w3g_set_tangent_precision). */
 #define W3G_TANGENT_FP64 0    /* plain form: everything FP64            */
 #define W3G_TANGENT_FP32 1    /* Ke in FP32 (CUDA-core FP32 FMA)        */
+#define W3G_TANGENT_TF32 2    /* B^T D B on the tensor cores, TF32 operands,
+                                 FP32 accumulation, Ke stored FP32 (8-node
+                                 bricks; other types as W3G_TANGENT_FP32) */
+#define W3G_TANGENT_BF16 3    /* the same with BF16 operands             */
 
 /*
  * One crystal definition of mm10 crystal plasticity: c_array(cnum) of

@@ -1,0 +1,142 @@
+"""Tensor-core precision forms of the tangent (TF32 / BF16 operands, FP32
+accumulation, tcgen05.mma) against the FP64 oracle.
+
+Element matrices: per element, max |Ke_gpu - Ke_oracle| / max |Ke_oracle|.
+The operands B and [D*]B are rounded once to the input format and the
+products accumulate in FP32, so the error scales with the format's unit
+roundoff: TF32 (10 stored mantissa bits, u = 2^-11) stays below 2e-3 and
+BF16 (7 bits, u = 2^-8) below 2e-2 of the element's largest entry.
+
+Newton: the precision form changes only the tangent, never the residual,
+so the solution at the 1e-8 relative residual is the FP64 one; the cost is
+extra iterations (the tangent error sets the linear convergence rate).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests.conftest import rel_err
+from tests.helpers import loaded_state, make_model
+from warp3d_gb300 import abi
+from warp3d_gb300.model import Bilinear, Crystal, Model, Part, cube_mesh, mixed_mesh, random_orientations, \
+    random_spans
+from warp3d_gb300.newton import NewtonDriver, uniaxial_bcs
+
+pytestmark = pytest.mark.gpu
+
+TOL = {abi.TANGENT_TF32: 2e-3, abi.TANGENT_BF16: 2e-2}
+NAMES = {abi.TANGENT_TF32: "tf32", abi.TANGENT_BF16: "bf16"}
+
+
+def _engine(model, **kw):
+    from warp3d_gb300.engine import Engine
+    return Engine(model, **kw)
+
+
+def _tangent_err(model, eng, ora, step, it, u, du):
+    est_o = model.estiff_blocks()
+    est_g = model.estiff_blocks()
+    ora.tanstf(step, it, model.c, u, du, est_o)
+    eng.tanstf(step, it, model.c, u, du, est_g)
+    assert all(np.all(np.isfinite(g)) for g in est_g)
+    return max(rel_err(g, o, axis=1) for g, o in zip(est_g, est_o))
+
+
+def _loaded(model, nxyz, origins=None):
+    ora, drv, du = loaded_state(model, nxyz, oracle.Oracle, steps=3, strain_per_step=0.0015,
+                                shear_per_step=0.0 if origins is not None else 0.001, origins=origins)
+    eng = _engine(model)
+    eng.upload(ora.state)
+    ifv = np.zeros(model.nodof)
+    o2 = oracle.Oracle(model, state=ora.state.copy())
+    assert o2.recover(4, 1, False, model.c, drv.u, du, ifv.copy())[0] == 0
+    assert eng.recover(4, 1, False, model.c, drv.u, du, ifv)[0] == 0
+    return eng, o2, drv.u, du
+
+
+@pytest.fixture(scope="module")
+def plastic_hex8():
+    # ragged blocks: tiles of 5 elements leave partial tiles at block ends
+    model, nxyz = make_model(n=5, jitter=0.1, spans=[64, 37, 1, 23])
+    return (model,) + _loaded(model, nxyz)
+
+
+@pytest.mark.parametrize("precision", [abi.TANGENT_TF32, abi.TANGENT_BF16])
+def test_tensor_core_tangent_plastic_state(plastic_hex8, precision):
+    model, eng, ora, u, du = plastic_hex8
+    eng.set_precision(precision)
+    err = _tangent_err(model, eng, ora, 4, 1, u, du)
+    eng.set_precision(abi.TANGENT_FP64)
+    print(f"{NAMES[precision]} tangent rel err vs fp64 oracle {err:.2e}")
+    assert err <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [abi.TANGENT_TF32, abi.TANGENT_BF16])
+def test_tensor_core_tangent_linear_iteration_zero(plastic_hex8, precision):
+    # iteration 0: no geometric term from the rotation update path, elastic D
+    model, eng, ora, u, du = plastic_hex8
+    eng.set_precision(precision)
+    err = _tangent_err(model, eng, ora, 4, 0, u, du)
+    eng.set_precision(abi.TANGENT_FP64)
+    assert err <= TOL[precision]
+
+
+def test_tensor_core_tangent_mixed_types():
+    """8-node bricks on the tensor cores; 20-node bricks and tetrahedra
+    take the FP32 CUDA-core kernels in the same call."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    coords, parts, origins = mixed_mesh(
+        [(abi.ETYPE_L3DISOP, 3), (abi.ETYPE_Q3DISOP, 2), (abi.ETYPE_TET10, 2)], ny=2, nz=3, jitter=0.05, seed=11)
+    plist = []
+    for etype, inc in parts:
+        spans = random_spans(inc.shape[0], rng, 1, 20)
+        plist.append(Part(etype, inc, spans, [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)] * len(spans)))
+    model = Model(coords, parts=plist)
+    eng, ora, u, du = _loaded(model, (3, 2, 3), origins=origins)
+    for precision in (abi.TANGENT_TF32, abi.TANGENT_BF16):
+        eng.set_precision(precision)
+        err = _tangent_err(model, eng, ora, 4, 1, u, du)
+        print(f"mixed {NAMES[precision]} tangent rel err {err:.2e}")
+        assert err <= TOL[precision]
+        # tensor-core bricks + 20-node + tetrahedra kernels
+        assert eng.last_launch_count() == 3
+
+
+def test_tensor_core_tangent_crystal_plasticity():
+    coords, incid = cube_mesh(3, jitter=0.05)
+    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(27, 7), block_spans=[20, 7])
+    ora = oracle.Oracle(model)
+    fixed, topz = uniaxial_bcs(model, (3, 3, 3))
+    drv = NewtonDriver(model, ora, fixed, tol=1e-8, maxit=60, extrapolate=True)
+    for s in range(1, 4):
+        imp = np.zeros(model.nodof)
+        imp[topz] = 0.0005 * 3
+        drv.step(s, imp)
+    eng = _engine(model)
+    eng.upload(ora.state)
+    for precision in (abi.TANGENT_TF32, abi.TANGENT_BF16):
+        eng.set_precision(precision)
+        err = _tangent_err(model, eng, ora, 3, 1, drv.u, np.zeros(model.nodof))
+        print(f"mm10 {NAMES[precision]} tangent rel err {err:.2e}")
+        assert err <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [abi.TANGENT_TF32])
+def test_tensor_core_tangent_newton_reaches_fp64_solution(precision):
+    n, nsteps = 6, 5
+    coords, incid = cube_mesh(n, jitter=0.1)
+    runs = []
+    for prec in (abi.TANGENT_FP64, precision):
+        model = Model(coords, incid)
+        eng = _engine(model, precision=prec)
+        fixed, topz = uniaxial_bcs(model, (n, n, n))
+        drv = NewtonDriver(model, eng, fixed, tol=1e-8, maxit=60)
+        for s in range(1, nsteps + 1):
+            imp = np.zeros(model.nodof)
+            imp[topz] = 0.01 * n / nsteps
+            drv.step(s, imp)
+        runs.append(drv)
+    its = [[h[1] for h in d.history] for d in runs]
+    print(f"newton iterations per step: fp64 {its[0]}, {NAMES[precision]} {its[1]}")
+    assert max(h[2][-1] for h in runs[1].history) <= 1e-8
+    assert rel_err(runs[1].u, runs[0].u) < 1e-7

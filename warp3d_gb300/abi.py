@@ -33,6 +33,8 @@ HIST_MM10 = 158       # one fcc crystal, one hardening variable
 
 TANGENT_FP64 = 0
 TANGENT_FP32 = 1
+TANGENT_TF32 = 2
+TANGENT_BF16 = 3
 
 SCHED_PER_TYPE = 0
 SCHED_PERSISTENT = 1

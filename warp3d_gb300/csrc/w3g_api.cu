@@ -63,7 +63,7 @@ void free_all(w3g_context* c) {
   DeviceModel& m = c->m;
   DeviceState& s = c->s;
   if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
-  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
+  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.tcchunks, s.tc_timeout, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
                   m.cdest, m.mat, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
                   m.ifv_rowptr, m.ifv_src, s.params, s.counters, m.xtal, m.xtype, m.mm10_gp, s.mm10_scr,
                   s.mm10_iters, s.mm10_order, s.mm10_ident, s.mm10_bins,
@@ -146,7 +146,7 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
   a.urcs_n1 = c->s.urcs_n1;
   a.cep = c->s.cep;
   a.hist1 = c->s.hist1;
-  a.estiff = c->precision == W3G_TANGENT_FP32 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
+  a.estiff = c->precision != W3G_TANGENT_FP64 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
   a.qbar = c->m.qbar;
   a.beta_fact = c->m.beta_fact;
   return a;
@@ -156,9 +156,13 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
 // a negative status
 int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
   TangentArgs a = tangent_args(c, d_c, d_u, d_du);
-  cudaError_t e = launch_tangent(c->m, a, c->precision == W3G_TANGENT_FP32, c->sched, c->s.counters + 1, st);
+  const bool tc = c->precision == W3G_TANGENT_TF32 || c->precision == W3G_TANGENT_BF16;
+  cudaError_t e = cudaSuccess;
+  if (tc) e = launch_tangent_tc_hex8(c->m, a, c->precision == W3G_TANGENT_BF16, c->s.tc_timeout, st);
+  if (e == cudaSuccess)
+    e = launch_tangent(c->m, a, c->precision != W3G_TANGENT_FP64, c->sched, c->s.counters + 1, st, tc);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
-  return tangent_kernel_launches(c->m, c->sched);
+  return tangent_kernel_launches(c->m, c->sched, tc);
 }
 
 int run_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
@@ -359,6 +363,11 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     tchunks.insert(tchunks.end(), ttype_chunks[t].begin(), ttype_chunks[t].end());
   }
   m.ntchunks = (int)tchunks.size();
+  std::vector<Chunk> tcchunks;   // tensor-core tiles: 5 elements of an 8-node-brick block
+  for (int b = 0; b < md->nelblk; ++b)
+    if (B[b].etype == W3G_ETYPE_L3DISOP)
+      for (int i0 = 0; i0 < B[b].span; i0 += 5) tcchunks.push_back(Chunk{b, i0, std::min(5, B[b].span - i0), 0});
+  m.ntcchunks = (int)tcchunks.size();
   m.nrchunks = (int)chunks.size();
   m.mm10_chunk0 = (int)chunks.size();
   m.mm10_chunks = (int)mm10_chunks.size();
@@ -478,6 +487,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(m.blocks, md->nelblk);
   AL(m.chunks, m.nchunks);
   AL(m.tchunks, m.ntchunks);
+  AL(m.tcchunks, m.ntcchunks);
+  AL(s.tc_timeout, 1);
   for (int k = 0; k < 2; ++k) {
     AL(m.rorder[k], m.nrchunks);
     AL(m.torder[k], m.ntchunks);
@@ -538,6 +549,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   UP(m.blocks, B.data(), md->nelblk);
   UP(m.chunks, chunks.data(), m.nchunks);
   UP(m.tchunks, tchunks.data(), m.ntchunks);
+  UP(m.tcchunks, tcchunks.data(), m.ntcchunks);
   for (int k = 0; k < 2; ++k) {
     UP(m.rorder[k], rord[k].data(), m.nrchunks);
     UP(m.torder[k], tord[k].data(), m.ntchunks);
@@ -565,6 +577,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   for (int k = 0; k < 10 && e == cudaSuccess; ++k) e = cudaMemsetAsync(zs[k], 0, (size_t)zn[k] * sizeof(double), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.geo_dirty, 0xff, sizeof(int), st);   // nonzero: not built
   if (e == cudaSuccess) e = cudaMemsetAsync(s.counters, 0, 3 * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.tc_timeout, 0, sizeof(int), st);
   if (e == cudaSuccess && n_mm10_gp > 0) e = cudaMemsetAsync(s.mm10_iters, 0, (size_t)n_mm10_gp * sizeof(int), st);
   if (e == cudaSuccess) e = init_kernels();
   if (e == cudaSuccess) {
@@ -592,9 +605,9 @@ int w3g_destroy(w3g_context* c) {
 
 int w3g_set_tangent_precision(w3g_context* c, int precision) {
   if (!c) return fail(W3G_EARG, "null context");
-  if (precision != W3G_TANGENT_FP64 && precision != W3G_TANGENT_FP32) return fail(W3G_EARG, "bad precision");
+  if (precision < W3G_TANGENT_FP64 || precision > W3G_TANGENT_BF16) return fail(W3G_EARG, "bad precision");
   CK(cudaSetDevice(c->device));
-  if (precision == W3G_TANGENT_FP32 && !c->s.estiff32) {
+  if (precision != W3G_TANGENT_FP64 && !c->s.estiff32) {
     CK(dalloc(&c->s.estiff32, (size_t)c->m.estiff_total));
     CK(cudaMemsetAsync(c->s.estiff32, 0, (size_t)c->m.estiff_total * sizeof(float), c->stream));
   }
@@ -696,6 +709,11 @@ int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const doubl
     }
   }
   CK(cudaStreamSynchronize(st));
+  if (c->precision == W3G_TANGENT_TF32 || c->precision == W3G_TANGENT_BF16) {
+    int timeout = 0;
+    CK(cudaMemcpy(&timeout, c->s.tc_timeout, sizeof(int), cudaMemcpyDeviceToHost));
+    if (timeout) return fail(W3G_EFATAL, "tensor-core tangent: MMA completion wait gave up (Ke set to NaN)");
+  }
   return 0;
 }
 
@@ -907,7 +925,7 @@ int w3g_autotune(w3g_context* c, int step, int iter, int extrapolated_du, const 
   // candidates: per-type launches, or the persistent kernels with each
   // CTAs-per-SM count up to occupancy, queue grain 1 or 4, either order
   const int occ_r = persistent_recover_occupancy();
-  const int occ_t = persistent_tangent_occupancy(c->precision == W3G_TANGENT_FP32);
+  const int occ_t = persistent_tangent_occupancy(c->precision != W3G_TANGENT_FP64);
   double total_best = 1e300;
   Schedule chosen = c->sched;
   int status = 0;
@@ -989,7 +1007,7 @@ int w3g_recover_info_get(w3g_context* c, w3g_recover_info* info) {
 
 int w3g_estiff_device(w3g_context* c, void** d_estiff, long long* count) {
   if (!c || !d_estiff || !count) return fail(W3G_EARG, "null argument");
-  *d_estiff = c->precision == W3G_TANGENT_FP32 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
+  *d_estiff = c->precision != W3G_TANGENT_FP64 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
   *count = c->m.estiff_total;
   return 0;
 }

@@ -171,6 +171,8 @@ struct DeviceModel {
   BlockDesc* blocks = nullptr;     // device
   Chunk* chunks = nullptr;         // device, recovery items grouped by type
   Chunk* tchunks = nullptr;        // device, tangent items grouped by type
+  Chunk* tcchunks = nullptr;       // device, tensor-core tangent tiles (8-node bricks, <= 5 elements)
+  int ntcchunks = 0;
   // schedule orders of the work items (W3G_ORDER_BLOCKS, _HEAVY_FIRST)
   int* rorder[2] = {nullptr, nullptr};
   int* torder[2] = {nullptr, nullptr};
@@ -208,6 +210,7 @@ struct DeviceState {
   unsigned long long* status = nullptr;  // first det[F] <= 0 point, w3g::bad_point_key order
   IterParams* params = nullptr;
   int* counters = nullptr;         // work-queue heads: recovery, tangent, mm10
+  int* tc_timeout = nullptr;       // set when a tensor-core tile's MMA wait gave up
   // mm10 per-GP scratch and scheduling
   double* mm10_scr = nullptr;      // kMm10Scratch * n_mm10_gp
   int* mm10_iters = nullptr;       // n_mm10_gp
@@ -288,11 +291,15 @@ struct RecoverArgs {
 // element kernels of one call: per-type launches or one persistent launch
 // (queue counters are reset inside)
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc,
-                           int* counter, cudaStream_t s);
+                           int* counter, cudaStream_t s, bool skip_hex8 = false);
+// precision forms on the tensor cores: 8-node bricks (w3g_tangent_tc.cu)
+cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
+                                   cudaStream_t s);
+cudaError_t init_tangent_tc_kernels();
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, const Schedule& sc,
                            int* counter, cudaStream_t s);
 // launches of the element kernels under a schedule
-int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc);
+int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8 = false);
 int recover_kernel_launches(const DeviceModel& m, const Schedule& sc);
 // mm10 recovery of the crystal-plasticity items (kinematics, local
 // solves from a work queue sorted by the last iteration counts, forces)
@@ -305,6 +312,7 @@ cudaError_t init_recover_kernels();
 cudaError_t init_mm10_kernels();
 inline cudaError_t init_kernels() {
   cudaError_t e = init_tangent_kernels();
+  if (e == cudaSuccess) e = init_tangent_tc_kernels();
   if (e == cudaSuccess) e = init_recover_kernels();
   return e == cudaSuccess ? init_mm10_kernels() : e;
 }

@@ -98,9 +98,10 @@ template <class T>
 int occupancy() { return std::max(1, g_occ[sizeof(T) == 4]); }
 
 template <class T>
-cudaError_t launch(const DeviceModel& m, const TangentArgs& a, const Schedule& sc, int* counter, cudaStream_t s) {
+cudaError_t launch(const DeviceModel& m, const TangentArgs& a, const Schedule& sc, int* counter, cudaStream_t s,
+                   bool skip_hex8) {
   cudaError_t e = cudaSuccess;
-  if (sc.mode == W3G_SCHED_PERSISTENT) {
+  if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) {
     const int occ = occupancy<T>();
     const int per_sm = sc.tangent_ctas_per_sm > 0 ? std::min(sc.tangent_ctas_per_sm, occ) : occ;
     const int grain = std::max(1, sc.tangent_grain);
@@ -111,7 +112,7 @@ cudaError_t launch(const DeviceModel& m, const TangentArgs& a, const Schedule& s
     k_tangent_persistent<T><<<grid, kTangentThreads, tangent_smem<T>(), s>>>(a, q);
     return cudaGetLastError();
   }
-  if (m.ttype_chunks[0] > 0) {
+  if (m.ttype_chunks[0] > 0 && !skip_hex8) {
     TangentArgs h = a;
     h.chunk0 = m.ttype_chunk0[0];
     k_tangent_hex8<T><<<m.ttype_chunks[0], kTangentThreads, hex8_smem<T>(), s>>>(h);
@@ -138,17 +139,17 @@ cudaError_t init_tangent_kernels() {
 
 int persistent_tangent_occupancy(bool fp32) { return fp32 ? occupancy<float>() : occupancy<double>(); }
 
-int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc) {
-  if (sc.mode == W3G_SCHED_PERSISTENT) return m.ntchunks > 0 ? 1 : 0;
-  int n = 0;
-  for (int t = 0; t < kNumTypes; ++t) n += m.ttype_chunks[t] > 0 ? 1 : 0;
+int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8) {
+  if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) return m.ntchunks > 0 ? 1 : 0;
+  int n = skip_hex8 && m.ntcchunks > 0 ? 1 : 0;
+  for (int t = skip_hex8 ? 1 : 0; t < kNumTypes; ++t) n += m.ttype_chunks[t] > 0 ? 1 : 0;
   return n;
 }
 
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc, int* counter,
-                           cudaStream_t s) {
+                           cudaStream_t s, bool skip_hex8) {
   if (m.ntchunks == 0) return cudaSuccess;
-  return fp32 ? launch<float>(m, a, sc, counter, s) : launch<double>(m, a, sc, counter, s);
+  return fp32 ? launch<float>(m, a, sc, counter, s, skip_hex8) : launch<double>(m, a, sc, counter, s, skip_hex8);
 }
 
 }  // namespace w3g

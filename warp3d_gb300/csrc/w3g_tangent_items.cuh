@@ -348,7 +348,7 @@ struct TangentSmemHex8F32 {
   float elem[kChunk][kPerElem32];
 };
 
-__device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cidx, unsigned char* smem) {
+static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cidx, unsigned char* smem) {
   TangentSmemHex8F32& S = *reinterpret_cast<TangentSmemHex8F32*>(smem);
   float* sdn = S.dn;
   auto& selem = S.elem;
