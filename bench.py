@@ -539,6 +539,15 @@ def main():
         ms32, tan32, rec32, launches32 = timed(abi.TANGENT_FP32)
         mixed = {"value": ne / (ms32 * 1e-3), "ms_per_step": ms32, "tangent_ms": tan32, "recovery_ms": rec32,
                  "speedup_vs_fp64": ms64 / ms32, "dtype": "tangent fp32 (FMA), recovery fp64"}
+        # tensor-core forms of the same tangent (tcgen05.mma), one
+        # Newton iteration each (tangent + FP64 recovery)
+        tcf = {}
+        for name, prec in (("tf32", abi.TANGENT_TF32), ("bf16", abi.TANGENT_BF16),
+                           ("tf32x3", abi.TANGENT_TF32X3), ("bf16x3", abi.TANGENT_BF16X3)):
+            ms_p, tan_p, rec_p, _ = timed(prec)
+            tcf[name] = {"tangent_ms": tan_p, "ms_per_step": ms_p, "value": ne / (ms_p * 1e-3),
+                         "tangent_hbm_gbs": TANGENT32_BYTES_PER_ELEM * ne / (tan_p * 1e-3) / 1e9}
+        mixed["tensor_core"] = tcf
         eng.set_precision(abi.TANGENT_FP64)
 
     # whole-job throughput: max time over ranks

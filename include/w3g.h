@@ -83,6 +83,9 @@ extern "C" {
                                  FP32 accumulation, Ke stored FP32 (8-node
                                  bricks; other types as W3G_TANGENT_FP32) */
 #define W3G_TANGENT_BF16 3    /* the same with BF16 operands             */
+#define W3G_TANGENT_TF32X3 4  /* TF32 with split operands (x = hi + lo,
+                                 three MMAs): near-FP32 Ke accuracy       */
+#define W3G_TANGENT_BF16X3 5  /* BF16 with split operands                */
 
 /*
  * One crystal definition of mm10 crystal plasticity: c_array(cnum) of
@@ -172,9 +175,13 @@ int w3g_create(int device, const w3g_model_desc* model, w3g_context** out);
 int w3g_destroy(w3g_context* ctx);
 const char* w3g_last_error(void);
 
-/* Selects the precision form of the tangent (W3G_TANGENT_*). The FP32
-   form writes Ke as float into a separate device array; w3g_tanstf then
-   widens to double only when host estiff pointers are given. */
+/* Selects the precision form of the tangent (W3G_TANGENT_*). Every form
+   but FP64 writes Ke as float into a separate device array; w3g_tanstf then
+   widens to double only when host estiff pointers are given. The tensor-
+   core forms (TF32, BF16, and their split X3 variants) cover 8-node bricks;
+   20-node bricks and tetrahedra take the FP32 kernels in the same call.
+   w3g_tanstf returns W3G_EFATAL if a tensor-core tile's bounded wait for
+   its MMAs gave up (that tile's Ke is then NaN). */
 int w3g_set_tangent_precision(w3g_context* ctx, int precision);
 
 /* ---- state transfer (restart, fixtures, output) -------------------- */
@@ -216,7 +223,7 @@ int w3g_recover_dev(w3g_context* ctx, int step, int iter,
 int w3g_recover_info_get(w3g_context* ctx, w3g_recover_info* info);
 
 /* Device pointer of the resident element stiffnesses: FP64 (utsz, span)
-   blocks back to back for W3G_TANGENT_FP64, FP32 for W3G_TANGENT_FP32.
+   blocks back to back for W3G_TANGENT_FP64, FP32 for the other forms.
    *count receives the number of values. */
 int w3g_estiff_device(w3g_context* ctx, void** d_estiff, long long* count);
 

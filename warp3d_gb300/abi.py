@@ -35,6 +35,8 @@ TANGENT_FP64 = 0
 TANGENT_FP32 = 1
 TANGENT_TF32 = 2
 TANGENT_BF16 = 3
+TANGENT_TF32X3 = 4
+TANGENT_BF16X3 = 5
 
 SCHED_PER_TYPE = 0
 SCHED_PERSISTENT = 1

@@ -156,9 +156,12 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
 // a negative status
 int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
   TangentArgs a = tangent_args(c, d_c, d_u, d_du);
-  const bool tc = c->precision == W3G_TANGENT_TF32 || c->precision == W3G_TANGENT_BF16;
+  const int p = c->precision;
+  const bool tc = p >= W3G_TANGENT_TF32;
   cudaError_t e = cudaSuccess;
-  if (tc) e = launch_tangent_tc_hex8(c->m, a, c->precision == W3G_TANGENT_BF16, c->s.tc_timeout, st);
+  if (tc)
+    e = launch_tangent_tc_hex8(c->m, a, p == W3G_TANGENT_BF16 || p == W3G_TANGENT_BF16X3,
+                               p == W3G_TANGENT_TF32X3 || p == W3G_TANGENT_BF16X3, c->s.tc_timeout, st);
   if (e == cudaSuccess)
     e = launch_tangent(c->m, a, c->precision != W3G_TANGENT_FP64, c->sched, c->s.counters + 1, st, tc);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
@@ -605,7 +608,7 @@ int w3g_destroy(w3g_context* c) {
 
 int w3g_set_tangent_precision(w3g_context* c, int precision) {
   if (!c) return fail(W3G_EARG, "null context");
-  if (precision < W3G_TANGENT_FP64 || precision > W3G_TANGENT_BF16) return fail(W3G_EARG, "bad precision");
+  if (precision < W3G_TANGENT_FP64 || precision > W3G_TANGENT_BF16X3) return fail(W3G_EARG, "bad precision");
   CK(cudaSetDevice(c->device));
   if (precision != W3G_TANGENT_FP64 && !c->s.estiff32) {
     CK(dalloc(&c->s.estiff32, (size_t)c->m.estiff_total));
@@ -709,7 +712,7 @@ int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const doubl
     }
   }
   CK(cudaStreamSynchronize(st));
-  if (c->precision == W3G_TANGENT_TF32 || c->precision == W3G_TANGENT_BF16) {
+  if (c->precision >= W3G_TANGENT_TF32) {
     int timeout = 0;
     CK(cudaMemcpy(&timeout, c->s.tc_timeout, sizeof(int), cudaMemcpyDeviceToHost));
     if (timeout) return fail(W3G_EFATAL, "tensor-core tangent: MMA completion wait gave up (Ke set to NaN)");

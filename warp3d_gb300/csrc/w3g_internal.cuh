@@ -293,8 +293,8 @@ struct RecoverArgs {
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc,
                            int* counter, cudaStream_t s, bool skip_hex8 = false);
 // precision forms on the tensor cores: 8-node bricks (w3g_tangent_tc.cu)
-cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
-                                   cudaStream_t s);
+cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
+                                   int* tc_timeout, cudaStream_t s);
 cudaError_t init_tangent_tc_kernels();
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, const Schedule& sc,
                            int* counter, cudaStream_t s);

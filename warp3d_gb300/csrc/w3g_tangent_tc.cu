@@ -92,24 +92,60 @@ __host__ __device__ constexpr uint32_t instr_desc() {
          | ((uint32_t)(kRows >> 4) << 24);     // M >> 4
 }
 
-// operands are rounded to the input format once, to nearest (the tensor
-// core would otherwise drop the low mantissa bits of an FP32 operand)
+// Operands are rounded to the input format to nearest (the tensor core
+// would otherwise drop the low mantissa bits of an FP32 operand). With
+// kSplit, v = hi + lo with both parts in the input format, and the product
+// of two split operands is taken as hi*hi + hi*lo + lo*hi (the lo*lo term is
+// below FP32 rounding for TF32): three MMAs instead of one, and an error
+// near FP32's for TF32 (about 2^-16 relative for BF16).
+// one tcgen05.mma: D[tmem] (+)= A B^T over one K step, both operands in
+// shared memory (K-major, no swizzle)
 template <bool kBF16>
-__device__ __forceinline__ void put(unsigned char* op, int r, int k, float v) {
-  if (kBF16) {
-    *reinterpret_cast<__nv_bfloat16*>(op + TcLayout<kBF16>::offset(r, k)) = __float2bfloat16_rn(v);
-  } else {
-    uint32_t t;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
-    *reinterpret_cast<uint32_t*>(op + TcLayout<kBF16>::offset(r, k)) = t;
-  }
+__device__ __forceinline__ void mma(uint32_t tmem, uint32_t a_addr, uint32_t b_addr, bool accumulate) {
+  using L = TcLayout<kBF16>;
+  const uint64_t da = smem_desc(a_addr, L::kLBO, L::kSBO);
+  const uint64_t db = smem_desc(b_addr, L::kLBO, L::kSBO);
+  const uint32_t idesc = instr_desc<kBF16>();
+  const uint32_t acc = accumulate ? 1u : 0u;
+  if (kBF16)
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+  else
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
 template <bool kBF16>
+__device__ __forceinline__ float round_in(float v) {
+  if (kBF16) return __bfloat162float(__float2bfloat16_rn(v));
+  uint32_t t;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
+  return __uint_as_float(t);
+}
+
+template <bool kBF16, bool kSplit>
+__device__ __forceinline__ void put(unsigned char* op, int r, int k, float v) {
+  const int o = TcLayout<kBF16>::offset(r, k);
+  const float hi = round_in<kBF16>(v);
+  if (kBF16) *reinterpret_cast<__nv_bfloat16*>(op + o) = __float2bfloat16_rn(hi);
+  else *reinterpret_cast<float*>(op + o) = hi;
+  if (kSplit) {
+    unsigned char* lo_op = op + 2 * TcLayout<kBF16>::kOpBytes;   // A_lo after B_hi, B_lo after A_lo
+    const float lo = round_in<kBF16>(v - hi);
+    if (kBF16) *reinterpret_cast<__nv_bfloat16*>(lo_op + o) = __float2bfloat16_rn(lo);
+    else *reinterpret_cast<float*>(lo_op + o) = lo;
+  }
+}
+
+template <bool kBF16, bool kSplit>
 __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int chunk0, int* tc_timeout) {
   using L = TcLayout<kBF16>;
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* opA = smem;
+  unsigned char* opA = smem;                  // then B, then (split) A_lo, B_lo
   unsigned char* opB = smem + L::kOpBytes;
   __shared__ TcStatic S;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -239,8 +275,8 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
         vb = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
       }
     }
-    put<kBF16>(opA, r, k, va);
-    put<kBF16>(opB, r, k, vb);
+    put<kBF16, kSplit>(opA, r, k, va);
+    put<kBF16, kSplit>(opB, r, k, vb);
   }
   // geometric stiffness per node pair (kgstiff): sum_gp g_a . ({T} g_b)
   for (int idx = tid; idx < kTcElems * 36; idx += kThreads) {
@@ -268,22 +304,16 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   if (tid == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t a0 = smem_u32(opA), b0 = smem_u32(opB);
-    const uint32_t idesc = instr_desc<kBF16>();
+    const uint32_t lo = 2 * L::kOpBytes;   // A_lo, B_lo follow A_hi, B_hi
 #pragma unroll
     for (int s = 0; s < L::kSteps; ++s) {
       // one k-step = two core matrices along K
-      const uint64_t da = smem_desc(a0 + s * 2 * L::kLBO, L::kLBO, L::kSBO);
-      const uint64_t db = smem_desc(b0 + s * 2 * L::kLBO, L::kLBO, L::kSBO);
-      if (kBF16)
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-            "l"(da), "l"(db), "r"(idesc), "r"(s));
-      else
-        asm volatile(
-            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-            "l"(da), "l"(db), "r"(idesc), "r"(s));
+      const uint32_t ks = s * 2 * L::kLBO;
+      mma<kBF16>(tmem, a0 + ks, b0 + ks, s > 0);
+      if (kSplit) {
+        mma<kBF16>(tmem, a0 + ks, b0 + lo + ks, true);
+        mma<kBF16>(tmem, a0 + lo + ks, b0 + ks, true);
+      }
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
         smem_u32(&S.mbar)));
@@ -352,34 +382,44 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   }
 }
 
-// Dynamic shared memory per CTA. At least 40 KB, so that no more than four
-// CTAs share an SM and their 4 x 128 TMEM columns always fit in the SM's 512:
-// tcgen05.alloc then never has to wait for another CTA's columns.
-template <bool kBF16>
+// Dynamic shared memory per CTA: A and B (and their low parts when split).
+// At least 40 KB, so that no more than four CTAs share an SM and their
+// 4 x 128 TMEM columns always fit in the SM's 512: tcgen05.alloc then never
+// has to wait for another CTA's columns.
+template <bool kBF16, bool kSplit>
 size_t tc_smem() {
-  const size_t need = 2 * (size_t)TcLayout<kBF16>::kOpBytes;
+  const size_t need = (kSplit ? 4 : 2) * (size_t)TcLayout<kBF16>::kOpBytes;
   return need > 40 * 1024 ? need : 40 * 1024;
+}
+
+template <bool kBF16, bool kSplit>
+cudaError_t set_smem() {
+  return cudaFuncSetAttribute(k_tangent_tc_hex8<kBF16, kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc_smem<kBF16, kSplit>());
+}
+
+template <bool kBF16, bool kSplit>
+void launch(const DeviceModel& m, const TangentArgs& h, int* tc_timeout, cudaStream_t s) {
+  k_tangent_tc_hex8<kBF16, kSplit><<<m.ntcchunks, kThreads, tc_smem<kBF16, kSplit>(), s>>>(h, 0, tc_timeout);
 }
 
 }  // namespace
 
 cudaError_t init_tangent_tc_kernels() {
-  cudaError_t e = cudaFuncSetAttribute(k_tangent_tc_hex8<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tc_smem<false>());
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_tangent_tc_hex8<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tc_smem<true>());
+  cudaError_t e = set_smem<false, false>();
+  if (e == cudaSuccess) e = set_smem<true, false>();
+  if (e == cudaSuccess) e = set_smem<false, true>();
+  if (e == cudaSuccess) e = set_smem<true, true>();
+  return e;
 }
 
-cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
-                                   cudaStream_t s) {
+cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
+                                   int* tc_timeout, cudaStream_t s) {
   if (m.ntcchunks == 0) return cudaSuccess;
   TangentArgs h = a;
   h.chunks = m.tcchunks;
-  if (bf16)
-    k_tangent_tc_hex8<true><<<m.ntcchunks, kThreads, tc_smem<true>(), s>>>(h, 0, tc_timeout);
-  else
-    k_tangent_tc_hex8<false><<<m.ntcchunks, kThreads, tc_smem<false>(), s>>>(h, 0, tc_timeout);
+  if (bf16) split ? launch<true, true>(m, h, tc_timeout, s) : launch<true, false>(m, h, tc_timeout, s);
+  else split ? launch<false, true>(m, h, tc_timeout, s) : launch<false, false>(m, h, tc_timeout, s);
   return cudaGetLastError();
 }
 
