@@ -99,6 +99,16 @@ def parse():
     ap.add_argument("--batched-elems", type=int, default=1_000_000, help="target elements of the batched workload")
     ap.add_argument("--no-crystal", action="store_true")
     ap.add_argument("--crystal-n", type=int, default=32, help="elements per cube edge of the mm10 workload")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="instead of the bench line: Newton solves of the cube under every tangent precision form")
+    ap.add_argument("--study-steps", type=int, default=20)
+    ap.add_argument("--study-strain", type=float, default=0.02)
+    ap.add_argument("--study-forms", default="fp64,fp32,tf32,bf16,tf32x3,bf16x3")
+    ap.add_argument("--study-maxit", type=int, default=25)
+    ap.add_argument("--study-lin-maxit", type=int, default=50000)
+    ap.add_argument("--study-no-extrapolate", action="store_true",
+                    help="start every step from zero instead of the scaled previous increment")
+    ap.add_argument("--study-no-adaptive", action="store_true", help="no subdivision of failing steps")
     return ap.parse_args()
 
 
@@ -459,6 +469,113 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def precision_study(args, dev):
+    """The precision forms on the n^3 cube (mm01, jitter 0.1h, blocks of
+    128) under uniaxial tension, args.study_strain in args.study_steps
+    equal steps, every Newton iteration on the device (element path, CSR
+    assembly, Jacobi PCG to 1e-10, residual norms) to the 1e-8 relative
+    residual; steps start from the scaled previous increment and a failing
+    step is subdivided (4 sub-increments, down to 1/16 of the step, step 1
+    included). Per form: Newton iterations per step, PCG iterations, wall
+    time, the final displacements' error against the FP64 run; per-element
+    Ke error against the FP64 tangent (checked against the oracle by the
+    tests) at the converged end state of the FP64 run."""
+    import torch
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+    from warp3d_gb300.newton import uniaxial_bcs
+    from warp3d_gb300.solver import DeviceCsr, DeviceNewtonDriver
+    forms = {"fp64": abi.TANGENT_FP64, "fp32": abi.TANGENT_FP32, "tf32": abi.TANGENT_TF32,
+             "bf16": abi.TANGENT_BF16, "tf32x3": abi.TANGENT_TF32X3, "bf16x3": abi.TANGENT_BF16X3}
+    n = args.n
+    model, _, _ = build_workload(n)
+    fixed, topz = uniaxial_bcs(model, (n, n, n))
+    t0 = time.perf_counter()
+    eng = Engine(model)
+    initial = model.new_state()
+    eng.download(initial)
+    csr = DeviceCsr(eng)
+    setup_s = time.perf_counter() - t0
+    out = {"workload": f"{n}^3 hex8 l3disop geonl (jitter 0.1h), mm01 bilinear, blocks of 128; uniaxial "
+                       f"{100 * args.study_strain:g}% in {args.study_steps} steps",
+           "elements": model.noelem, "dofs": model.nodof, "csr_nnz": csr.nnz, "setup_s": setup_s,
+           "newton_tol": 1e-8, "pcg_rtol": 1e-10, "forms": {}}
+    u_ref = None
+    for name in args.study_forms.split(","):
+        eng.set_precision(forms[name])
+        eng.upload(initial)
+        drv = DeviceNewtonDriver(model, eng, fixed, tol=1e-8, maxit=args.study_maxit, lin_rtol=1e-10,
+                                 lin_maxit=args.study_lin_maxit, csr=csr, extrapolate=not args.study_no_extrapolate,
+                                 adaptive=not args.study_no_adaptive, adaptive_step1=True)
+        rec = {"steps": [], "failed": None}
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for st in range(1, args.study_steps + 1):
+            imp = np.zeros(model.nodof)
+            imp[topz] = args.study_strain * n / args.study_steps
+            k0, cuts0 = len(drv.history), drv.cuts
+            try:
+                drv.step(st, imp)
+            except RuntimeError as exc:
+                rec["failed"] = {"step": st, "reason": str(exc)[:300],
+                                 "trace": [[a, b, float(f"{c:.3e}"), None if d is None else float(f"{d:.3e}")]
+                                           for a, b, c, d in drv.trace]}
+                break
+            incs = drv.history[k0:]
+            rec["steps"].append({"step": st, "newton": sum(h[1] for h in incs), "increments": len(incs),
+                                 "cuts": drv.cuts - cuts0,
+                                 "residuals": [[float(f"{r:.3e}") for r in h[2]] for h in incs],
+                                 "pcg": [x for _, l in drv.lin_history[k0:] for x in l]})
+        torch.cuda.synchronize()
+        rec["wall_s"] = time.perf_counter() - t1
+        its = [x["newton"] for x in rec["steps"]]
+        rec["newton_per_step"] = its
+        rec["increments_per_step"] = [x["increments"] for x in rec["steps"]]
+        rec["mean_newton_per_step"] = float(np.mean(its)) if its else None
+        rec["pcg_total"] = int(sum(sum(x["pcg"]) for x in rec["steps"]))
+        u = drv.u
+        if name == "fp64":
+            u_ref = u
+            end_state = model.new_state()
+            eng.download(end_state)
+        elif u_ref is not None and rec["failed"] is None:
+            rec["u_rel_err_vs_fp64"] = float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref)))
+        out["forms"][name] = rec
+        print(f"[study] {name}: newton {its} failed={rec['failed'] is not None} {rec['wall_s']:.1f}s",
+              file=sys.stderr, flush=True)
+    # per-element Ke error at the FP64 run's converged end state
+    if u_ref is not None:
+        tu = torch.from_numpy(u_ref).to(dev)
+        tz = torch.zeros_like(tu)
+        tc = torch.from_numpy(model.c).to(dev)
+        ne, ut = model.noelem, model.utsz
+
+        def ke(prec):
+            eng.set_precision(prec)
+            eng.upload(end_state)
+            eng.tanstf_dev(args.study_steps, 1, tc.data_ptr(), tu.data_ptr(), tz.data_ptr())
+            torch.cuda.synchronize()
+            p, cnt = eng.estiff_device()
+            dt = torch.float64 if prec == abi.TANGENT_FP64 else torch.float32
+            t = torch.empty(cnt, dtype=dt, device=dev)
+            cudart = C.CDLL("libcudart.so")
+            assert cudart.cudaMemcpy(C.c_void_p(t.data_ptr()), C.c_void_p(p), C.c_size_t(t.element_size() * cnt),
+                                     3) == 0
+            return t.double().reshape(ne, ut)
+
+        k64 = ke(abi.TANGENT_FP64)
+        scale = k64.abs().amax(dim=1)
+        for name in args.study_forms.split(","):
+            if name == "fp64":
+                continue
+            e = (ke(forms[name]) - k64).abs().amax(dim=1) / scale
+            out["forms"][name]["ke_rel_err"] = {"max": float(e.max()), "median": float(e.median()),
+                                                "p99": float(torch.quantile(e[:: max(1, ne // 100000)], 0.99))}
+        eng.set_precision(abi.TANGENT_FP64)
+    csr.close()
+    return out
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -475,6 +592,10 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+
+    if args.precision_study:
+        print(json.dumps({"precision_study": precision_study(args, dev)}))
+        return
 
     from warp3d_gb300 import abi
     from warp3d_gb300.engine import Engine

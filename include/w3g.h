@@ -288,6 +288,53 @@ int w3g_autotune(w3g_context* ctx, int step, int iter, int extrapolated_du,
                  const void* d_c, const void* d_u, const void* d_du, void* d_ifv,
                  void* stream, int reps, w3g_schedule* best, double* best_ms);
 
+/* ---- global stiffness on the device and its solve -------------------
+   The step after the element path in WARP3D's Newton iteration:
+   drive_assemble_solve (src/drive_assemble_solve.f:11) builds the
+   sparsity of the equilibrium equations once (ds_setup_sparsity_local,
+   :358), assembles the element stiffnesses row by row (assem_by_row,
+   src/assemble_code.f:659; a thread builds a whole equation row) and
+   calls a sparse solver (direct, or hypre's PCG, :990). Here the pattern
+   and an (element, local pair) gather map are built once per context; the
+   assembly reads the resident element stiffnesses (FP64, or the FP32 of
+   the precision forms) on the device, summing every coefficient's
+   contributions in a fixed order (bitwise reproducible), into a CSR
+   matrix over all nodof dofs (full rows, both triangles, 0-based).
+   The solve is a Jacobi-preconditioned conjugate gradient restricted to
+   the free dofs (fixed_mask[dof] != 0: constrained, solution 0 there),
+   with deterministic reductions; its iterations replay as CUDA graphs. */
+typedef struct w3g_csr w3g_csr;
+
+int w3g_csr_create(w3g_context* ctx, w3g_csr** out);
+int w3g_csr_destroy(w3g_csr* csr);
+/* sizes and device pointers: rowptr (n+1, int32), colind (nnz, int32),
+   values (nnz, double); any output may be NULL */
+int w3g_csr_info(w3g_csr* csr, int* n, long long* nnz, void** d_rowptr,
+                 void** d_colind, void** d_values);
+/* assembles the values from ctx's current element stiffnesses */
+int w3g_csr_assemble_dev(w3g_csr* csr, void* stream);
+/* host copies of the pattern and values (arrays of n+1, nnz, nnz) */
+int w3g_csr_download(w3g_csr* csr, int* rowptr, int* colind, double* values);
+
+/* Solves K_ff x_f = b_scale * b_f (device vectors of nodof doubles; the
+   mask is nodof bytes) to ||r|| <= rtol ||b_f|| in at most maxit
+   iterations; x = 0 on constrained dofs. Returns 0 when converged,
+   W3G_PCG_MAXIT when not within maxit, W3G_PCG_BREAKDOWN when p.Kp <= 0
+   (the matrix is not positive definite on the free dofs); *iters and
+   *relres (either may be NULL) receive the iterations and ||r|| / ||b_f||.
+   Blocks until the solve ends; ordered after prior work on `stream`. */
+#define W3G_PCG_MAXIT 1
+#define W3G_PCG_BREAKDOWN 2
+int w3g_pcg_dev(w3g_csr* csr, const void* d_fixed_mask, const void* d_b,
+                double b_scale, void* d_x, double rtol, int maxit,
+                void* stream, int* iters, double* relres);
+
+/* Newton convergence norms as one device reduction (the residual-force
+   norm of cvtest, src/cvtest.f:20-60): d_out[0] = ||v_f||^2 over the free
+   dofs, d_out[1] = ||v||^2 over all dofs (device doubles). */
+int w3g_residual_norms_dev(w3g_csr* csr, const void* d_v, const void* d_fixed_mask,
+                           void* d_out, void* stream);
+
 /* ---- internal-force assembly without device allocation --------------
    No counterpart in the reference. For callers that cannot allocate
    device memory -- a Fortran code whose device arrays come from a pool or

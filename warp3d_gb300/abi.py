@@ -37,6 +37,8 @@ TANGENT_TF32 = 2
 TANGENT_BF16 = 3
 TANGENT_TF32X3 = 4
 TANGENT_BF16X3 = 5
+PCG_MAXIT = 1
+PCG_BREAKDOWN = 2
 
 SCHED_PER_TYPE = 0
 SCHED_PERSISTENT = 1
@@ -162,6 +164,15 @@ PROTOTYPES = [
     ("w3g_iteration_dev", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("w3g_autotune", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, C.c_int,
                                C.POINTER(Schedule), C.POINTER(C.c_double)]),
+    ("w3g_csr_create", C.c_int, [_vp, C.POINTER(_vp)]),
+    ("w3g_csr_destroy", C.c_int, [_vp]),
+    ("w3g_csr_info", C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(_vp), C.POINTER(_vp),
+                               C.POINTER(_vp)]),
+    ("w3g_csr_assemble_dev", C.c_int, [_vp, _vp]),
+    ("w3g_csr_download", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("w3g_pcg_dev", C.c_int, [_vp, _vp, _vp, C.c_double, _vp, C.c_double, C.c_int, _vp, C.POINTER(C.c_int),
+                              C.POINTER(C.c_double)]),
+    ("w3g_residual_norms_dev", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
 ]
 
 _lib = None

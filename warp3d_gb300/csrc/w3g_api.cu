@@ -12,30 +12,7 @@
 
 using namespace w3g;
 
-// one captured iteration (w3g_iteration_dev) and what it was captured for
-struct IterationGraph {
-  cudaGraphExec_t exec = nullptr;
-  int what = 0, precision = -1;
-  const void *c = nullptr, *u = nullptr, *du = nullptr, *ifv = nullptr;
-  Schedule sched{};
-  int launches = 0;
-};
-
-struct w3g_context {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  DeviceModel m;
-  DeviceState s;
-  int precision = W3G_TANGENT_FP64;
-  Schedule sched{W3G_SCHED_PER_TYPE, 0, 0, 1, 1, W3G_ORDER_HEAVY_FIRST};
-  IterationGraph graph;
-  int ifv_parts = 0;
-  int last_launches = 0;
-  // host copies needed for state transfer
-  std::vector<BlockDesc> blocks;
-  double* h_stage = nullptr;   // pinned staging, max(estiff_total, ...) doubles
-  size_t h_stage_n = 0;
-};
+#include "w3g_context.cuh"
 
 namespace {
 
@@ -1018,3 +995,5 @@ int w3g_estiff_device(w3g_context* c, void** d_estiff, long long* count) {
 int w3g_last_launch_count(w3g_context* c) { return c ? c->last_launches : 0; }
 
 }  // extern "C"
+
+int w3g_fail(int code, const std::string& msg) { return fail(code, msg); }

@@ -1,0 +1,36 @@
+// w3g_context.cuh -- the opaque w3g_context of include/w3g.h: resident
+// device model and state, schedule, captured iteration graph. Shared by the
+// C-ABI translation units (w3g_api.cu, w3g_solve.cu).
+#pragma once
+#include <string>
+#include <vector>
+#include "w3g_internal.cuh"
+
+// one captured iteration (w3g_iteration_dev) and what it was captured for
+struct IterationGraph {
+  cudaGraphExec_t exec = nullptr;
+  int what = 0, precision = -1;
+  const void *c = nullptr, *u = nullptr, *du = nullptr, *ifv = nullptr;
+  w3g::Schedule sched{};
+  int launches = 0;
+};
+
+struct w3g_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  w3g::DeviceModel m;
+  w3g::DeviceState s;
+  int precision = W3G_TANGENT_FP64;
+  w3g::Schedule sched{W3G_SCHED_PER_TYPE, 0, 0, 1, 1, W3G_ORDER_HEAVY_FIRST};
+  IterationGraph graph;
+  int ifv_parts = 0;
+  int last_launches = 0;
+  // host copies needed for state transfer
+  std::vector<w3g::BlockDesc> blocks;
+  double* h_stage = nullptr;   // pinned staging, max(estiff_total, ...) doubles
+  size_t h_stage_n = 0;
+};
+
+
+// records msg as the thread's last error (w3g_last_error) and returns code
+int w3g_fail(int code, const std::string& msg);

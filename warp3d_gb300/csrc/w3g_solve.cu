@@ -1,0 +1,581 @@
+// w3g_solve.cu -- the global stiffness on the device and its solve.
+//
+// WARP3D assembles its equilibrium equations row by row from the element
+// stiffnesses (drive_assemble_solve, src/drive_assemble_solve.f:654-929;
+// assem_by_row / assem_a_row, src/assemble_code.f:659,785) after building
+// the sparsity once (ds_setup_sparsity_local, :358), then calls a sparse
+// solver. Here:
+//
+//   pattern   built once on the host from edest: for every equation row,
+//             the (column, element-stiffness index) contributions of the
+//             elements sharing the row's dof, in ascending element-vector
+//             order, sorted stably by column; rows split over host threads
+//   assembly  one thread per stored coefficient sums its contributions in
+//             that fixed order from the resident element stiffnesses (FP64,
+//             or FP32 under the precision forms): no atomics, bitwise
+//             reproducible. Traffic per launch: the contribution indices
+//             (4 B each), the element stiffness values they name, and the
+//             coefficients (8 B each)
+//   PCG       Jacobi-preconditioned conjugate gradient on the free dofs,
+//             five kernels per iteration (warp-per-row SpMV with the p.Kp
+//             partial, alpha, vector update with the r.z and r.r partials,
+//             beta and the stopping test, direction update) reading the
+//             scalars from device memory; a batch of iterations replays as
+//             one CUDA graph and the host reads the state between batches.
+//             Reductions go through per-CTA partials over a fixed grid,
+//             summed in a fixed order: the same inputs give the same
+//             iterates bit for bit.
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <utility>
+#include <vector>
+#include "w3g_context.cuh"
+
+using namespace w3g;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kBatch = 16;   // CG iterations per graph replay
+
+struct PcgScal {
+  double rz, pap, alpha, beta, rr, bb, tol2;
+  int done, iters, breakdown;
+};
+
+__device__ __forceinline__ double warp_sum_down(double v) {
+  // tree towards lane 0 (fixed association: deterministic)
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sum of one value per thread, fixed order; result valid in thread 0
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum_down(v);
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < kWarps; ++k) t += sh[k];
+  __syncthreads();
+  return t;
+}
+
+// sum of nparts partials (stride `stride`, offset `off`) by one block
+__device__ double sum_partials(const double* partials, int nparts, int stride, int off, double* sh) {
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) v += partials[(size_t)k * stride + off];
+  return block_sum(v, sh);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_assemble(long long nnz, const int* __restrict__ cptr,
+                                                       const int* __restrict__ csrc, const T* __restrict__ est,
+                                                       double* __restrict__ val) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nnz;
+       j += (long long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    const int e = cptr[j + 1];
+    for (int k = cptr[j]; k < e; ++k) s += (double)est[csrc[k]];
+    val[j] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_dinv(int n, const int* __restrict__ diag,
+                                                   const double* __restrict__ val,
+                                                   const unsigned char* __restrict__ fixed, double* dinv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double d = val[diag[i]];
+    dinv[i] = (fixed[i] || d == 0.0) ? 0.0 : 1.0 / d;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_pcg_init(int n, const unsigned char* __restrict__ fixed,
+                                                       const double* __restrict__ b, double bscale,
+                                                       const double* __restrict__ dinv, double* x, double* r,
+                                                       double* z, double* p, double* partials) {
+  __shared__ double sh[kWarps];
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = fixed[i] ? 0.0 : bscale * b[i];
+    const double zi = dinv[i] * ri;
+    x[i] = 0.0;
+    r[i] = ri;
+    z[i] = zi;
+    p[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_pcg_init_fin(const double* partials, int nparts, double rtol,
+                                                           PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  const double rz = sum_partials(partials, nparts, 2, 0, sh);
+  const double rr = sum_partials(partials, nparts, 2, 1, sh);
+  if (threadIdx.x == 0) {
+    sc->rz = rz;
+    sc->rr = rr;
+    sc->bb = rr;
+    sc->tol2 = rtol * rtol * rr;
+    sc->alpha = sc->beta = sc->pap = 0.0;
+    sc->iters = 0;
+    sc->breakdown = 0;
+    sc->done = rr <= sc->tol2 ? 1 : 0;
+  }
+}
+
+// q = K p on the free rows (0 on constrained rows), partial of p.q
+__global__ void __launch_bounds__(kThreads) k_spmv(int n, const int* __restrict__ rowptr,
+                                                   const int* __restrict__ colind, const double* __restrict__ val,
+                                                   const unsigned char* __restrict__ fixed,
+                                                   const double* __restrict__ p, double* __restrict__ q,
+                                                   double* partials, const PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  if (sc->done) return;
+  const int lane = threadIdx.x & 31;
+  const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+  double acc = 0.0;
+  for (int row = warp; row < n; row += nw) {
+    const int b = rowptr[row], e = rowptr[row + 1];
+    double s = 0.0;
+    for (int k = b + lane; k < e; k += 32) s += val[k] * p[colind[k]];
+    s = warp_sum_down(s);
+    if (lane == 0) {
+      const double qi = fixed[row] ? 0.0 : s;
+      q[row] = qi;
+      acc += qi * p[row];
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(kThreads) k_alpha(const double* partials, int nparts, PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  if (sc->done) return;
+  const double pap = sum_partials(partials, nparts, 1, 0, sh);
+  if (threadIdx.x == 0) {
+    sc->pap = pap;
+    if (!(pap > 0.0) || !isfinite(pap)) {
+      sc->alpha = 0.0;
+      sc->breakdown = 1;
+      sc->done = 1;
+    } else {
+      sc->alpha = sc->rz / pap;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_update(int n, const double* __restrict__ dinv, double* x, double* r,
+                                                     double* z, const double* __restrict__ p,
+                                                     const double* __restrict__ q, double* partials,
+                                                     const PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  if (sc->done) return;
+  const double a = sc->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    const double ri = r[i] - a * q[i];
+    const double zi = dinv[i] * ri;
+    r[i] = ri;
+    z[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_beta(const double* partials, int nparts, PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  if (sc->done) return;
+  const double rz = sum_partials(partials, nparts, 2, 0, sh);
+  const double rr = sum_partials(partials, nparts, 2, 1, sh);
+  if (threadIdx.x == 0) {
+    sc->iters += 1;
+    sc->beta = sc->rz != 0.0 ? rz / sc->rz : 0.0;
+    sc->rz = rz;
+    sc->rr = rr;
+    if (rr <= sc->tol2 || !isfinite(rr)) sc->done = 1;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_pupdate(int n, const double* __restrict__ z, double* p,
+                                                      const PcgScal* sc) {
+  if (sc->done) return;
+  const double bt = sc->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + bt * p[i];
+}
+
+__global__ void __launch_bounds__(kThreads) k_norms(int n, const double* __restrict__ v,
+                                                    const unsigned char* __restrict__ fixed, double* partials) {
+  __shared__ double sh[kWarps];
+  double f = 0.0, a = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double vi = v[i];
+    a += vi * vi;
+    if (!fixed[i]) f += vi * vi;
+  }
+  f = block_sum(f, sh);
+  a = block_sum(a, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = f;
+    partials[2 * blockIdx.x + 1] = a;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_norms_fin(const double* partials, int nparts, double* out) {
+  __shared__ double sh[kWarps];
+  const double f = sum_partials(partials, nparts, 2, 0, sh);
+  const double a = sum_partials(partials, nparts, 2, 1, sh);
+  if (threadIdx.x == 0) {
+    out[0] = f;
+    out[1] = a;
+  }
+}
+
+}  // namespace
+
+struct w3g_csr {
+  w3g_context* ctx = nullptr;
+  int n = 0;
+  long long nnz = 0, ncontrib = 0;
+  int *rowptr = nullptr, *colind = nullptr, *diag = nullptr, *cptr = nullptr, *csrc = nullptr;
+  double* val = nullptr;
+  // PCG work
+  int grid = 0;
+  double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+  double* partials = nullptr;
+  PcgScal* sc = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t batch = nullptr;
+  const void* graph_fixed = nullptr;   // mask the batch graph was captured with
+};
+
+namespace {
+
+#define CKS(call)                                                                    \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return w3g_fail(W3G_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void csr_free(w3g_csr* m) {
+  if (m->batch) cudaGraphExecDestroy(m->batch);
+  void* ptrs[] = {m->rowptr, m->colind, m->diag, m->cptr, m->csrc, m->val, m->x, m->r, m->z, m->p, m->q,
+                  m->dinv, m->partials, m->sc};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (m->ev_in) cudaEventDestroy(m->ev_in);
+  if (m->ev_out) cudaEventDestroy(m->ev_out);
+  if (m->stream) cudaStreamDestroy(m->stream);
+}
+
+// the part of the pattern built by one host thread: rows [r0, r1)
+struct RowsPart {
+  int r0 = 0, r1 = 0;
+  std::vector<int> row_nnz, diag_rel, col, cnt, src;
+};
+
+// block holding element-vector entry `e` (blocks are in einf_off order)
+int block_of(const std::vector<BlockDesc>& B, long long e) {
+  int lo = 0, hi = (int)B.size() - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (B[mid].einf_off <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+void build_rows(const std::vector<BlockDesc>& B, const std::vector<int>& ed, const std::vector<int>& ifv_ptr,
+                const std::vector<long long>& ifv_src, RowsPart& P) {
+  std::vector<std::pair<int, int>> pr;   // (column, element-stiffness index)
+  for (int g = P.r0; g < P.r1; ++g) {
+    pr.clear();
+    for (int k = ifv_ptr[g]; k < ifv_ptr[g + 1]; ++k) {
+      // ifv_src entries ascend in element-vector order: block, dof, element
+      const long long e = ifv_src[k];
+      const BlockDesc& d = B[block_of(B, e)];
+      const long long rel = e - d.einf_off;
+      const int r = (int)(rel / d.span), i = (int)(rel % d.span);
+      const int* dofs = &ed[d.einf_off + (size_t)i * d.totdof];
+      const long long base = d.estiff_off + (long long)i * d.utsz;
+      for (int c = 0; c < d.totdof; ++c) {
+        const int lo = std::min(r, c), hi = std::max(r, c);
+        pr.emplace_back(dofs[c] - 1, (int)(base + (long long)hi * (hi + 1) / 2 + lo));
+      }
+    }
+    if (pr.empty()) {   // a dof no element touches: an empty coefficient on the diagonal
+      P.col.push_back(g);
+      P.cnt.push_back(0);
+      P.row_nnz.push_back(1);
+      P.diag_rel.push_back(0);
+      continue;
+    }
+    std::stable_sort(pr.begin(), pr.end(),
+                     [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
+    int nz = 0, drel = -1;
+    for (size_t k = 0; k < pr.size(); ++k) {
+      if (k == 0 || pr[k].first != pr[k - 1].first) {
+        if (pr[k].first == g) drel = nz;
+        P.col.push_back(pr[k].first);
+        P.cnt.push_back(0);
+        ++nz;
+      }
+      P.cnt.back()++;
+      P.src.push_back(pr[k].second);
+    }
+    P.row_nnz.push_back(nz);
+    P.diag_rel.push_back(drel);
+  }
+}
+
+int grid_for(int device) {
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  return std::max(1, sms) * 8;
+}
+
+}  // namespace
+
+extern "C" {
+
+int w3g_csr_create(w3g_context* c, w3g_csr** out) {
+  if (!c || !out) return w3g_fail(W3G_EARG, "null argument");
+  CKS(cudaSetDevice(c->device));
+  const DeviceModel& m = c->m;
+  const int n = m.nodof;
+  if (m.estiff_total >= INT_MAX) return w3g_fail(W3G_EUNSUPPORTED, "element stiffnesses exceed 2^31 values");
+  std::vector<int> ed(m.einf_total);
+  std::vector<int> ifv_ptr(n + 1);
+  std::vector<long long> ifv_src(m.einf_total);
+  CKS(cudaMemcpy(ed.data(), m.edest, ed.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  CKS(cudaMemcpy(ifv_ptr.data(), m.ifv_rowptr, ifv_ptr.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  CKS(cudaMemcpy(ifv_src.data(), m.ifv_src, ifv_src.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+
+  // rows in parts of similar contribution counts, one host thread each
+  const int nthreads = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  std::vector<RowsPart> parts(nthreads);
+  {
+    const long long total = ifv_ptr[n];
+    int r = 0;
+    for (int t = 0; t < nthreads; ++t) {
+      parts[t].r0 = r;
+      const long long target = total * (t + 1) / nthreads;
+      while (r < n && (t == nthreads - 1 || ifv_ptr[r] < target)) ++r;
+      parts[t].r1 = r;
+    }
+    parts[nthreads - 1].r1 = n;
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t)
+      th.emplace_back(build_rows, std::cref(c->blocks), std::cref(ed), std::cref(ifv_ptr), std::cref(ifv_src),
+                      std::ref(parts[t]));
+    for (auto& t : th) t.join();
+  }
+  long long nnz = 0, ncontrib = 0;
+  for (const RowsPart& P : parts) {
+    nnz += (long long)P.col.size();
+    ncontrib += (long long)P.src.size();
+  }
+  if (nnz >= INT_MAX || ncontrib >= INT_MAX) return w3g_fail(W3G_EUNSUPPORTED, "global stiffness exceeds 2^31 entries");
+  for (const RowsPart& P : parts)
+    for (int d : P.diag_rel)
+      if (d < 0) return w3g_fail(W3G_EARG, "equation row without its diagonal coefficient");
+
+  w3g_csr* s = new w3g_csr;
+  s->ctx = c;
+  s->n = n;
+  s->nnz = nnz;
+  s->ncontrib = ncontrib;
+  s->grid = grid_for(c->device);
+  std::vector<int> rowptr(n + 1), diag(n), cptr(nnz + 1);
+  {
+    int row = 0;
+    long long z = 0, k = 0;
+    rowptr[0] = 0;
+    for (const RowsPart& P : parts) {
+      for (size_t j = 0; j < P.row_nnz.size(); ++j) {
+        diag[row] = (int)z + P.diag_rel[j];
+        z += P.row_nnz[j];
+        rowptr[++row] = (int)z;
+      }
+    }
+    long long zz = 0;
+    for (const RowsPart& P : parts)
+      for (int cn : P.cnt) {
+        cptr[zz++] = (int)k;
+        k += cn;
+      }
+    cptr[nnz] = (int)k;
+  }
+  cudaError_t e = cudaSuccess;
+  auto al = [&](auto** p, size_t count) {
+    if (e == cudaSuccess) e = cudaMalloc((void**)p, std::max<size_t>(1, count) * sizeof(**p));
+  };
+  al(&s->rowptr, n + 1);
+  al(&s->colind, nnz);
+  al(&s->diag, n);
+  al(&s->cptr, nnz + 1);
+  al(&s->csrc, ncontrib);
+  al(&s->val, nnz);
+  al(&s->x, n);
+  al(&s->r, n);
+  al(&s->z, n);
+  al(&s->p, n);
+  al(&s->q, n);
+  al(&s->dinv, n);
+  al(&s->partials, 4 * (size_t)s->grid);   // PCG partials, then the norms' partials
+  al(&s->sc, 1);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_out, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMemcpy(s->rowptr, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s->diag, diag.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s->cptr, cptr.data(), (nnz + 1) * sizeof(int), cudaMemcpyHostToDevice);
+  long long zo = 0, ko = 0;
+  for (const RowsPart& P : parts) {
+    if (e == cudaSuccess && !P.col.empty())
+      e = cudaMemcpy(s->colind + zo, P.col.data(), P.col.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !P.src.empty())
+      e = cudaMemcpy(s->csrc + ko, P.src.data(), P.src.size() * sizeof(int), cudaMemcpyHostToDevice);
+    zo += (long long)P.col.size();
+    ko += (long long)P.src.size();
+  }
+  if (e == cudaSuccess) e = cudaMemset(s->val, 0, nnz * sizeof(double));
+  if (e != cudaSuccess) {
+    csr_free(s);
+    delete s;
+    return w3g_fail(W3G_ECUDA, std::string("w3g_csr_create: ") + cudaGetErrorString(e));
+  }
+  *out = s;
+  return 0;
+}
+
+int w3g_csr_destroy(w3g_csr* s) {
+  if (!s) return 0;
+  cudaSetDevice(s->ctx->device);
+  csr_free(s);
+  delete s;
+  return 0;
+}
+
+int w3g_csr_info(w3g_csr* s, int* n, long long* nnz, void** d_rowptr, void** d_colind, void** d_values) {
+  if (!s) return w3g_fail(W3G_EARG, "null csr");
+  if (n) *n = s->n;
+  if (nnz) *nnz = s->nnz;
+  if (d_rowptr) *d_rowptr = s->rowptr;
+  if (d_colind) *d_colind = s->colind;
+  if (d_values) *d_values = s->val;
+  return 0;
+}
+
+int w3g_csr_assemble_dev(w3g_csr* s, void* stream) {
+  if (!s) return w3g_fail(W3G_EARG, "null csr");
+  w3g_context* c = s->ctx;
+  CKS(cudaSetDevice(c->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  const int grid = (int)std::min<long long>((s->nnz + kThreads - 1) / kThreads, 16LL * s->grid);
+  if (c->precision == W3G_TANGENT_FP64)
+    k_assemble<double><<<std::max(1, grid), kThreads, 0, st>>>(s->nnz, s->cptr, s->csrc, c->s.estiff, s->val);
+  else
+    k_assemble<float><<<std::max(1, grid), kThreads, 0, st>>>(s->nnz, s->cptr, s->csrc, c->s.estiff32, s->val);
+  CKS(cudaGetLastError());
+  return 0;
+}
+
+int w3g_csr_download(w3g_csr* s, int* rowptr, int* colind, double* values) {
+  if (!s) return w3g_fail(W3G_EARG, "null csr");
+  CKS(cudaSetDevice(s->ctx->device));
+  CKS(cudaDeviceSynchronize());
+  if (rowptr) CKS(cudaMemcpy(rowptr, s->rowptr, (s->n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+  if (colind) CKS(cudaMemcpy(colind, s->colind, s->nnz * sizeof(int), cudaMemcpyDeviceToHost));
+  if (values) CKS(cudaMemcpy(values, s->val, s->nnz * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale, void* d_x, double rtol, int maxit,
+                void* stream, int* iters, double* relres) {
+  if (!s || !d_fixed || !d_b || !d_x) return w3g_fail(W3G_EARG, "null argument");
+  if (maxit < 0 || !(rtol >= 0.0)) return w3g_fail(W3G_EARG, "bad rtol / maxit");
+  CKS(cudaSetDevice(s->ctx->device));
+  const int n = s->n, G = s->grid;
+  const unsigned char* fixed = (const unsigned char*)d_fixed;
+  cudaStream_t st = s->stream;
+  // ordered after the caller's stream
+  CKS(cudaEventRecord(s->ev_in, (cudaStream_t)stream));
+  CKS(cudaStreamWaitEvent(st, s->ev_in, 0));
+  k_dinv<<<G, kThreads, 0, st>>>(n, s->diag, s->val, fixed, s->dinv);
+  k_pcg_init<<<G, kThreads, 0, st>>>(n, fixed, (const double*)d_b, b_scale, s->dinv, s->x, s->r, s->z, s->p,
+                                     s->partials);
+  k_pcg_init_fin<<<1, kThreads, 0, st>>>(s->partials, G, rtol, s->sc);
+  CKS(cudaGetLastError());
+  if (!s->batch || s->graph_fixed != d_fixed) {
+    if (s->batch) cudaGraphExecDestroy(s->batch);
+    s->batch = nullptr;
+    cudaGraph_t g;
+    CKS(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < kBatch; ++it) {
+      k_spmv<<<G, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+      k_alpha<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
+      k_update<<<G, kThreads, 0, st>>>(n, s->dinv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
+      k_beta<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
+      k_pupdate<<<G, kThreads, 0, st>>>(n, s->z, s->p, s->sc);
+    }
+    CKS(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&s->batch, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return w3g_fail(W3G_ECUDA, std::string("pcg graph: ") + cudaGetErrorString(e));
+    s->graph_fixed = d_fixed;
+  }
+  PcgScal h{};
+  CKS(cudaMemcpyAsync(&h, s->sc, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  while (!h.done && h.iters < maxit) {
+    CKS(cudaGraphLaunch(s->batch, st));
+    CKS(cudaMemcpyAsync(&h, s->sc, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CKS(cudaStreamSynchronize(st));
+  }
+  CKS(cudaMemcpyAsync(d_x, s->x, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  CKS(cudaEventRecord(s->ev_out, st));
+  CKS(cudaStreamWaitEvent((cudaStream_t)stream, s->ev_out, 0));
+  CKS(cudaStreamSynchronize(st));
+  if (iters) *iters = h.iters;
+  const double rel = h.bb > 0.0 ? std::sqrt(h.rr / h.bb) : 0.0;
+  if (relres) *relres = rel;
+  if (h.breakdown) return W3G_PCG_BREAKDOWN;
+  return (h.rr <= h.tol2) ? 0 : W3G_PCG_MAXIT;
+}
+
+int w3g_residual_norms_dev(w3g_csr* s, const void* d_v, const void* d_fixed, void* d_out, void* stream) {
+  if (!s || !d_v || !d_fixed || !d_out) return w3g_fail(W3G_EARG, "null argument");
+  CKS(cudaSetDevice(s->ctx->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  // its own partials (after the PCG's), so that it may run on any stream
+  double* part = s->partials + 2 * (size_t)s->grid;
+  k_norms<<<s->grid, kThreads, 0, st>>>(s->n, (const double*)d_v, (const unsigned char*)d_fixed, part);
+  k_norms_fin<<<1, kThreads, 0, st>>>(part, s->grid, (double*)d_out);
+  CKS(cudaGetLastError());
+  return 0;
+}
+
+}  // extern "C"

@@ -1,9 +1,9 @@
-// w3g_tangent_tc.cu -- precision form of the 8-node brick tangent on the
+// w3g_tangent_tc.cu -- precision forms of the 8-node brick tangent on the
 // fifth-generation tensor cores: Ke = sum_gp B^T [D*] B in TF32 or BF16
 // operands with FP32 accumulation (tcgen05.mma, accumulator in tensor
 // memory), plus the geometric stiffness G^T T G in FP32 on the CUDA cores.
 //
-// One CTA (4 warps) = one tile of up to 5 elements of one block. Per
+// One CTA (8 warps) = one tile of up to 5 elements of one block. Per
 // element the material part is a 24 x 24 x 48 product: with the 48
 // contraction indices (Gauss point, strain component) as K,
 //   A (dof x K) = B^T,   Bop (dof x K) = ([D*] B)^T,   Ke = A Bop^T.
@@ -13,18 +13,34 @@
 // the element matrices (the rest is discarded: the tensor core has the
 // throughput to spare, the tangent is bound by its operands and Ke in HBM).
 //
-//   phase 1  (40 threads) per (element, Gauss point) as in the FP32 kernel:
-//            gradients at x(n+1), w det[J] [D*] = [q][D][q]^T - Q-bar, and
-//            w det[J] {T}, to shared memory (FP32)
-//   phase 2  (128 threads) operands written in the canonical no-swizzle
-//            K-major layout (8-row x 16-byte core matrices), geometric
-//            stiffness per node pair; fence.proxy.async
+//   phase 1  per (element, Gauss point), 6 threads each (240 of 256): the
+//            gradients at x(n+1), the rotation q(R), and one row each of
+//            w det[J] [D*] = [q][D][q]^T - Q-bar, and w det[J] {T}, to
+//            shared memory (FP32)
+//   phase 2  operands written in the canonical no-swizzle K-major layout
+//            (8-row x 16-byte core matrices), one 16-byte store per core
+//            matrix row; geometric stiffness per node pair;
+//            fence.proxy.async
 //   phase 3  thread 0 issues the MMAs (tcgen05.mma.cta_group::1 with shared
 //            memory descriptors) and commits to an mbarrier; all threads
 //            wait (bounded)
-//   phase 4  each warp reads its 32 TMEM lanes (rows) with tcgen05.ld,
-//            keeps the element's upper triangle, adds the geometric part,
-//            stages Ke in shared memory and stores it coalesced (FP32)
+//   phase 4  warps 0-3 read their 32 TMEM lanes (rows) with tcgen05.ld; the
+//            element matrices are symmetrised, the geometric part added,
+//            and each is projected onto the matrices that annihilate rigid
+//            translations, K' = P K P with P = I - T T^T / 8 (T: the three
+//            unit translations of the element's 8 nodes); Ke is staged in
+//            shared memory and stored coalesced (FP32)
+//
+// The projection. The exact element tangent annihilates rigid translations
+// (the shape-function gradients sum to zero at every point), so P Ke P = Ke
+// in exact arithmetic; rounding the operands to 11 (TF32) or 8 (BF16)
+// significant bits breaks this at the level of the format's unit roundoff,
+// and the tensor core's FP32 accumulation adds a systematic bias on the
+// diagonal. Assembled over the mesh, that error acts coherently on the
+// near-rigid modes that only the displacement constraints hold (its energy
+// grows with the element count while theirs does not), and the global
+// Newton iteration stops converging on large meshes. The projection removes
+// exactly that component of the error and nothing of the exact matrix.
 #include <cstdint>
 #include <cuda_bf16.h>
 #include "w3g_internal.cuh"
@@ -38,9 +54,11 @@ namespace {
 
 constexpr int NN = Hex8::NN, NG = Hex8::NG, TOT = Hex8::TOTDOF, UT = Hex8::UTSZ;
 constexpr int kTcElems = 5;            // elements per tile
+constexpr int kTcRows = kTcElems * TOT;   // 120 live rows
 constexpr int kRows = 128;             // M = N
 constexpr int kK = NG * 6;             // 48
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;
+constexpr int kSubs = 6;               // threads per (element, Gauss point) in phase 1
 constexpr int kTmemCols = 128;
 constexpr long long kWaitLimit = 1ll << 22;   // mbarrier polls before giving up
 
@@ -48,13 +66,14 @@ template <bool kBF16>
 struct TcLayout {
   static constexpr int kBytes = kBF16 ? 2 : 4;
   static constexpr int kPerCore = 16 / kBytes;          // K elements per core-matrix row
+  static constexpr int kChunks = kK / kPerCore;         // core matrices along K
   static constexpr int kLBO = 128;                      // next core matrix along K
-  static constexpr int kSBO = (kK / kPerCore) * 128;    // next 8-row group
+  static constexpr int kSBO = kChunks * 128;            // next 8-row group
   static constexpr int kOpBytes = kRows * kK * kBytes;  // one operand
   static constexpr int kKStep = kBF16 ? 16 : 8;         // K per MMA
   static constexpr int kSteps = kK / kKStep;
-  __device__ static __forceinline__ int offset(int r, int k) {
-    return (r >> 3) * kSBO + (k / kPerCore) * kLBO + (r & 7) * 16 + (k % kPerCore) * kBytes;
+  __device__ static __forceinline__ int offset(int r, int chunk) {
+    return (r >> 3) * kSBO + chunk * kLBO + (r & 7) * 16;
   }
 };
 
@@ -65,6 +84,16 @@ struct TcStatic {
   float D[kTcElems][NG][21];
   float T[kTcElems][NG][6];
   float kg[kTcElems][36];
+  union {
+    struct {                         // phase 1
+      float C[kTcElems][NG][21];
+      float cs[kTcElems][NG][6];
+    } p1;
+    struct {                         // phase 4
+      float mrow[kTcRows][3];        // row means over the nodes, per column component
+      float mblk[kTcElems][9];       // means of the row means, per (row, column) component
+    } p4;
+  } u;
   unsigned long long mbar;
   uint32_t tmem_base;
   int timeout;
@@ -92,12 +121,6 @@ __host__ __device__ constexpr uint32_t instr_desc() {
          | ((uint32_t)(kRows >> 4) << 24);     // M >> 4
 }
 
-// Operands are rounded to the input format to nearest (the tensor core
-// would otherwise drop the low mantissa bits of an FP32 operand). With
-// kSplit, v = hi + lo with both parts in the input format, and the product
-// of two split operands is taken as hi*hi + hi*lo + lo*hi (the lo*lo term is
-// below FP32 rounding for TF32): three MMAs instead of one, and an error
-// near FP32's for TF32 (about 2^-16 relative for BF16).
 // one tcgen05.mma: D[tmem] (+)= A B^T over one K step, both operands in
 // shared memory (K-major, no swizzle)
 template <bool kBF16>
@@ -119,6 +142,12 @@ __device__ __forceinline__ void mma(uint32_t tmem, uint32_t a_addr, uint32_t b_a
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 
+// Operands are rounded to the input format to nearest (the tensor core
+// would otherwise drop the low mantissa bits of an FP32 operand). With
+// kSplit, v = hi + lo with both parts in the input format, and the product
+// of two split operands is taken as hi*hi + hi*lo + lo*hi (the lo*lo term is
+// below FP32 rounding for TF32): three MMAs instead of one, and an error
+// near FP32's for TF32 (about 2^-16 relative for BF16).
 template <bool kBF16>
 __device__ __forceinline__ float round_in(float v) {
   if (kBF16) return __bfloat162float(__float2bfloat16_rn(v));
@@ -127,17 +156,46 @@ __device__ __forceinline__ float round_in(float v) {
   return __uint_as_float(t);
 }
 
+// one core-matrix row (16 bytes) of an operand: kPerCore consecutive K
+// values of row r, split into hi and lo parts when kSplit
 template <bool kBF16, bool kSplit>
-__device__ __forceinline__ void put(unsigned char* op, int r, int k, float v) {
-  const int o = TcLayout<kBF16>::offset(r, k);
-  const float hi = round_in<kBF16>(v);
-  if (kBF16) *reinterpret_cast<__nv_bfloat16*>(op + o) = __float2bfloat16_rn(hi);
-  else *reinterpret_cast<float*>(op + o) = hi;
-  if (kSplit) {
-    unsigned char* lo_op = op + 2 * TcLayout<kBF16>::kOpBytes;   // A_lo after B_hi, B_lo after A_lo
-    const float lo = round_in<kBF16>(v - hi);
-    if (kBF16) *reinterpret_cast<__nv_bfloat16*>(lo_op + o) = __float2bfloat16_rn(lo);
-    else *reinterpret_cast<float*>(lo_op + o) = lo;
+__device__ __forceinline__ void put_chunk(unsigned char* op, int r, int chunk, const float* v) {
+  using L = TcLayout<kBF16>;
+  const int o = L::offset(r, chunk);
+  float hi[L::kPerCore], lo[L::kPerCore];
+#pragma unroll
+  for (int j = 0; j < L::kPerCore; ++j) {
+    hi[j] = round_in<kBF16>(v[j]);
+    lo[j] = kSplit ? round_in<kBF16>(v[j] - hi[j]) : 0.f;
+  }
+  uint4 wh, wl;
+  if (kBF16) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      h[j] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi[2 * j])) |
+             ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi[2 * j + 1])) << 16);
+      l[j] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo[2 * j])) |
+             ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo[2 * j + 1])) << 16);
+    }
+    wh = make_uint4(h[0], h[1], h[2], h[3]);
+    wl = make_uint4(l[0], l[1], l[2], l[3]);
+  } else {
+    wh = make_uint4(__float_as_uint(hi[0]), __float_as_uint(hi[1]), __float_as_uint(hi[2]), __float_as_uint(hi[3]));
+    wl = make_uint4(__float_as_uint(lo[0]), __float_as_uint(lo[1]), __float_as_uint(lo[2]), __float_as_uint(lo[3]));
+  }
+  *reinterpret_cast<uint4*>(op + o) = wh;
+  if (kSplit) *reinterpret_cast<uint4*>(op + 2 * L::kOpBytes + o) = wl;   // A_lo after B_hi, B_lo after A_lo
+}
+
+// row j (run-time) of the 6x6 q held in registers, without local memory
+__device__ __forceinline__ void row_of(const float* q, int j, float* out) {
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    float v = q[m];
+#pragma unroll
+    for (int jj = 1; jj < 6; ++jj) v = j == jj ? q[6 * jj + m] : v;
+    out[m] = v;
   }
 }
 
@@ -164,21 +222,19 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
     S.timeout = 0;
   }
   for (int k = tid; k < NG * 3 * NN + NG; k += kThreads) S.dn[k] = (float)a.dn[0][k];
-  // ---- gather: x(n+1) relative to node 1 of each element ----
-  for (int idx = tid; idx < kTcElems * NN; idx += kThreads) {
-    const int e = idx / NN, node = idx % NN;
+  // ---- gather: x(n+1) relative to node 1, one coordinate per thread ----
+  if (tid < kTcElems * 3 * NN) {
+    const int e = tid / (3 * NN), dn = tid % (3 * NN), d = dn / NN, node = dn % NN;
     if (e < ch.n) {
       const long long dbase = bd.einf_off + (long long)(ch.i0 + e) * TOT;
-      for (int d = 0; d < 3; ++d) {
-        double ref = a.c[a.cdest[dbase + d * NN] - 1];
-        double v = a.c[a.cdest[dbase + d * NN + node] - 1];
-        if (bd.geonl) {
-          const int e0 = a.edest[dbase + d * NN] - 1, e1 = a.edest[dbase + d * NN + node] - 1;
-          ref = ref + a.u[e0] + a.du[e0];
-          v = v + a.u[e1] + a.du[e1];
-        }
-        S.x[e][d * NN + node] = (float)(v - ref);
+      double ref = a.c[a.cdest[dbase + d * NN] - 1];
+      double v = a.c[a.cdest[dbase + d * NN + node] - 1];
+      if (bd.geonl) {
+        const int e0 = a.edest[dbase + d * NN] - 1, e1 = a.edest[dbase + d * NN + node] - 1;
+        ref = ref + a.u[e0] + a.du[e0];
+        v = v + a.u[e1] + a.du[e1];
       }
+      S.x[e][dn] = (float)(v - ref);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -186,101 +242,145 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = S.tmem_base;
 
-  // ---- phase 1: one (element, Gauss point) per thread ----
-  if (tid < kTcElems * NG) {
-    const int e = tid / NG, gp = tid % NG;
-    if (e < ch.n) {
-      const int i = ch.i0 + e;
-      const float* dnx = S.dn + (gp * 3 + 0) * NN;
-      const float* dne = S.dn + (gp * 3 + 1) * NN;
-      const float* dnz = S.dn + (gp * 3 + 2) * NN;
-      const float w = S.dn[NG * 3 * NN + gp];
-      float gama[9], dj;
-      jacobian_inverse<NN, float>(dnx, dne, dnz, S.x[e], S.x[e] + NN, S.x[e] + 2 * NN, gama, dj);
-      float* g = S.g[e][gp];
-      for (int n = 0; n < NN; ++n)
-        shape_gradient<float>(gama, dnx[n], dne[n], dnz[n], g[3 * n], g[3 * n + 1], g[3 * n + 2]);
-      const float f = w * dj;
-      float C[21];
-      load_D21<float, NG>(a, bd, i, gp, f, C);
-      float* D = S.D[e][gp];
-      float* Tw = S.T[e][gp];
-      if (bd.geonl) {
-        const long long gpi = bd.gp_off + (long long)i * NG + gp;
-        float R[9], q[36], ur[6], cs[6];
-        for (int k = 0; k < 9; ++k) R[k] = (float)a.rot_n1[gpi * 9 + k];
-        for (int k = 0; k < 6; ++k) ur[k] = (float)a.urcs_n1[gpi * 9 + k];
-        rotation_q2<float>(R, q);
-        qmply<float>(q, ur, cs);
-        for (int j = 0; j < 6; ++j) {
-          float tc[6];
-          for (int kk = 0; kk < 6; ++kk) {
-            float s = 0.f;
-            for (int m = 0; m < 6; ++m) s += q[6 * j + m] * C[low(m, kk)];
-            tc[kk] = s;
-          }
-          for (int kk = 0; kk <= j; ++kk) {
-            float s = 0.f;
-            for (int m = 0; m < 6; ++m) s += tc[m] * q[6 * kk + m];
-            D[low(j, kk)] = s;
-          }
-        }
-        if (a.qbar) {
-          const float wf = dj * w, halfw = 0.5f * wf;
-          const float xx = cs[0], yy = cs[1], zz = cs[2], xy = cs[3], yz = cs[4], xz = cs[5];
-          D[low(0, 0)] -= 2.f * xx * wf;
-          D[low(1, 1)] -= 2.f * yy * wf;
-          D[low(2, 2)] -= 2.f * zz * wf;
-          D[low(3, 0)] -= xy * wf;
-          D[low(5, 0)] -= xz * wf;
-          D[low(3, 1)] -= xy * wf;
-          D[low(4, 1)] -= yz * wf;
-          D[low(4, 2)] -= yz * wf;
-          D[low(5, 2)] -= xz * wf;
-          D[low(3, 3)] -= halfw * (xx + yy);
-          D[low(4, 4)] -= halfw * (yy + zz);
-          D[low(5, 5)] -= halfw * (xx + zz);
-          D[low(4, 3)] -= wf * xz;
-          D[low(5, 3)] -= wf * yz;
-          D[low(5, 4)] -= wf * xy;
-        }
-        for (int k = 0; k < 6; ++k) Tw[k] = cs[k] * f;
-      } else {
-        for (int k = 0; k < 21; ++k) D[k] = C[k];
-        for (int k = 0; k < 6; ++k) Tw[k] = 0.f;
+  // ---- phase 1: 6 threads per (element, Gauss point) ----
+  const int item = tid / kSubs, sub = tid % kSubs;
+  const int pe = item / NG, pgp = item % NG;
+  const bool p1 = tid < kTcElems * NG * kSubs && pe < ch.n;
+  float q[36];
+  float f = 0.f, dj = 0.f;
+  if (p1) {
+    const int i = ch.i0 + pe;
+    const float* dnx = S.dn + (pgp * 3 + 0) * NN;
+    const float* dne = S.dn + (pgp * 3 + 1) * NN;
+    const float* dnz = S.dn + (pgp * 3 + 2) * NN;
+    const float w = S.dn[NG * 3 * NN + pgp];
+    float gama[9];
+    jacobian_inverse<NN, float>(dnx, dne, dnz, S.x[pe], S.x[pe] + NN, S.x[pe] + 2 * NN, gama, dj);
+    float* g = S.g[pe][pgp];
+    for (int n = sub; n < NN; n += kSubs)
+      shape_gradient<float>(gama, dnx[n], dne[n], dnz[n], g[3 * n], g[3 * n + 1], g[3 * n + 2]);
+    f = w * dj;
+    // w det[J] [D], lower triangle row-wise, entries sub, sub + 6, ... (as
+    // load_D21: cep_blocks, or for mm10 history1 words 0-35)
+    if (bd.mat == W3G_MAT_CRYSTAL) {
+      const double* H = a.hist1 + bd.hist_off + ((long long)i * NG + pgp) * kHistMM10;
+      for (int k = sub; k < 21; k += kSubs) {
+        int r = 0, c = k;
+        while (c > r) { c -= r + 1; ++r; }   // k = r(r+1)/2 + c, c <= r
+        S.u.p1.C[pe][pgp][k] = f * (float)H[r + 6 * c];
       }
+    } else {
+      const long long cb = bd.cep_off + ((long long)pgp * bd.span + i) * 21;
+      for (int k = sub; k < 21; k += kSubs) S.u.p1.C[pe][pgp][k] = f * (float)a.cep[cb + k];
+    }
+    if (bd.geonl) {
+      const long long gpi = bd.gp_off + (long long)i * NG + pgp;
+      float R[9];
+      for (int k = 0; k < 9; ++k) R[k] = (float)a.rot_n1[gpi * 9 + k];
+      rotation_q2<float>(R, q);
+      float qrow[6];
+      row_of(q, sub, qrow);
+      float s = 0.f;
+      for (int m = 0; m < 6; ++m) s += qrow[m] * (float)a.urcs_n1[gpi * 9 + m];
+      S.u.p1.cs[pe][pgp][sub] = s;   // Cauchy stress component `sub`
+    }
+  }
+  __syncthreads();
+  if (p1) {
+    float* D = S.D[pe][pgp];
+    const float* C = S.u.p1.C[pe][pgp];
+    const int j = sub;
+    if (bd.geonl) {
+      // row j of q C q^T (entries kk <= j), then the Q-bar terms of row j
+      float tc[6], qrow[6];
+      row_of(q, j, qrow);
+#pragma unroll
+      for (int kk = 0; kk < 6; ++kk) {
+        float s = 0.f;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) s += qrow[m] * C[low(m, kk)];
+        tc[kk] = s;
+      }
+#pragma unroll
+      for (int kk = 0; kk < 6; ++kk) {
+        float s = 0.f;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) s += tc[m] * q[6 * kk + m];
+        if (kk <= j) D[low(j, kk)] = s;
+      }
+      const float* cs = S.u.p1.cs[pe][pgp];
+      if (a.qbar) {
+        const float wf = f, halfw = 0.5f * wf;
+        const float xx = cs[0], yy = cs[1], zz = cs[2], xy = cs[3], yz = cs[4], xz = cs[5];
+        switch (j) {
+          case 0: D[low(0, 0)] -= 2.f * xx * wf; break;
+          case 1: D[low(1, 1)] -= 2.f * yy * wf; break;
+          case 2: D[low(2, 2)] -= 2.f * zz * wf; break;
+          case 3:
+            D[low(3, 0)] -= xy * wf;
+            D[low(3, 1)] -= xy * wf;
+            D[low(3, 3)] -= halfw * (xx + yy);
+            break;
+          case 4:
+            D[low(4, 1)] -= yz * wf;
+            D[low(4, 2)] -= yz * wf;
+            D[low(4, 3)] -= wf * xz;
+            D[low(4, 4)] -= halfw * (yy + zz);
+            break;
+          default:
+            D[low(5, 0)] -= xz * wf;
+            D[low(5, 2)] -= xz * wf;
+            D[low(5, 3)] -= wf * yz;
+            D[low(5, 4)] -= wf * xy;
+            D[low(5, 5)] -= halfw * (xx + zz);
+            break;
+        }
+      }
+      S.T[pe][pgp][j] = cs[j] * f;
+    } else {
+      for (int kk = 0; kk <= j; ++kk) D[low(j, kk)] = C[low(j, kk)];
+      S.T[pe][pgp][j] = 0.f;
     }
   }
   __syncthreads();
 
   // ---- phase 2: operands (row = 24 e + dof, dof = 8 i + a; k = 6 gp + m) ----
-  for (int idx = tid; idx < kRows * kK; idx += kThreads) {
-    const int r = idx / kK, k = idx % kK;
-    const int e = r / TOT;
-    float va = 0.f, vb = 0.f;
-    if (r < kTcElems * TOT && e < ch.n) {
-      const int d = r % TOT, di = d / NN, na = d % NN;
-      const int gp = k / 6, m = k % 6;
-      const float* g = S.g[e][gp];
-      const float gx = g[3 * na], gy = g[3 * na + 1], gz = g[3 * na + 2];
-      const float* D = S.D[e][gp];
-      if (di == 0) {
-        va = m == 0 ? gx : m == 3 ? gy : m == 5 ? gz : 0.f;
-        vb = D[low(m, 0)] * gx + D[low(m, 3)] * gy + D[low(m, 5)] * gz;
-      } else if (di == 1) {
-        va = m == 1 ? gy : m == 3 ? gx : m == 4 ? gz : 0.f;
-        vb = D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz;
-      } else {
-        va = m == 2 ? gz : m == 4 ? gy : m == 5 ? gx : 0.f;
-        vb = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
+  {
+    const int r = tid & (kRows - 1);
+    const int e = r / TOT, d = r % TOT, di = d / NN, na = d % NN;
+    const bool live = r < kTcRows && e < ch.n;
+    const int c0 = (tid >> 7) * (L::kChunks / 2), c1 = c0 + L::kChunks / 2;
+    for (int c = c0; c < c1; ++c) {
+      float va[L::kPerCore], vb[L::kPerCore];
+#pragma unroll
+      for (int j = 0; j < L::kPerCore; ++j) {
+        const int k = c * L::kPerCore + j, gp = k / 6, m = k % 6;
+        float x = 0.f, y = 0.f;
+        if (live) {
+          const float* g = S.g[e][gp];
+          const float gx = g[3 * na], gy = g[3 * na + 1], gz = g[3 * na + 2];
+          const float* D = S.D[e][gp];
+          if (di == 0) {
+            x = m == 0 ? gx : m == 3 ? gy : m == 5 ? gz : 0.f;
+            y = D[low(m, 0)] * gx + D[low(m, 3)] * gy + D[low(m, 5)] * gz;
+          } else if (di == 1) {
+            x = m == 1 ? gy : m == 3 ? gx : m == 4 ? gz : 0.f;
+            y = D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz;
+          } else {
+            x = m == 2 ? gz : m == 4 ? gy : m == 5 ? gx : 0.f;
+            y = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
+          }
+        }
+        va[j] = x;
+        vb[j] = y;
       }
+      put_chunk<kBF16, kSplit>(opA, r, c, va);
+      put_chunk<kBF16, kSplit>(opB, r, c, vb);
     }
-    put<kBF16, kSplit>(opA, r, k, va);
-    put<kBF16, kSplit>(opB, r, k, vb);
   }
   // geometric stiffness per node pair (kgstiff): sum_gp g_a . ({T} g_b)
-  for (int idx = tid; idx < kTcElems * 36; idx += kThreads) {
-    const int e = idx / 36, p = idx % 36;
+  if (tid < kTcElems * 36) {
+    const int e = tid / 36, p = tid % 36;
     int na = 0, r = p;
     while (r >= NN - na) { r -= NN - na; ++na; }
     const int nb = na + r;
@@ -335,42 +435,82 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   __syncthreads();
   const bool ok = S.timeout == 0;
 
-  // ---- phase 4: TMEM -> upper triangles (+ geometric part) -> Ke ----
-  float* ke = reinterpret_cast<float*>(opA);   // operands are consumed
-  const int r = 32 * warp + lane;
-  const int e = r / TOT, dr = r % TOT, ir = dr / NN, ar = dr % NN;
-  const float bf = (float)a.beta_fact;
+  // ---- phase 4: TMEM -> element matrices (full, FP32) in shared memory ----
+  float* kf = reinterpret_cast<float*>(opA);                 // [kTcElems][24][24]; operands are consumed
+  float* ke = reinterpret_cast<float*>(opA) + kTcElems * TOT * TOT;   // [kTcElems][UT]
+  if (warp < 4) {
+    const int r = 32 * warp + lane;
+    const int e = r / TOT, dr = r % TOT;
+    // the 32-column TMEM chunks holding this warp's elements' columns
+    const int e_lo = (32 * warp) / TOT, e_hi = min(kTcElems - 1, (32 * warp + 31) / TOT);
+    const int p_lo = (TOT * e_lo) / 32, p_hi = min(kRows / 32 - 1, (TOT * e_hi + TOT - 1) / 32);
+    for (int pass = p_lo; pass <= p_hi; ++pass) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * pass);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+            "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+            "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+            "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (r < kTcRows) {
 #pragma unroll
-  for (int pass = 0; pass < kRows / 32; ++pass) {
-    uint32_t v[32];
-    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(32 * pass);
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;");
-    if (r < kTcElems * TOT && e < ch.n) {
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int col = 32 * pass + j;
-        const int dc = col - TOT * e;
-        if (dc >= dr && dc < TOT) {
-          const int ic = dc / NN, ac = dc % NN;
-          float val = __uint_as_float(v[j]);
-          if (ic == ir) {
-            const int lo = ar < ac ? ar : ac, hi = ar < ac ? ac : ar;
-            val += S.kg[e][lo * NN - lo * (lo - 1) / 2 + (hi - lo)];
-          }
-          ke[e * UT + dc * (dc + 1) / 2 + dr] = ok ? val * bf : __int_as_float(0x7fc00000);
+        for (int j = 0; j < 32; ++j) {
+          const int dc = 32 * pass + j - TOT * e;
+          if (dc >= 0 && dc < TOT) kf[(e * TOT + dr) * TOT + dc] = __uint_as_float(v[j]);
         }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  // symmetrise, add the geometric part, row means over the nodes
+  float krow[TOT];
+  const int r = tid;
+  const int e = r / TOT, dr = r % TOT, ir = dr / NN, ar = dr % NN;
+  const bool row_live = r < kTcRows && e < ch.n;
+  if (row_live) {
+    const float* K = kf + e * TOT * TOT;
+    float m3[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int dc = 0; dc < TOT; ++dc) {
+      const int ic = dc / NN, ac = dc % NN;
+      float val = 0.5f * (K[dr * TOT + dc] + K[dc * TOT + dr]);
+      if (ic == ir) {
+        const int lo = ar < ac ? ar : ac, hi = ar < ac ? ac : ar;
+        val += S.kg[e][lo * NN - lo * (lo - 1) / 2 + (hi - lo)];
+      }
+      krow[dc] = val;
+      m3[ic] += val;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) S.u.p4.mrow[r][j] = m3[j] * (1.f / NN);
+  }
+  __syncthreads();
+  if (tid < kTcElems * 9) {
+    const int be = tid / 9, i = (tid % 9) / 3, j = tid % 3;
+    float s = 0.f;
+    if (be < ch.n)
+      for (int an = 0; an < NN; ++an) s += S.u.p4.mrow[be * TOT + i * NN + an][j];
+    S.u.p4.mblk[be][tid % 9] = s * (1.f / NN);
+  }
+  __syncthreads();
+  // K' = P K P: subtract the row and column means, add back the block mean
+  if (row_live) {
+    const float bf = (float)a.beta_fact;
+    const float* mr = S.u.p4.mrow[r];
+#pragma unroll
+    for (int dc = 0; dc < TOT; ++dc) {
+      if (dc < dr) continue;
+      const int ic = dc / NN;
+      const float val = krow[dc] - mr[ic] - S.u.p4.mrow[e * TOT + dc][ir] + S.u.p4.mblk[e][ir * 3 + ic];
+      ke[e * UT + dc * (dc + 1) / 2 + dr] = ok ? val * bf : __int_as_float(0x7fc00000);
+    }
+  }
   __syncthreads();
   if (tid == 0 && !ok) atomicExch(tc_timeout, 1);
   float* out = reinterpret_cast<float*>(a.estiff);
@@ -382,7 +522,8 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   }
 }
 
-// Dynamic shared memory per CTA: A and B (and their low parts when split).
+// Dynamic shared memory per CTA: A and B (and their low parts when split),
+// re-used in phase 4 for the full element matrices and the packed result.
 // At least 40 KB, so that no more than four CTAs share an SM and their
 // 4 x 128 TMEM columns always fit in the SM's 512: tcgen05.alloc then never
 // has to wait for another CTA's columns.
@@ -391,6 +532,10 @@ size_t tc_smem() {
   const size_t need = (kSplit ? 4 : 2) * (size_t)TcLayout<kBF16>::kOpBytes;
   return need > 40 * 1024 ? need : 40 * 1024;
 }
+
+// phase 4's staging must fit in the smallest operand area
+static_assert((kTcElems * TOT * TOT + kTcElems * UT) * 4 <= 40 * 1024, "phase-4 staging exceeds shared memory");
+static_assert(kTcElems * NG * kSubs <= kThreads && kTcRows <= kThreads, "tile larger than the CTA");
 
 template <bool kBF16, bool kSplit>
 cudaError_t set_smem() {

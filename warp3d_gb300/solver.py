@@ -1,0 +1,215 @@
+"""Global stiffness, its solve and the Newton loop, all on the device.
+
+``DeviceCsr`` mirrors the assembly-and-solve step that follows the element
+path in WARP3D's Newton iteration (drive_assemble_solve,
+src/drive_assemble_solve.f:11): the element stiffnesses left resident by
+``Engine.tanstf_dev`` are assembled into a CSR matrix on the device
+(row-wise gather in a fixed order, as assem_by_row builds whole rows,
+src/assemble_code.f:659) and solved by a Jacobi-preconditioned conjugate
+gradient on the free dofs.
+
+``DeviceNewtonDriver`` restates the host driver of ``newton.py`` (the loop
+of mnralg, src/mnralg.f:249-569) with every vector on the device: the
+element path, the assembly, the solve and the convergence norms (cvtest,
+src/cvtest.f:20) run there; per iteration the host reads only the
+recovery status, the solver's iteration count and two norms. PyTorch
+provides the device vectors and the few vector updates of the driver.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import abi
+
+
+class DeviceCsr:
+    def __init__(self, engine):
+        self.engine = engine
+        self.lib = engine.lib
+        self.h = C.c_void_p()
+        abi.check(self.lib, self.lib.w3g_csr_create(engine.ctx, C.byref(self.h)))
+        n, nnz = C.c_int(), C.c_longlong()
+        abi.check(self.lib, self.lib.w3g_csr_info(self.h, C.byref(n), C.byref(nnz), None, None, None))
+        self.n, self.nnz = n.value, nnz.value
+
+    def close(self):
+        if self.h:
+            self.lib.w3g_csr_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def assemble(self, stream: int = 0):
+        """K from the context's current element stiffnesses (FP64, or the
+        FP32 element matrices of a precision form)."""
+        abi.check(self.lib, self.lib.w3g_csr_assemble_dev(self.h, stream or None))
+
+    def to_scipy(self) -> sp.csr_matrix:
+        rowptr = np.empty(self.n + 1, dtype=np.int32)
+        colind = np.empty(self.nnz, dtype=np.int32)
+        val = np.empty(self.nnz, dtype=np.float64)
+        abi.check(self.lib, self.lib.w3g_csr_download(self.h, rowptr.ctypes.data, colind.ctypes.data,
+                                                      val.ctypes.data))
+        return sp.csr_matrix((val, colind, rowptr), shape=(self.n, self.n))
+
+    def pcg(self, d_fixed: int, d_b: int, b_scale: float, d_x: int, rtol: float, maxit: int, stream: int = 0):
+        """Solves K_ff x = b_scale b on the free dofs. Returns (status,
+        iterations, ||r|| / ||b_f||), status 0, abi.PCG_MAXIT or
+        abi.PCG_BREAKDOWN."""
+        its, rel = C.c_int(), C.c_double()
+        st = self.lib.w3g_pcg_dev(self.h, d_fixed, d_b, b_scale, d_x, rtol, maxit, stream or None, C.byref(its),
+                                  C.byref(rel))
+        abi.check(self.lib, st, allow=(abi.OK, abi.PCG_MAXIT, abi.PCG_BREAKDOWN))
+        return st, its.value, rel.value
+
+    def residual_norms(self, d_v: int, d_fixed: int, d_out: int, stream: int = 0):
+        abi.check(self.lib, self.lib.w3g_residual_norms_dev(self.h, d_v, d_fixed, d_out, stream or None))
+
+
+class _IncrementFailed(RuntimeError):
+    pass
+
+
+class DeviceNewtonDriver:
+    """Displacement-controlled Newton loop on the device; same interface,
+    convergence test and history as ``newton.NewtonDriver``.
+
+    With ``adaptive`` a load step whose Newton iterations fail (no
+    convergence within maxit, a step-cut request of the recovery, or a
+    tangent that is not positive definite) is subdivided as WARP3D's
+    adaptive solution does it (adapt_check, src/adapt_check.f:15-120;
+    defaults :181-182): the failed increment is replaced by
+    ``adapt_divisions`` equal sub-increments, down to ``adapt_min_fact`` of
+    the step, and the first sub-increment after a cut starts without
+    extrapolation. WARP3D does not subdivide step 1 (mnralg.f:131);
+    ``adaptive_step1`` lifts that restriction. Extrapolated starts scale
+    the last converged increment by the ratio of the increments' sizes
+    (mnralg.f:257-285). ``history`` gets one entry per converged
+    (sub-)increment; ``cuts`` counts subdivisions."""
+
+    def __init__(self, model, engine, fixed, tol: float = 1e-8, maxit: int = 25, extrapolate: bool = False,
+                 lin_rtol: float = 1e-10, lin_maxit: int = 50000, device: int = 0, csr: DeviceCsr | None = None,
+                 adaptive: bool = False, adaptive_step1: bool = False, adapt_divisions: int = 4,
+                 adapt_min_fact: float = 1.0 / 16.0):
+        import torch
+        self.torch = torch
+        self.model = model
+        self.engine = engine
+        self.tol, self.maxit, self.extrapolate = tol, maxit, extrapolate
+        self.lin_rtol, self.lin_maxit = lin_rtol, lin_maxit
+        self.adaptive, self.adaptive_step1 = adaptive, adaptive_step1
+        self.adapt_divisions, self.adapt_min_fact = adapt_divisions, adapt_min_fact
+        dev = torch.device("cuda", device)
+        n = model.nodof
+        z = lambda: torch.zeros(n, dtype=torch.float64, device=dev)
+        self.c = torch.from_numpy(np.ascontiguousarray(model.c)).to(dev)
+        self.ud, self.du, self.ifv, self.d = z(), z(), z(), z()
+        self.du_prev = None
+        self.frac_prev = 1.0
+        self.fixed_idx = torch.from_numpy(np.asarray(fixed, dtype=np.int64)).to(dev)
+        self.mask = torch.zeros(n, dtype=torch.uint8, device=dev)
+        self.mask[self.fixed_idx] = 1
+        self.norms = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.csr = csr if csr is not None else DeviceCsr(engine)   # the pattern is the model's: shareable
+        self.history = []       # (step, iterations, relative residuals) per converged increment
+        self.lin_history = []   # (step, [PCG iterations per Newton iteration])
+        self.fractions = []     # fraction of its step each converged increment carried
+        self.trace = []         # last increment: (PCG status, iterations, relative residual, Newton residual)
+        self.cuts = 0
+
+    @property
+    def u(self) -> np.ndarray:
+        return self.ud.cpu().numpy()
+
+    def _ptrs(self):
+        return self.c.data_ptr(), self.ud.data_ptr(), self.du.data_ptr()
+
+    def _recover(self, step, it, extrap):
+        c, u, du = self._ptrs()
+        self.engine.recover_dev(step, it, extrap, c, u, du, self.ifv.data_ptr())
+        st, _ = self.engine.recover_info()
+        return st
+
+    def _tangent(self, step, it):
+        c, u, du = self._ptrs()
+        self.engine.tanstf_dev(step, it, c, u, du)
+        self.csr.assemble()
+
+    def _increment(self, step: int, imp, extrap_scale):
+        """One (sub-)increment: imposed increments imp (device vector,
+        values on fixed dofs), extrapolated start du_prev * extrap_scale
+        when extrap_scale is not None."""
+        extrap = extrap_scale is not None
+        if extrap:
+            self.du.copy_(self.du_prev)
+            self.du *= extrap_scale
+        else:
+            self.du.zero_()
+        self.du[self.fixed_idx] = imp[self.fixed_idx]
+        res_hist, lin = [], []
+        self.trace = []
+        if self._recover(step, 0, extrap) != 0:
+            raise _IncrementFailed(f"step {step}: recovery requested a step cut at iteration 0")
+        self._tangent(step, 0)
+        for it in range(1, self.maxit + 1):
+            st, nits, rel = self.csr.pcg(self.mask.data_ptr(), self.ifv.data_ptr(), -1.0, self.d.data_ptr(),
+                                         self.lin_rtol, self.lin_maxit)
+            lin.append(nits)
+            self.trace.append([st, nits, rel, None])
+            if st == abi.PCG_BREAKDOWN:
+                raise _IncrementFailed(f"step {step}: tangent not positive definite on the free dofs "
+                                       f"(iteration {it})")
+            self.du += self.d
+            if self._recover(step, it, extrap) != 0:
+                raise _IncrementFailed(f"step {step}: step cut requested at iteration {it}")
+            self.csr.residual_norms(self.ifv.data_ptr(), self.mask.data_ptr(), self.norms.data_ptr())
+            rf, ra = self.norms.cpu().numpy()
+            rn, scale = float(np.sqrt(rf)), max(float(np.sqrt(ra)), 1e-300)
+            res_hist.append(rn / scale)
+            self.trace[-1][3] = rn / scale
+            if rn <= self.tol * scale:
+                return res_hist, lin
+            self._tangent(step, it)
+        raise _IncrementFailed(f"step {step}: no convergence in {self.maxit} iterations: {res_hist}")
+
+    def step(self, step: int, imposed: np.ndarray):
+        """imposed: full-length vector; its values on fixed dofs are the
+        displacement increments of this step."""
+        torch = self.torch
+        imp = torch.from_numpy(np.asarray(imposed, dtype=np.float64)).to(self.du.device)
+        adaptive = self.adaptive and (step > 1 or self.adaptive_step1)
+        pending = [1.0]            # fractions of the step still to run, in order
+        after_cut = False
+        out = []
+        while pending:
+            f = pending.pop(0)
+            extrap_scale = None
+            if self.extrapolate and self.du_prev is not None and step > 1 and not after_cut:
+                extrap_scale = f / self.frac_prev
+            try:
+                res_hist, lin = self._increment(step, imp * f, extrap_scale)
+            except _IncrementFailed as exc:
+                sub = f / self.adapt_divisions
+                if not adaptive or sub < self.adapt_min_fact * (1.0 - 1e-12):
+                    raise RuntimeError(str(exc)) from None
+                self.cuts += 1
+                pending = [sub] * self.adapt_divisions + pending
+                after_cut = True
+                continue
+            after_cut = False
+            self.engine.update()
+            self.ud += self.du
+            self.du_prev = self.du.clone()
+            self.frac_prev = f
+            self.history.append((step, len(res_hist), res_hist))
+            self.lin_history.append((step, lin))
+            self.fractions.append(f)
+            out.extend(res_hist)
+        return out
