@@ -60,6 +60,7 @@ constexpr int kK = NG * 6;             // 48
 constexpr int kThreads = 256;
 constexpr int kSubs = 6;               // threads per (element, Gauss point) in phase 1
 constexpr int kTmemCols = 128;
+constexpr int kKfStride = TOT + 1;     // padded row of the staged element matrices
 constexpr long long kWaitLimit = 1ll << 22;   // mbarrier polls before giving up
 
 template <bool kBF16>
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
     asm volatile("fence.mbarrier_init.release.cluster;");
     S.timeout = 0;
   }
-  for (int k = tid; k < NG * 3 * NN + NG; k += kThreads) S.dn[k] = (float)a.dn[0][k];
+  for (int k = tid; k < NG * 3 * NN + NG; k += kThreads) S.dn[k] = a.dn32[0][k];
   // ---- gather: x(n+1) relative to node 1, one coordinate per thread ----
   if (tid < kTcElems * 3 * NN) {
     const int e = tid / (3 * NN), dn = tid % (3 * NN), d = dn / NN, node = dn % NN;
@@ -344,38 +345,49 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   }
   __syncthreads();
 
-  // ---- phase 2: operands (row = 24 e + dof, dof = 8 i + a; k = 6 gp + m) ----
+  // ---- phase 2: operands (row = 24 e + dof, dof = 8 i + a; k = 6 gp + m).
+  // Threads 0-127 write row r of A = B^T, threads 128-255 row r of
+  // Bop = ([D*] B)^T, half of the Gauss points at a time from registers.
+  // Column (i, a) of B has three non-zeros: strain components p0..p2 take
+  // gradient components c0..c2 of node a:
+  //   i = 0: (xx, xy, xz) <- (gx, gy, gz)   i = 1: (yy, xy, yz) <- (gy, gx, gz)
+  //   i = 2: (zz, yz, xz) <- (gz, gy, gx)
   {
     const int r = tid & (kRows - 1);
+    const bool isB = tid >= kRows;
     const int e = r / TOT, d = r % TOT, di = d / NN, na = d % NN;
     const bool live = r < kTcRows && e < ch.n;
-    const int c0 = (tid >> 7) * (L::kChunks / 2), c1 = c0 + L::kChunks / 2;
-    for (int c = c0; c < c1; ++c) {
-      float va[L::kPerCore], vb[L::kPerCore];
+    const int ee = live ? e : 0;
+    const int p0 = di, p1 = di == 2 ? 4 : 3, p2 = di == 0 ? 5 : di == 1 ? 4 : 5;
+    const int c0 = di, c1 = di == 0 ? 1 : di == 1 ? 0 : 1, c2 = di == 2 ? 0 : 2;
+    int ix[6][3];   // packed [D*] index of (m, p_j)
 #pragma unroll
-      for (int j = 0; j < L::kPerCore; ++j) {
-        const int k = c * L::kPerCore + j, gp = k / 6, m = k % 6;
-        float x = 0.f, y = 0.f;
-        if (live) {
-          const float* g = S.g[e][gp];
-          const float gx = g[3 * na], gy = g[3 * na + 1], gz = g[3 * na + 2];
-          const float* D = S.D[e][gp];
-          if (di == 0) {
-            x = m == 0 ? gx : m == 3 ? gy : m == 5 ? gz : 0.f;
-            y = D[low(m, 0)] * gx + D[low(m, 3)] * gy + D[low(m, 5)] * gz;
-          } else if (di == 1) {
-            x = m == 1 ? gy : m == 3 ? gx : m == 4 ? gz : 0.f;
-            y = D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz;
-          } else {
-            x = m == 2 ? gz : m == 4 ? gy : m == 5 ? gx : 0.f;
-            y = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
-          }
+    for (int m = 0; m < 6; ++m) {
+      ix[m][0] = low(m, p0);
+      ix[m][1] = low(m, p1);
+      ix[m][2] = low(m, p2);
+    }
+    unsigned char* op = isB ? opB : opA;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float v[kK / 2];
+#pragma unroll
+      for (int q4 = 0; q4 < NG / 2; ++q4) {
+        const int gp = (NG / 2) * h + q4;
+        const float* g = S.g[ee][gp] + 3 * na;
+        const float u0 = g[c0], u1 = g[c1], u2 = g[c2];
+        const float* D = S.D[ee][gp];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+          float val;
+          if (isB) val = D[ix[m][0]] * u0 + D[ix[m][1]] * u1 + D[ix[m][2]] * u2;
+          else val = m == p0 ? u0 : m == p1 ? u1 : m == p2 ? u2 : 0.f;
+          v[6 * q4 + m] = live ? val : 0.f;
         }
-        va[j] = x;
-        vb[j] = y;
       }
-      put_chunk<kBF16, kSplit>(opA, r, c, va);
-      put_chunk<kBF16, kSplit>(opB, r, c, vb);
+#pragma unroll
+      for (int c = 0; c < L::kChunks / 2; ++c)
+        put_chunk<kBF16, kSplit>(op, r, (L::kChunks / 2) * h + c, v + c * L::kPerCore);
     }
   }
   // geometric stiffness per node pair (kgstiff): sum_gp g_a . ({T} g_b)
@@ -436,8 +448,10 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   const bool ok = S.timeout == 0;
 
   // ---- phase 4: TMEM -> element matrices (full, FP32) in shared memory ----
-  float* kf = reinterpret_cast<float*>(opA);                 // [kTcElems][24][24]; operands are consumed
-  float* ke = reinterpret_cast<float*>(opA) + kTcElems * TOT * TOT;   // [kTcElems][UT]
+  // [kTcElems][24][kKfStride]: rows padded to 25 words so that column reads
+  // by consecutive rows fall in distinct banks; operands are consumed
+  float* kf = reinterpret_cast<float*>(opA);
+  float* ke = reinterpret_cast<float*>(opA) + kTcElems * TOT * kKfStride;   // [kTcElems][UT]
   if (warp < 4) {
     const int r = 32 * warp + lane;
     const int e = r / TOT, dr = r % TOT;
@@ -461,7 +475,7 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int dc = 32 * pass + j - TOT * e;
-          if (dc >= 0 && dc < TOT) kf[(e * TOT + dr) * TOT + dc] = __uint_as_float(v[j]);
+          if (dc >= 0 && dc < TOT) kf[(e * TOT + dr) * kKfStride + dc] = __uint_as_float(v[j]);
         }
       }
     }
@@ -474,12 +488,12 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
   const int e = r / TOT, dr = r % TOT, ir = dr / NN, ar = dr % NN;
   const bool row_live = r < kTcRows && e < ch.n;
   if (row_live) {
-    const float* K = kf + e * TOT * TOT;
+    const float* K = kf + e * TOT * kKfStride;
     float m3[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int dc = 0; dc < TOT; ++dc) {
       const int ic = dc / NN, ac = dc % NN;
-      float val = 0.5f * (K[dr * TOT + dc] + K[dc * TOT + dr]);
+      float val = 0.5f * (K[dr * kKfStride + dc] + K[dc * kKfStride + dr]);
       if (ic == ir) {
         const int lo = ar < ac ? ar : ac, hi = ar < ac ? ac : ar;
         val += S.kg[e][lo * NN - lo * (lo - 1) / 2 + (hi - lo)];
@@ -534,7 +548,7 @@ size_t tc_smem() {
 }
 
 // phase 4's staging must fit in the smallest operand area
-static_assert((kTcElems * TOT * TOT + kTcElems * UT) * 4 <= 40 * 1024, "phase-4 staging exceeds shared memory");
+static_assert((kTcElems * TOT * kKfStride + kTcElems * UT) * 4 <= 40 * 1024, "phase-4 staging exceeds shared memory");
 static_assert(kTcElems * NG * kSubs <= kThreads && kTcRows <= kThreads, "tile larger than the CTA");
 
 template <bool kBF16, bool kSplit>
