@@ -99,6 +99,7 @@ def parse():
     ap.add_argument("--batched-elems", type=int, default=1_000_000, help="target elements of the batched workload")
     ap.add_argument("--no-crystal", action="store_true")
     ap.add_argument("--crystal-n", type=int, default=32, help="elements per cube edge of the mm10 workload")
+    ap.add_argument("--no-solver", action="store_true", help="skip the device assembly / PCG measurement")
     ap.add_argument("--precision-study", action="store_true",
                     help="instead of the bench line: Newton solves of the cube under every tangent precision form")
     ap.add_argument("--study-steps", type=int, default=20)
@@ -469,6 +470,68 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def hbm_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f).get("hbm_gbs")
+    except OSError:
+        return None
+
+
+def bench_solver(args, eng, model, tc, tu, tdu, dev):
+    """Device assembly of K from the resident FP64 element stiffnesses and
+    the Jacobi-PCG iteration on the same workload; both HBM-bound. Bytes:
+    assembly = contributions x (4 B index + 8 B value) + coefficients x
+    (4 B pointer + 8 B write); one CG iteration = nnz x 12 B (values,
+    columns) + nodof x 109 B (row pointers, mask, the gathered direction,
+    and the vector updates' reads and writes)."""
+    import torch
+    from warp3d_gb300.newton import uniaxial_bcs
+    from warp3d_gb300.solver import DeviceCsr
+    n = args.n
+    eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr())
+    t0 = time.perf_counter()
+    csr = DeviceCsr(eng)
+    setup_s = time.perf_counter() - t0
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for _ in range(2):
+        csr.assemble()
+    torch.cuda.synchronize()
+    reps = 5
+    ev[0].record()
+    for _ in range(reps):
+        csr.assemble()
+    ev[1].record()
+    torch.cuda.synchronize()
+    asm_ms = ev[0].elapsed_time(ev[1]) / reps
+    ncontrib = int(sum(model.block_totdof[b] ** 2 * model.spans[b] for b in range(model.nelblk)))
+    asm_bytes = 12 * ncontrib + 12 * csr.nnz
+    fixed, _ = uniaxial_bcs(model, (n, n, n))
+    mask = torch.zeros(model.nodof, dtype=torch.uint8, device=dev)
+    mask[torch.from_numpy(fixed).to(dev)] = 1
+    g = torch.Generator(device="cpu").manual_seed(11)
+    b = torch.randn(model.nodof, generator=g, dtype=torch.float64).to(dev)
+    x = torch.zeros_like(b)
+    csr.pcg(mask.data_ptr(), b.data_ptr(), 1.0, x.data_ptr(), 0.0, 32)   # warm-up, graph capture
+    its_req = 320
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, its, rel = csr.pcg(mask.data_ptr(), b.data_ptr(), 1.0, x.data_ptr(), 0.0, its_req)
+    torch.cuda.synchronize()
+    it_ms = 1e3 * (time.perf_counter() - t0) / max(its, 1)
+    it_bytes = 12 * csr.nnz + 109 * model.nodof
+    peak = hbm_peak_gbs()
+    out = {"dofs": model.nodof, "nnz": csr.nnz, "contributions": ncontrib, "pattern_setup_s": setup_s,
+           "assemble_ms": asm_ms, "assemble_gbs": asm_bytes / (asm_ms * 1e-3) / 1e9,
+           "pcg_iterations_timed": its, "pcg_iteration_ms": it_ms,
+           "pcg_iteration_gbs": it_bytes / (it_ms * 1e-3) / 1e9, "hbm_peak_gbs": peak}
+    if peak:
+        out["assemble_frac"] = out["assemble_gbs"] / peak
+        out["pcg_iteration_frac"] = out["pcg_iteration_gbs"] / peak
+    csr.close()
+    return out
+
+
 def precision_study(args, dev):
     """The precision forms on the n^3 cube (mm01, jitter 0.1h, blocks of
     128) under uniaxial tension, args.study_strain in args.study_steps
@@ -705,6 +768,11 @@ def main():
         e2e = {"value": world * ne / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "ms_per_step": 1e3 * t_e2e, "estiff_to_host": True}
 
+    solver = None
+    if not args.no_solver:
+        eng.set_precision(abi.TANGENT_FP64)
+        solver = bench_solver(args, eng, model, tc, tu, tdu, dev)
+
     # ---- roofline of the dominant kernel ----
     traffic = load_traffic()
     if tan64 >= rec64:
@@ -725,11 +793,7 @@ def main():
                 "recovery": {"ms": rec64, "tflops": RECOVER_FLOP_PER_ELEM * ne / (rec64 * 1e-3) / 1e12,
                              "tflops_refdense_count": RECOVER_FLOP_PER_ELEM_REFDENSE * ne / (rec64 * 1e-3) / 1e12,
                              "hbm_gbs": RECOVER_BYTES_PER_ELEM * ne / (rec64 * 1e-3) / 1e9}}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            roofline["hbm_peak_gbs_measured"] = json.load(f).get("hbm_gbs")
-    except OSError:
-        pass
+    roofline["hbm_peak_gbs_measured"] = hbm_peak_gbs()
     if mixed:
         mixed["tangent_hbm_gbs"] = TANGENT32_BYTES_PER_ELEM * ne / (mixed["tangent_ms"] * 1e-3) / 1e9
 
@@ -761,7 +825,7 @@ def main():
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "tangent_ms": tan64, "recovery_ms": rec64,
             "mixed": mixed, "e2e": e2e, "roofline": roofline, "cpu_baseline": cb, "clocks": clocks,
-            "gpu_launches": launches64, "batched": batched, "crystal": crystal,
+            "gpu_launches": launches64, "batched": batched, "crystal": crystal, "solver": solver,
         }
         print(json.dumps(line), flush=True)
     eng.close()

@@ -89,6 +89,8 @@ struct TcStatic {
     struct {                         // phase 1
       float C[kTcElems][NG][21];
       float cs[kTcElems][NG][6];
+      float R[kTcElems][NG][9];
+      float ur[kTcElems][NG][6];
     } p1;
     struct {                         // phase 4
       float mrow[kTcRows][3];        // row means over the nodes, per column component
@@ -201,7 +203,7 @@ __device__ __forceinline__ void row_of(const float* q, int j, float* out) {
 }
 
 template <bool kBF16, bool kSplit>
-__global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int chunk0, int* tc_timeout) {
+__global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, int chunk0, int* tc_timeout) {
   using L = TcLayout<kBF16>;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* opA = smem;                  // then B, then (split) A_lo, B_lo
@@ -275,16 +277,22 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
       for (int k = sub; k < 21; k += kSubs) S.u.p1.C[pe][pgp][k] = f * (float)a.cep[cb + k];
     }
     if (bd.geonl) {
+      // R and the unrotated stress: each value loaded and converted once
       const long long gpi = bd.gp_off + (long long)i * NG + pgp;
-      float R[9];
-      for (int k = 0; k < 9; ++k) R[k] = (float)a.rot_n1[gpi * 9 + k];
-      rotation_q2<float>(R, q);
-      float qrow[6];
-      row_of(q, sub, qrow);
-      float s = 0.f;
-      for (int m = 0; m < 6; ++m) s += qrow[m] * (float)a.urcs_n1[gpi * 9 + m];
-      S.u.p1.cs[pe][pgp][sub] = s;   // Cauchy stress component `sub`
+      S.u.p1.R[pe][pgp][sub] = (float)a.rot_n1[gpi * 9 + sub];
+      if (sub < 3) S.u.p1.R[pe][pgp][sub + 6] = (float)a.rot_n1[gpi * 9 + sub + 6];
+      S.u.p1.ur[pe][pgp][sub] = (float)a.urcs_n1[gpi * 9 + sub];
     }
+  }
+  __syncthreads();
+  if (p1 && bd.geonl) {
+    rotation_q2<float>(S.u.p1.R[pe][pgp], q);
+    float qrow[6];
+    row_of(q, sub, qrow);
+    const float* ur = S.u.p1.ur[pe][pgp];
+    float s = 0.f;
+    for (int m = 0; m < 6; ++m) s += qrow[m] * ur[m];
+    S.u.p1.cs[pe][pgp][sub] = s;   // Cauchy stress component `sub`
   }
   __syncthreads();
   if (p1) {
@@ -538,17 +546,18 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex8(TangentArgs a, int
 
 // Dynamic shared memory per CTA: A and B (and their low parts when split),
 // re-used in phase 4 for the full element matrices and the packed result.
-// At least 40 KB, so that no more than four CTAs share an SM and their
-// 4 x 128 TMEM columns always fit in the SM's 512: tcgen05.alloc then never
-// has to wait for another CTA's columns.
+// At least kMinDyn, so that with the static part no more than four CTAs fit
+// in an SM's 228 KB and their 4 x 128 TMEM columns always fit in its 512:
+// tcgen05.alloc then never has to wait for another CTA's columns.
+constexpr int kMinDyn = 30 * 1024;
+static_assert(sizeof(TcStatic) + kMinDyn + 1024 > 228 * 1024 / 5, "five CTAs could share an SM's TMEM");
+static_assert((kTcElems * TOT * kKfStride + kTcElems * UT) * 4 <= kMinDyn, "phase-4 staging exceeds shared memory");
+
 template <bool kBF16, bool kSplit>
 size_t tc_smem() {
   const size_t need = (kSplit ? 4 : 2) * (size_t)TcLayout<kBF16>::kOpBytes;
-  return need > 40 * 1024 ? need : 40 * 1024;
+  return need > (size_t)kMinDyn ? need : (size_t)kMinDyn;
 }
-
-// phase 4's staging must fit in the smallest operand area
-static_assert((kTcElems * TOT * kKfStride + kTcElems * UT) * 4 <= 40 * 1024, "phase-4 staging exceeds shared memory");
 static_assert(kTcElems * NG * kSubs <= kThreads && kTcRows <= kThreads, "tile larger than the CTA");
 
 template <bool kBF16, bool kSplit>
