@@ -748,19 +748,17 @@ def main():
         pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
         c_h, u_h, du_h = pin(model.c), pin(u1), pin(du)
         ifv_p = pin(np.zeros(model.nodof))
+        # all blocks' Ke back to back in one pinned buffer (estiff_blocks(blk)%ptr
+        # would point into it)
         est_all = torch.empty(ne * model.utsz, dtype=torch.float64).pin_memory().numpy()
-        est_blocks, off = [], 0
-        for s in model.spans:
-            est_blocks.append(est_all[off:off + s * model.utsz].reshape(s, model.utsz))
-            off += s * model.utsz
         for _ in range(2):
-            eng.tanstf(2, 1, c_h, u_h, du_h, est_blocks)
+            eng.tanstf(2, 1, c_h, u_h, du_h, est_all)
             eng.recover(2, 1, False, c_h, u_h, du_h, ifv_p)
         barrier()
         reps = max(3, args.steps // 4)
         t0 = time.perf_counter()
         for _ in range(reps):
-            eng.tanstf(2, 1, c_h, u_h, du_h, est_blocks)
+            eng.tanstf(2, 1, c_h, u_h, du_h, est_all)
             eng.recover(2, 1, False, c_h, u_h, du_h, ifv_p)
         t_e2e = (time.perf_counter() - t0) / reps
         h2d = 2 * 8 * (model.ncoord + 2 * model.nodof)

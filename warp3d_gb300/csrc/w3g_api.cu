@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <thread>
 #include "w3g_internal.cuh"
 #include "w3g_elem.cuh"
 
@@ -51,6 +52,9 @@ void free_all(w3g_context* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_stage) cudaFreeHost(c->h_stage);
+  for (cudaEvent_t& ev : c->part_done)
+    if (ev) cudaEventDestroy(ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -219,6 +223,105 @@ int run_recover(w3g_context* c, int step, int iter, int extrap, const double* d_
 
 void w3g::set_last_error(const std::string& msg) { g_err = msg; }
 
+namespace {
+
+// copies Ke of blocks [b0, b1) to the host pointers, blocks whose host
+// arrays follow each other in memory in one copy
+int copy_estiff_range(w3g_context* c, double* const* estiff, int b0, int b1, cudaStream_t st) {
+  for (int b = b0; b < b1; ++b) {
+    const BlockDesc& bd = c->blocks[b];
+    if (!estiff[b]) continue;
+    int e = b;
+    size_t run = (size_t)bd.utsz * bd.span;
+    while (e + 1 < b1 && estiff[e + 1] && estiff[e + 1] == estiff[e] + (size_t)c->blocks[e].utsz * c->blocks[e].span) {
+      ++e;
+      run += (size_t)c->blocks[e].utsz * c->blocks[e].span;
+    }
+    CK(cudaMemcpyAsync(estiff[b], c->s.estiff + bd.estiff_off, run * sizeof(double), cudaMemcpyDeviceToHost, st));
+    b = e;
+  }
+  return 0;
+}
+
+// FP64 tangent with host Ke: the blocks are cut into parts of similar Ke
+// size; each part's kernels run on the compute stream and its Ke is copied
+// to the host on a second stream while the next part computes, so that
+// only the last part's copy is exposed
+int tanstf_overlapped(w3g_context* c, double* const* estiff, cudaStream_t st) {
+  constexpr int kParts = 8;
+  if (!c->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& ev : c->part_done) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  const int nb = c->m.nelblk;
+  const long long total = c->m.estiff_total;
+  TangentArgs a = tangent_args(c, c->s.d_c, c->s.d_u, c->s.d_du);
+  int launches = 0, b0 = 0;
+  for (int k = 0; k < kParts && b0 < nb; ++k) {
+    int b1 = b0 + 1;
+    const long long target = total * (k + 1) / kParts;
+    while (b1 < nb && (k == kParts - 1 || c->blocks[b1].estiff_off < target)) ++b1;
+    // per type: the work items of blocks [b0, b1) (items are in block order within a type)
+    int first[kNumTypes], count[kNumTypes];
+    for (int t = 0; t < kNumTypes; ++t) {
+      const Chunk* beg = c->h_tchunks.data() + c->m.ttype_chunk0[t];
+      const Chunk* end = beg + c->m.ttype_chunks[t];
+      const Chunk* lo = std::lower_bound(beg, end, b0, [](const Chunk& x, int v) { return x.blk < v; });
+      const Chunk* hi = std::lower_bound(lo, end, b1, [](const Chunk& x, int v) { return x.blk < v; });
+      first[t] = (int)(lo - c->h_tchunks.data());
+      count[t] = (int)(hi - lo);
+    }
+    int n = 0;
+    cudaError_t e = launch_tangent_ranges(c->m, a, false, first, count, st, &n);
+    if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
+    launches += n;
+    CK(cudaEventRecord(c->part_done[k], st));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->part_done[k], 0));
+    int r = copy_estiff_range(c, estiff, b0, b1, c->copy_stream);
+    if (r) return r;
+    b0 = b1;
+  }
+  c->last_launches = launches;
+  CK(cudaStreamSynchronize(c->copy_stream));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+// precision forms with host Ke: one copy of the FP32 matrices, widened to
+// double by host threads
+int download_estiff32(w3g_context* c, double* const* estiff, cudaStream_t st) {
+  const size_t total = (size_t)c->m.estiff_total;
+  if (c->h_stage_n < total) {
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    c->h_stage_n = 0;
+    CK(cudaMallocHost((void**)&c->h_stage, total * sizeof(double)));
+    c->h_stage_n = total;
+  }
+  float* f = reinterpret_cast<float*>(c->h_stage);
+  CK(cudaMemcpyAsync(f, c->s.estiff32, total * sizeof(float), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const int nb = c->m.nelblk;
+  const int nth = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  auto work = [&](int t) {
+    for (int b = t; b < nb; b += nth) {
+      if (!estiff[b]) continue;
+      const BlockDesc& bd = c->blocks[b];
+      const float* src = f + bd.estiff_off;
+      double* dst = estiff[b];
+      const size_t n = (size_t)bd.utsz * bd.span;
+      for (size_t k = 0; k < n; ++k) dst[k] = src[k];
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nth; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& t : th) t.join();
+  return 0;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* w3g_last_error(void) { return g_err.c_str(); }
@@ -343,6 +446,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     tchunks.insert(tchunks.end(), ttype_chunks[t].begin(), ttype_chunks[t].end());
   }
   m.ntchunks = (int)tchunks.size();
+  c->h_tchunks = tchunks;
   std::vector<Chunk> tcchunks;   // tensor-core tiles: 5 elements of an 8-node-brick block
   for (int b = 0; b < md->nelblk; ++b)
     if (B[b].etype == W3G_ETYPE_L3DISOP)
@@ -655,38 +759,16 @@ int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const doubl
   CK(cudaMemcpyAsync(c->s.d_c, hc, (size_t)c->m.ncoord * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->s.d_u, hu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->s.d_du, hdu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (estiff && c->precision == W3G_TANGENT_FP64 && c->sched.mode == W3G_SCHED_PER_TYPE)
+    return tanstf_overlapped(c, estiff, st);
   int r = run_tangent(c, c->s.d_c, c->s.d_u, c->s.d_du, st);
   if (r) return r;
-  if (estiff) {
-    for (int b = 0; b < c->m.nelblk; ++b) {
-      const BlockDesc& bd = c->blocks[b];
-      if (!estiff[b]) continue;
-      size_t n = (size_t)bd.utsz * bd.span;
-      if (c->precision == W3G_TANGENT_FP64) {
-        // blocks whose host arrays follow each other in memory go in one copy
-        int e = b;
-        size_t run = n;
-        while (e + 1 < c->m.nelblk && estiff[e + 1] &&
-               estiff[e + 1] == estiff[e] + (size_t)c->blocks[e].utsz * c->blocks[e].span) {
-          ++e;
-          run += (size_t)c->blocks[e].utsz * c->blocks[e].span;
-        }
-        CK(cudaMemcpyAsync(estiff[b], c->s.estiff + bd.estiff_off, run * sizeof(double), cudaMemcpyDeviceToHost, st));
-        b = e;
-      } else {
-        // FP32 form: widen on the host
-        if (c->h_stage_n < n) {
-          if (c->h_stage) cudaFreeHost(c->h_stage);
-          c->h_stage = nullptr;
-          CK(cudaMallocHost((void**)&c->h_stage, n * sizeof(double)));
-          c->h_stage_n = n;
-        }
-        float* f = reinterpret_cast<float*>(c->h_stage);
-        CK(cudaMemcpyAsync(f, c->s.estiff32 + bd.estiff_off, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        for (size_t k = 0; k < n; ++k) estiff[b][k] = f[k];
-      }
-    }
+  if (estiff && c->precision == W3G_TANGENT_FP64) {
+    r = copy_estiff_range(c, estiff, 0, c->m.nelblk, st);
+    if (r) return r;
+  } else if (estiff) {
+    r = download_estiff32(c, estiff, st);   // FP32 forms: widened on the host
+    if (r) return r;
   }
   CK(cudaStreamSynchronize(st));
   if (c->precision >= W3G_TANGENT_TF32) {

@@ -29,6 +29,11 @@ struct w3g_context {
   std::vector<w3g::BlockDesc> blocks;
   double* h_stage = nullptr;   // pinned staging, max(estiff_total, ...) doubles
   size_t h_stage_n = 0;
+  // w3g_tanstf with host Ke: the tangent runs in parts whose Ke goes to the
+  // host on copy_stream while the next part computes
+  std::vector<w3g::Chunk> h_tchunks;   // host copy of the tangent work items
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t part_done[8] = {};
 };
 
 

@@ -292,6 +292,10 @@ struct RecoverArgs {
 // (queue counters are reset inside)
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc,
                            int* counter, cudaStream_t s, bool skip_hex8 = false);
+// per-type launches over explicit work-item ranges (first item, count per
+// type); returns the number of kernels launched through *launches
+cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bool fp32, const int* first,
+                                  const int* count, cudaStream_t s, int* launches);
 // precision forms on the tensor cores: 8-node bricks (w3g_tangent_tc.cu)
 cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
                                    int* tc_timeout, cudaStream_t s);

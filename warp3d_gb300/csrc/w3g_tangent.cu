@@ -139,6 +139,41 @@ cudaError_t init_tangent_kernels() {
 
 int persistent_tangent_occupancy(bool fp32) { return fp32 ? occupancy<float>() : occupancy<double>(); }
 
+namespace {
+
+template <class T>
+cudaError_t launch_ranges(const TangentArgs& a, const int* first, const int* count, cudaStream_t s, int* launches) {
+  int n = 0;
+  if (count[0] > 0) {
+    TangentArgs h = a;
+    h.chunk0 = first[0];
+    k_tangent_hex8<T><<<count[0], kTangentThreads, hex8_smem<T>(), s>>>(h);
+    ++n;
+  }
+  if (count[1] > 0) {
+    TangentArgs h = a;
+    h.chunk0 = first[1];
+    k_tangent_type<Hex20, 32, 1, T><<<count[1], kTangentThreads, sizeof(TangentSmemGen<Hex20, 1, T>), s>>>(h);
+    ++n;
+  }
+  if (count[2] > 0) {
+    TangentArgs h = a;
+    h.chunk0 = first[2];
+    k_tangent_type<Tet10, 8, 4, T><<<count[2], kTangentThreads, sizeof(TangentSmemGen<Tet10, 4, T>), s>>>(h);
+    ++n;
+  }
+  if (launches) *launches = n;
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bool fp32, const int* first,
+                                  const int* count, cudaStream_t s, int* launches) {
+  (void)m;
+  return fp32 ? launch_ranges<float>(a, first, count, s, launches) : launch_ranges<double>(a, first, count, s, launches);
+}
+
 int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8) {
   if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) return m.ntchunks > 0 ? 1 : 0;
   int n = skip_hex8 && m.ntcchunks > 0 ? 1 : 0;

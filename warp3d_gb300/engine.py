@@ -60,10 +60,26 @@ class Engine:
 
     # ---- hot path, host arrays --------------------------------------------
     def tanstf(self, step: int, it: int, c: np.ndarray, u: np.ndarray, du: np.ndarray, estiff_blocks=None):
+        """estiff_blocks: a list of per-block (span, utsz) arrays, or one
+        C-contiguous float64 array holding all blocks back to back (its
+        per-block pointers are then computed without a Python loop)."""
         ptrs = None
-        if estiff_blocks is not None:
+        if isinstance(estiff_blocks, np.ndarray):
+            ptrs = C.cast(self._contiguous_ptrs(estiff_blocks), C.POINTER(C.POINTER(C.c_double)))
+        elif estiff_blocks is not None:
             ptrs = C.cast(block_ptrs(estiff_blocks), C.POINTER(C.POINTER(C.c_double)))
         return abi.check(self.lib, self.lib.w3g_tanstf(self.ctx, step, it, dptr(c), dptr(u), dptr(du), ptrs))
+
+    def _contiguous_ptrs(self, buf: np.ndarray):
+        m = self.model
+        if not hasattr(self, "_estiff_off"):
+            sizes = np.array(m.spans, dtype=np.uintp) * np.array(m.block_utsz, dtype=np.uintp)
+            self._estiff_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uintp) * np.uintp(8)
+            self._estiff_total = int(sizes.sum())
+        if buf.dtype != np.float64 or not buf.flags.c_contiguous or buf.size != self._estiff_total:
+            raise ValueError("estiff buffer must be C-contiguous float64 with all blocks' values")
+        addr = self._estiff_off + np.uintp(buf.ctypes.data)
+        return (C.c_void_p * m.nelblk).from_buffer(addr)
 
     def recover(self, step: int, it: int, extrapolated: bool, c, u, du, ifv):
         info = abi.RecoverInfo()

@@ -445,7 +445,11 @@ class Model:
 
 
 def _ptrs(arrs):
-    return (C.POINTER(C.c_double) * len(arrs))(*[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs])
+    """C array of the arrays' data addresses (a ctypes view of a numpy
+    address vector: about 0.3 us per array instead of a ctypes pointer
+    object each); callers cast it to the pointer-to-pointer they need."""
+    addr = np.fromiter((a.__array_interface__["data"][0] for a in arrs), dtype=np.uintp, count=len(arrs))
+    return (C.c_void_p * len(arrs)).from_buffer(addr)
 
 
 class HostState:
