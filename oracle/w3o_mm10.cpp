@@ -45,6 +45,26 @@ inline double& M3(double* a, int r, int c) { return a[r + 3 * c]; }
 inline double M3(const double* a, int r, int c) { return a[r + 3 * c]; }
 inline double sign1(double b) { return b >= 0.0 ? 1.0 : -1.0; }   // Fortran sign(one, b)
 
+// x^y for y a non-negative integer up to 64 (the slip-rate exponents n,
+// n - 1, n - 2 and the Voce exponent m of the usual data): binary
+// powering, the same multiplications in the oracle and on the device, a
+// few roundings instead of pow's log/exp sequence, which costs ~100 FP64
+// instructions on GB300's narrow FP64 pipe; any other y: pow
+inline double powr(double x, double y) {
+  const int k = (int)y;
+  if ((double)k == y && k >= 0 && k <= 64) {
+    double r = 1.0, b = x;
+    for (int e = k;;) {
+      if (e & 1) r = r * b;
+      e >>= 1;
+      if (!e) break;
+      b = b * b;
+    }
+    return r;
+  }
+  return std::pow(x, y);
+}
+
 // ---- history locations (mm10_set_history_locs, 1 crystal, 0-based) ----
 constexpr int H_TAN = 0, H_GRADFE = 36, H_R = 63, H_WORK = 72, H_SLIP = 75;
 constexpr int C0 = 87;
@@ -222,7 +242,7 @@ double rs_of(const State& np1, const double* stress, int i) {
 }
 double slipinc_of(const CrystalProps& p, const State& np1, const double* stress, double tt, int i) {
   const double rs = rs_of(np1, stress, i);
-  return np1.dg / tt * std::pow(std::fabs(rs / tt), p.rate_n - one) * rs;
+  return np1.dg / tt * powr(std::fabs(rs / tt), p.rate_n - one) * rs;
 }
 
 void form_dbarp(const CrystalProps& p, const State& np1, const double* stress, double tt, double* dbar) {
@@ -269,7 +289,7 @@ double formR2(const CrystalProps& p, State& np1, const State& n, const double* s
   for (int i = 0; i < NS; ++i) {
     const double slipinc = slipinc_of(p, np1, stress, tt, i);
     const double h_term = one - (tt - p.tau_y) / p.tau_v + np1.tau_l[i] / (tt - p.tau_y);
-    h = h + std::pow(std::fabs(h_term), p.voche_m) * sign1(h_term) * std::fabs(slipinc);
+    h = h + powr(std::fabs(h_term), p.voche_m) * sign1(h_term) * std::fabs(slipinc);
   }
   h = n.tau_tilde + p.theta_0 * h;
   np1.tt_rate = (h - n.tau_tilde) / np1.tinc;
@@ -296,8 +316,8 @@ void symswmat(const double* s, const State& np1, double sw[NS][6]) {
 void dgdt_voche(const CrystalProps& p, const State& np1, const double* stress, double tt, double* dgdt) {
   for (int s = 0; s < NS; ++s) {
     const double rs = rs_of(np1, stress, s);
-    double d = std::pow(std::fabs(rs), p.rate_n - one);
-    d = np1.dg * p.rate_n / std::pow(tt, p.rate_n) * d;
+    double d = powr(std::fabs(rs), p.rate_n - one);
+    d = np1.dg * p.rate_n / powr(tt, p.rate_n) * d;
     d = d + np1.tinc * p.iD_v;
     dgdt[s] = d;
   }
@@ -347,10 +367,10 @@ void formJ(const CrystalProps& p, const State& np1, const double* x, double* J /
     for (int i = 0; i < NS; ++i) {
       const double rs = rs_of(np1, stress, i);
       const double h_term = one - (tt - p.tau_y) / p.tau_v + np1.tau_l[i] / (tt - p.tau_y);
-      const double f = std::pow(std::fabs(h_term), p.voche_m) * sign1(h_term) * std::pow(std::fabs(rs), p.rate_n - two) * rs;
+      const double f = powr(std::fabs(h_term), p.voche_m) * sign1(h_term) * powr(std::fabs(rs), p.rate_n - two) * rs;
       for (int k = 0; k < 6; ++k) et[k] = et[k] + f * np1.ms[i][k];
     }
-    const double f = p.theta_0 * np1.dg * p.rate_n / std::pow(tt, p.rate_n);
+    const double f = p.theta_0 * np1.dg * p.rate_n / powr(tt, p.rate_n);
     for (int k = 0; k < 6; ++k) J21[k] = -(f * et[k]);
   }
   // J22 = ehard_voche, restated with the reference's sign(one, slipinc)
@@ -366,7 +386,7 @@ void formJ(const CrystalProps& p, const State& np1, const double* x, double* J /
       const double d = tt - p.tau_y;
       etau = etau + (p.voche_m * (-one / p.tau_v - np1.tau_l[i] / (d * d)) * std::fabs(slipinc) / std::fabs(h_term) -
                      std::fabs(slipinc) * p.rate_n / tt * sign1(h_term) * sign1(slipinc)) *
-                        std::pow(std::fabs(h_term), p.voche_m);
+                        powr(std::fabs(h_term), p.voche_m);
     }
     etau = p.theta_0 * etau;
     J22 = one - etau;

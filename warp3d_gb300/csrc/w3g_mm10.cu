@@ -182,6 +182,26 @@ struct Rate {
   double dg, tinc, tt_rate;
 };
 
+// x^y for y a non-negative integer up to 64 (the slip-rate exponents n,
+// n - 1, n - 2 and the Voce exponent m of the usual data): binary
+// powering, the same multiplications in the oracle and on the device, a
+// few roundings instead of pow's log/exp sequence, which costs ~100 FP64
+// instructions on GB300's narrow FP64 pipe; any other y: pow
+__device__ __forceinline__ double powr(double x, double y) {
+  const int k = (int)y;
+  if ((double)k == y && k >= 0 && k <= 64) {
+    double r = 1.0, b = x;
+    for (int e = k;;) {
+      if (e & 1) r = r * b;
+      e >>= 1;
+      if (!e) break;
+      b = b * b;
+    }
+    return r;
+  }
+  return pow(x, y);
+}
+
 __device__ void symsw(const double* s, const double* w, double* sw) {
   sw[0] = s[3] * w[2] - s[5] * w[1];
   sw[1] = s[3] * w[2] - s[4] * w[0];
@@ -206,7 +226,7 @@ __device__ __forceinline__ void slip_terms(const CrystalType& t, const Geo& G, c
   for (int i = 0; i < NS; ++i) {
     rs[i] = s[0] * G.ms[i][0] + s[1] * G.ms[i][1] + s[2] * G.ms[i][2] + s[3] * G.ms[i][3] + s[4] * G.ms[i][4] +
             s[5] * G.ms[i][5];
-    sl[i] = q.dg / tt * pow(fabs(rs[i] / tt), t.rate_n - 1.0) * rs[i];
+    sl[i] = q.dg / tt * powr(fabs(rs[i] / tt), t.rate_n - 1.0) * rs[i];
   }
 }
 
@@ -240,7 +260,7 @@ __device__ void formR1(const CrystalElem& x, const CrystalType& t, const Geo& G,
 // systems (tau_l = 0: no lattice-curvature data in this scope)
 __device__ double formR2(const CrystalType& t, Rate& q, const Nstate& n, const double* sl, double tt) {
   const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
-  const double ph = pow(fabs(h_term), t.voche_m) * sgn1(h_term);
+  const double ph = powr(fabs(h_term), t.voche_m) * sgn1(h_term);
   double h = 0.0;
   for (int i = 0; i < NS; ++i) h = h + ph * fabs(sl[i]);
   h = n.tt + t.theta_0 * h;
@@ -274,13 +294,13 @@ __device__ __noinline__ void formJ(const CrystalElem& x, const CrystalType& t, c
   slip_terms(t, G, q, s, tt, rs, sl);
   for (int c = 0; c < 6; ++c)
     for (int r = 0; r < 6; ++r) J[r + ld * c] = 0.0;
-  const double A = q.dg * t.rate_n / pow(tt, t.rate_n);
+  const double A = q.dg * t.rate_n / powr(tt, t.rate_n);
   const double B = -t.rate_n / tt;
   double J12[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = 0; i < NS; ++i) {
     double sw[6], wv[6];
     symsw(s, G.qc[i], sw);
-    double d = pow(fabs(rs[i]), t.rate_n - 1.0);
+    double d = powr(fabs(rs[i]), t.rate_n - 1.0);
     d = A * d;
     d = d + q.tinc * t.iD_v;
     for (int r = 0; r < 6; ++r) wv[r] = 2.0 * sw[r];
@@ -321,14 +341,14 @@ __device__ __noinline__ void formJ(const CrystalElem& x, const CrystalType& t, c
   if (!kFull) return;
   for (int r = 0; r < 6; ++r) J[r + 7 * 6] = J12[r];
   const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
-  const double phm = pow(fabs(h_term), t.voche_m);
+  const double phm = powr(fabs(h_term), t.voche_m);
   const double ph = phm * sgn1(h_term);
   double et[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = 0; i < NS; ++i) {
-    const double f = ph * pow(fabs(rs[i]), t.rate_n - 2.0) * rs[i];
+    const double f = ph * powr(fabs(rs[i]), t.rate_n - 2.0) * rs[i];
     for (int k = 0; k < 6; ++k) et[k] = et[k] + f * G.ms[i][k];
   }
-  const double fe = t.theta_0 * q.dg * t.rate_n / pow(tt, t.rate_n);
+  const double fe = t.theta_0 * q.dg * t.rate_n / powr(tt, t.rate_n);
   for (int c = 0; c < 6; ++c) J[6 + 7 * c] = -(fe * et[c]);
   const double dd = tt - t.tau_y;
   const double dh = t.voche_m * (-1.0 / t.tau_v - 0.0 / (dd * dd));
@@ -834,8 +854,8 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
       n_eff = 0.0;
       for (int s = 0; s < NS; ++s) {
         const double rs = rsc[s];
-        double d = pow(fabs(rs), t.rate_n - 1.0);
-        d = q.dg * t.rate_n / pow(tt, t.rate_n) * d;
+        double d = powr(fabs(rs), t.rate_n - 1.0);
+        d = q.dg * t.rate_n / powr(tt, t.rate_n) * d;
         d = d + q.tinc * t.iD_v;
         t1 = G.ms[s][0] * ep[0] + G.ms[s][1] * ep[1] + G.ms[s][2] * ep[2];
         t2 = G.ms[s][3] * ep[3] + G.ms[s][4] * ep[4] + G.ms[s][5] * ep[5];
