@@ -110,6 +110,9 @@ def parse():
     ap.add_argument("--study-no-extrapolate", action="store_true",
                     help="start every step from zero instead of the scaled previous increment")
     ap.add_argument("--study-no-adaptive", action="store_true", help="no subdivision of failing steps")
+    ap.add_argument("--batched-study", action="store_true",
+                    help="instead of the bench line: Newton solves of the mixed-type bars, FP64 and FP32 tangent")
+    ap.add_argument("--study-section", type=int, default=32, help="cells per side of the bars' section")
     return ap.parse_args()
 
 
@@ -137,8 +140,8 @@ def build_batched_workload(target, seed=2025, ny=64, nz=64):
     from warp3d_gb300.model import Bilinear, Model, Part, mixed_mesh, random_spans
     a = ny * nz
     nx = (max(1, round(0.60 * target / a)), max(1, round(0.25 * target / a)), max(1, round(0.15 * target / (6 * a))))
-    coords, parts, _ = mixed_mesh([(abi.ETYPE_L3DISOP, nx[0]), (abi.ETYPE_Q3DISOP, nx[1]), (abi.ETYPE_TET10, nx[2])],
-                                  ny, nz, jitter=0.05, seed=seed)
+    coords, parts, origins = mixed_mesh([(abi.ETYPE_L3DISOP, nx[0]), (abi.ETYPE_Q3DISOP, nx[1]),
+                                         (abi.ETYPE_TET10, nx[2])], ny, nz, jitter=0.05, seed=seed)
     rng = np.random.Generator(np.random.PCG64(seed))
     plist = []
     for etype, inc in parts:
@@ -152,7 +155,7 @@ def build_batched_workload(target, seed=2025, ny=64, nz=64):
     r2 = np.random.Generator(np.random.PCG64(seed + 1))
     dF = np.diag([-0.0005, -0.0005, 0.001])
     du = ((dF @ X.T).T + r2.normal(0.0, 2e-5, X.shape)).ravel()
-    return model, u1, du, nx
+    return model, u1, du, nx, origins
 
 
 def bench_batched(args, dev, local):
@@ -162,7 +165,7 @@ def bench_batched(args, dev, local):
     from warp3d_gb300 import abi
     from warp3d_gb300.engine import Engine
     t0 = time.perf_counter()
-    model, u1, du, nx = build_batched_workload(args.batched_elems)
+    model, u1, du, nx, _ = build_batched_workload(args.batched_elems)
     t_build = time.perf_counter() - t0
     ne = model.noelem
     counts = {}
@@ -532,40 +535,22 @@ def bench_solver(args, eng, model, tc, tu, tdu, dev):
     return out
 
 
-def precision_study(args, dev):
-    """The precision forms on the n^3 cube (mm01, jitter 0.1h, blocks of
-    128) under uniaxial tension, args.study_strain in args.study_steps
-    equal steps, every Newton iteration on the device (element path, CSR
-    assembly, Jacobi PCG to 1e-10, residual norms) to the 1e-8 relative
-    residual; steps start from the scaled previous increment and a failing
-    step is subdivided (4 sub-increments, down to 1/16 of the step, step 1
-    included). Per form: Newton iterations per step, PCG iterations, wall
-    time, the final displacements' error against the FP64 run; per-element
-    Ke error against the FP64 tangent (checked against the oracle by the
-    tests) at the converged end state of the FP64 run."""
+STUDY_FORMS = {"fp64": 0, "fp32": 1, "tf32": 2, "bf16": 3, "tf32x3": 4, "bf16x3": 5}   # abi.TANGENT_*
+
+
+def newton_forms(args, model, fixed, topz, nz, names, eng, csr):
+    """Runs the displacement-controlled load history on the device once per
+    tangent form (DeviceNewtonDriver: extrapolated starts, adaptive
+    subdivision with step 1 included); returns per-form records, the FP64
+    run's displacements and its converged end state."""
     import torch
-    from warp3d_gb300 import abi
-    from warp3d_gb300.engine import Engine
-    from warp3d_gb300.newton import uniaxial_bcs
-    from warp3d_gb300.solver import DeviceCsr, DeviceNewtonDriver
-    forms = {"fp64": abi.TANGENT_FP64, "fp32": abi.TANGENT_FP32, "tf32": abi.TANGENT_TF32,
-             "bf16": abi.TANGENT_BF16, "tf32x3": abi.TANGENT_TF32X3, "bf16x3": abi.TANGENT_BF16X3}
-    n = args.n
-    model, _, _ = build_workload(n)
-    fixed, topz = uniaxial_bcs(model, (n, n, n))
-    t0 = time.perf_counter()
-    eng = Engine(model)
+    from warp3d_gb300.solver import DeviceNewtonDriver
     initial = model.new_state()
+    eng.set_precision(STUDY_FORMS["fp64"])
     eng.download(initial)
-    csr = DeviceCsr(eng)
-    setup_s = time.perf_counter() - t0
-    out = {"workload": f"{n}^3 hex8 l3disop geonl (jitter 0.1h), mm01 bilinear, blocks of 128; uniaxial "
-                       f"{100 * args.study_strain:g}% in {args.study_steps} steps",
-           "elements": model.noelem, "dofs": model.nodof, "csr_nnz": csr.nnz, "setup_s": setup_s,
-           "newton_tol": 1e-8, "pcg_rtol": 1e-10, "forms": {}}
-    u_ref = None
-    for name in args.study_forms.split(","):
-        eng.set_precision(forms[name])
+    forms, u_ref, end_state = {}, None, None
+    for name in names:
+        eng.set_precision(STUDY_FORMS[name])
         eng.upload(initial)
         drv = DeviceNewtonDriver(model, eng, fixed, tol=1e-8, maxit=args.study_maxit, lin_rtol=1e-10,
                                  lin_maxit=args.study_lin_maxit, csr=csr, extrapolate=not args.study_no_extrapolate,
@@ -575,7 +560,7 @@ def precision_study(args, dev):
         t1 = time.perf_counter()
         for st in range(1, args.study_steps + 1):
             imp = np.zeros(model.nodof)
-            imp[topz] = args.study_strain * n / args.study_steps
+            imp[topz] = args.study_strain * nz / args.study_steps
             k0, cuts0 = len(drv.history), drv.cuts
             try:
                 drv.step(st, imp)
@@ -603,9 +588,65 @@ def precision_study(args, dev):
             eng.download(end_state)
         elif u_ref is not None and rec["failed"] is None:
             rec["u_rel_err_vs_fp64"] = float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref)))
-        out["forms"][name] = rec
+        forms[name] = rec
         print(f"[study] {name}: newton {its} failed={rec['failed'] is not None} {rec['wall_s']:.1f}s",
               file=sys.stderr, flush=True)
+    return forms, u_ref, end_state
+
+
+def batched_study(args, dev):
+    """The batching form's Newton solve: the mixed hex8/hex20/tet10 bars
+    (random blocks, per-block yield) in uniaxial tension, plain FP64
+    against the FP32 precision form, every iteration on the device."""
+    from warp3d_gb300.engine import Engine
+    from warp3d_gb300.newton import uniaxial_bcs
+    from warp3d_gb300.solver import DeviceCsr
+    ny = nz = args.study_section
+    model, _, _, nx, origins = build_batched_workload(args.batched_elems, ny=ny, nz=nz)
+    fixed, topz = uniaxial_bcs(model, (nx[0], ny, nz), origins=origins)
+    t0 = time.perf_counter()
+    eng = Engine(model)
+    csr = DeviceCsr(eng)
+    setup_s = time.perf_counter() - t0
+    names = args.study_forms.split(",")
+    forms, _, _ = newton_forms(args, model, fixed, topz, nz, names, eng, csr)
+    csr.close()
+    return {"workload": f"mixed bars hex8/hex20/tet10 ({ny}x{nz} cells in section, nx {list(nx)}), random blocks "
+                        f"[16,128], per-block yield U(250,550) MPa; uniaxial {100 * args.study_strain:g}% in "
+                        f"{args.study_steps} steps",
+            "elements": model.noelem, "blocks": model.nelblk, "dofs": model.nodof, "csr_nnz": csr.nnz,
+            "setup_s": setup_s, "newton_tol": 1e-8, "pcg_rtol": 1e-10, "forms": forms}
+
+
+def precision_study(args, dev):
+    """The precision forms on the n^3 cube (mm01, jitter 0.1h, blocks of
+    128) under uniaxial tension, args.study_strain in args.study_steps
+    equal steps, every Newton iteration on the device (element path, CSR
+    assembly, Jacobi PCG to 1e-10, residual norms) to the 1e-8 relative
+    residual; steps start from the scaled previous increment and a failing
+    step is subdivided (4 sub-increments, down to 1/16 of the step, step 1
+    included). Per form: Newton iterations per step, PCG iterations, wall
+    time, the final displacements' error against the FP64 run; per-element
+    Ke error against the FP64 tangent (checked against the oracle by the
+    tests) at the converged end state of the FP64 run."""
+    import torch
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+    from warp3d_gb300.newton import uniaxial_bcs
+    from warp3d_gb300.solver import DeviceCsr
+    forms = {k: v for k, v in STUDY_FORMS.items()}
+    n = args.n
+    model, _, _ = build_workload(n)
+    fixed, topz = uniaxial_bcs(model, (n, n, n))
+    t0 = time.perf_counter()
+    eng = Engine(model)
+    csr = DeviceCsr(eng)
+    setup_s = time.perf_counter() - t0
+    out = {"workload": f"{n}^3 hex8 l3disop geonl (jitter 0.1h), mm01 bilinear, blocks of 128; uniaxial "
+                       f"{100 * args.study_strain:g}% in {args.study_steps} steps",
+           "elements": model.noelem, "dofs": model.nodof, "csr_nnz": csr.nnz, "setup_s": setup_s,
+           "newton_tol": 1e-8, "pcg_rtol": 1e-10, "forms": {}}
+    out["forms"], u_ref, end_state = newton_forms(args, model, fixed, topz, n, args.study_forms.split(","), eng, csr)
     # per-element Ke error at the FP64 run's converged end state
     if u_ref is not None:
         tu = torch.from_numpy(u_ref).to(dev)
@@ -658,6 +699,9 @@ def main():
 
     if args.precision_study:
         print(json.dumps({"precision_study": precision_study(args, dev)}))
+        return
+    if args.batched_study:
+        print(json.dumps({"batched_study": batched_study(args, dev)}))
         return
 
     from warp3d_gb300 import abi
