@@ -356,6 +356,32 @@ int w3g_assemble_ifv_noalloc(int nelblk, const int* elblks, const int* totdof,
                              const int* d_edest, double* d_ifv,
                              double* d_sum_ifv, void* stream);
 
+/* ---- timing and output checks --------------------------------------
+   Host wall time of the entry points, accumulated per context under
+   WARP3D's own timing categories (thyme calc 2 "tangent stiffness" and
+   calc 6 "sig-eps & internal force", src/thyme.f:15-35, printed by
+   src/outime.f); for the *_dev entry points this is the enqueue time. Each
+   call is also an NVTX range named after its entry point. */
+typedef struct w3g_timers {
+  double tangent_s;            /* w3g_tanstf, w3g_tanstf_dev              */
+  double recover_s;            /* w3g_recover, w3g_recover_dev            */
+  double update_s;             /* w3g_update                              */
+  long long tangent_calls, recover_calls, update_calls;
+} w3g_timers;
+int w3g_timers_get(w3g_context* ctx, w3g_timers* t);
+int w3g_timers_reset(w3g_context* ctx);
+
+/* Number of non-finite values (NaN, Inf) in the resident outputs:
+   urcs_n1, eps_n1, history1, einfvec and the element stiffnesses of the
+   current precision. WARP3D has no such scan (a NaN input travels through
+   its element routines without a step cut, as it does here); a driver can
+   call this after a recovery or a tangent. */
+int w3g_check_finite(w3g_context* ctx, long long* bad);
+
+/* Name of CUDA device `device` (NUL-terminated, truncated to len), e.g.
+   for keying an autotuning cache. */
+int w3g_device_name(int device, char* name, int len);
+
 /* ---- measurement helper (no WARP3D counterpart) ---------------------
    Sustained FP64 FMA throughput of `device` in TFLOP/s (2 flops per FMA),
    the roofline denominator of the FP64-bound element kernels. */

@@ -137,6 +137,11 @@ class Schedule(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Timers(C.Structure):
+    _fields_ = [("tangent_s", C.c_double), ("recover_s", C.c_double), ("update_s", C.c_double),
+                ("tangent_calls", C.c_longlong), ("recover_calls", C.c_longlong), ("update_calls", C.c_longlong)]
+
+
 # exported symbols and their prototypes: (name, restype, argtypes)
 _vp = C.c_void_p
 _d = C.POINTER(C.c_double)
@@ -173,6 +178,10 @@ PROTOTYPES = [
     ("w3g_pcg_dev", C.c_int, [_vp, _vp, _vp, C.c_double, _vp, C.c_double, C.c_int, _vp, C.POINTER(C.c_int),
                               C.POINTER(C.c_double)]),
     ("w3g_residual_norms_dev", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    ("w3g_timers_get", C.c_int, [_vp, C.POINTER(Timers)]),
+    ("w3g_timers_reset", C.c_int, [_vp]),
+    ("w3g_check_finite", C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    ("w3g_device_name", C.c_int, [C.c_int, C.c_char_p, C.c_int]),
 ]
 
 _lib = None

@@ -225,6 +225,23 @@ void w3g::set_last_error(const std::string& msg) { g_err = msg; }
 
 namespace {
 
+// number of non-finite values among n (device counter, order-free)
+template <class T>
+__global__ void k_count_nonfinite(const T* __restrict__ v, long long n, unsigned long long* bad) {
+  unsigned long long local = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    local += isfinite(v[i]) ? 0ull : 1ull;
+  if (local) atomicAdd(bad, local);
+}
+
+template <class T>
+cudaError_t count_nonfinite(const T* v, long long n, unsigned long long* bad, cudaStream_t st) {
+  if (n <= 0 || !v) return cudaSuccess;
+  const long long blocks = std::min<long long>((n + 255) / 256, 4096);
+  k_count_nonfinite<T><<<(int)blocks, 256, 0, st>>>(v, n, bad);
+  return cudaGetLastError();
+}
+
 // copies Ke of blocks [b0, b1) to the host pointers, blocks whose host
 // arrays follow each other in memory in one copy
 int copy_estiff_range(w3g_context* c, double* const* estiff, int b0, int b1, cudaStream_t st) {
@@ -615,7 +632,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(s.partials, 2 * m.nchunks);
   c->ifv_parts = assemble_ifv_parts(md->nodof);
   AL(s.ifv_partials, c->ifv_parts);
-  AL(s.status, 1);
+  AL(s.status, 2);   // [0] step-cut key, [1] scratch counter of w3g_check_finite
   AL(s.d_info, 1);
   AL(s.d_c, md->ncoord);
   AL(s.d_u, md->nodof);
@@ -752,6 +769,7 @@ int w3g_state_download(w3g_context* c, const w3g_block_state* h) {
 
 int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const double* hu, const double* hdu,
                double* const* estiff) {
+  CallScope scope_("w3g_tanstf", c ? &c->t_tangent : nullptr, c ? &c->n_tangent : nullptr);
   (void)step; (void)iter;
   if (!c || !hc || !hu || !hdu) return fail(W3G_EARG, "null argument");
   CK(cudaSetDevice(c->device));
@@ -781,6 +799,7 @@ int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const doubl
 
 int w3g_recover(w3g_context* c, int step, int iter, int extrapolated_du, const double* hc, const double* hu,
                 const double* hdu, double* hifv, w3g_recover_info* info) {
+  CallScope scope_("w3g_recover", c ? &c->t_recover : nullptr, c ? &c->n_recover : nullptr);
   if (!c || !hc || !hu || !hdu) return fail(W3G_EARG, "null argument");
   CK(cudaSetDevice(c->device));
   cudaStream_t st = c->stream;
@@ -802,6 +821,7 @@ int w3g_recover(w3g_context* c, int step, int iter, int extrapolated_du, const d
 }
 
 int w3g_update(w3g_context* c) {
+  CallScope scope_("w3g_update", c ? &c->t_update : nullptr, c ? &c->n_update : nullptr);
   if (!c) return fail(W3G_EARG, "null context");
   CK(cudaSetDevice(c->device));
   const long long gp = c->m.ngp_total;
@@ -815,6 +835,7 @@ int w3g_update(w3g_context* c) {
 
 int w3g_tanstf_dev(w3g_context* c, int step, int iter, const void* d_c, const void* d_u, const void* d_du,
                    void* stream) {
+  CallScope scope_("w3g_tanstf_dev", c ? &c->t_tangent : nullptr, c ? &c->n_tangent : nullptr);
   (void)step; (void)iter;
   if (!c || !d_c || !d_u || !d_du) return fail(W3G_EARG, "null argument");
   CK(cudaSetDevice(c->device));
@@ -823,6 +844,7 @@ int w3g_tanstf_dev(w3g_context* c, int step, int iter, const void* d_c, const vo
 
 int w3g_recover_dev(w3g_context* c, int step, int iter, int extrapolated_du, const void* d_c, const void* d_u,
                     const void* d_du, void* d_ifv, void* stream) {
+  CallScope scope_("w3g_recover_dev", c ? &c->t_recover : nullptr, c ? &c->n_recover : nullptr);
   if (!c || !d_c || !d_u || !d_du || !d_ifv) return fail(W3G_EARG, "null argument");
   CK(cudaSetDevice(c->device));
   return run_recover(c, step, iter, extrapolated_du, (const double*)d_c, (const double*)d_u, (const double*)d_du,
@@ -1075,6 +1097,57 @@ int w3g_estiff_device(w3g_context* c, void** d_estiff, long long* count) {
 }
 
 int w3g_last_launch_count(w3g_context* c) { return c ? c->last_launches : 0; }
+
+
+int w3g_timers_get(w3g_context* c, w3g_timers* t) {
+  if (!c || !t) return fail(W3G_EARG, "null argument");
+  t->tangent_s = c->t_tangent;
+  t->recover_s = c->t_recover;
+  t->update_s = c->t_update;
+  t->tangent_calls = c->n_tangent;
+  t->recover_calls = c->n_recover;
+  t->update_calls = c->n_update;
+  return 0;
+}
+
+int w3g_timers_reset(w3g_context* c) {
+  if (!c) return fail(W3G_EARG, "null context");
+  c->t_tangent = c->t_recover = c->t_update = 0.0;
+  c->n_tangent = c->n_recover = c->n_update = 0;
+  return 0;
+}
+
+int w3g_check_finite(w3g_context* c, long long* bad) {
+  if (!c || !bad) return fail(W3G_EARG, "null argument");
+  CK(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  unsigned long long* d_bad = reinterpret_cast<unsigned long long*>(c->s.status) + 1;   // scratch word
+  CK(cudaMemsetAsync(d_bad, 0, sizeof(unsigned long long), st));
+  const long long gp = c->m.ngp_total;
+  cudaError_t e = count_nonfinite(c->s.urcs_n1, 9 * gp, d_bad, st);
+  if (e == cudaSuccess) e = count_nonfinite(c->s.eps_n1, 6 * gp, d_bad, st);
+  if (e == cudaSuccess) e = count_nonfinite(c->s.hist1, c->m.hist_total, d_bad, st);
+  if (e == cudaSuccess) e = count_nonfinite(c->s.einf, c->m.einf_total, d_bad, st);
+  if (e == cudaSuccess) {
+    if (c->precision == W3G_TANGENT_FP64) e = count_nonfinite(c->s.estiff, c->m.estiff_total, d_bad, st);
+    else e = count_nonfinite(c->s.estiff32, c->m.estiff_total, d_bad, st);
+  }
+  if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("w3g_check_finite: ") + cudaGetErrorString(e));
+  unsigned long long h = 0;
+  CK(cudaMemcpyAsync(&h, d_bad, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *bad = (long long)h;
+  return 0;
+}
+
+int w3g_device_name(int device, char* name, int len) {
+  if (!name || len <= 0) return fail(W3G_EARG, "null argument");
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  std::strncpy(name, prop.name, (size_t)len - 1);
+  name[len - 1] = '\0';
+  return 0;
+}
 
 }  // extern "C"
 

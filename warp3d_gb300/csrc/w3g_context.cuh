@@ -2,8 +2,10 @@
 // device model and state, schedule, captured iteration graph. Shared by the
 // C-ABI translation units (w3g_api.cu, w3g_solve.cu).
 #pragma once
+#include <chrono>
 #include <string>
 #include <vector>
+#include <nvtx3/nvToolsExt.h>
 #include "w3g_internal.cuh"
 
 // one captured iteration (w3g_iteration_dev) and what it was captured for
@@ -34,6 +36,30 @@ struct w3g_context {
   std::vector<w3g::Chunk> h_tchunks;   // host copy of the tangent work items
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t part_done[8] = {};
+  // host wall time per entry point (w3g_timers_get)
+  double t_tangent = 0.0, t_recover = 0.0, t_update = 0.0;
+  long long n_tangent = 0, n_recover = 0, n_update = 0;
+};
+
+// One C-ABI call: an NVTX range (visible in Nsight timelines) and its host
+// wall time added to one of the context's accumulators, named after
+// WARP3D's own timing categories (thyme calc 2 "tangent stiffness" around
+// tanstf, calc 6 "sig-eps & internal force" around
+// drive_eps_sig_internal_forces; src/thyme.f, src/outime.f).
+struct CallScope {
+  double* acc;
+  long long* count;
+  std::chrono::steady_clock::time_point t0;
+  CallScope(const char* name, double* a, long long* n) : acc(a), count(n), t0(std::chrono::steady_clock::now()) {
+    nvtxRangePushA(name);
+  }
+  ~CallScope() {
+    nvtxRangePop();
+    if (acc) {
+      *acc += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      ++*count;
+    }
+  }
 };
 
 

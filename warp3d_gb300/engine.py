@@ -24,12 +24,32 @@ from . import abi
 from .model import HostState, Model, block_ptrs, dptr
 
 
+def _read_cache(path: str) -> dict:
+    import json
+    import os
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return json.load(f)
+
+
+def _write_cache(path: str, data: dict):
+    import json
+    import os
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
 class Engine:
     def __init__(self, model: Model, device: int = 0, precision: int = abi.TANGENT_FP64):
         self.lib = abi.load()
         self.model = model
         self.desc = model.desc()
         self.ctx = C.c_void_p()
+        self.device = device
+        self.precision = abi.TANGENT_FP64
         abi.check(self.lib, self.lib.w3g_create(device, C.byref(self.desc), C.byref(self.ctx)))
         if precision != abi.TANGENT_FP64:
             self.set_precision(precision)
@@ -48,6 +68,24 @@ class Engine:
 
     def set_precision(self, precision: int):
         abi.check(self.lib, self.lib.w3g_set_tangent_precision(self.ctx, precision))
+        self.precision = precision
+
+    # ---- timing and output checks -----------------------------------------
+    def timers(self) -> dict:
+        """Host wall time and call counts per entry point (WARP3D's timing
+        categories: tangent stiffness, sig-eps & internal force, update)."""
+        t = abi.Timers()
+        abi.check(self.lib, self.lib.w3g_timers_get(self.ctx, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def reset_timers(self):
+        abi.check(self.lib, self.lib.w3g_timers_reset(self.ctx))
+
+    def check_finite(self) -> int:
+        """Number of NaN/Inf values in the resident outputs."""
+        n = C.c_longlong()
+        abi.check(self.lib, self.lib.w3g_check_finite(self.ctx, C.byref(n)))
+        return n.value
 
     # ---- state transfer ----------------------------------------------------
     def upload(self, state: HostState, names=None):
@@ -117,12 +155,41 @@ class Engine:
                                                               d_c, d_u, d_du, d_ifv or None, stream or None))
 
     def autotune(self, step, it, extrapolated, d_c: int, d_u: int, d_du: int, d_ifv: int, stream: int = 0,
-                 reps: int = 3):
+                 reps: int = 3, cache: str | None = None):
+        """Times the candidate schedules on this model and keeps the fastest
+        (w3g_autotune). With ``cache`` (a JSON file), the choice is stored
+        under a key of the device, the tangent precision and, per element
+        type and material model, the element and Gauss-point counts, and
+        reused without timing when the key is already there."""
+        key = self.tuning_key() if cache else None
+        if cache:
+            entry = _read_cache(cache).get(key)
+            if entry is not None:
+                self.set_schedule(**entry["schedule"])
+                return dict(entry["schedule"]), float(entry["ms"])
         sc = abi.Schedule()
         ms = C.c_double()
         abi.check(self.lib, self.lib.w3g_autotune(self.ctx, step, it, 1 if extrapolated else 0, d_c, d_u, d_du,
                                                   d_ifv, stream or None, reps, C.byref(sc), C.byref(ms)))
+        if cache:
+            data = _read_cache(cache)
+            data[key] = {"schedule": sc.as_dict(), "ms": ms.value}
+            _write_cache(cache, data)
         return sc.as_dict(), ms.value
+
+    def tuning_key(self) -> str:
+        """Autotuning cache key: device name, precision, and per (element
+        type, Gauss points, material model) the elements and blocks."""
+        m = self.model
+        buf = C.create_string_buffer(256)
+        abi.check(self.lib, self.lib.w3g_device_name(self.device, buf, 256))
+        groups = {}
+        for b in range(m.nelblk):
+            k = (m.block_etype[b], m.block_ngp[b], "mm10" if m.block_crystal[b] else "mm01")
+            e, n = groups.get(k, (0, 0))
+            groups[k] = (e + m.spans[b], n + 1)
+        parts = [f"{t}/{g}/{mat}:{e}e{n}b" for (t, g, mat), (e, n) in sorted(groups.items())]
+        return f"{buf.value.decode()}|p{self.precision}|" + ",".join(parts)
 
     # ---- hot path, device pointers (ints) ----------------------------------
     def tanstf_dev(self, step, it, d_c: int, d_u: int, d_du: int, stream: int = 0):
