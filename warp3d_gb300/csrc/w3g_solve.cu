@@ -16,9 +16,12 @@
 //             reproducible. Traffic per launch: the contribution indices
 //             (4 B each), the element stiffness values they name, and the
 //             coefficients (8 B each)
-//   PCG       Jacobi-preconditioned conjugate gradient on the free dofs,
-//             five kernels per iteration (warp-per-row SpMV with the p.Kp
-//             partial, alpha, vector update with the r.z and r.r partials,
+//   PCG       preconditioned conjugate gradient on the free dofs (the
+//             inverse 3x3 diagonal block of each node, or the diagonal),
+//             five kernels per iteration (SpMV with the p.Kp partial: a
+//             warp per node when the three rows of every node share their
+//             column pattern, else a warp per row; alpha; vector update
+//             with the r.z and r.r partials,
 //             beta and the stopping test, direction update) reading the
 //             scalars from device memory; a batch of iterations replays as
 //             one CUDA graph and the host reads the state between batches.
@@ -95,6 +98,110 @@ __global__ void __launch_bounds__(kThreads) k_dinv(int n, const int* __restrict_
   }
 }
 
+// Node-block Jacobi (three rows of a node sharing their pattern): the
+// inverse of each node's 3x3 diagonal block over its free dofs (a
+// constrained dof's row and column are the identity's, its entries of the
+// inverse zero). A block that is not positive (det <= 0 or not finite)
+// falls back to the scalar diagonal.
+__global__ void __launch_bounds__(kThreads) k_binv(int nn, const int* __restrict__ diag,
+                                                   const double* __restrict__ val,
+                                                   const unsigned char* __restrict__ fixed, double* binv) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    double M[9];
+    bool f[3];
+    for (int i = 0; i < 3; ++i) f[i] = fixed[3 * k + i] != 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        M[3 * i + j] = (f[i] || f[j]) ? (i == j ? 1.0 : 0.0) : val[diag[3 * k + i] + (j - i)];
+    const double c0 = M[4] * M[8] - M[5] * M[7], c1 = M[5] * M[6] - M[3] * M[8], c2 = M[3] * M[7] - M[4] * M[6];
+    const double det = M[0] * c0 + M[1] * c1 + M[2] * c2;
+    double* B = binv + 9 * (long long)k;
+    if (det > 0.0 && isfinite(det)) {
+      const double r = 1.0 / det;
+      B[0] = c0 * r;
+      B[1] = (M[2] * M[7] - M[1] * M[8]) * r;
+      B[2] = (M[1] * M[5] - M[2] * M[4]) * r;
+      B[3] = c1 * r;
+      B[4] = (M[0] * M[8] - M[2] * M[6]) * r;
+      B[5] = (M[2] * M[3] - M[0] * M[5]) * r;
+      B[6] = c2 * r;
+      B[7] = (M[1] * M[6] - M[0] * M[7]) * r;
+      B[8] = (M[0] * M[4] - M[1] * M[3]) * r;
+    } else {
+      for (int q = 0; q < 9; ++q) B[q] = 0.0;
+      for (int i = 0; i < 3; ++i) B[4 * i] = (M[4 * i] != 0.0) ? 1.0 / M[4 * i] : 0.0;
+    }
+    for (int i = 0; i < 3; ++i)
+      if (f[i])
+        for (int j = 0; j < 3; ++j) B[3 * i + j] = B[3 * j + i] = 0.0;
+  }
+}
+
+// z = B^-1 r for one node (3 dofs)
+__device__ __forceinline__ void apply_binv(const double* B, const double* r, double* z) {
+  z[0] = B[0] * r[0] + B[1] * r[1] + B[2] * r[2];
+  z[1] = B[3] * r[0] + B[4] * r[1] + B[5] * r[2];
+  z[2] = B[6] * r[0] + B[7] * r[1] + B[8] * r[2];
+}
+
+__global__ void __launch_bounds__(kThreads) k_pcg_init3(int nn, const unsigned char* __restrict__ fixed,
+                                                        const double* __restrict__ b, double bscale,
+                                                        const double* __restrict__ binv, double* x, double* r,
+                                                        double* z, double* p, double* partials) {
+  __shared__ double sh[kWarps];
+  double rz = 0.0, rr = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    double rk[3], zk[3];
+    for (int i = 0; i < 3; ++i) rk[i] = fixed[3 * k + i] ? 0.0 : bscale * b[3 * k + i];
+    apply_binv(binv + 9 * (long long)k, rk, zk);
+    for (int i = 0; i < 3; ++i) {
+      x[3 * k + i] = 0.0;
+      r[3 * k + i] = rk[i];
+      z[3 * k + i] = zk[i];
+      p[3 * k + i] = zk[i];
+      rz += rk[i] * zk[i];
+      rr += rk[i] * rk[i];
+    }
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_update3(int nn, const double* __restrict__ binv, double* x, double* r,
+                                                      double* z, const double* __restrict__ p,
+                                                      const double* __restrict__ q, double* partials,
+                                                      const PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  if (sc->done) return;
+  const double a = sc->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
+    double rk[3], zk[3];
+    for (int i = 0; i < 3; ++i) {
+      const int d = 3 * k + i;
+      x[d] += a * p[d];
+      rk[i] = r[d] - a * q[d];
+      r[d] = rk[i];
+    }
+    apply_binv(binv + 9 * (long long)k, rk, zk);
+    for (int i = 0; i < 3; ++i) {
+      z[3 * k + i] = zk[i];
+      rz += rk[i] * zk[i];
+      rr += rk[i] * rk[i];
+    }
+  }
+  rz = block_sum(rz, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = rz;
+    partials[2 * blockIdx.x + 1] = rr;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_pcg_init(int n, const unsigned char* __restrict__ fixed,
                                                        const double* __restrict__ b, double bscale,
                                                        const double* __restrict__ dinv, double* x, double* r,
@@ -156,6 +263,67 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int n, const int* __restrict_
       const double qi = fixed[row] ? 0.0 : s;
       q[row] = qi;
       acc += qi * p[row];
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+}
+
+// the same product when the three rows of each node share one column
+// pattern: a warp per node reads the column indices and the gathered
+// direction once for the node's three rows
+__global__ void __launch_bounds__(kThreads) k_spmv3(int n, const int* __restrict__ rowptr,
+                                                    const int* __restrict__ colind, const double* __restrict__ val,
+                                                    const unsigned char* __restrict__ fixed,
+                                                    const double* __restrict__ p, double* __restrict__ q,
+                                                    double* partials, const PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  if (sc->done) return;
+  const int lane = threadIdx.x & 31;
+  const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+  double acc = 0.0;
+  for (int node = warp; node < n / 3; node += nw) {
+    const int r0 = 3 * node;
+    const int b0 = rowptr[r0], b1 = rowptr[r0 + 1], b2 = rowptr[r0 + 2], len = b1 - b0;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    // 96 stored columns per pass (3 per lane), all loads issued before the
+    // products: the 81-column rows of a 3D brick mesh take one pass
+    for (int kb = 0; kb < len; kb += 96) {
+      int c[3];
+      bool ok[3];
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int k = kb + lane + 32 * u;
+        ok[u] = k < len;
+        c[u] = ok[u] ? colind[b0 + k] : 0;
+      }
+      double x[3], v0[3], v1[3], v2[3];
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int k = kb + lane + 32 * u;
+        x[u] = ok[u] ? p[c[u]] : 0.0;
+        v0[u] = ok[u] ? val[b0 + k] : 0.0;
+        v1[u] = ok[u] ? val[b1 + k] : 0.0;
+        v2[u] = ok[u] ? val[b2 + k] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        s0 += v0[u] * x[u];
+        s1 += v1[u] * x[u];
+        s2 += v2[u] * x[u];
+      }
+    }
+    s0 = warp_sum_down(s0);
+    s1 = warp_sum_down(s1);
+    s2 = warp_sum_down(s2);
+    if (lane == 0) {
+      const double q0 = fixed[r0] ? 0.0 : s0, q1 = fixed[r0 + 1] ? 0.0 : s1, q2 = fixed[r0 + 2] ? 0.0 : s2;
+      q[r0] = q0;
+      q[r0 + 1] = q1;
+      q[r0 + 2] = q2;
+      acc += q0 * p[r0];
+      acc += q1 * p[r0 + 1];
+      acc += q2 * p[r0 + 2];
     }
   }
   acc = block_sum(acc, sh);
@@ -261,6 +429,8 @@ struct w3g_csr {
   double* val = nullptr;
   // PCG work
   int grid = 0;
+  bool triplet = false;   // dofs 3k..3k+2 of a node share their column pattern
+  double* binv = nullptr;  // node-block Jacobi inverses (triplet patterns)
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
   double* partials = nullptr;
   PcgScal* sc = nullptr;
@@ -282,7 +452,7 @@ namespace {
 void csr_free(w3g_csr* m) {
   if (m->batch) cudaGraphExecDestroy(m->batch);
   void* ptrs[] = {m->rowptr, m->colind, m->diag, m->cptr, m->csrc, m->val, m->x, m->r, m->z, m->p, m->q,
-                  m->dinv, m->partials, m->sc};
+                  m->dinv, m->binv, m->partials, m->sc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (m->ev_in) cudaEventDestroy(m->ev_in);
@@ -428,6 +598,24 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
       }
     cptr[nnz] = (int)k;
   }
+  // the stored pattern of a node's three rows: identical when every dof
+  // belongs to a node of three consecutive dofs (WARP3D's dstmap); the
+  // matrix product then reads the column indices and x once per node
+  std::vector<int> colind_all;
+  colind_all.reserve((size_t)nnz);
+  for (const RowsPart& P : parts) colind_all.insert(colind_all.end(), P.col.begin(), P.col.end());
+  bool triplet = n % 3 == 0;
+  for (int k = 0; triplet && k < n / 3; ++k) {
+    const int r0 = 3 * k, len = rowptr[r0 + 1] - rowptr[r0];
+    for (int d = 1; d < 3 && triplet; ++d) {
+      const int rd = r0 + d;
+      if (rowptr[rd + 1] - rowptr[rd] != len ||
+          !std::equal(colind_all.begin() + rowptr[r0], colind_all.begin() + rowptr[r0] + len,
+                      colind_all.begin() + rowptr[rd]))
+        triplet = false;
+    }
+  }
+  s->triplet = triplet;
   cudaError_t e = cudaSuccess;
   auto al = [&](auto** p, size_t count) {
     if (e == cudaSuccess) e = cudaMalloc((void**)p, std::max<size_t>(1, count) * sizeof(**p));
@@ -444,6 +632,7 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
   al(&s->p, n);
   al(&s->q, n);
   al(&s->dinv, n);
+  if (triplet) al(&s->binv, 3 * (size_t)n);
   al(&s->partials, 4 * (size_t)s->grid);   // PCG partials, then the norms' partials
   al(&s->sc, 1);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
@@ -452,13 +641,11 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
   if (e == cudaSuccess) e = cudaMemcpy(s->rowptr, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->diag, diag.data(), n * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->cptr, cptr.data(), (nnz + 1) * sizeof(int), cudaMemcpyHostToDevice);
-  long long zo = 0, ko = 0;
+  long long ko = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(s->colind, colind_all.data(), nnz * sizeof(int), cudaMemcpyHostToDevice);
   for (const RowsPart& P : parts) {
-    if (e == cudaSuccess && !P.col.empty())
-      e = cudaMemcpy(s->colind + zo, P.col.data(), P.col.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !P.src.empty())
       e = cudaMemcpy(s->csrc + ko, P.src.data(), P.src.size() * sizeof(int), cudaMemcpyHostToDevice);
-    zo += (long long)P.col.size();
     ko += (long long)P.src.size();
   }
   if (e == cudaSuccess) e = cudaMemset(s->val, 0, nnz * sizeof(double));
@@ -524,9 +711,15 @@ int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale
   // ordered after the caller's stream
   CKS(cudaEventRecord(s->ev_in, (cudaStream_t)stream));
   CKS(cudaStreamWaitEvent(st, s->ev_in, 0));
-  k_dinv<<<G, kThreads, 0, st>>>(n, s->diag, s->val, fixed, s->dinv);
-  k_pcg_init<<<G, kThreads, 0, st>>>(n, fixed, (const double*)d_b, b_scale, s->dinv, s->x, s->r, s->z, s->p,
+  if (s->triplet) {
+    k_binv<<<G, kThreads, 0, st>>>(n / 3, s->diag, s->val, fixed, s->binv);
+    k_pcg_init3<<<G, kThreads, 0, st>>>(n / 3, fixed, (const double*)d_b, b_scale, s->binv, s->x, s->r, s->z, s->p,
+                                        s->partials);
+  } else {
+    k_dinv<<<G, kThreads, 0, st>>>(n, s->diag, s->val, fixed, s->dinv);
+    k_pcg_init<<<G, kThreads, 0, st>>>(n, fixed, (const double*)d_b, b_scale, s->dinv, s->x, s->r, s->z, s->p,
                                      s->partials);
+  }
   k_pcg_init_fin<<<1, kThreads, 0, st>>>(s->partials, G, rtol, s->sc);
   CKS(cudaGetLastError());
   if (!s->batch || s->graph_fixed != d_fixed) {
@@ -535,9 +728,15 @@ int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale
     cudaGraph_t g;
     CKS(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < kBatch; ++it) {
-      k_spmv<<<G, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+      if (s->triplet)
+        k_spmv3<<<G, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+      else
+        k_spmv<<<G, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
       k_alpha<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
-      k_update<<<G, kThreads, 0, st>>>(n, s->dinv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
+      if (s->triplet)
+        k_update3<<<G, kThreads, 0, st>>>(n / 3, s->binv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
+      else
+        k_update<<<G, kThreads, 0, st>>>(n, s->dinv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
       k_beta<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
       k_pupdate<<<G, kThreads, 0, st>>>(n, s->z, s->p, s->sc);
     }
