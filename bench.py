@@ -321,11 +321,15 @@ def bench_crystal(args, dev, local, with_cpu):
         ms_rec, _ = timed(abi.ITER_RECOVER, steps)
         out["recovery_ms_" + ("natural_order" if order == abi.ORDER_BLOCKS else "sorted_queue")] = ms_rec
     its = eng.local_iterations()
-    for name, prec in (("plain_fp64", abi.TANGENT_FP64), ("mixed", abi.TANGENT_FP32)):
+    for name, prec in (("plain_fp64", abi.TANGENT_FP64), ("mixed", abi.TANGENT_FP32),
+                       ("mixed_tf32", abi.TANGENT_TF32)):
         eng.set_precision(prec)
         ms, launches = timed(both, steps)
         out[name] = {"value": ne / (ms * 1e-3), "ms_per_step": ms, "gpu_launches": launches}
-    out["mixed"]["speedup_vs_plain"] = out["plain_fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    for name in ("mixed", "mixed_tf32"):
+        out[name]["speedup_vs_plain"] = out["plain_fp64"]["ms_per_step"] / out[name]["ms_per_step"]
+    out["mixed_tf32"]["dtype"] = "tangent TF32 on the tensor cores (tcgen05), recovery fp64"
+    eng.set_precision(abi.TANGENT_FP64)
     hist = np.bincount(its, minlength=1)
     out["local_newton_iterations"] = {"min": int(its.min()), "mean": float(its.mean()), "max": int(its.max()),
                                       "p99": float(np.percentile(its, 99)),

@@ -923,8 +923,17 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
   return true;
 }
 
+// CTAs of k_mm10_update resident per SM (registers: 65536 / (128 x this)).
+// Measured on the 32^3 polycrystal (recovery, sorted queue): 2 -> 24.4 ms,
+// 3 -> 26.2 ms, 4 -> 26.5 ms: the local solve's working set outgrows the
+// registers, and the added spills cost more than the added warps hide
+#ifndef W3G_MM10_MIN_CTAS
+#define W3G_MM10_MIN_CTAS 2
+#endif
+constexpr int kMm10MinCtas = W3G_MM10_MIN_CTAS;
+
 // persistent: warps take 32 queue entries at a time
-__global__ void __launch_bounds__(128) k_mm10_update(RecoverArgs a, WorkQueue q) {
+__global__ void __launch_bounds__(128, kMm10MinCtas) k_mm10_update(RecoverArgs a, WorkQueue q) {
   const IterParams p = *a.params;
   const int lane = threadIdx.x & 31;
   for (;;) {
