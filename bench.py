@@ -457,6 +457,19 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+def whole_job_throughput(units_per_rank, ms_local, world, dist=None, device="cpu"):
+    """Replicas (one independent copy of the workload per rank, no data-path
+    collective): the step time is the maximum over ranks and the value is
+    all ranks' units over it. Returns (units/s, max ms)."""
+    t_step = ms_local
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    return world * units_per_rank / (t_step * 1e-3), t_step
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -786,12 +799,7 @@ def main():
         eng.set_precision(abi.TANGENT_FP64)
 
     # whole-job throughput: max time over ranks
-    t_step = ms64
-    if dist is not None:
-        t = torch.tensor([ms64], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = world * ne / (t_step * 1e-3)
+    value, t_step = whole_job_throughput(ne, ms64, world, dist, dev)
 
     # ---- e2e through the host-array C-ABI ----
     e2e = None
