@@ -38,8 +38,18 @@ __device__ __forceinline__ void hex8_item<float>(const TangentArgs& a, int cidx,
   tangent_item_hex8_f32(a, cidx, smem);
 }
 
+// resident one-warp CTAs per SM for the FP32 brick tangent (registers:
+// 65536 / (32 x this)); the FP64 form is bound by the FP64 pipe at any
+// occupancy. Measured on 262,144 bricks: 12 -> 0.530 ms, 16 -> 0.547 ms,
+// 20 -> 0.692 ms, 24 -> 0.821 ms (the 81 accumulators of a lane's node
+// pairs want registers more than the kernel wants warps)
+#ifndef W3G_TAN32_MIN_CTAS
+#define W3G_TAN32_MIN_CTAS 12
+#endif
+
 template <class T>
-__global__ void __launch_bounds__(kTangentThreads, sizeof(T) == 8 ? 1 : 12) k_tangent_hex8(TangentArgs a) {
+__global__ void __launch_bounds__(kTangentThreads, sizeof(T) == 8 ? 1 : W3G_TAN32_MIN_CTAS)
+    k_tangent_hex8(TangentArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   hex8_item<T>(a, a.chunk0 + blockIdx.x, smem);
 }
