@@ -270,8 +270,10 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int n, const int* __restrict_
 }
 
 // the same product when the three rows of each node share one column
-// pattern: a warp per node reads the column indices and the gathered
-// direction once for the node's three rows
+// pattern: eight lanes per node (four nodes per warp in flight) read the
+// column indices and the gathered direction once for the node's three
+// rows, 32 columns per pass with all loads issued first, and reduce over
+// their eight lanes in a fixed order
 __global__ void __launch_bounds__(kThreads) k_spmv3(int n, const int* __restrict__ rowptr,
                                                     const int* __restrict__ colind, const double* __restrict__ val,
                                                     const unsigned char* __restrict__ fixed,
@@ -279,44 +281,53 @@ __global__ void __launch_bounds__(kThreads) k_spmv3(int n, const int* __restrict
                                                     double* partials, const PcgScal* sc) {
   __shared__ double sh[kWarps];
   if (sc->done) return;
-  const int lane = threadIdx.x & 31;
-  const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+  const int lane = threadIdx.x & 31, sl = lane & 7;
+  const int group = (blockIdx.x * kWarps + (threadIdx.x >> 5)) * 4 + (lane >> 3);
+  const int ngroups = gridDim.x * kWarps * 4;
+  const int nn = n / 3;
   double acc = 0.0;
-  for (int node = warp; node < n / 3; node += nw) {
-    const int r0 = 3 * node;
-    const int b0 = rowptr[r0], b1 = rowptr[r0 + 1], b2 = rowptr[r0 + 2], len = b1 - b0;
+  // every lane of a warp runs the same number of passes (shuffles need the
+  // whole warp): the loop bound is the warp's largest node index
+  const int first = group - (lane >> 3);
+  for (int base = first; base < nn; base += ngroups) {
+    const int node = base + (lane >> 3);
+    const bool live = node < nn;
+    const int r0 = 3 * (live ? node : 0);
+    const int b0 = rowptr[r0], b1 = rowptr[r0 + 1], b2 = rowptr[r0 + 2];
+    const int len = live ? b1 - b0 : 0;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    // 96 stored columns per pass (3 per lane), all loads issued before the
-    // products: the 81-column rows of a 3D brick mesh take one pass
-    for (int kb = 0; kb < len; kb += 96) {
-      int c[3];
-      bool ok[3];
+    for (int kb = 0; kb < len; kb += 32) {
+      int c[4];
+      bool ok[4];
 #pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        const int k = kb + lane + 32 * u;
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + sl + 8 * u;
         ok[u] = k < len;
         c[u] = ok[u] ? colind[b0 + k] : 0;
       }
-      double x[3], v0[3], v1[3], v2[3];
+      double x[4], v0[4], v1[4], v2[4];
 #pragma unroll
-      for (int u = 0; u < 3; ++u) {
-        const int k = kb + lane + 32 * u;
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + sl + 8 * u;
         x[u] = ok[u] ? p[c[u]] : 0.0;
         v0[u] = ok[u] ? val[b0 + k] : 0.0;
         v1[u] = ok[u] ? val[b1 + k] : 0.0;
         v2[u] = ok[u] ? val[b2 + k] : 0.0;
       }
 #pragma unroll
-      for (int u = 0; u < 3; ++u) {
+      for (int u = 0; u < 4; ++u) {
         s0 += v0[u] * x[u];
         s1 += v1[u] * x[u];
         s2 += v2[u] * x[u];
       }
     }
-    s0 = warp_sum_down(s0);
-    s1 = warp_sum_down(s1);
-    s2 = warp_sum_down(s2);
-    if (lane == 0) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o, 8);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o, 8);
+      s2 += __shfl_down_sync(0xffffffffu, s2, o, 8);
+    }
+    if (live && sl == 0) {
       const double q0 = fixed[r0] ? 0.0 : s0, q1 = fixed[r0 + 1] ? 0.0 : s1, q2 = fixed[r0 + 2] ? 0.0 : s2;
       q[r0] = q0;
       q[r0 + 1] = q1;
@@ -429,6 +440,7 @@ struct w3g_csr {
   double* val = nullptr;
   // PCG work
   int grid = 0;
+  int grid_spmv = 0;      // resident CTAs of the matrix-product kernel (one wave)
   bool triplet = false;   // dofs 3k..3k+2 of a node share their column pattern
   double* binv = nullptr;  // node-block Jacobi inverses (triplet patterns)
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
@@ -616,6 +628,15 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
     }
   }
   s->triplet = triplet;
+  {
+    // one wave of the product kernel: its per-CTA partials are summed in a
+    // fixed order, so the grid is fixed per matrix
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, triplet ? (const void*)k_spmv3 : (const void*)k_spmv,
+                                                  kThreads, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    s->grid_spmv = std::max(1, std::min(s->grid, per_sm * sms));
+  }
   cudaError_t e = cudaSuccess;
   auto al = [&](auto** p, size_t count) {
     if (e == cudaSuccess) e = cudaMalloc((void**)p, std::max<size_t>(1, count) * sizeof(**p));
@@ -728,11 +749,12 @@ int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale
     cudaGraph_t g;
     CKS(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < kBatch; ++it) {
+      const int GS = s->grid_spmv;
       if (s->triplet)
-        k_spmv3<<<G, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+        k_spmv3<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
       else
-        k_spmv<<<G, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
-      k_alpha<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
+        k_spmv<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+      k_alpha<<<1, kThreads, 0, st>>>(s->partials, GS, s->sc);
       if (s->triplet)
         k_update3<<<G, kThreads, 0, st>>>(n / 3, s->binv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
       else
