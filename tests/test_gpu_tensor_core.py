@@ -165,3 +165,34 @@ def test_bf16_tangent_newton_rate_on_small_mesh():
         print("bf16 tangent: step 1 converged in", drv.history[-1][1], "iterations")
     except RuntimeError as exc:
         print("bf16 tangent: step 1 stalls:", str(exc)[:160])
+
+
+def test_tensor_core_tangent_in_a_graph_replay_equals_direct_launch(plastic_hex8):
+    """w3g_iteration_dev captures the tensor-core kernel in its CUDA graph;
+    the replayed Ke equals the directly launched one bit for bit."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    model, eng, ora, u, du = plastic_hex8
+    dev = torch.device("cuda", 0)
+    tc, tu, tdu = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (model.c, u, du))
+    tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    cudart = C.CDLL("libcudart.so")
+
+    def ke():
+        p, n = eng.estiff_device()
+        t = torch.empty(n, dtype=torch.float32, device=dev)
+        assert cudart.cudaMemcpy(C.c_void_p(t.data_ptr()), C.c_void_p(p), C.c_size_t(4 * n), 3) == 0
+        return t.cpu().numpy()
+
+    for precision in (abi.TANGENT_TF32, abi.TANGENT_BF16X3):
+        eng.set_precision(precision)
+        eng.tanstf_dev(4, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), stream)
+        torch.cuda.synchronize()
+        direct = ke()
+        for _ in range(2):
+            eng.iteration_dev(4, 1, False, abi.ITER_TANGENT, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(),
+                              tifv.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(ke(), direct)
+    eng.set_precision(abi.TANGENT_FP64)
