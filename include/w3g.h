@@ -311,6 +311,12 @@ int w3g_csr_destroy(w3g_csr* csr);
    values (nnz, double); any output may be NULL */
 int w3g_csr_info(w3g_csr* csr, int* n, long long* nnz, void** d_rowptr,
                  void** d_colind, void** d_values);
+/* The matrix product and preconditioner use the node blocks (a warp
+   reads a node's three rows with one set of column indices; inverse 3x3
+   diagonal blocks) when the three dofs of every node share their column
+   pattern, the default; enable = 0 selects the row kernels and the
+   diagonal preconditioner. Returns 1 when the node kernels are in use. */
+int w3g_csr_set_node_blocks(w3g_csr* csr, int enable);
 /* assembles the values from ctx's current element stiffnesses */
 int w3g_csr_assemble_dev(w3g_csr* csr, void* stream);
 /* host copies of the pattern and values (arrays of n+1, nnz, nnz) */

@@ -99,6 +99,13 @@ def test_device_pcg_matches_direct_solve():
     # iteration limit
     st3, its3, rel3 = csr.pcg(mask.data_ptr(), tb.data_ptr(), 1.0, tx2.data_ptr(), 1e-12, 5)
     assert st3 == abi.PCG_MAXIT and rel3 > 1e-12
+    # the row kernels with the diagonal preconditioner reach the same solution
+    assert csr.set_node_blocks(False) is False
+    tx3 = torch.zeros_like(tx)
+    st4, its4, rel4 = csr.pcg(mask.data_ptr(), tb.data_ptr(), -2.0, tx3.data_ptr(), 1e-12, 20000)
+    print(f"pcg, row kernels and diagonal preconditioner: {its4} iterations (node blocks: {its})")
+    assert st4 == 0 and rel_err(tx3.cpu().numpy()[free], ref) < 1e-9
+    assert csr.set_node_blocks(True) is True
     # norms on the device
     out = torch.zeros(2, dtype=torch.float64, device=dev)
     csr.residual_norms(tb.data_ptr(), mask.data_ptr(), out.data_ptr())

@@ -175,6 +175,7 @@ PROTOTYPES = [
                                C.POINTER(_vp)]),
     ("w3g_csr_assemble_dev", C.c_int, [_vp, _vp]),
     ("w3g_csr_download", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("w3g_csr_set_node_blocks", C.c_int, [_vp, C.c_int]),
     ("w3g_pcg_dev", C.c_int, [_vp, _vp, _vp, C.c_double, _vp, C.c_double, C.c_int, _vp, C.POINTER(C.c_int),
                               C.POINTER(C.c_double)]),
     ("w3g_residual_norms_dev", C.c_int, [_vp, _vp, _vp, _vp, _vp]),

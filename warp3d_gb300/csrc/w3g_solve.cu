@@ -249,17 +249,41 @@ __global__ void __launch_bounds__(kThreads) k_spmv(int n, const int* __restrict_
                                                    const unsigned char* __restrict__ fixed,
                                                    const double* __restrict__ p, double* __restrict__ q,
                                                    double* partials, const PcgScal* sc) {
+  // eight lanes per row, four rows per warp in flight, 32 columns per pass
+  // with all loads issued first, fixed-order reduction over the eight lanes
   __shared__ double sh[kWarps];
   if (sc->done) return;
-  const int lane = threadIdx.x & 31;
-  const int warp = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+  const int lane = threadIdx.x & 31, sl = lane & 7;
+  const int first = (blockIdx.x * kWarps + (threadIdx.x >> 5)) * 4;
+  const int ngroups = gridDim.x * kWarps * 4;
   double acc = 0.0;
-  for (int row = warp; row < n; row += nw) {
-    const int b = rowptr[row], e = rowptr[row + 1];
+  for (int base = first; base < n; base += ngroups) {
+    const int row = base + (lane >> 3);
+    const bool live = row < n;
+    const int b = rowptr[live ? row : 0];
+    const int len = live ? rowptr[row + 1] - b : 0;
     double s = 0.0;
-    for (int k = b + lane; k < e; k += 32) s += val[k] * p[colind[k]];
-    s = warp_sum_down(s);
-    if (lane == 0) {
+    for (int kb = 0; kb < len; kb += 32) {
+      int c[4];
+      bool ok[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = kb + sl + 8 * u;
+        ok[u] = k < len;
+        c[u] = ok[u] ? colind[b + k] : 0;
+      }
+      double x[4], v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        x[u] = ok[u] ? p[c[u]] : 0.0;
+        v[u] = ok[u] ? val[b + kb + sl + 8 * u] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s += v[u] * x[u];
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, 8);
+    if (live && sl == 0) {
       const double qi = fixed[row] ? 0.0 : s;
       q[row] = qi;
       acc += qi * p[row];
@@ -440,8 +464,10 @@ struct w3g_csr {
   double* val = nullptr;
   // PCG work
   int grid = 0;
-  int grid_spmv = 0;      // resident CTAs of the matrix-product kernel (one wave)
-  bool triplet = false;   // dofs 3k..3k+2 of a node share their column pattern
+  int grid_spmv = 0;      // resident CTAs of the node matrix-product kernel (one wave)
+  int grid_spmv_rows = 0; // ... of the row kernel
+  bool triplet = false;   // node kernels in use (w3g_csr_set_node_blocks)
+  bool pattern_triplet = false;   // dofs 3k..3k+2 of every node share their column pattern
   double* binv = nullptr;  // node-block Jacobi inverses (triplet patterns)
   double *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
   double* partials = nullptr;
@@ -628,14 +654,16 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
     }
   }
   s->triplet = triplet;
+  s->pattern_triplet = triplet;
   {
     // one wave of the product kernel: its per-CTA partials are summed in a
     // fixed order, so the grid is fixed per matrix
-    int per_sm = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, triplet ? (const void*)k_spmv3 : (const void*)k_spmv,
-                                                  kThreads, 0);
+    int per_sm = 0, per_sm_rows = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_spmv3, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_rows, (const void*)k_spmv, kThreads, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     s->grid_spmv = std::max(1, std::min(s->grid, per_sm * sms));
+    s->grid_spmv_rows = std::max(1, std::min(s->grid, per_sm_rows * sms));
   }
   cudaError_t e = cudaSuccess;
   auto al = [&](auto** p, size_t count) {
@@ -749,7 +777,7 @@ int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale
     cudaGraph_t g;
     CKS(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < kBatch; ++it) {
-      const int GS = s->grid_spmv;
+      const int GS = s->triplet ? s->grid_spmv : s->grid_spmv_rows;
       if (s->triplet)
         k_spmv3<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
       else
@@ -797,6 +825,17 @@ int w3g_residual_norms_dev(w3g_csr* s, const void* d_v, const void* d_fixed, voi
   k_norms_fin<<<1, kThreads, 0, st>>>(part, s->grid, (double*)d_out);
   CKS(cudaGetLastError());
   return 0;
+}
+
+int w3g_csr_set_node_blocks(w3g_csr* s, int enable) {
+  if (!s) return w3g_fail(W3G_EARG, "null csr");
+  const bool t = enable && s->pattern_triplet;
+  if (t != s->triplet) {
+    s->triplet = t;
+    if (s->batch) cudaGraphExecDestroy(s->batch);   // recaptured with the other kernels
+    s->batch = nullptr;
+  }
+  return t ? 1 : 0;
 }
 
 }  // extern "C"

@@ -46,6 +46,13 @@ class DeviceCsr:
         except Exception:
             pass
 
+    def set_node_blocks(self, enable: bool) -> bool:
+        """Node-block product and preconditioner (default when the pattern
+        allows) or the row kernels with the diagonal preconditioner."""
+        r = self.lib.w3g_csr_set_node_blocks(self.h, 1 if enable else 0)
+        abi.check(self.lib, r, allow=(0, 1))
+        return r == 1
+
     def assemble(self, stream: int = 0):
         """K from the context's current element stiffnesses (FP64, or the
         FP32 element matrices of a precision form)."""
