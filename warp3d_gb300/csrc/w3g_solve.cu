@@ -82,9 +82,20 @@ __global__ void __launch_bounds__(kThreads) k_assemble(long long nnz, const int*
                                                        double* __restrict__ val) {
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nnz;
        j += (long long)gridDim.x * blockDim.x) {
+    // contributions in their fixed order, four gathers in flight at a time
     double s = 0.0;
     const int e = cptr[j + 1];
-    for (int k = cptr[j]; k < e; ++k) s += (double)est[csrc[k]];
+    for (int k = cptr[j]; k < e; k += 4) {
+      int idx[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) idx[u] = k + u < e ? csrc[k + u] : -1;
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = idx[u] >= 0 ? (double)est[idx[u]] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (idx[u] >= 0) s += v[u];
+    }
     val[j] = s;
   }
 }
