@@ -248,7 +248,6 @@ def bench_batched(args, dev, local):
 def bench_crystal(args, dev, local, with_cpu):
     """mm10 line: 1% tension in 10 homogeneous steps, then timed iterations."""
     import torch
-    import oracle
     from warp3d_gb300 import abi
     from warp3d_gb300.engine import Engine
     from warp3d_gb300.model import Crystal, Model, cube_mesh, random_orientations
@@ -335,7 +334,9 @@ def bench_crystal(args, dev, local, with_cpu):
                                       "p99": float(np.percentile(its, 99)),
                                       "histogram": {int(k): int(v) for k, v in enumerate(hist) if v}}
     if with_cpu:
-        # the oracle on the first 16 blocks (2,048 elements) of the same state
+        # CPU baseline leg: the oracle on the first 16 blocks (2,048
+        # elements) of the same state
+        import oracle
         st = model.new_state()
         eng.download(st)
         nb = min(16, model.nelblk)
