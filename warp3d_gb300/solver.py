@@ -80,8 +80,36 @@ class DeviceCsr:
         abi.check(self.lib, self.lib.w3g_residual_norms_dev(self.h, d_v, d_fixed, d_out, stream or None))
 
 
-class _IncrementFailed(RuntimeError):
-    pass
+class IncrementFailed(RuntimeError):
+    """A (sub-)increment did not converge, or its recovery or solve asked
+    for a smaller step."""
+
+
+def run_subdivided(attempt, adaptive: bool, divisions: int = 4, min_fact: float = 1.0 / 16.0):
+    """One load step under WARP3D's adaptive solution (adapt_check,
+    src/adapt_check.f:15-120): attempt(fraction, after_cut) runs the whole
+    step first; when it raises IncrementFailed, the failed increment is
+    replaced by `divisions` equal sub-increments, down to `min_fact` of the
+    step, and the first sub-increment after a cut runs with after_cut =
+    True (the reference starts it without extrapolation). Returns the
+    fractions that converged, in order, and the number of cuts; raises
+    RuntimeError when a failed increment cannot be divided further."""
+    pending, after_cut, done, cuts = [1.0], False, [], 0
+    while pending:
+        f = pending.pop(0)
+        try:
+            attempt(f, after_cut)
+        except IncrementFailed as exc:
+            sub = f / divisions
+            if not adaptive or sub < min_fact * (1.0 - 1e-12):
+                raise RuntimeError(str(exc)) from None
+            cuts += 1
+            pending = [sub] * divisions + pending
+            after_cut = True
+            continue
+        after_cut = False
+        done.append(f)
+    return done, cuts
 
 
 class DeviceNewtonDriver:
@@ -163,7 +191,7 @@ class DeviceNewtonDriver:
         res_hist, lin = [], []
         self.trace = []
         if self._recover(step, 0, extrap) != 0:
-            raise _IncrementFailed(f"step {step}: recovery requested a step cut at iteration 0")
+            raise IncrementFailed(f"step {step}: recovery requested a step cut at iteration 0")
         self._tangent(step, 0)
         for it in range(1, self.maxit + 1):
             st, nits, rel = self.csr.pcg(self.mask.data_ptr(), self.ifv.data_ptr(), -1.0, self.d.data_ptr(),
@@ -171,11 +199,11 @@ class DeviceNewtonDriver:
             lin.append(nits)
             self.trace.append([st, nits, rel, None])
             if st == abi.PCG_BREAKDOWN:
-                raise _IncrementFailed(f"step {step}: tangent not positive definite on the free dofs "
+                raise IncrementFailed(f"step {step}: tangent not positive definite on the free dofs "
                                        f"(iteration {it})")
             self.du += self.d
             if self._recover(step, it, extrap) != 0:
-                raise _IncrementFailed(f"step {step}: step cut requested at iteration {it}")
+                raise IncrementFailed(f"step {step}: step cut requested at iteration {it}")
             self.csr.residual_norms(self.ifv.data_ptr(), self.mask.data_ptr(), self.norms.data_ptr())
             rf, ra = self.norms.cpu().numpy()
             rn, scale = float(np.sqrt(rf)), max(float(np.sqrt(ra)), 1e-300)
@@ -184,7 +212,7 @@ class DeviceNewtonDriver:
             if rn <= self.tol * scale:
                 return res_hist, lin
             self._tangent(step, it)
-        raise _IncrementFailed(f"step {step}: no convergence in {self.maxit} iterations: {res_hist}")
+        raise IncrementFailed(f"step {step}: no convergence in {self.maxit} iterations: {res_hist}")
 
     def step(self, step: int, imposed: np.ndarray):
         """imposed: full-length vector; its values on fixed dofs are the
@@ -192,25 +220,13 @@ class DeviceNewtonDriver:
         torch = self.torch
         imp = torch.from_numpy(np.asarray(imposed, dtype=np.float64)).to(self.du.device)
         adaptive = self.adaptive and (step > 1 or self.adaptive_step1)
-        pending = [1.0]            # fractions of the step still to run, in order
-        after_cut = False
         out = []
-        while pending:
-            f = pending.pop(0)
+
+        def attempt(f, after_cut):
             extrap_scale = None
             if self.extrapolate and self.du_prev is not None and step > 1 and not after_cut:
                 extrap_scale = f / self.frac_prev
-            try:
-                res_hist, lin = self._increment(step, imp * f, extrap_scale)
-            except _IncrementFailed as exc:
-                sub = f / self.adapt_divisions
-                if not adaptive or sub < self.adapt_min_fact * (1.0 - 1e-12):
-                    raise RuntimeError(str(exc)) from None
-                self.cuts += 1
-                pending = [sub] * self.adapt_divisions + pending
-                after_cut = True
-                continue
-            after_cut = False
+            res_hist, lin = self._increment(step, imp * f, extrap_scale)
             self.engine.update()
             self.ud += self.du
             self.du_prev = self.du.clone()
@@ -219,4 +235,7 @@ class DeviceNewtonDriver:
             self.lin_history.append((step, lin))
             self.fractions.append(f)
             out.extend(res_hist)
+
+        _, cuts = run_subdivided(attempt, adaptive, self.adapt_divisions, self.adapt_min_fact)
+        self.cuts += cuts
         return out
