@@ -105,7 +105,7 @@ int dgesv(int n, int nrhs, double* a, double* b) {
     for (int k = j + 1; k < n; ++k) {   // DGER, column k
       const double temp = -a[j + n * k];
       if (temp != zero)
-        for (int i = j + 1; i < n; ++i) a[i + n * k] = a[i + n * k] + a[i + n * j] * temp;
+        for (int i = j + 1; i < n; ++i) a[i + n * k] = std::fma(a[i + n * j], temp, a[i + n * k]);
     }
   }
   if (info) return info;
@@ -115,11 +115,11 @@ int dgesv(int n, int nrhs, double* a, double* b) {
       if (ipiv[i] != i) { double t = x[i]; x[i] = x[ipiv[i]]; x[ipiv[i]] = t; }
     for (int k = 0; k < n; ++k)
       if (x[k] != zero)
-        for (int i = k + 1; i < n; ++i) x[i] = x[i] - x[k] * a[i + n * k];
+        for (int i = k + 1; i < n; ++i) x[i] = std::fma(-x[k], a[i + n * k], x[i]);
     for (int k = n - 1; k >= 0; --k)
       if (x[k] != zero) {
         x[k] = x[k] / a[k + n * k];
-        for (int i = 0; i < k; ++i) x[i] = x[i] - x[k] * a[i + n * k];
+        for (int i = 0; i < k; ++i) x[i] = std::fma(-x[k], a[i + n * k], x[i]);
       }
   }
   return 0;
@@ -215,6 +215,22 @@ void mult_type_4(double* a, const double* b, const double* c, const double* d, d
     for (int r = 0; r < 6; ++r) a[r] = a[r] + M6(b, r, j) * c[j];
 }
 
+// The products of the local solve's inner loops (resolved shears, plastic
+// strain rate and spin, [C] times a vector, the Jacobian's outer products,
+// the LU updates) are fused multiply-adds in a fixed order, as on the
+// device (on FMA hardware the reference's compiler contracts them as
+// well); everything else stays unfused (-ffp-contract=off).
+void mult_type_2f(double* a, const double* b, const double* c) {   // a = [b] c, fused
+  for (int r = 0; r < 6; ++r) a[r] = M6(b, r, 0) * c[0];
+  for (int j = 1; j < 6; ++j)
+    for (int r = 0; r < 6; ++r) a[r] = std::fma(M6(b, r, j), c[j], a[r]);
+}
+void mult_type_4f(double* a, const double* b, const double* c, const double* d, double cst) {   // fused
+  for (int r = 0; r < 6; ++r) a[r] = cst * d[r];
+  for (int j = 0; j < 6; ++j)
+    for (int r = 0; r < 6; ++r) a[r] = std::fma(M6(b, r, j), c[j], a[r]);
+}
+
 void symsw(const double* s, const double* w, double* sw) {   // mm10_symsw
   sw[0] = s[3] * w[2] - s[5] * w[1];
   sw[1] = s[3] * w[2] - s[4] * w[0];
@@ -237,8 +253,9 @@ void iw_mat(const double* w, double* iw) {   // mm10_iw
 
 // ---- Voce slip law (mm10_b.f:1813-2082) -------------------------------
 double rs_of(const State& np1, const double* stress, int i) {
-  return stress[0] * np1.ms[i][0] + stress[1] * np1.ms[i][1] + stress[2] * np1.ms[i][2] +
-         stress[3] * np1.ms[i][3] + stress[4] * np1.ms[i][4] + stress[5] * np1.ms[i][5];
+  double r = stress[0] * np1.ms[i][0];
+  for (int k = 1; k < 6; ++k) r = std::fma(stress[k], np1.ms[i][k], r);
+  return r;
 }
 double slipinc_of(const CrystalProps& p, const State& np1, const double* stress, double tt, int i) {
   const double rs = rs_of(np1, stress, i);
@@ -251,7 +268,7 @@ void form_dbarp(const CrystalProps& p, const State& np1, const double* stress, d
     const double slipinc = slipinc_of(p, np1, stress, tt, i);
     const double rs = rs_of(np1, stress, i);
     const double f = rs * np1.tinc * p.iD_v + slipinc;
-    for (int k = 0; k < 6; ++k) dbar[k] = dbar[k] + f * np1.ms[i][k];
+    for (int k = 0; k < 6; ++k) dbar[k] = std::fma(f, np1.ms[i][k], dbar[k]);
   }
 }
 void form_wbarp(const CrystalProps& p, const State& np1, const double* stress, double tt, double* w) {
@@ -267,9 +284,9 @@ void form_wp(const CrystalProps& p, const State& np1, const double* stress, doub
   for (int k = 0; k < 3; ++k) w[k] = zero;
   for (int i = 0; i < NS; ++i) {
     const double slipinc = slipinc_of(p, np1, stress, tt, i);
-    for (int k = 0; k < 3; ++k) w[k] = w[k] + slipinc * np1.qc[i][k];
+    for (int k = 0; k < 3; ++k) w[k] = std::fma(slipinc, np1.qc[i][k], w[k]);
     const double rs = rs_of(np1, stress, i);
-    for (int k = 0; k < 3; ++k) w[k] = w[k] + rs * np1.tinc * p.iD_v * np1.qc[i][k];
+    for (int k = 0; k < 3; ++k) w[k] = std::fma(rs * np1.tinc * p.iD_v, np1.qc[i][k], w[k]);
   }
 }
 
@@ -279,7 +296,7 @@ void formR1(const CrystalProps& p, const State& np1, const State& n, const doubl
   form_wp(p, np1, stress, tt, wp);
   symsw(stress, wp, symTW);
   for (int k = 0; k < 6; ++k) wv1[k] = np1.D[k] - dbarp[k];
-  mult_type_2(wv2, p.stiffness, wv1);
+  mult_type_2f(wv2, p.stiffness, wv1);
   for (int k = 0; k < 6; ++k) R1[k] = stress[k] - n.stress[k] - wv2[k] + two * symTW[k];
 }
 
@@ -289,7 +306,7 @@ double formR2(const CrystalProps& p, State& np1, const State& n, const double* s
   for (int i = 0; i < NS; ++i) {
     const double slipinc = slipinc_of(p, np1, stress, tt, i);
     const double h_term = one - (tt - p.tau_y) / p.tau_v + np1.tau_l[i] / (tt - p.tau_y);
-    h = h + powr(std::fabs(h_term), p.voche_m) * sign1(h_term) * std::fabs(slipinc);
+    h = std::fma(powr(std::fabs(h_term), p.voche_m) * sign1(h_term), std::fabs(slipinc), h);
   }
   h = n.tau_tilde + p.theta_0 * h;
   np1.tt_rate = (h - n.tau_tilde) / np1.tinc;
@@ -329,11 +346,11 @@ void formJ11(const CrystalProps& p, const State& np1, const double* stress, doub
   symswmat(stress, np1, symtq);
   dgdt_voche(p, np1, stress, tt, dgdt);
   for (int i = 0; i < NS; ++i) {
-    mult_type_4(wv, p.stiffness, np1.ms[i], symtq[i], two);
+    mult_type_4f(wv, p.stiffness, np1.ms[i], symtq[i], two);
     for (int c = 0; c < 6; ++c) {   // DGER
       const double temp = dgdt[i] * np1.ms[i][c];
       if (temp != zero)
-        for (int r = 0; r < 6; ++r) M6(J11, r, c) = M6(J11, r, c) + wv[r] * temp;
+        for (int r = 0; r < 6; ++r) M6(J11, r, c) = std::fma(wv[r], temp, M6(J11, r, c));
     }
   }
   form_wp(p, np1, stress, tt, wp);
@@ -355,10 +372,10 @@ void formJ(const CrystalProps& p, const State& np1, const double* x, double* J /
     for (int i = 0; i < NS; ++i) {
       const double dgam = slipinc_of(p, np1, stress, tt, i);
       const double dgdtt = -p.rate_n / tt * dgam;
-      mult_type_4(tempmat, p.stiffness, np1.ms[i], symtq[i], two);
+      mult_type_4f(tempmat, p.stiffness, np1.ms[i], symtq[i], two);
       const double temp = one * dgdtt;
       if (temp != zero)
-        for (int r = 0; r < 6; ++r) J12[r] = J12[r] + tempmat[r] * temp;
+        for (int r = 0; r < 6; ++r) J12[r] = std::fma(tempmat[r], temp, J12[r]);
     }
   }
   // J21 = -estress_voche
@@ -368,7 +385,7 @@ void formJ(const CrystalProps& p, const State& np1, const double* x, double* J /
       const double rs = rs_of(np1, stress, i);
       const double h_term = one - (tt - p.tau_y) / p.tau_v + np1.tau_l[i] / (tt - p.tau_y);
       const double f = powr(std::fabs(h_term), p.voche_m) * sign1(h_term) * powr(std::fabs(rs), p.rate_n - two) * rs;
-      for (int k = 0; k < 6; ++k) et[k] = et[k] + f * np1.ms[i][k];
+      for (int k = 0; k < 6; ++k) et[k] = std::fma(f, np1.ms[i][k], et[k]);
     }
     const double f = p.theta_0 * np1.dg * p.rate_n / powr(tt, p.rate_n);
     for (int k = 0; k < 6; ++k) J21[k] = -(f * et[k]);

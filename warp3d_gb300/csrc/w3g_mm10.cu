@@ -218,14 +218,33 @@ __device__ __forceinline__ void cmul(const double* C, const double* c, double* a
     for (int r = 0; r < 6; ++r) a[r] = a[r] + C[r + 6 * j] * c[j];
 }
 
+// The products of the local solve's inner loops (resolved shears,
+// plastic strain rate and spin, C times a vector, the Jacobian's outer
+// products, the LU updates) are fused multiply-adds in a fixed order, the
+// same in the oracle (on FMA hardware the reference's compiler contracts
+// them as well); they are most of the FP64 instructions of a local
+// iteration on GB300's narrow FP64 pipe. The translation unit is compiled
+// with -fmad=false, so nothing else is contracted.
+__device__ __forceinline__ double rs_dot(const double* s, const double* m) {
+  double r = s[0] * m[0];
+  for (int k = 1; k < 6; ++k) r = fma(s[k], m[k], r);
+  return r;
+}
+
+// C (column-major 6x6) times c, column by column, fused
+__device__ __forceinline__ void cmul_f(const double* C, const double* c, double* a) {
+  for (int r = 0; r < 6; ++r) a[r] = C[r] * c[0];
+  for (int j = 1; j < 6; ++j)
+    for (int r = 0; r < 6; ++r) a[r] = fma(C[r + 6 * j], c[j], a[r]);
+}
+
 // resolved shears and slip increments of all systems (mm10_rs,
 // mm10_slipinc): computed once per evaluation point and reused by every
 // term that the reference evaluates at that point
 __device__ __forceinline__ void slip_terms(const CrystalType& t, const Geo& G, const Rate& q, const double* s,
                                            double tt, double* rs, double* sl) {
   for (int i = 0; i < NS; ++i) {
-    rs[i] = s[0] * G.ms[i][0] + s[1] * G.ms[i][1] + s[2] * G.ms[i][2] + s[3] * G.ms[i][3] + s[4] * G.ms[i][4] +
-            s[5] * G.ms[i][5];
+    rs[i] = rs_dot(s, G.ms[i]);
     sl[i] = q.dg / tt * powr(fabs(rs[i] / tt), t.rate_n - 1.0) * rs[i];
   }
 }
@@ -235,8 +254,8 @@ __device__ __forceinline__ void form_wp(const CrystalType& t, const Geo& G, cons
                                         const double* sl, double* w) {
   w[0] = 0.0; w[1] = 0.0; w[2] = 0.0;
   for (int i = 0; i < NS; ++i) {
-    for (int k = 0; k < 3; ++k) w[k] = w[k] + sl[i] * G.qc[i][k];
-    for (int k = 0; k < 3; ++k) w[k] = w[k] + rs[i] * q.tinc * t.iD_v * G.qc[i][k];
+    for (int k = 0; k < 3; ++k) w[k] = fma(sl[i], G.qc[i][k], w[k]);
+    for (int k = 0; k < 3; ++k) w[k] = fma(rs[i] * q.tinc * t.iD_v, G.qc[i][k], w[k]);
   }
 }
 
@@ -246,12 +265,12 @@ __device__ void formR1(const CrystalElem& x, const CrystalType& t, const Geo& G,
   double dbarp[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, wp[3], symTW[6], wv1[6], wv2[6];
   for (int i = 0; i < NS; ++i) {
     const double f = rs[i] * q.tinc * t.iD_v + sl[i];
-    for (int k = 0; k < 6; ++k) dbarp[k] = dbarp[k] + f * G.ms[i][k];
+    for (int k = 0; k < 6; ++k) dbarp[k] = fma(f, G.ms[i][k], dbarp[k]);
   }
   form_wp(t, G, q, rs, sl, wp);
   symsw(s, wp, symTW);
   for (int k = 0; k < 6; ++k) wv1[k] = q.D[k] - dbarp[k];
-  cmul(x.C, wv1, wv2);
+  cmul_f(x.C, wv1, wv2);
   for (int k = 0; k < 6; ++k) R1[k] = s[k] - n.stress[k] - wv2[k] + 2.0 * symTW[k];
 }
 
@@ -262,7 +281,7 @@ __device__ double formR2(const CrystalType& t, Rate& q, const Nstate& n, const d
   const double h_term = 1.0 - (tt - t.tau_y) / t.tau_v + 0.0 / (tt - t.tau_y);
   const double ph = powr(fabs(h_term), t.voche_m) * sgn1(h_term);
   double h = 0.0;
-  for (int i = 0; i < NS; ++i) h = h + ph * fabs(sl[i]);
+  for (int i = 0; i < NS; ++i) h = fma(ph, fabs(sl[i]), h);
   h = n.tt + t.theta_0 * h;
   q.tt_rate = (h - n.tt) / q.tinc;
   return tt - h;
@@ -305,16 +324,16 @@ __device__ __noinline__ void formJ(const CrystalElem& x, const CrystalType& t, c
     d = d + q.tinc * t.iD_v;
     for (int r = 0; r < 6; ++r) wv[r] = 2.0 * sw[r];
     for (int j = 0; j < 6; ++j)
-      for (int r = 0; r < 6; ++r) wv[r] = wv[r] + x.C[r + 6 * j] * G.ms[i][j];
+      for (int r = 0; r < 6; ++r) wv[r] = fma(x.C[r + 6 * j], G.ms[i][j], wv[r]);
     for (int c = 0; c < 6; ++c) {
       const double temp = d * G.ms[i][c];
       if (temp != 0.0)
-        for (int r = 0; r < 6; ++r) J[r + ld * c] = J[r + ld * c] + wv[r] * temp;
+        for (int r = 0; r < 6; ++r) J[r + ld * c] = fma(wv[r], temp, J[r + ld * c]);
     }
     if (kFull) {
       const double temp = 1.0 * (B * sl[i]);
       if (temp != 0.0)
-        for (int r = 0; r < 6; ++r) J12[r] = J12[r] + wv[r] * temp;
+        for (int r = 0; r < 6; ++r) J12[r] = fma(wv[r], temp, J12[r]);
     }
   }
   double w[3];
@@ -346,7 +365,7 @@ __device__ __noinline__ void formJ(const CrystalElem& x, const CrystalType& t, c
   double et[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = 0; i < NS; ++i) {
     const double f = ph * powr(fabs(rs[i]), t.rate_n - 2.0) * rs[i];
-    for (int k = 0; k < 6; ++k) et[k] = et[k] + f * G.ms[i][k];
+    for (int k = 0; k < 6; ++k) et[k] = fma(f, G.ms[i][k], et[k]);
   }
   const double fe = t.theta_0 * q.dg * t.rate_n / powr(tt, t.rate_n);
   for (int c = 0; c < 6; ++c) J[6 + 7 * c] = -(fe * et[c]);
@@ -379,7 +398,7 @@ __device__ __noinline__ void lu_solve(int n, double* a, double* b, int nrhs) {
     for (int k = j + 1; k < n; ++k) {
       const double temp = -a[j + n * k];
       if (temp != 0.0)
-        for (int i = j + 1; i < n; ++i) a[i + n * k] = a[i + n * k] + a[i + n * j] * temp;
+        for (int i = j + 1; i < n; ++i) a[i + n * k] = fma(a[i + n * j], temp, a[i + n * k]);
     }
   }
   for (int c = 0; c < nrhs; ++c) {
@@ -388,11 +407,11 @@ __device__ __noinline__ void lu_solve(int n, double* a, double* b, int nrhs) {
       if (ipiv[i] != i) { const double tt = x[i]; x[i] = x[ipiv[i]]; x[ipiv[i]] = tt; }
     for (int k = 0; k < n; ++k)
       if (x[k] != 0.0)
-        for (int i = k + 1; i < n; ++i) x[i] = x[i] - x[k] * a[i + n * k];
+        for (int i = k + 1; i < n; ++i) x[i] = fma(-x[k], a[i + n * k], x[i]);
     for (int k = n - 1; k >= 0; --k)
       if (x[k] != 0.0) {
         x[k] = x[k] / a[k + n * k];
-        for (int i = 0; i < k; ++i) x[i] = x[i] - x[k] * a[i + n * k];
+        for (int i = 0; i < k; ++i) x[i] = fma(-x[k], a[i + n * k], x[i]);
       }
   }
 }
