@@ -132,6 +132,8 @@ typedef struct w3g_model_desc {
   const int* elem_crystal;      /* noelem: 0-based crystal of the element */
   const double* elem_angles;    /* 3*noelem: Euler angles, degrees, Kocks */
   double dt;                    /* time increment of the load step       */
+  double eps_bbar;              /* b-bar stabilization factor (0), the
+                                   global eps_bbar, src/initst.f:537      */
 } w3g_model_desc;
 
 /*

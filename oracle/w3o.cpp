@@ -330,6 +330,60 @@ void blcmp1(int span, A2& b, int totdof, A2& gama, const double* nxi, const doub
   }
 }
 
+// ---------------------------------------------------------------------
+// b-bar (mean dilatation) of the 8-node brick. vol: (span, 8, 3) held as
+// A2 with index j + 8k (node j, derivative k = x, y, z).
+// ---------------------------------------------------------------------
+// vol_terms, src/vol_terms.f:14-108: adds one Gauss point's
+// det[J] dN_j/dx_k to vol and det[J] to volume
+void vol_terms(int span, A2& gama, const double* dj, A2& vol, const double* nxi, const double* neta,
+               const double* nzeta, double* volume) {
+  for (int i = 0; i < span; ++i) {
+    const double d = dj[i];
+    for (int k = 1; k <= 3; ++k) {
+      const double a = G(k, 1), bb = G(k, 2), c = G(k, 3);
+      for (int j = 0; j < 8; ++j)
+        vol(i, j + 8 * (k - 1)) = vol(i, j + 8 * (k - 1)) + (a * nxi[j] + bb * neta[j] + c * nzeta[j]) * d;
+    }
+    volume[i] = volume[i] + d;
+  }
+}
+
+// vol_avg, src/vol_avg.f:13-68: volume-averaged derivatives
+void vol_avg(int span, A2& vol, const double* volume) {
+  for (int i = 0; i < span; ++i) {
+    const double voli = one / volume[i];
+    for (int k = 0; k < 24; ++k) vol(i, k) = vol(i, k) * voli;
+  }
+}
+
+// bmod, src/bmod.f:16-205: replaces the dilatational part of [B] (rows
+// xx, yy, zz) by the element's mean dilatation, in the reference's order
+// of updates (the second loop reads entries the first has rewritten)
+void bmod(int span, A2& b, int totdof, A2& vol, double eps_stab) {
+  const double alpha = (two + eps_stab) * third;
+  const double beta = (one - eps_stab) * third;
+#define BB(i, j, k) b(i, (j) + totdof * (k))
+#define VB(i, j, k) vol(i, (j) + 8 * (k))
+  for (int i = 0; i < span; ++i) {
+    double dummy[8];
+    for (int j = 0; j < 8; ++j) dummy[j] = BB(i, j, 0);
+    for (int j = 0; j < 8; ++j) BB(i, j, 0) = alpha * dummy[j] + beta * VB(i, j, 0);
+    for (int j = 0; j < 8; ++j) BB(i, j, 1) = beta * (VB(i, j, 0) - dummy[j]);
+  }
+  for (int i = 0; i < span; ++i) {
+    for (int j = 0; j < 8; ++j) BB(i, 8 + j, 0) = beta * (VB(i, j, 1) - BB(i, 8 + j, 1));
+    for (int j = 0; j < 8; ++j) BB(i, 16 + j, 0) = beta * (VB(i, j, 2) - BB(i, 16 + j, 2));
+    for (int j = 0; j < 8; ++j) BB(i, 8 + j, 1) = alpha * BB(i, 8 + j, 1) + beta * VB(i, j, 1);
+    for (int j = 0; j < 8; ++j) BB(i, 16 + j, 1) = BB(i, 16 + j, 0);
+    for (int j = 0; j < 8; ++j) BB(i, j, 2) = BB(i, j, 1);
+    for (int j = 0; j < 8; ++j) BB(i, 8 + j, 2) = BB(i, 8 + j, 0);
+    for (int j = 0; j < 8; ++j) BB(i, 16 + j, 2) = alpha * BB(i, 16 + j, 2) + beta * VB(i, j, 2);
+  }
+#undef BB
+#undef VB
+}
+
 // getrm1, src/gtmat1.f:740-960. r: (span, 9) column-major 3x3 at one GP
 // (rot(r,c) -> r + 3c). q: (span, 36), q(i, r, c) -> (r-1) + 6(c-1).
 void getrm1(int span, A2& q, const double* const* rcol /* 9 columns */, int opt) {
@@ -848,11 +902,17 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
     mv.lnelas[i] = flog(lp[16]); mv.yld[i] = p[22];
   }
 
-  // rknstr_geonl (src/rknstr.f:455-540): [J] at mid-step configuration
+  // rknstr_geonl (src/rknstr.f:455-540): [J] at the mid-step
+  // configuration; rknstr_sm_displ (:555-610): [J] at t = 0. For 8-node
+  // bricks with b-bar, the mean-dilatation terms of that configuration
+  // (vol_terms per Gauss point, then vol_avg).
+  const bool bbar = B.bbar && B.etype == W3G_ETYPE_L3DISOP;
   std::vector<double> nxi((size_t)ngp * nnode), neta((size_t)ngp * nnode), nzeta((size_t)ngp * nnode),
       weights(ngp);
   std::vector<std::vector<double>> det_j_mid(ngp, std::vector<double>(MXVL));
   std::vector<A2> gama_mid(ngp, A2(9));
+  A2 vol(24);
+  std::vector<double> volume(MXVL, zero);
   for (int g = 0; g < ngp; ++g) {
     double xi, eta, zeta;
     getgpts(B.etype, B.order, g + 1, xi, eta, zeta, weights[g]);
@@ -863,7 +923,11 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
     else
       jacob1(span, nnode, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], ce0,
              det_j_mid[g].data(), gama_mid[g]);
+    if (bbar)
+      vol_terms(span, gama_mid[g], det_j_mid[g].data(), vol, &nxi[g * nnode], &neta[g * nnode],
+                &nzeta[g * nnode], volume.data());
   }
+  if (bbar) vol_avg(span, vol, volume.data());
 
   std::vector<std::vector<double>> det_j(ngp, std::vector<double>(MXVL));
   std::vector<A2> gama(ngp, A2(9));
@@ -873,42 +937,49 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
   std::vector<double> dfn1_all((size_t)ngp * MXVL);
 
   for (int g = 0; g < ngp; ++g) {
-    // ---- rstgp1 (src/rstgp1.f:19-332), geonl branch
+    // ---- rstgp1 (src/rstgp1.f:19-332) for geonl blocks, rstgp2
+    // (:351-598) for small-displacement blocks
     A2 ddt(NSTR), uddt(NSTR);
-    // rstgp1_a
-    for (int j = 0; j < totdof; ++j)
-      for (int i = 0; i < span; ++i) {
-        uenh(i, j) = ue(i, j) + half * due(i, j);
-        uen1(i, j) = ue(i, j) + due(i, j);
-      }
-    // gtmat1 (src/gtmat1.f:17-190)
     A2 theta(9), fn1(9), fnh(9), qnhalf(36);
     double dfn1[MXVL], dfh[MXVL];
     A2 rnh(9);
-    jacob1(span, nnode, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], ce0, det_j[g].data(), gama[g]);
-    tcomp1(span, theta, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], gama[g], uen1, nnode);
-    int bad = fcomp1(span, fn1, dfn1, theta);
-    if (bad >= 0) { out.status = W3G_STEP_CUT; out.bad_elem = B.felem + bad; return out; }
-    {
-      double* rc[9];
-      for (int k = 0; k < 9; ++k) rc[k] = rot[g].col(k);
-      rtcmp1(span, fn1, rc);
+    if (B.geonl) {
+      // rstgp1_a
+      for (int j = 0; j < totdof; ++j)
+        for (int i = 0; i < span; ++i) {
+          uenh(i, j) = ue(i, j) + half * due(i, j);
+          uen1(i, j) = ue(i, j) + due(i, j);
+        }
+      // gtmat1 (src/gtmat1.f:17-190)
+      jacob1(span, nnode, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], ce0, det_j[g].data(), gama[g]);
+      tcomp1(span, theta, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], gama[g], uen1, nnode);
+      int bad = fcomp1(span, fn1, dfn1, theta);
+      if (bad >= 0) { out.status = W3G_STEP_CUT; out.bad_elem = B.felem + bad; return out; }
+      {
+        double* rc[9];
+        for (int k = 0; k < 9; ++k) rc[k] = rot[g].col(k);
+        rtcmp1(span, fn1, rc);
+      }
+      tcomp1(span, theta, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], gama[g], uenh, nnode);
+      bad = fcomp1(span, fnh, dfh, theta);
+      if (bad >= 0) { out.status = W3G_STEP_CUT; out.bad_elem = B.felem + bad; return out; }
+      {
+        double* rc[9];
+        for (int k = 0; k < 9; ++k) rc[k] = rnh.col(k);
+        rtcmp1(span, fnh, rc);
+        const double* rcc[9];
+        for (int k = 0; k < 9; ++k) rcc[k] = rnh.col(k);
+        getrm1(span, qnhalf, rcc, 1);
+      }
+      for (int i = 0; i < span; ++i) dfn1_all[(size_t)g * MXVL + i] = dfn1[i];
+    } else {
+      // rstgp2: det[J] of rknstr_sm_displ
+      for (int i = 0; i < span; ++i) det_j[g][i] = det_j_mid[g][i];
     }
-    tcomp1(span, theta, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], gama[g], uenh, nnode);
-    bad = fcomp1(span, fnh, dfh, theta);
-    if (bad >= 0) { out.status = W3G_STEP_CUT; out.bad_elem = B.felem + bad; return out; }
-    {
-      double* rc[9];
-      for (int k = 0; k < 9; ++k) rc[k] = rnh.col(k);
-      rtcmp1(span, fnh, rc);
-      const double* rcc[9];
-      for (int k = 0; k < 9; ++k) rcc[k] = rnh.col(k);
-      getrm1(span, qnhalf, rcc, 1);
-    }
-    for (int i = 0; i < span; ++i) dfn1_all[(size_t)g * MXVL + i] = dfn1[i];
-    // gtlsn1 (src/gtlsn1.f:25-85)
+    // gtlsn1 (src/gtlsn1.f:25-85), with bmod for b-bar
     b.zero();
     blcmp1(span, b, totdof, gama_mid[g], &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], nnode);
+    if (bbar) bmod(span, b, totdof, vol, m->eps_bbar);
     ddt.zero();
     {
       int bpos1 = nnode, bpos2 = 2 * nnode;
@@ -927,11 +998,17 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
         }
 #undef BB
     }
-    // qmply1 + rstgp1_update_strains
+    // qmply1 (geonl: unrotated increment; rstgp2 takes ddt as it is) +
+    // rstgp1_update_strains
     {
-      const double* m1[6]; double* m2[6];
-      for (int k = 0; k < 6; ++k) { m1[k] = ddt.col(k); m2[k] = uddt.col(k); }
-      qmply1(span, qnhalf, m1, m2);
+      if (B.geonl) {
+        const double* m1[6]; double* m2[6];
+        for (int k = 0; k < 6; ++k) { m1[k] = ddt.col(k); m2[k] = uddt.col(k); }
+        qmply1(span, qnhalf, m1, m2);
+      } else {
+        for (int k = 0; k < 6; ++k)
+          for (int i = 0; i < span; ++i) uddt(i, k) = ddt(i, k);
+      }
       for (int i = 0; i < span; ++i)
         for (int k = 0; k < 6; ++k) ddtse[g](i, k) = ddtse[g](i, k) + uddt(i, k);
     }
@@ -988,10 +1065,12 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
         for (int k = 0; k < 21; ++k)
           gc[((size_t)g * span + i) * 21 + k] = cep(i, (kLowerR[k] - 1) + 6 * (kLowerC[k] - 1));
     }
-    // rstgp1_b (src/rstgp1.f:5189-5241), large-strain branch
+    // rstgp1_b (src/rstgp1.f:5189-5241): large-strain (itype 1) or
+    // small-strain (itype 2) branch
     if (iter != 0) {
       for (int i = 0; i < span; ++i) {
-        double factor = dfn1[i] * det_j[g][i] * m->beta_fact * weights[g];
+        double factor = B.geonl ? dfn1[i] * det_j[g][i] * m->beta_fact * weights[g]
+                                : det_j[g][i] * m->beta_fact * weights[g];
         internal_energy = internal_energy + urcs_n1[g](i, 6) * factor;
         plastic_work = plastic_work + urcs_n1[g](i, 7) * factor;
       }
@@ -1022,12 +1101,22 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
   eleifv.zero();
   double elem_vol[MXVL];
   for (int i = 0; i < span; ++i) elem_vol[i] = zero;
-  for (int g = 0; g < ngp; ++g)
+  if (bbar) {
+    vol.zero();
+    for (int i = 0; i < span; ++i) volume[i] = zero;
+  }
+  for (int g = 0; g < ngp; ++g) {
     jacob1(span, nnode, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], cen1, det_j[g].data(), gama[g]);
+    if (bbar)
+      vol_terms(span, gama[g], det_j[g].data(), vol, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode],
+                volume.data());
+  }
+  if (bbar) vol_avg(span, vol, volume.data());
   for (int g = 0; g < ngp; ++g) {
     double w = weights[g] * adjust_scalar(B.etype);   // gpifv1.f:43-47
     b.zero();
     blcmp1(span, b, totdof, gama[g], &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], nnode);
+    if (bbar) bmod(span, b, totdof, vol, m->eps_bbar);
     const double* dj = det_j[g].data();
     if (B.geonl) {
       A2 qtn1(36), cs(6);
@@ -1098,17 +1187,25 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
       const double* up = s->urcs_n1[B.blk] + ((size_t)i * ngp + g) * NSTRS;
       for (int k = 0; k < NSTRS; ++k) urcs[g](i, k) = up[k];
     }
-  // rktstf GP loop 1
+  // rktstf GP loop 1 (src/rktstf.f:98-145), with the b-bar volume terms
+  // of the configuration at n+1 (geonl) or t = 0
+  const bool bbar = B.bbar && B.etype == W3G_ETYPE_L3DISOP;
   std::vector<double> nxi((size_t)ngp * nnode), neta((size_t)ngp * nnode), nzeta((size_t)ngp * nnode),
       weights(ngp);
   std::vector<std::vector<double>> dj(ngp, std::vector<double>(MXVL));
   std::vector<A2> gama(ngp, A2(9));
+  A2 vol(24);
+  std::vector<double> volume(MXVL, zero);
   for (int g = 0; g < ngp; ++g) {
     double xi, eta, zeta;
     getgpts(B.etype, B.order, g + 1, xi, eta, zeta, weights[g]);
     derivs(B.etype, xi, eta, zeta, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode]);
     jacob1(span, nnode, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], ce, dj[g].data(), gama[g]);
+    if (bbar)
+      vol_terms(span, gama[g], dj[g].data(), vol, &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode],
+                volume.data());
   }
+  if (bbar) vol_avg(span, vol, volume.data());
   A2 ek(utsz);
   ek.zero();
   A2 b(totdof * 6), bd(totdof * 6);
@@ -1134,6 +1231,7 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
       qmply1(span, qn1, m1, m2);
     }
     blcmp1(span, b, totdof, gama[g], &nxi[g * nnode], &neta[g * nnode], &nzeta[g * nnode], nnode);
+    if (bbar) bmod(span, b, totdof, vol, m->eps_bbar);
     // drive_01_cnst -> extract_D_symmetric (src/gptns1.f:1174-1266), or
     // drive_10_cnst (:1371-1455): [D] = w det[J] history1(1:36)
     A2 cep(36);
@@ -1228,12 +1326,19 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
 #undef BB
 #undef BD
 #undef CE
-    // kgstiff (src/kg1.f:16-110), symmetric assembly
+    // kgstiff (src/kg1.f:16-110), symmetric assembly; with b-bar the
+    // volume-averaged derivatives replace the Gauss point's (kg1.f:46-54)
     if (B.geonl) {
       std::vector<double> gxi((size_t)MXVL * nnode), geta((size_t)MXVL * nnode), gzeta((size_t)MXVL * nnode);
       A2& gm = gama[g];
       for (int j = 0; j < nnode; ++j)
         for (int i = 0; i < span; ++i) {
+          if (bbar) {
+            gxi[(size_t)j * MXVL + i] = vol(i, j);
+            geta[(size_t)j * MXVL + i] = vol(i, j + 8);
+            gzeta[(size_t)j * MXVL + i] = vol(i, j + 16);
+            continue;
+          }
           const double* nx = &nxi[g * nnode]; const double* ne = &neta[g * nnode]; const double* nz = &nzeta[g * nnode];
           gxi[(size_t)j * MXVL + i] = gm(i, 0) * nx[j] + gm(i, 3) * ne[j] + gm(i, 6) * nz[j];
           geta[(size_t)j * MXVL + i] = gm(i, 1) * nx[j] + gm(i, 4) * ne[j] + gm(i, 7) * nz[j];
@@ -1301,6 +1406,8 @@ int w3o_tanstf(const w3g_model_desc* m, const w3g_block_state* s, int step, int 
   for (int blk = 0; blk < m->nelblk; ++blk) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
+    if (B.mat_type == W3G_MAT_CRYSTAL && (!B.geonl || (B.bbar && B.etype == W3G_ETYPE_L3DISOP)))
+      return W3G_EUNSUPPORTED;
   }
 #ifdef _OPENMP
   if (g_threads > 0) omp_set_num_threads(g_threads);
@@ -1325,7 +1432,11 @@ int w3o_recover(const w3g_model_desc* m, const w3g_block_state* s, int step, int
   for (int blk = 0; blk < m->nelblk; ++blk) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
-    if ((B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL) || !B.geonl) return W3G_EUNSUPPORTED;
+    if (B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL) return W3G_EUNSUPPORTED;
+    // mm10 is restated on the finite-strain path only; with b-bar WARP3D
+    // gives mm10 bricks the F-bar kinematics (gtmat1_make_fbar), not restated
+    if (B.mat_type == W3G_MAT_CRYSTAL && (!B.geonl || (B.bbar && B.etype == W3G_ETYPE_L3DISOP)))
+      return W3G_EUNSUPPORTED;
     if (B.mat_type == W3G_MAT_CRYSTAL && (!m->crystals || !m->elem_crystal || !m->elem_angles))
       return W3G_EARG;
   }

@@ -16,11 +16,12 @@ MESHES = {abi.ETYPE_L3DISOP: cube_mesh, abi.ETYPE_Q3DISOP: cube_mesh_hex20, abi.
 
 
 def make_model(n=6, jitter=0.1, seed=12345, block_size=128, spans=None, beta=1.0, n_xyz=None, materials=None,
-               etype=abi.ETYPE_L3DISOP):
+               etype=abi.ETYPE_L3DISOP, **kw):
+    """kw: Model options (geonl, bbar, eps_bbar, qbar)."""
     nxyz = (n, n, n) if n_xyz is None else n_xyz
     coords, incid = MESHES[etype](n, jitter=jitter, seed=seed, n_xyz=nxyz)
     mats = materials or [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0, beta=beta)]
-    return Model(coords, incid, block_size=block_size, block_spans=spans, materials=mats, etype=etype), nxyz
+    return Model(coords, incid, block_size=block_size, block_spans=spans, materials=mats, etype=etype, **kw), nxyz
 
 
 def loaded_state(model, nxyz, engine_cls, steps=3, strain_per_step=0.0015, shear_per_step=0.0,

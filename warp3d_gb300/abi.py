@@ -94,6 +94,7 @@ class ModelDesc(C.Structure):
         ("elem_crystal", C.POINTER(C.c_int)),
         ("elem_angles", C.POINTER(C.c_double)),
         ("dt", C.c_double),
+        ("eps_bbar", C.c_double),
     ]
 
 

@@ -310,13 +310,14 @@ class Model:
     never mix types, as in WARP3D)."""
 
     def __init__(self, coords, incid=None, *, parts=None, block_size=128, etype=abi.ETYPE_L3DISOP, geonl=True,
-                 bbar=False, qbar=True, materials=None, block_spans=None, angles=None, dt=1.0):
+                 bbar=False, qbar=True, materials=None, block_spans=None, angles=None, dt=1.0, eps_bbar=0.0):
         if parts is None:
             parts = [Part(etype, np.asarray(incid), block_spans, materials)]
         self.coords = np.asarray(coords, dtype=np.float64)
         self.parts = parts
         self.block_size = block_size
         self.geonl, self.bbar, self.qbar = geonl, bbar, qbar
+        self.eps_bbar = float(eps_bbar)
         self.nnode = self.coords.shape[0]
         self.nodof = 3 * self.nnode
         self.ncoord = 3 * self.nnode
@@ -395,7 +396,9 @@ class Model:
             self.iprops[rows, 24] = abi.MAT_CRYSTAL if isinstance(mat, Crystal) else abi.MAT_BILINEAR
             self.iprops[rows, 37] = 1
             self.lprops[rows, 17] = 1 if self.geonl else 0
-            self.lprops[rows, 18] = 1 if self.bbar else 0
+            # b-bar is an option of the 8-node brick only (elprp.f sets
+            # lprops(19) false for every other type)
+            self.lprops[rows, 18] = 1 if (self.bbar and t == abi.ETYPE_L3DISOP) else 0
             if isinstance(mat, Crystal):
                 self.props[rows, 6] = np.float32(mat.e)
                 self.props[rows, 7] = np.float32(mat.nu)
@@ -435,6 +438,7 @@ class Model:
             d.elem_crystal = self.elem_crystal.ctypes.data_as(C.POINTER(C.c_int))
             d.elem_angles = self.elem_angles.ctypes.data_as(C.POINTER(C.c_double))
         d.dt = self.dt
+        d.eps_bbar = self.eps_bbar
         return d
 
     def new_state(self) -> "HostState":
