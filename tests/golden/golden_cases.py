@@ -34,11 +34,13 @@ def path(name: str) -> str:
 
 
 # ---- the cases (kept small: the fixtures are committed) -------------------
-def _mm01_case(etype, nxyz, spans, shear):
+def _mm01_case(etype, nxyz, spans, shear, dyld=25.0, **opts):
+    """dyld: yield-stress step between blocks; opts: Model options (geonl,
+    bbar, eps_bbar)."""
     from tests.helpers import MESHES
     coords, incid = MESHES[etype](nxyz[0], jitter=0.08, seed=31, n_xyz=nxyz)
-    mats = [Bilinear.from_hprime(200000.0, 0.3, 400.0 + 25.0 * b, 2000.0) for b in range(len(spans))]
-    model = Model(coords, parts=[Part(etype, incid, spans, mats)])
+    mats = [Bilinear.from_hprime(200000.0, 0.3, 400.0 + dyld * b, 2000.0) for b in range(len(spans))]
+    model = Model(coords, parts=[Part(etype, incid, spans, mats)], **opts)
     return model, nxyz, {"strain": 0.0015, "shear": shear, "extrapolate": False}
 
 
@@ -53,13 +55,23 @@ CASES = {
     "hex20_mm01": lambda: _mm01_case(abi.ETYPE_Q3DISOP, (2, 1, 1), [1, 1], 0.0),
     "tet10_mm01": lambda: _mm01_case(abi.ETYPE_TET10, (1, 1, 2), [7, 5], 0.0),
     "hex8_mm10": _mm10_case,
+    # b-bar bricks (WARP3D's default l3disop formulation), finite strain
+    # with a stabilization factor, and small displacement (rstgp2)
+    "hex8_mm01_bbar": lambda: _mm01_case(abi.ETYPE_L3DISOP, (2, 2, 2), [5, 3], 0.001, bbar=True, eps_bbar=0.05),
+    "hex8_mm01_small_bbar": lambda: _mm01_case(abi.ETYPE_L3DISOP, (2, 2, 2), [5, 3], 0.001, geonl=False,
+                                               bbar=True),
+    # (one yield stress: with the two of the other cases, the second load
+    # step's Newton iterates grow to the element size and do not converge
+    # without a line search, although the tangent matches central
+    # differences of the internal forces to 1e-9)
+    "tet10_mm01_small": lambda: _mm01_case(abi.ETYPE_TET10, (1, 1, 2), [7, 5], 0.0, dyld=0.0, geonl=False),
 }
 
 
 # ---- model spec <-> npz ------------------------------------------------------
 def model_spec(model: Model) -> dict:
     d = {"coords": model.coords, "nparts": np.int64(len(model.parts)), "geonl": np.int64(model.geonl),
-         "qbar": np.int64(model.qbar)}
+         "qbar": np.int64(model.qbar), "bbar": np.int64(model.bbar), "eps_bbar": np.float64(model.eps_bbar)}
     for k, p in enumerate(model.parts):
         d[f"part{k}_etype"] = np.int64(p.etype)
         d[f"part{k}_incid"] = np.asarray(p.incid, dtype=np.int64)
@@ -91,7 +103,10 @@ def model_from(z) -> Model:
     for p in parts:
         p.materials = mats[off:off + len(p.spans)]
         off += len(p.spans)
-    return Model(z["coords"], parts=parts, geonl=bool(z["geonl"]), qbar=bool(z["qbar"]))
+    bbar = bool(z["bbar"]) if "bbar" in z else False
+    eps_bbar = float(z["eps_bbar"]) if "eps_bbar" in z else 0.0
+    return Model(z["coords"], parts=parts, geonl=bool(z["geonl"]), qbar=bool(z["qbar"]), bbar=bbar,
+                 eps_bbar=eps_bbar)
 
 
 def state_from(z, model: Model, prefix: str) -> HostState:

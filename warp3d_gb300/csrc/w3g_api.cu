@@ -130,6 +130,7 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
   a.estiff = c->precision != W3G_TANGENT_FP64 ? (void*)c->s.estiff32 : (void*)c->s.estiff;
   a.qbar = c->m.qbar;
   a.beta_fact = c->m.beta_fact;
+  a.bbar_beta = c->m.bbar_beta;
   return a;
 }
 
@@ -183,6 +184,7 @@ int enqueue_recover(w3g_context* c, const double* d_c, const double* d_u, const 
   a.geo_dirty = c->s.geo_dirty;
   a.params = c->s.params;
   a.beta_fact = c->m.beta_fact;
+  a.bbar_beta = c->m.bbar_beta;
   a.xtal = c->m.xtal;
   a.xtype = c->m.xtype;
   a.mm10_scr = c->s.mm10_scr;
@@ -360,6 +362,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   m.nelblk = md->nelblk; m.noelem = md->noelem; m.nodof = md->nodof; m.ncoord = md->ncoord;
   m.qbar = md->qbar_flag ? 1 : 0;
   m.beta_fact = md->beta_fact;
+  m.bbar_beta = (1.0 - md->eps_bbar) * (1.0 / 3.0);   // bmod.f: beta = (one - eps_stab)*third
 
   // ---- block table (elblks, iprops, lprops) ----
   std::vector<BlockDesc>& B = c->blocks;
@@ -387,7 +390,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     d.etype = ip[0]; d.nnode = ip[1]; d.ngp = ip[5]; d.mat = ip[24];
     d.totdof = d.nnode * ip[3];
     d.utsz = (d.totdof * d.totdof - d.totdof) / 2 + d.totdof;
-    d.geonl = lp[17] != 0; d.bbar = lp[18] != 0;
+    // b-bar is an option of the 8-node brick (elprp.f); other types ignore lprops(19)
+    d.geonl = lp[17] != 0; d.bbar = lp[18] != 0 && d.etype == W3G_ETYPE_L3DISOP;
     // (etype, nnode, ngp, integration order) with a GPU path
     const bool ok_type = ip[3] == 3 &&
                          ((d.etype == W3G_ETYPE_L3DISOP && d.nnode == 8 && d.ngp == 8 && ip[4] == 1) ||
@@ -424,10 +428,12 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
         }
       }
     }
-    if (!d.geonl || d.bbar) {
+    if (d.mat == W3G_MAT_CRYSTAL && (!d.geonl || d.bbar)) {
+      // WARP3D gives mm10 bricks with b-bar the F-bar kinematics (gtmat1_make_fbar)
       delete c;
-      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": small-strain or b-bar not supported");
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": mm10 needs geonl without b-bar");
     }
+    if (d.bbar) m.has_bbar = 1;
     d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf; d.geo_off = geo;
     d.hist = d.mat == W3G_MAT_CRYSTAL ? kHistMM10 : kHistMM01;
     d.hist_off = hist;
@@ -1009,7 +1015,7 @@ int w3g_autotune(w3g_context* c, int step, int iter, int extrapolated_du, const 
   // candidates: per-type launches, or the persistent kernels with each
   // CTAs-per-SM count up to occupancy, queue grain 1 or 4, either order
   const int occ_r = persistent_recover_occupancy();
-  const int occ_t = persistent_tangent_occupancy(c->precision != W3G_TANGENT_FP64);
+  const int occ_t = persistent_tangent_occupancy(c->m, c->precision != W3G_TANGENT_FP64);
   double total_best = 1e300;
   Schedule chosen = c->sched;
   int status = 0;

@@ -151,6 +151,8 @@ struct DeviceModel {
   int nelblk = 0, noelem = 0, nodof = 0, ncoord = 0;
   int qbar = 1;
   double beta_fact = 1.0;
+  double bbar_beta = 1.0 / 3.0;    // bmod's beta = (1 - eps_bbar) / 3
+  int has_bbar = 0;                // any 8-node brick block with b-bar
   int nsm = 0;
   int nchunks = 0;                          // recovery work items (partials)
   int nrchunks = 0;                         // of these, items of the three element types
@@ -244,6 +246,7 @@ struct TangentArgs {
   void* estiff;          // double* or float*
   int qbar;
   double beta_fact;
+  double bbar_beta;      // (1 - eps_bbar) / 3
 };
 
 struct RecoverArgs {
@@ -273,6 +276,7 @@ struct RecoverArgs {
   int* geo_dirty;
   const IterParams* params;
   double beta_fact;
+  double bbar_beta;          // (1 - eps_bbar) / 3
   // mm10 blocks
   const CrystalElem* xtal;   // noelem entries (mm10 elements)
   const CrystalType* xtype;
@@ -321,7 +325,7 @@ inline cudaError_t init_kernels() {
   return e == cudaSuccess ? init_mm10_kernels() : e;
 }
 // resident CTAs per SM of the persistent kernels
-int persistent_tangent_occupancy(bool fp32);
+int persistent_tangent_occupancy(const DeviceModel& m, bool fp32);
 int persistent_recover_occupancy();
 // writes the iteration scalars and resets the step-cut status
 cudaError_t launch_begin_recover(IterParams* params, unsigned long long* status, int step, int iter, int nonlinear,

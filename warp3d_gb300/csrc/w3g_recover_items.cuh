@@ -129,33 +129,44 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
     }
 
     // ---- gtmat1: tcomp1/fcomp1 for u_{n+1} and u_{n+1/2} (rstgp1_a),
-    // reference-order arithmetic up to the polar decompositions
-    double th1[9], thh[9];
+    // reference-order arithmetic up to the polar decompositions; small-
+    // displacement blocks (rstgp2) have no deformation gradient
+    double F1[9], Fh[9], R1[9], Rh[9];
+    double dfn1 = 1.0, dfh = 1.0;
+    if (bd.geonl) {
+      double th1[9], thh[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) { th1[k] = 0.0; thh[k] = 0.0; }
+      for (int k = 0; k < 9; ++k) { th1[k] = 0.0; thh[k] = 0.0; }
 #pragma unroll
-    for (int n = 0; n < NN; ++n) {
-      const double tx = tg0[3 * n], ty = tg0[3 * n + 1], tz = tg0[3 * n + 2];
-      const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]),
-                   u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
-      const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
-                   uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
-      th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
-      th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
-      th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
-      thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
-      thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
-      thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+      for (int n = 0; n < NN; ++n) {
+        const double tx = tg0[3 * n], ty = tg0[3 * n + 1], tz = tg0[3 * n + 2];
+        const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]),
+                     u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
+        const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
+                     uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
+        th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
+        th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
+        th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
+        thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
+        thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
+        thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+      }
+      F1[0] = th1[0] + 1.0; F1[1] = th1[1]; F1[2] = th1[2]; F1[3] = th1[3]; F1[4] = th1[4] + 1.0;
+      F1[5] = th1[5]; F1[6] = th1[6]; F1[7] = th1[7]; F1[8] = th1[8] + 1.0;
+      Fh[0] = thh[0] + 1.0; Fh[1] = thh[1]; Fh[2] = thh[2]; Fh[3] = thh[3]; Fh[4] = thh[4] + 1.0;
+      Fh[5] = thh[5]; Fh[6] = thh[6]; Fh[7] = thh[7]; Fh[8] = thh[8] + 1.0;
+      dfn1 = det_ref(F1);
+      dfh = det_ref(Fh);
+      if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
+      else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
+      polar_rotation_ref(F1, R1);
+      polar_rotation_ref(Fh, Rh);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) F1[k] = Fh[k] = R1[k] = Rh[k] = (k % 4 == 0) ? 1.0 : 0.0;
     }
-    const double F1[9] = {th1[0] + 1.0, th1[1], th1[2], th1[3], th1[4] + 1.0, th1[5], th1[6], th1[7], th1[8] + 1.0};
-    const double Fh[9] = {thh[0] + 1.0, thh[1], thh[2], thh[3], thh[4] + 1.0, thh[5], thh[6], thh[7], thh[8] + 1.0};
-    const double dfn1 = det_ref(F1);
-    const double dfh = det_ref(Fh);
-    if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
-    else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
-    double R1[9], Rh[9];
-    polar_rotation_ref(F1, R1);
-    polar_rotation_ref(Fh, Rh);
+    // the element's 8 Gauss-point lanes (b-bar sums over them)
+    const unsigned gmask = 0xFFu << (tid & 24);
 
     // ---- rate of deformation over the step: d = sym(dDu/dx_mid) with
     // x_mid = X + u + du/2 (gtlsn1 with [B] at the mid-step shape,
@@ -187,9 +198,30 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
         for (int k = 0; k < 9; ++k) L[k] = dth[k];
       }
     }
-    const double ddt[6] = {L[0], L[4], L[8], L[3] + L[1], L[7] + L[5], L[6] + L[2]};
+    double ddt[6] = {L[0], L[4], L[8], L[3] + L[1], L[7] + L[5], L[6] + L[2]};
+    if (bd.bbar) {
+      // b-bar (rknstr vol_terms/vol_avg at the mid-step shape, gtlsn1 with
+      // bmod): column (n, k) of B-bar adds beta (v_nk - g_nk) to the three
+      // normal rows, so each normal component of d gains beta (tr_bar -
+      // tr L), tr_bar = sum_gp det[J_mid] tr L / sum_gp det[J_mid] being the
+      // element's mean dilatation rate
+      const double jm = update_coords ? dfh * dj0 : dj0;
+      const double trl = L[0] + L[4] + L[8];
+      double s1 = jm * trl, s0 = jm;
+#pragma unroll
+      for (int off = 1; off < NG; off <<= 1) {
+        s1 += __shfl_xor_sync(gmask, s1, off);
+        s0 += __shfl_xor_sync(gmask, s0, off);
+      }
+      const double cb = a.bbar_beta * (s1 * (1.0 / s0) - trl);
+      ddt[0] += cb; ddt[1] += cb; ddt[2] += cb;
+    }
     double uddt[6];
-    rotate_to_unrotated(Rh, ddt, uddt);   // qmply1 with getrm1 opt 1 at n+1/2
+    if (bd.geonl) rotate_to_unrotated(Rh, ddt, uddt);   // qmply1 with getrm1 opt 1 at n+1/2
+    else {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) uddt[k] = ddt[k];    // rstgp2: the increment as it is
+    }
 
     // ---- state at n ----
     double cgn[9], hist[11], cgn1[9], hist1[11], cep21[21], eps1[6];
@@ -222,9 +254,9 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
     double* cp = a.cep + bd.cep_off + ((long long)g * bd.span + i) * 21;
 #pragma unroll
     for (int k = 0; k < 21; ++k) cp[k] = cep21[k];
-    // rstgp1_b: energy and plastic work (large-strain branch)
+    // rstgp1_b: energy and plastic work (large- or small-strain branch)
     if (p.iter != 0) {
-      const double factor = dfn1 * dj0 * a.beta_fact * w;
+      const double factor = bd.geonl ? dfn1 * dj0 * a.beta_fact * w : dj0 * a.beta_fact * w;
       en = cgn1[6] * factor;
       pw = cgn1[7] * factor;
     }
@@ -252,13 +284,32 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
 #pragma unroll
       for (int k = 0; k < 6; ++k) S[k] = cgn1[k];
     }
+    // b-bar (rknifv vol_terms/vol_avg at n+1, gpifv1 with bmod): B-bar^T
+    // {T} = B^T {T} + beta tr(T) (v - g), i.e. each point's pressure part
+    // beta tr(T) is replaced by the element's mean, added back as
+    // cb det[J_{n+1}] on the diagonal, cb = beta sum_gp w det[J] tr(T) /
+    // sum_gp det[J]
+    const double j1 = update_coords ? dfn1 * dj0 : dj0;
+    double pdiag = 0.0;
+    if (bd.bbar) {
+      const double trs = S[0] + S[1] + S[2];
+      double s1 = w * j1 * trs, s0 = j1;
+#pragma unroll
+      for (int off = 1; off < NG; off <<= 1) {
+        s1 += __shfl_xor_sync(gmask, s1, off);
+        s0 += __shfl_xor_sync(gmask, s0, off);
+      }
+      const double ptr = a.bbar_beta * trs;
+      S[0] -= ptr; S[1] -= ptr; S[2] -= ptr;
+      pdiag = a.bbar_beta * (s1 * (1.0 / s0)) * j1;
+    }
     double P[9];
     if (update_coords) {
       double Fi[9];
       inverse3(F1, dfn1, Fi);
-      const double wdj = w * (dfn1 * dj0);
-      const double T[9] = {S[0] * wdj, S[3] * wdj, S[5] * wdj, S[3] * wdj, S[1] * wdj,
-                           S[4] * wdj, S[5] * wdj, S[4] * wdj, S[2] * wdj};
+      const double wdj = w * j1;
+      const double T[9] = {S[0] * wdj + pdiag, S[3] * wdj, S[5] * wdj, S[3] * wdj, S[1] * wdj + pdiag,
+                           S[4] * wdj, S[5] * wdj, S[4] * wdj, S[2] * wdj + pdiag};
       // P_rc = sum_k T_rk Fi_ck
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -266,10 +317,10 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
         for (int r = 0; r < 3; ++r) P[r + 3 * c] = T[r] * Fi[c] + T[r + 3] * Fi[c + 3] + T[r + 6] * Fi[c + 6];
       vol = wdj;
     } else {
-      const double wdj = w * dj0;
-      P[0] = S[0] * wdj; P[1] = S[3] * wdj; P[2] = S[5] * wdj;
-      P[3] = S[3] * wdj; P[4] = S[1] * wdj; P[5] = S[4] * wdj;
-      P[6] = S[5] * wdj; P[7] = S[4] * wdj; P[8] = S[2] * wdj;
+      const double wdj = w * j1;
+      P[0] = S[0] * wdj + pdiag; P[1] = S[3] * wdj; P[2] = S[5] * wdj;
+      P[3] = S[3] * wdj; P[4] = S[1] * wdj + pdiag; P[5] = S[4] * wdj;
+      P[6] = S[5] * wdj; P[7] = S[4] * wdj; P[8] = S[2] * wdj + pdiag;
       vol = wdj;
     }
     double* fe = &sfe[ge][g][0];
@@ -390,32 +441,41 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
     const double* tg0 = geo;   // dN/dX per node (own writes, or the cache)
     const double dj0 = geo[3 * NN];
 
-    // tcomp1/fcomp1 at n+1 and n+1/2, reference order
-    double th1[9], thh[9];
+    // tcomp1/fcomp1 at n+1 and n+1/2, reference order (geonl blocks;
+    // rstgp2 has no deformation gradient)
+    double F1[9], Fh[9], R1[9], Rh[9];
+    double dfn1 = 1.0, dfh = 1.0;
+    if (bd.geonl) {
+      double th1[9], thh[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) { th1[k] = 0.0; thh[k] = 0.0; }
-    for (int n = 0; n < NN; ++n) {
-      const double tx = tg0[3 * n], ty = tg0[3 * n + 1], tz = tg0[3 * n + 2];
-      const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]),
-                   u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
-      const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
-                   uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
-      th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
-      th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
-      th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
-      thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
-      thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
-      thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+      for (int k = 0; k < 9; ++k) { th1[k] = 0.0; thh[k] = 0.0; }
+      for (int n = 0; n < NN; ++n) {
+        const double tx = tg0[3 * n], ty = tg0[3 * n + 1], tz = tg0[3 * n + 2];
+        const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]),
+                     u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
+        const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
+                     uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
+        th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
+        th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
+        th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
+        thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
+        thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
+        thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+      }
+      F1[0] = th1[0] + 1.0; F1[1] = th1[1]; F1[2] = th1[2]; F1[3] = th1[3]; F1[4] = th1[4] + 1.0;
+      F1[5] = th1[5]; F1[6] = th1[6]; F1[7] = th1[7]; F1[8] = th1[8] + 1.0;
+      Fh[0] = thh[0] + 1.0; Fh[1] = thh[1]; Fh[2] = thh[2]; Fh[3] = thh[3]; Fh[4] = thh[4] + 1.0;
+      Fh[5] = thh[5]; Fh[6] = thh[6]; Fh[7] = thh[7]; Fh[8] = thh[8] + 1.0;
+      dfn1 = det_ref(F1);
+      dfh = det_ref(Fh);
+      if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
+      else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
+      polar_rotation_ref(F1, R1);
+      polar_rotation_ref(Fh, Rh);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) F1[k] = Fh[k] = R1[k] = Rh[k] = (k % 4 == 0) ? 1.0 : 0.0;
     }
-    const double F1[9] = {th1[0] + 1.0, th1[1], th1[2], th1[3], th1[4] + 1.0, th1[5], th1[6], th1[7], th1[8] + 1.0};
-    const double Fh[9] = {thh[0] + 1.0, thh[1], thh[2], thh[3], thh[4] + 1.0, thh[5], thh[6], thh[7], thh[8] + 1.0};
-    const double dfn1 = det_ref(F1);
-    const double dfh = det_ref(Fh);
-    if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
-    else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
-    double R1[9], Rh[9];
-    polar_rotation_ref(F1, R1);
-    polar_rotation_ref(Fh, Rh);
 
     // d = sym(dDu/dX Fh^-1)
     double L[9], dth[9];
@@ -443,7 +503,11 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
     }
     const double ddt[6] = {L[0], L[4], L[8], L[3] + L[1], L[7] + L[5], L[6] + L[2]};
     double uddt[6];
-    rotate_to_unrotated(Rh, ddt, uddt);
+    if (bd.geonl) rotate_to_unrotated(Rh, ddt, uddt);
+    else {
+#pragma unroll
+      for (int k = 0; k < 6; ++k) uddt[k] = ddt[k];
+    }
 
     double cgn[9], hist[11], cgn1[9], hist1[11], cep21[21], eps1[6];
 #pragma unroll
@@ -472,7 +536,7 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
 #pragma unroll
     for (int k = 0; k < 21; ++k) cp[k] = cep21[k];
     if (p.iter != 0) {   // rstgp1_b: weight without the tetrahedral 1/6
-      const double factor = dfn1 * dj0 * a.beta_fact * w;
+      const double factor = bd.geonl ? dfn1 * dj0 * a.beta_fact * w : dj0 * a.beta_fact * w;
       en = cgn1[6] * factor;
       pw = cgn1[7] * factor;
     }

@@ -16,26 +16,33 @@ namespace w3g {
 
 namespace {
 
+// shared memory of the brick items; models with b-bar blocks launch with
+// the larger b-bar layout (more per element), the others keep the smaller
+// one and its occupancy
 template <class T>
-constexpr size_t hex8_smem() {
-  return sizeof(T) == 8 ? sizeof(TangentSmemHex8<double>) : sizeof(TangentSmemHex8F32);
+constexpr size_t hex8_smem(bool bbar) {
+  return sizeof(T) == 8 ? (bbar ? sizeof(TangentSmemHex8<double, true>) : sizeof(TangentSmemHex8<double>))
+                        : (bbar ? sizeof(TangentSmemHex8F32<true>) : sizeof(TangentSmemHex8F32<>));
 }
 
 template <class T>
-constexpr size_t tangent_smem() {
-  return std::max({hex8_smem<T>(), sizeof(TangentSmemGen<Hex20, 1, T>), sizeof(TangentSmemGen<Tet10, 4, T>)});
+constexpr size_t tangent_smem(bool bbar) {
+  return std::max({hex8_smem<T>(bbar), sizeof(TangentSmemGen<Hex20, 1, T>), sizeof(TangentSmemGen<Tet10, 4, T>)});
 }
 
-// the FP32 coordinates are relative to the element's first node
+// the FP32 coordinates are relative to the element's first node; b-bar
+// blocks take the b-bar instantiation of the item
 template <class T>
 __device__ __forceinline__ void hex8_item(const TangentArgs& a, int cidx, unsigned char* smem);
 template <>
 __device__ __forceinline__ void hex8_item<double>(const TangentArgs& a, int cidx, unsigned char* smem) {
-  tangent_item_hex8<double, double, false>(a, cidx, smem);
+  if (a.blocks[a.chunks[cidx].blk].bbar) tangent_item_hex8<double, double, false, true>(a, cidx, smem);
+  else tangent_item_hex8<double, double, false>(a, cidx, smem);
 }
 template <>
 __device__ __forceinline__ void hex8_item<float>(const TangentArgs& a, int cidx, unsigned char* smem) {
-  tangent_item_hex8_f32(a, cidx, smem);
+  if (a.blocks[a.chunks[cidx].blk].bbar) tangent_item_hex8_f32<true>(a, cidx, smem);
+  else tangent_item_hex8_f32<false>(a, cidx, smem);
 }
 
 // resident one-warp CTAs per SM for the FP32 brick tangent (registers:
@@ -88,44 +95,48 @@ cudaError_t prepare(K kern, size_t smem) {
   return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-int g_occ[2] = {0, 0};   // persistent CTAs per SM: FP64, FP32
+int g_occ[2][2] = {{0, 0}, {0, 0}};   // persistent CTAs per SM: [FP32][b-bar layout]
 
 template <class T>
 cudaError_t init() {
   cudaError_t e;
-  if ((e = prepare(k_tangent_hex8<T>, hex8_smem<T>())) != cudaSuccess) return e;
+  if ((e = prepare(k_tangent_hex8<T>, hex8_smem<T>(true))) != cudaSuccess) return e;
   if ((e = prepare(k_tangent_type<Hex20, 32, 1, T>, sizeof(TangentSmemGen<Hex20, 1, T>))) != cudaSuccess) return e;
   if ((e = prepare(k_tangent_type<Tet10, 8, 4, T>, sizeof(TangentSmemGen<Tet10, 4, T>))) != cudaSuccess) return e;
-  if ((e = prepare(k_tangent_persistent<T>, tangent_smem<T>())) != cudaSuccess) return e;
-  int n = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tangent_persistent<T>, kTangentThreads, tangent_smem<T>());
-  if (e != cudaSuccess) return e;
-  g_occ[sizeof(T) == 4] = std::max(1, n);
+  if ((e = prepare(k_tangent_persistent<T>, tangent_smem<T>(true))) != cudaSuccess) return e;
+  for (int bb = 0; bb < 2; ++bb) {
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tangent_persistent<T>, kTangentThreads,
+                                                      tangent_smem<T>(bb != 0));
+    if (e != cudaSuccess) return e;
+    g_occ[sizeof(T) == 4][bb] = std::max(1, n);
+  }
   return cudaSuccess;
 }
 
 template <class T>
-int occupancy() { return std::max(1, g_occ[sizeof(T) == 4]); }
+int occupancy(bool bbar) { return std::max(1, g_occ[sizeof(T) == 4][bbar ? 1 : 0]); }
 
 template <class T>
 cudaError_t launch(const DeviceModel& m, const TangentArgs& a, const Schedule& sc, int* counter, cudaStream_t s,
                    bool skip_hex8) {
   cudaError_t e = cudaSuccess;
+  const bool bb = m.has_bbar != 0;
   if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) {
-    const int occ = occupancy<T>();
+    const int occ = occupancy<T>(bb);
     const int per_sm = sc.tangent_ctas_per_sm > 0 ? std::min(sc.tangent_ctas_per_sm, occ) : occ;
     const int grain = std::max(1, sc.tangent_grain);
     const int need = (m.ntchunks + grain - 1) / grain;
     const int grid = std::max(1, std::min(m.nsm * per_sm, need));
     WorkQueue q{m.torder[sc.order == W3G_ORDER_HEAVY_FIRST ? 1 : 0], m.ntchunks, grain, counter};
     if ((e = cudaMemsetAsync(counter, 0, sizeof(int), s)) != cudaSuccess) return e;
-    k_tangent_persistent<T><<<grid, kTangentThreads, tangent_smem<T>(), s>>>(a, q);
+    k_tangent_persistent<T><<<grid, kTangentThreads, tangent_smem<T>(bb), s>>>(a, q);
     return cudaGetLastError();
   }
   if (m.ttype_chunks[0] > 0 && !skip_hex8) {
     TangentArgs h = a;
     h.chunk0 = m.ttype_chunk0[0];
-    k_tangent_hex8<T><<<m.ttype_chunks[0], kTangentThreads, hex8_smem<T>(), s>>>(h);
+    k_tangent_hex8<T><<<m.ttype_chunks[0], kTangentThreads, hex8_smem<T>(bb), s>>>(h);
   }
   if (m.ttype_chunks[1] > 0) {
     TangentArgs h = a;
@@ -147,17 +158,20 @@ cudaError_t init_tangent_kernels() {
   return e == cudaSuccess ? init<float>() : e;
 }
 
-int persistent_tangent_occupancy(bool fp32) { return fp32 ? occupancy<float>() : occupancy<double>(); }
+int persistent_tangent_occupancy(const DeviceModel& m, bool fp32) {
+  return fp32 ? occupancy<float>(m.has_bbar != 0) : occupancy<double>(m.has_bbar != 0);
+}
 
 namespace {
 
 template <class T>
-cudaError_t launch_ranges(const TangentArgs& a, const int* first, const int* count, cudaStream_t s, int* launches) {
+cudaError_t launch_ranges(const DeviceModel& m, const TangentArgs& a, const int* first, const int* count,
+                          cudaStream_t s, int* launches) {
   int n = 0;
   if (count[0] > 0) {
     TangentArgs h = a;
     h.chunk0 = first[0];
-    k_tangent_hex8<T><<<count[0], kTangentThreads, hex8_smem<T>(), s>>>(h);
+    k_tangent_hex8<T><<<count[0], kTangentThreads, hex8_smem<T>(m.has_bbar != 0), s>>>(h);
     ++n;
   }
   if (count[1] > 0) {
@@ -180,8 +194,8 @@ cudaError_t launch_ranges(const TangentArgs& a, const int* first, const int* cou
 
 cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bool fp32, const int* first,
                                   const int* count, cudaStream_t s, int* launches) {
-  (void)m;
-  return fp32 ? launch_ranges<float>(a, first, count, s, launches) : launch_ranges<double>(a, first, count, s, launches);
+  return fp32 ? launch_ranges<float>(m, a, first, count, s, launches)
+              : launch_ranges<double>(m, a, first, count, s, launches);
 }
 
 int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8) {

@@ -74,18 +74,70 @@ constexpr int kPerElem = 3 * NN              // coordinates
                          + NN * 18 + NN * 3;           // D*B per node, {T}g per node
 constexpr int kDnSize = NG * 3 * NN + NG;
 
+// b-bar blocks add per element the volume-averaged gradients v (24), and
+// per node of the current Gauss point h = beta (v - g) (24) and the sums
+// over the normal-strain rows of [D*] B-bar (24)
+constexpr int kBbarExtra = 3 * 3 * NN;
+static_assert(kHalf * (3 * NN + 21 + 6) >= NG * (3 * NN + 1), "b-bar staging must fit");
+
 static_assert(kHalf * (3 * NN + 21 + 6) + NN * 18 + NN * 3 >= UT, "Ke staging must fit");
 
-template <class T>
+template <class T, bool kBbar = false>
 struct TangentSmemHex8 {
   unsigned char pa[40], pb[40];     // node pairs of the 3x3 blocks (36 used)
   T dn[kDnSize];
-  T elem[kChunk][kPerElem];
+  T elem[kChunk][kPerElem + (kBbar ? kBbarExtra : 0)];
 };
 
-template <class T, class KOut, bool kRelative>
+// b-bar, phase 0 (rktstf's vol_terms + vol_avg, src/vol_terms.f:14-108,
+// src/vol_avg.f:13-68): lane t evaluates Gauss points t and t + 4 and
+// stages det[J] dN/dx and det[J]; then lane t sums nodes 2t, 2t + 1 over
+// the eight points in Gauss-point order and scales by 1 / volume. stage
+// holds NG x (3 NN + 1) values; v receives the 3 NN averaged gradients.
+template <class T>
+__device__ __forceinline__ void hex8_mean_gradients(const T* sdn, const T* sx, const T* sy, const T* sz, int t,
+                                                    bool active, T* stage, T* v) {
+  if (active) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int gp = t + 4 * k;
+      const T* dnx = sdn + (gp * 3 + 0) * NN;
+      const T* dne = sdn + (gp * 3 + 1) * NN;
+      const T* dnz = sdn + (gp * 3 + 2) * NN;
+      T gama[9], dj;
+      jacobian_inverse<NN, T>(dnx, dne, dnz, sx, sy, sz, gama, dj);
+      T* st = stage + gp * (3 * NN + 1);
+#pragma unroll
+      for (int n = 0; n < NN; ++n) {
+        T gx, gy, gz;
+        shape_gradient<T>(gama, dnx[n], dne[n], dnz[n], gx, gy, gz);
+        st[3 * n] = gx * dj; st[3 * n + 1] = gy * dj; st[3 * n + 2] = gz * dj;
+      }
+      st[3 * NN] = dj;
+    }
+  }
+  __syncwarp();
+  if (active) {
+    T vol = T(0);
+#pragma unroll
+    for (int gp = 0; gp < NG; ++gp) vol += stage[gp * (3 * NN + 1) + 3 * NN];
+    const T voli = T(1) / vol;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const int j = 6 * t + k;   // nodes 2t, 2t + 1
+      T s = T(0);
+#pragma unroll
+      for (int gp = 0; gp < NG; ++gp) s += stage[gp * (3 * NN + 1) + j];
+      v[j] = s * voli;
+    }
+  }
+  __syncwarp();
+}
+
+template <class T, class KOut, bool kRelative, bool kBbar = false>
 __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, unsigned char* smem) {
-  TangentSmemHex8<T>& S = *reinterpret_cast<TangentSmemHex8<T>*>(smem);
+  TangentSmemHex8<T, kBbar>& S = *reinterpret_cast<TangentSmemHex8<T, kBbar>*>(smem);
+  constexpr int kStride = kPerElem + (kBbar ? kBbarExtra : 0);
   T* sdn = S.dn;
   T* selem = &S.elem[0][0];
   unsigned char* pa = S.pa;
@@ -117,7 +169,7 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
       }
   }
 
-  T* E = selem + ge * kPerElem;
+  T* E = selem + ge * kStride;
   T* sx = E;
   T* sy = E + NN;
   T* sz = E + 2 * NN;
@@ -126,6 +178,9 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
   T* sT = sD + kHalf * 21;                 // [slot][6]
   T* sDB = sT + kHalf * 6;                 // [a][6][3]
   T* sTg = sDB + NN * 18;                  // [a][3]
+  T* sV = E + kPerElem;                    // b-bar: [a][3] averaged gradients
+  T* sH = sV + 3 * NN;                     //        [a][3] beta (v - g) at the GP
+  T* sS = sH + 3 * NN;                     //        [a][3] normal-row sums of D* B-bar
 
   // ---- gather (dptstf) ----
   if (active) {
@@ -159,6 +214,8 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
     }
   }
   __syncwarp();
+  if (kBbar) hex8_mean_gradients<T>(sdn, sx, sy, sz, t, active, sg, sV);
+  const T beta = (T)a.bbar_beta;
 
   T acc[9][9];
 #pragma unroll
@@ -257,16 +314,38 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
           const int n = 2 * t + h;
           const T gx = g[3 * n], gy = g[3 * n + 1], gz = g[3 * n + 2];
           T* db = sDB + n * 18;   // db[m*3 + k]: row m of D*B_n, column k
+          if (kBbar) {
+            // bmod (src/bmod.f:16-205): column (n, k) of B-bar is column
+            // (n, k) of B plus h_k = beta (v_k - g_k) in the three normal
+            // rows, so D* B-bar_n = D* B_n + (D* m) h^T, m = (1,1,1,0,0,0)
+            const T hx = beta * (sV[3 * n] - gx), hy = beta * (sV[3 * n + 1] - gy),
+                    hz = beta * (sV[3 * n + 2] - gz);
+            T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
-          for (int m = 0; m < 6; ++m) {
-            db[m * 3 + 0] = D[low(m, 0)] * gx + D[low(m, 3)] * gy + D[low(m, 5)] * gz;
-            db[m * 3 + 1] = D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz;
-            db[m * 3 + 2] = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
+            for (int m = 0; m < 6; ++m) {
+              const T dm = D[low(m, 0)] + D[low(m, 1)] + D[low(m, 2)];
+              const T v0 = fma(dm, hx, D[low(m, 0)] * gx + D[low(m, 3)] * gy + D[low(m, 5)] * gz);
+              const T v1 = fma(dm, hy, D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz);
+              const T v2 = fma(dm, hz, D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx);
+              db[m * 3 + 0] = v0; db[m * 3 + 1] = v1; db[m * 3 + 2] = v2;
+              if (m < 3) { s0 += v0; s1 += v1; s2 += v2; }
+            }
+            sH[3 * n] = hx; sH[3 * n + 1] = hy; sH[3 * n + 2] = hz;
+            sS[3 * n] = s0; sS[3 * n + 1] = s1; sS[3 * n + 2] = s2;
+          } else {
+#pragma unroll
+            for (int m = 0; m < 6; ++m) {
+              db[m * 3 + 0] = D[low(m, 0)] * gx + D[low(m, 3)] * gy + D[low(m, 5)] * gz;
+              db[m * 3 + 1] = D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz;
+              db[m * 3 + 2] = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
+            }
           }
+          // kgstiff: with b-bar the averaged gradients (src/kg1.f:46-54)
+          const T kx = kBbar ? sV[3 * n] : gx, ky = kBbar ? sV[3 * n + 1] : gy, kz = kBbar ? sV[3 * n + 2] : gz;
           T* tg = sTg + n * 3;
-          tg[0] = Tw[0] * gx + Tw[3] * gy + Tw[5] * gz;
-          tg[1] = Tw[3] * gx + Tw[1] * gy + Tw[4] * gz;
-          tg[2] = Tw[5] * gx + Tw[4] * gy + Tw[2] * gz;
+          tg[0] = Tw[0] * kx + Tw[3] * ky + Tw[5] * kz;
+          tg[1] = Tw[3] * kx + Tw[1] * ky + Tw[4] * kz;
+          tg[2] = Tw[5] * kx + Tw[4] * ky + Tw[2] * kz;
         }
       }
       __syncwarp();
@@ -290,9 +369,19 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
             if (p >= 2 || kk >= 2)
               acc[p][2 * 3 + kk] = fma(az, db[2 * 3 + kk], fma(ay, db[4 * 3 + kk], fma(ax, db[5 * 3 + kk], acc[p][2 * 3 + kk])));
           }
+          if (kBbar) {   // the normal rows of B-bar_a: + h_a (x) sum_m (D* B-bar_b)_m
+            const T* ha = sH + 3 * na;
+            const T* sb = sS + 3 * nb;
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk)
+                if (p >= 2 || kk >= ii) acc[p][ii * 3 + kk] = fma(ha[ii], sb[kk], acc[p][ii * 3 + kk]);
+          }
           if (bd.geonl) {   // kgstiff (src/kg1.f:16-110)
             const T* tg = sTg + nb * 3;
-            const T gtg = ax * tg[0] + ay * tg[1] + az * tg[2];
+            const T gtg = kBbar ? sV[3 * na] * tg[0] + sV[3 * na + 1] * tg[1] + sV[3 * na + 2] * tg[2]
+                                : ax * tg[0] + ay * tg[1] + az * tg[2];
             acc[p][0] += gtg; acc[p][4] += gtg; acc[p][8] += gtg;
           }
         }
@@ -325,7 +414,7 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
   // elements i0..i0+n-1 are contiguous: out[estiff_off + (i0 + e)*UT + pos]
   const long long obase = bd.estiff_off + (long long)ch.i0 * UT;
   for (int e = 0; e < ch.n; ++e) {
-    const T* src = selem + e * kPerElem + 3 * NN;
+    const T* src = selem + e * kStride + 3 * NN;
     for (int k = lane; k < UT; k += 32) out[obase + (long long)e * UT + k] = (KOut)src[k];
   }
 }
@@ -343,13 +432,15 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
 // ---------------------------------------------------------------------
 constexpr int kPerElem32 = 3 * NN + kHalf * (3 * NN + 21 + 6) > UT ? 3 * NN + kHalf * (3 * NN + 21 + 6) : UT + 3 * NN;
 
+template <bool kBbar = false>
 struct TangentSmemHex8F32 {
   float dn[kDnSize];
-  float elem[kChunk][kPerElem32];
+  float elem[kChunk][kPerElem32 + (kBbar ? 3 * NN : 0)];   // b-bar: averaged gradients
 };
 
-static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cidx, unsigned char* smem) {
-  TangentSmemHex8F32& S = *reinterpret_cast<TangentSmemHex8F32*>(smem);
+template <bool kBbar = false>
+__device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cidx, unsigned char* smem) {
+  TangentSmemHex8F32<kBbar>& S = *reinterpret_cast<TangentSmemHex8F32<kBbar>*>(smem);
   float* sdn = S.dn;
   auto& selem = S.elem;
 
@@ -369,6 +460,7 @@ static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, 
   float* sg = E + 3 * NN;                  // [slot][a][3]
   float* sD = sg + kHalf * 3 * NN;         // [slot][21]
   float* sT = sD + kHalf * 21;             // [slot][6]
+  float* sV = E + kPerElem32;              // b-bar: [a][3] averaged gradients
 
   // ---- gather: x_{n+1} relative to node 1 ----
   if (active) {
@@ -400,6 +492,8 @@ static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, 
     }
   }
   __syncwarp();
+  if (kBbar) hex8_mean_gradients<float>(sdn, sx, sy, sz, t, active, sg, sV);
+  const float beta = (float)a.bbar_beta;
 
   const int b1 = t, b2 = 7 - t;
   float acc[9][9];
@@ -492,12 +586,13 @@ static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, 
         const float* D = sD + s * 21;
         const float* Tw = sT + s * 6;
         const float* g = sg + s * 3 * NN;
-        float db1[18], db2[18], tg1[3], tg2[3];
+        float db1[18], db2[18], tg1[3], tg2[3], sb1[3], sb2[3];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int n = h == 0 ? b1 : b2;
           float* db = h == 0 ? db1 : db2;
           float* tg = h == 0 ? tg1 : tg2;
+          float* sb = h == 0 ? sb1 : sb2;
           const float gx = g[3 * n], gy = g[3 * n + 1], gz = g[3 * n + 2];
 #pragma unroll
           for (int m = 0; m < 6; ++m) {
@@ -505,9 +600,23 @@ static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, 
             db[m * 3 + 1] = D[low(m, 1)] * gy + D[low(m, 3)] * gx + D[low(m, 4)] * gz;
             db[m * 3 + 2] = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
           }
-          tg[0] = Tw[0] * gx + Tw[3] * gy + Tw[5] * gz;
-          tg[1] = Tw[3] * gx + Tw[1] * gy + Tw[4] * gz;
-          tg[2] = Tw[5] * gx + Tw[4] * gy + Tw[2] * gz;
+          float kx = gx, ky = gy, kz = gz;
+          if (kBbar) {   // D* B-bar_n = D* B_n + (D* m) h^T (bmod)
+            kx = sV[3 * n]; ky = sV[3 * n + 1]; kz = sV[3 * n + 2];
+            const float hx = beta * (kx - gx), hy = beta * (ky - gy), hz = beta * (kz - gz);
+            sb[0] = sb[1] = sb[2] = 0.f;
+#pragma unroll
+            for (int m = 0; m < 6; ++m) {
+              const float dm = D[low(m, 0)] + D[low(m, 1)] + D[low(m, 2)];
+              db[m * 3 + 0] = fmaf(dm, hx, db[m * 3 + 0]);
+              db[m * 3 + 1] = fmaf(dm, hy, db[m * 3 + 1]);
+              db[m * 3 + 2] = fmaf(dm, hz, db[m * 3 + 2]);
+              if (m < 3) { sb[0] += db[m * 3 + 0]; sb[1] += db[m * 3 + 1]; sb[2] += db[m * 3 + 2]; }
+            }
+          }
+          tg[0] = Tw[0] * kx + Tw[3] * ky + Tw[5] * kz;
+          tg[1] = Tw[3] * kx + Tw[1] * ky + Tw[4] * kz;
+          tg[2] = Tw[5] * kx + Tw[4] * ky + Tw[2] * kz;
         }
 #pragma unroll
         for (int p = 0; p < 9; ++p) {
@@ -526,11 +635,21 @@ static __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, 
             acc[p][1 * 3 + kk] = fmaf(ay, d1, fmaf(ax, d3, fmaf(az, d4, acc[p][1 * 3 + kk])));
             acc[p][2 * 3 + kk] = fmaf(az, d2, fmaf(ay, d4, fmaf(ax, d5, acc[p][2 * 3 + kk])));
           }
+          float kx = ax, ky = ay, kz = az;
+          if (kBbar) {   // normal rows of B-bar_a: + h_a (x) sum_m (D* B-bar_b)_m
+            kx = sV[3 * na]; ky = sV[3 * na + 1]; kz = sV[3 * na + 2];
+            const float ha[3] = {beta * (kx - ax), beta * (ky - ay), beta * (kz - az)};
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk)
+                acc[p][ii * 3 + kk] = fmaf(ha[ii], first ? sb1[kk] : sb2[kk], acc[p][ii * 3 + kk]);
+          }
           if (bd.geonl) {
             const float t0 = first ? tg1[0] : tg2[0];
             const float t1 = first ? tg1[1] : tg2[1];
             const float t2 = first ? tg1[2] : tg2[2];
-            const float gtg = ax * t0 + ay * t1 + az * t2;
+            const float gtg = kx * t0 + ky * t1 + kz * t2;
             acc[p][0] += gtg; acc[p][4] += gtg; acc[p][8] += gtg;
           }
         }

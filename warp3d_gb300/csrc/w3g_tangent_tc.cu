@@ -85,6 +85,8 @@ struct TcStatic {
   float D[kTcElems][NG][21];
   float T[kTcElems][NG][6];
   float kg[kTcElems][36];
+  float dj[kTcElems][NG];            // det[J] per Gauss point (b-bar averages)
+  float v[kTcElems][3 * NN];         // b-bar: volume-averaged gradients
   union {
     struct {                         // phase 1
       float C[kTcElems][NG][21];
@@ -263,6 +265,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     for (int n = sub; n < NN; n += kSubs)
       shape_gradient<float>(gama, dnx[n], dne[n], dnz[n], g[3 * n], g[3 * n + 1], g[3 * n + 2]);
     f = w * dj;
+    if (sub == 0) S.dj[pe][pgp] = dj;
     // w det[J] [D], lower triangle row-wise, entries sub, sub + 6, ... (as
     // load_D21: cep_blocks, or for mm10 history1 words 0-35)
     if (bd.mat == W3G_MAT_CRYSTAL) {
@@ -352,6 +355,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     }
   }
   __syncthreads();
+  // b-bar: volume-averaged gradients (vol_terms + vol_avg), one thread per
+  // (element, node, component)
+  if (bd.bbar && tid < kTcElems * 3 * NN) {
+    const int e = tid / (3 * NN), k = tid % (3 * NN);
+    if (e < ch.n) {
+      float sv = 0.f, vol = 0.f;
+      for (int gp = 0; gp < NG; ++gp) {
+        sv += S.g[e][gp][k] * S.dj[e][gp];
+        vol += S.dj[e][gp];
+      }
+      S.v[e][k] = sv * (1.f / vol);
+    }
+  }
+  __syncthreads();
 
   // ---- phase 2: operands (row = 24 e + dof, dof = 8 i + a; k = 6 gp + m).
   // Threads 0-127 write row r of A = B^T, threads 128-255 row r of
@@ -376,6 +393,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
       ix[m][2] = low(m, p2);
     }
     unsigned char* op = isB ? opB : opA;
+    // b-bar (bmod): column (i, a) of B-bar adds h = beta (v_ai - g_ai) to
+    // the three normal rows; [D*] B-bar adds h times the row sums of the
+    // first three columns of [D*]
+    const bool bb = bd.bbar != 0;
+    const float beta = (float)a.bbar_beta;
+    const float va = bb ? S.v[ee][3 * na + di] : 0.f;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       float v[kK / 2];
@@ -384,12 +407,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
         const int gp = (NG / 2) * h + q4;
         const float* g = S.g[ee][gp] + 3 * na;
         const float u0 = g[c0], u1 = g[c1], u2 = g[c2];
+        const float hb = bb ? beta * (va - u0) : 0.f;
         const float* D = S.D[ee][gp];
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
           float val;
-          if (isB) val = D[ix[m][0]] * u0 + D[ix[m][1]] * u1 + D[ix[m][2]] * u2;
-          else val = m == p0 ? u0 : m == p1 ? u1 : m == p2 ? u2 : 0.f;
+          if (isB)
+            val = D[ix[m][0]] * u0 + D[ix[m][1]] * u1 + D[ix[m][2]] * u2 +
+                  hb * (D[low(m, 0)] + D[low(m, 1)] + D[low(m, 2)]);
+          else val = (m == p0 ? u0 : m == p1 ? u1 : m == p2 ? u2 : 0.f) + (m < 3 ? hb : 0.f);
           v[6 * q4 + m] = live ? val : 0.f;
         }
       }
@@ -407,7 +433,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     float s = 0.f;
     if (e < ch.n && bd.geonl)
       for (int gp = 0; gp < NG; ++gp) {
-        const float* g = S.g[e][gp];
+        const float* g = bd.bbar ? S.v[e] : S.g[e][gp];   // b-bar: averaged gradients (kg1.f:46-54)
         const float* Tw = S.T[e][gp];
         const float bx = g[3 * nb], by = g[3 * nb + 1], bz = g[3 * nb + 2];
         const float t0 = Tw[0] * bx + Tw[3] * by + Tw[5] * bz;
