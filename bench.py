@@ -27,6 +27,10 @@ batched: the batching-form workload -- about 1M elements in blocks of
         per step through w3g_iteration_dev (graph replay), FP64 and with
         the FP32 tangent, each under the schedule w3g_autotune picks, next
         to the per-type launches without a graph.
+formulations: the same mesh, state and increment with WARP3D's default
+        l3disop formulation (b-bar mean dilatation, finite strain) and with
+        the small-displacement b-bar brick of its published example model;
+        FP64, FP32 and TF32 tangents.
 crystal: mm10 crystal plasticity -- 32^3 8-node bricks (32,768 elements,
         262,144 Gauss points), one fcc crystal per Gauss point with Euler
         angles uniform on SO(3) (PCG64), Voce hardening (tau_y 90, tau_v
@@ -100,6 +104,7 @@ def parse():
     ap.add_argument("--no-crystal", action="store_true")
     ap.add_argument("--crystal-n", type=int, default=32, help="elements per cube edge of the mm10 workload")
     ap.add_argument("--no-solver", action="store_true", help="skip the device assembly / PCG measurement")
+    ap.add_argument("--no-formulations", action="store_true", help="skip the b-bar / small-displacement lines")
     ap.add_argument("--precision-study", action="store_true",
                     help="instead of the bench line: Newton solves of the cube under every tangent precision form")
     ap.add_argument("--study-steps", type=int, default=20)
@@ -116,11 +121,13 @@ def parse():
     return ap.parse_args()
 
 
-def build_workload(n):
+def build_workload(n, **opts):
+    """opts: element formulation (geonl, bbar) -- the default is the
+    finite-strain displacement brick."""
     from warp3d_gb300.model import Bilinear, Model, cube_mesh
     coords, incid = cube_mesh(n, jitter=0.1, seed=12345)
     mat = Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0, beta=1.0)
-    model = Model(coords, incid, block_size=128, materials=[mat])
+    model = Model(coords, incid, block_size=128, materials=[mat], **opts)
     X = coords
     # load step 1: homogeneous 1% tension with plastic lateral contraction
     F1 = np.diag([1 - 0.005, 1 - 0.005, 1 + 0.01])
@@ -360,6 +367,61 @@ def bench_crystal(args, dev, local, with_cpu):
                         "random orientations, state after 1% tension in 10 steps",
             "elements": ne, "gauss_points": ne * 8, "load_s": t_load, "load_steps": step, "step_cuts": cuts,
             "timed_increment": f"{0.1 * h_last:.3f}% axial strain (+ noise 1e-7)", **out}
+
+
+# other formulations of the same brick, timed on the config-1 mesh and
+# state: WARP3D's default l3disop (b-bar, finite strain) and the
+# small-displacement b-bar brick of its published 18,081-element model
+FORMULATIONS = {"bbar": dict(bbar=True), "small_bbar": dict(geonl=False, bbar=True)}
+
+
+def bench_formulations(args, dev, local):
+    import torch
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+    out = {}
+    for name, opts in FORMULATIONS.items():
+        model, u1, du = build_workload(args.n, **opts)
+        ne = model.noelem
+        eng = Engine(model, device=local)
+        ifv_h = np.zeros(model.nodof)
+        assert eng.recover(1, 1, False, model.c, np.zeros(model.nodof), u1, ifv_h)[0] == 0
+        eng.update()
+        tc = torch.from_numpy(model.c).to(dev)
+        tu = torch.from_numpy(u1).to(dev)
+        tdu = torch.from_numpy(du).to(dev)
+        tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+        stream = torch.cuda.Stream(device=dev)
+        sh = stream.cuda_stream
+        res = {"workload": f"{args.n}^3 hex8 l3disop {'geonl' if opts.get('geonl', True) else 'small displacement'}"
+                           f" b-bar, mm01, state and increment as the headline"}
+        for pname, prec in (("fp64", abi.TANGENT_FP64), ("fp32", abi.TANGENT_FP32), ("tf32", abi.TANGENT_TF32)):
+            eng.set_precision(prec)
+            with torch.cuda.stream(stream):
+                for _ in range(args.warmup):
+                    eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), sh)
+                    eng.recover_dev(2, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), sh)
+            torch.cuda.synchronize()
+            evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps + 1)]
+            with torch.cuda.stream(stream):
+                evs[0].record(stream)
+                for k in range(args.steps):
+                    eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), sh)
+                    evs[2 * k + 1].record(stream)
+                    eng.recover_dev(2, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), sh)
+                    evs[2 * k + 2].record(stream)
+            torch.cuda.synchronize()
+            assert eng.recover_info()[0] == 0
+            t_tan = sum(evs[2 * k].elapsed_time(evs[2 * k + 1]) for k in range(args.steps)) / args.steps
+            t_rec = sum(evs[2 * k + 1].elapsed_time(evs[2 * k + 2]) for k in range(args.steps)) / args.steps
+            ms = evs[0].elapsed_time(evs[-1]) / args.steps
+            res[pname] = {"value": ne / (ms * 1e-3), "ms_per_step": ms, "tangent_ms": t_tan, "recovery_ms": t_rec}
+        res["mixed_speedup"] = res["fp64"]["ms_per_step"] / res["fp32"]["ms_per_step"]
+        out[name] = res
+        eng.close()
+        del tc, tu, tdu, tifv
+        torch.cuda.empty_cache()
+    return out
 
 
 def sample_clocks():
@@ -859,6 +921,10 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.n, args.cpu_sample_blocks, host_threads())
 
+    formulations = None
+    if not args.no_formulations:
+        formulations = bench_formulations(args, dev, local)
+
     crystal = None
     if not args.no_crystal:
         eng.close()
@@ -884,6 +950,7 @@ def main():
             "tangent_ms": tan64, "recovery_ms": rec64,
             "mixed": mixed, "e2e": e2e, "roofline": roofline, "cpu_baseline": cb, "clocks": clocks,
             "gpu_launches": launches64, "batched": batched, "crystal": crystal, "solver": solver,
+            "formulations": formulations,
         }
         print(json.dumps(line), flush=True)
     eng.close()

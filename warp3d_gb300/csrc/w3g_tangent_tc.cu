@@ -84,9 +84,7 @@ struct TcStatic {
   float g[kTcElems][NG][3 * NN];
   float D[kTcElems][NG][21];
   float T[kTcElems][NG][6];
-  float kg[kTcElems][36];
-  float dj[kTcElems][NG];            // det[J] per Gauss point (b-bar averages)
-  float v[kTcElems][3 * NN];         // b-bar: volume-averaged gradients
+  float kg[kTcElems][36];            // b-bar: det[J] per Gauss point until phase 2
   union {
     struct {                         // phase 1
       float C[kTcElems][NG][21];
@@ -94,6 +92,9 @@ struct TcStatic {
       float R[kTcElems][NG][9];
       float ur[kTcElems][NG][6];
     } p1;
+    struct {                         // b-bar, phase 2
+      float v[kTcElems][3 * NN];     // volume-averaged gradients
+    } p2;
     struct {                         // phase 4
       float mrow[kTcRows][3];        // row means over the nodes, per column component
       float mblk[kTcElems][9];       // means of the row means, per (row, column) component
@@ -204,7 +205,9 @@ __device__ __forceinline__ void row_of(const float* q, int j, float* out) {
   }
 }
 
-template <bool kBF16, bool kSplit>
+// kBbar: the instantiation launched for models with b-bar blocks (the
+// others keep the operand code without the b-bar terms)
+template <bool kBF16, bool kSplit, bool kBbar>
 __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, int chunk0, int* tc_timeout) {
   using L = TcLayout<kBF16>;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -265,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     for (int n = sub; n < NN; n += kSubs)
       shape_gradient<float>(gama, dnx[n], dne[n], dnz[n], g[3 * n], g[3 * n + 1], g[3 * n + 2]);
     f = w * dj;
-    if (sub == 0) S.dj[pe][pgp] = dj;
+    if (kBbar && sub == 0) S.kg[pe][pgp] = dj;
     // w det[J] [D], lower triangle row-wise, entries sub, sub + 6, ... (as
     // load_D21: cep_blocks, or for mm10 history1 words 0-35)
     if (bd.mat == W3G_MAT_CRYSTAL) {
@@ -357,18 +360,20 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
   __syncthreads();
   // b-bar: volume-averaged gradients (vol_terms + vol_avg), one thread per
   // (element, node, component)
-  if (bd.bbar && tid < kTcElems * 3 * NN) {
-    const int e = tid / (3 * NN), k = tid % (3 * NN);
-    if (e < ch.n) {
-      float sv = 0.f, vol = 0.f;
-      for (int gp = 0; gp < NG; ++gp) {
-        sv += S.g[e][gp][k] * S.dj[e][gp];
-        vol += S.dj[e][gp];
+  if (kBbar) {
+    if (bd.bbar && tid < kTcElems * 3 * NN) {
+      const int e = tid / (3 * NN), k = tid % (3 * NN);
+      if (e < ch.n) {
+        float sv = 0.f, vol = 0.f;
+        for (int gp = 0; gp < NG; ++gp) {
+          sv += S.g[e][gp][k] * S.kg[e][gp];
+          vol += S.kg[e][gp];
+        }
+        S.u.p2.v[e][k] = sv * (1.f / vol);
       }
-      S.v[e][k] = sv * (1.f / vol);
     }
+    __syncthreads();
   }
-  __syncthreads();
 
   // ---- phase 2: operands (row = 24 e + dof, dof = 8 i + a; k = 6 gp + m).
   // Threads 0-127 write row r of A = B^T, threads 128-255 row r of
@@ -396,9 +401,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     // b-bar (bmod): column (i, a) of B-bar adds h = beta (v_ai - g_ai) to
     // the three normal rows; [D*] B-bar adds h times the row sums of the
     // first three columns of [D*]
-    const bool bb = bd.bbar != 0;
+    const bool bb = kBbar && bd.bbar != 0;
     const float beta = (float)a.bbar_beta;
-    const float va = bb ? S.v[ee][3 * na + di] : 0.f;
+    const float va = bb ? S.u.p2.v[ee][3 * na + di] : 0.f;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       float v[kK / 2];
@@ -412,10 +417,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
           float val;
-          if (isB)
-            val = D[ix[m][0]] * u0 + D[ix[m][1]] * u1 + D[ix[m][2]] * u2 +
-                  hb * (D[low(m, 0)] + D[low(m, 1)] + D[low(m, 2)]);
-          else val = (m == p0 ? u0 : m == p1 ? u1 : m == p2 ? u2 : 0.f) + (m < 3 ? hb : 0.f);
+          if (isB) {
+            val = D[ix[m][0]] * u0 + D[ix[m][1]] * u1 + D[ix[m][2]] * u2;
+            if (kBbar) val += hb * (D[low(m, 0)] + D[low(m, 1)] + D[low(m, 2)]);
+          } else {
+            val = m == p0 ? u0 : m == p1 ? u1 : m == p2 ? u2 : 0.f;
+            if (kBbar && m < 3) val += hb;
+          }
           v[6 * q4 + m] = live ? val : 0.f;
         }
       }
@@ -433,7 +441,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     float s = 0.f;
     if (e < ch.n && bd.geonl)
       for (int gp = 0; gp < NG; ++gp) {
-        const float* g = bd.bbar ? S.v[e] : S.g[e][gp];   // b-bar: averaged gradients (kg1.f:46-54)
+        const float* g = kBbar && bd.bbar ? S.u.p2.v[e] : S.g[e][gp];   // b-bar: averaged gradients (kg1.f:46-54)
         const float* Tw = S.T[e][gp];
         const float bx = g[3 * nb], by = g[3 * nb + 1], bz = g[3 * nb + 2];
         const float t0 = Tw[0] * bx + Tw[3] * by + Tw[5] * bz;
@@ -577,6 +585,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
 // tcgen05.alloc then never has to wait for another CTA's columns.
 constexpr int kMinDyn = 30 * 1024;
 static_assert(sizeof(TcStatic) + kMinDyn + 1024 > 228 * 1024 / 5, "five CTAs could share an SM's TMEM");
+// the split forms (four operands, 96 KB) fit two CTAs in an SM's 228 KB
+// only while the static part, rounded to 1 KB, stays within 17 KB
+static_assert(sizeof(TcStatic) <= 17 * 1024, "split-form tiles would drop to one CTA per SM");
 static_assert((kTcElems * TOT * kKfStride + kTcElems * UT) * 4 <= kMinDyn, "phase-4 staging exceeds shared memory");
 
 template <bool kBF16, bool kSplit>
@@ -588,13 +599,19 @@ static_assert(kTcElems * NG * kSubs <= kThreads && kTcRows <= kThreads, "tile la
 
 template <bool kBF16, bool kSplit>
 cudaError_t set_smem() {
-  return cudaFuncSetAttribute(k_tangent_tc_hex8<kBF16, kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_tangent_tc_hex8<kBF16, kSplit, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem<kBF16, kSplit>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_tangent_tc_hex8<kBF16, kSplit, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)tc_smem<kBF16, kSplit>());
 }
 
 template <bool kBF16, bool kSplit>
 void launch(const DeviceModel& m, const TangentArgs& h, int* tc_timeout, cudaStream_t s) {
-  k_tangent_tc_hex8<kBF16, kSplit><<<m.ntcchunks, kThreads, tc_smem<kBF16, kSplit>(), s>>>(h, 0, tc_timeout);
+  if (m.has_bbar)
+    k_tangent_tc_hex8<kBF16, kSplit, true><<<m.ntcchunks, kThreads, tc_smem<kBF16, kSplit>(), s>>>(h, 0, tc_timeout);
+  else
+    k_tangent_tc_hex8<kBF16, kSplit, false><<<m.ntcchunks, kThreads, tc_smem<kBF16, kSplit>(), s>>>(h, 0, tc_timeout);
 }
 
 }  // namespace
