@@ -417,6 +417,12 @@ def bench_formulations(args, dev, local):
             ms = evs[0].elapsed_time(evs[-1]) / args.steps
             res[pname] = {"value": ne / (ms * 1e-3), "ms_per_step": ms, "tangent_ms": t_tan, "recovery_ms": t_rec}
         res["mixed_speedup"] = res["fp64"]["ms_per_step"] / res["fp32"]["ms_per_step"]
+        if name == "small_bbar":
+            # the only figures WARP3D publishes for this path: its 18,081-element
+            # small-displacement b-bar example (mm01 with temperature curves), 10
+            # OpenMP threads on an Intel Mac (example_3_nonlinear/output_20C_temp)
+            res["reference_published"] = {"value": 0.68e6, "tangent_elem_s": 1.54e6, "recovery_elem_s": 1.22e6,
+                                          "unit": UNIT, "hardware": "Intel Mac, 10 OpenMP threads (ifort + MKL)"}
         out[name] = res
         eng.close()
         del tc, tu, tdu, tifv
