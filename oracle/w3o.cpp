@@ -1406,8 +1406,7 @@ int w3o_tanstf(const w3g_model_desc* m, const w3g_block_state* s, int step, int 
   for (int blk = 0; blk < m->nelblk; ++blk) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
-    if (B.mat_type == W3G_MAT_CRYSTAL && (!B.geonl || (B.bbar && B.etype == W3G_ETYPE_L3DISOP)))
-      return W3G_EUNSUPPORTED;
+    if (B.mat_type == W3G_MAT_CRYSTAL && !B.geonl) return W3G_EUNSUPPORTED;
   }
 #ifdef _OPENMP
   if (g_threads > 0) omp_set_num_threads(g_threads);
@@ -1433,10 +1432,11 @@ int w3o_recover(const w3g_model_desc* m, const w3g_block_state* s, int step, int
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
     if (B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL) return W3G_EUNSUPPORTED;
-    // mm10 is restated on the finite-strain path only; with b-bar WARP3D
-    // gives mm10 bricks the F-bar kinematics (gtmat1_make_fbar), not restated
-    if (B.mat_type == W3G_MAT_CRYSTAL && (!B.geonl || (B.bbar && B.etype == W3G_ETYPE_L3DISOP)))
-      return W3G_EUNSUPPORTED;
+    // mm10 is restated on the finite-strain path only. With b-bar WARP3D
+    // also scales F_n and F_n+1 to F-bar (gtmat1_make_fbar, gtmat1.f:145-151),
+    // but only UMATs read those (rstgp1.f:3786-3787): mm10 blocks take the
+    // b-bar strain increment, internal forces and tangent restated here.
+    if (B.mat_type == W3G_MAT_CRYSTAL && !B.geonl) return W3G_EUNSUPPORTED;
     if (B.mat_type == W3G_MAT_CRYSTAL && (!m->crystals || !m->elem_crystal || !m->elem_angles))
       return W3G_EARG;
   }

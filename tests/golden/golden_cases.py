@@ -44,9 +44,10 @@ def _mm01_case(etype, nxyz, spans, shear, dyld=25.0, **opts):
     return model, nxyz, {"strain": 0.0015, "shear": shear, "extrapolate": False}
 
 
-def _mm10_case():
+def _mm10_case(**opts):
     coords, incid = cube_mesh(1, jitter=0.05, seed=31, n_xyz=(1, 1, 2))
-    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(2, 17), block_spans=[1, 1])
+    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(2, 17), block_spans=[1, 1],
+                  **opts)
     return model, (1, 1, 2), {"strain": 0.0005, "shear": 0.0, "extrapolate": True}
 
 
@@ -64,6 +65,7 @@ CASES = {
     # step's Newton iterates grow to the element size and do not converge
     # without a line search, although the tangent matches central
     # differences of the internal forces to 1e-9)
+    "hex8_mm10_bbar": lambda: _mm10_case(bbar=True),
     "tet10_mm01_small": lambda: _mm01_case(abi.ETYPE_TET10, (1, 1, 2), [7, 5], 0.0, dyld=0.0, geonl=False),
 }
 
@@ -97,7 +99,8 @@ def model_from(z) -> Model:
         cr = Crystal(**vals)
         p = parts[0]
         return Model(z["coords"], p.incid, etype=p.etype, block_spans=p.spans, materials=[cr],
-                     angles=z["angles"], dt=float(z["dt"]), geonl=bool(z["geonl"]), qbar=bool(z["qbar"]))
+                     angles=z["angles"], dt=float(z["dt"]), geonl=bool(z["geonl"]), qbar=bool(z["qbar"]),
+                     bbar=bool(z["bbar"]) if "bbar" in z else False)
     mats = [Bilinear(*row) for row in z["bilinear"]]
     off = 0
     for p in parts:

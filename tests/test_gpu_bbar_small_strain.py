@@ -153,8 +153,8 @@ def test_newton_engine_matches_oracle(opts):
     assert rel_err(runs["gpu"][0], runs["oracle"][0]) < 10 * tol
 
 
-@pytest.mark.parametrize("geonl,bbar", [(False, False), (True, True)])
-def test_crystal_blocks_reject_small_displacement_and_bbar(geonl, bbar):
+@pytest.mark.parametrize("geonl,bbar", [(False, False), (False, True)])
+def test_crystal_blocks_reject_small_displacement(geonl, bbar):
     coords, incid = cube_mesh(1)
     model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(1, 3), geonl=geonl, bbar=bbar)
     with pytest.raises(abi.W3GError):

@@ -30,15 +30,14 @@ def _engine(model, **kw):
     return Engine(model, **kw)
 
 
-def _model(n=3, seed=7, spans=None):
+def _model(n=3, seed=7, spans=None, **kw):
     coords, incid = cube_mesh(n, jitter=0.05)
     return Model(coords, incid, materials=[Crystal()], angles=random_orientations(n ** 3, seed),
-                 block_spans=spans), (n, n, n)
+                 block_spans=spans, **kw), (n, n, n)
 
 
-@pytest.fixture(scope="module")
-def crystal_case():
-    model, nxyz = _model(3, spans=[20, 7])
+def _loaded_case(**kw):
+    model, nxyz = _model(3, spans=[20, 7], **kw)
     ora = oracle.Oracle(model)
     fixed, topz = uniaxial_bcs(model, nxyz)
     drv = NewtonDriver(model, ora, fixed, tol=1e-8, maxit=60, extrapolate=True)
@@ -51,6 +50,17 @@ def crystal_case():
     du[topz] = 0.0005 * nxyz[2]
     du[drv.free] = drv.du_prev[drv.free] + rng.normal(0.0, 2e-5, size=len(drv.free))
     return model, ora.state, drv.u.copy(), du
+
+
+@pytest.fixture(scope="module")
+def crystal_case():
+    return _loaded_case()
+
+
+@pytest.fixture(scope="module")
+def crystal_bbar_case():
+    # WARP3D's default l3disop formulation (b-bar) on crystal blocks
+    return _loaded_case(bbar=True)
 
 
 def _flat(blocks):
@@ -104,6 +114,16 @@ def test_mm10_recover_and_tangent_parity(crystal_case):
     _tangent(model, eng, ora, 4, 1, u, du)
     eng.set_precision(abi.TANGENT_FP32)
     _tangent(model, eng, ora, 4, 1, u, du, tol=TOL_FP32)
+
+
+def test_mm10_bbar_parity(crystal_bbar_case):
+    model, state, u, du = crystal_bbar_case
+    eng, ora = _compare(model, state, 4, 1, False, u, du)
+    _tangent(model, eng, ora, 4, 1, u, du)
+    eng.set_precision(abi.TANGENT_FP32)
+    _tangent(model, eng, ora, 4, 1, u, du, tol=TOL_FP32)
+    eng.set_precision(abi.TANGENT_TF32)
+    _tangent(model, eng, ora, 4, 1, u, du, tol=2e-3)
 
 
 def test_mm10_iteration_zero_paths(crystal_case):

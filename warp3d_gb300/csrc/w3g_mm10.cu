@@ -148,7 +148,21 @@ __global__ void __launch_bounds__(kRecoverThreads) k_mm10_kin(RecoverArgs a, int
   } else {
     for (int k = 0; k < 9; ++k) L[k] = dth[k];
   }
-  const double ddt[6] = {L[0], L[4], L[8], L[3] + L[1], L[7] + L[5], L[6] + L[2]};
+  double ddt[6] = {L[0], L[4], L[8], L[3] + L[1], L[7] + L[5], L[6] + L[2]};
+  if (bd.bbar) {
+    // b-bar at the mid-step shape (as for mm01): the element's mean
+    // dilatation rate over its 8 Gauss-point lanes replaces each point's
+    const unsigned gmask = 0xFFu << (tid & 24);
+    const double jm = update_coords ? dfh * geo[3 * NN] : geo[3 * NN];
+    const double trl = L[0] + L[4] + L[8];
+    double s1 = jm * trl, s0 = jm;
+    for (int off = 1; off < NG; off <<= 1) {
+      s1 += __shfl_xor_sync(gmask, s1, off);
+      s0 += __shfl_xor_sync(gmask, s0, off);
+    }
+    const double cb = a.bbar_beta * (s1 * (1.0 / s0) - trl);
+    ddt[0] += cb; ddt[1] += cb; ddt[2] += cb;
+  }
   double uddt[6];
   rotate_to_unrotated(Rh, ddt, uddt);
   for (int k = 0; k < 6; ++k) a.eps_n1[gpi * 6 + k] = a.eps_n[gpi * 6 + k] + uddt[k];
@@ -1028,10 +1042,26 @@ __global__ void __launch_bounds__(kRecoverThreads) k_mm10_forces(RecoverArgs a, 
     double S[6];
     if (bd.geonl) rotate_to_spatial(R1, cgn1, S);
     else for (int k = 0; k < 6; ++k) S[k] = cgn1[k];
+    const double j1 = update_coords ? dfn1 * dj0 : dj0;
+    double pdiag = 0.0;
+    if (bd.bbar) {
+      // b-bar at n+1 (as for mm01): the element's mean pressure replaces
+      // each point's
+      const unsigned gmask = 0xFFu << (tid & 24);
+      const double trs = S[0] + S[1] + S[2];
+      double s1 = w * j1 * trs, s0 = j1;
+      for (int off = 1; off < NG; off <<= 1) {
+        s1 += __shfl_xor_sync(gmask, s1, off);
+        s0 += __shfl_xor_sync(gmask, s0, off);
+      }
+      const double ptr = a.bbar_beta * trs;
+      S[0] = S[0] - ptr; S[1] = S[1] - ptr; S[2] = S[2] - ptr;
+      pdiag = a.bbar_beta * (s1 * (1.0 / s0)) * j1;
+    }
     double P[9];
-    const double wdj = update_coords ? w * (dfn1 * dj0) : w * dj0;
-    const double T[9] = {S[0] * wdj, S[3] * wdj, S[5] * wdj, S[3] * wdj, S[1] * wdj,
-                         S[4] * wdj, S[5] * wdj, S[4] * wdj, S[2] * wdj};
+    const double wdj = w * j1;
+    const double T[9] = {S[0] * wdj + pdiag, S[3] * wdj, S[5] * wdj, S[3] * wdj, S[1] * wdj + pdiag,
+                         S[4] * wdj, S[5] * wdj, S[4] * wdj, S[2] * wdj + pdiag};
     if (update_coords) {
       const double r = 1.0 / dfn1;
       double Fi[9];
