@@ -115,6 +115,9 @@ def parse():
     ap.add_argument("--study-no-extrapolate", action="store_true",
                     help="start every step from zero instead of the scaled previous increment")
     ap.add_argument("--study-no-adaptive", action="store_true", help="no subdivision of failing steps")
+    ap.add_argument("--study-formulation", default="disp", choices=["disp", "bbar", "small_bbar"],
+                    help="brick formulation of the precision study: displacement (finite strain), b-bar, or "
+                         "small-displacement b-bar")
     ap.add_argument("--batched-study", action="store_true",
                     help="instead of the bench line: Newton solves of the mixed-type bars, FP64 and FP32 tangent")
     ap.add_argument("--study-section", type=int, default=32, help="cells per side of the bars' section")
@@ -725,13 +728,15 @@ def precision_study(args, dev):
     from warp3d_gb300.solver import DeviceCsr
     forms = {k: v for k, v in STUDY_FORMS.items()}
     n = args.n
-    model, _, _ = build_workload(n)
+    opts = FORMULATIONS.get(args.study_formulation, {})
+    model, _, _ = build_workload(n, **opts)
     fixed, topz = uniaxial_bcs(model, (n, n, n))
     t0 = time.perf_counter()
     eng = Engine(model)
     csr = DeviceCsr(eng)
     setup_s = time.perf_counter() - t0
-    out = {"workload": f"{n}^3 hex8 l3disop geonl (jitter 0.1h), mm01 bilinear, blocks of 128; uniaxial "
+    form = {"disp": "geonl", "bbar": "geonl b-bar", "small_bbar": "small-displacement b-bar"}[args.study_formulation]
+    out = {"workload": f"{n}^3 hex8 l3disop {form} (jitter 0.1h), mm01 bilinear, blocks of 128; uniaxial "
                        f"{100 * args.study_strain:g}% in {args.study_steps} steps",
            "elements": model.noelem, "dofs": model.nodof, "csr_nnz": csr.nnz, "setup_s": setup_s,
            "newton_tol": 1e-8, "pcg_rtol": 1e-10, "forms": {}}
