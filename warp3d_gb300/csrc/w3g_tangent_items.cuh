@@ -216,6 +216,11 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
   __syncwarp();
   if (kBbar) hex8_mean_gradients<T>(sdn, sx, sy, sz, t, active, sg, sV);
   const T beta = (T)a.bbar_beta;
+  // b-bar: the geometric stiffness takes the averaged gradients at every
+  // point, so it is v_a^T (sum_gp w det[J] {T}) v_b, formed once per
+  // element; the stress sum accumulates in the (otherwise unused) {T}g
+  // region, components 2t, 2t + 1 by lane t < 3
+  if (kBbar && active && t < 3) { sTg[2 * t] = T(0); sTg[2 * t + 1] = T(0); }
 
   T acc[9][9];
 #pragma unroll
@@ -302,6 +307,15 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
       }
     }
     __syncwarp();
+    if (kBbar && active && t < 3) {
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        T v = sTg[2 * t + j];
+#pragma unroll
+        for (int q = 0; q < kHalf; ++q) v += sT[q * 6 + 2 * t + j];
+        sTg[2 * t + j] = v;
+      }
+    }
 
     // ---- phase 2 ----
     for (int s = 0; s < kHalf; ++s) {
@@ -340,12 +354,12 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
               db[m * 3 + 2] = D[low(m, 2)] * gz + D[low(m, 4)] * gy + D[low(m, 5)] * gx;
             }
           }
-          // kgstiff: with b-bar the averaged gradients (src/kg1.f:46-54)
-          const T kx = kBbar ? sV[3 * n] : gx, ky = kBbar ? sV[3 * n + 1] : gy, kz = kBbar ? sV[3 * n + 2] : gz;
-          T* tg = sTg + n * 3;
-          tg[0] = Tw[0] * kx + Tw[3] * ky + Tw[5] * kz;
-          tg[1] = Tw[3] * kx + Tw[1] * ky + Tw[4] * kz;
-          tg[2] = Tw[5] * kx + Tw[4] * ky + Tw[2] * kz;
+          if (!kBbar) {   // kgstiff per point (b-bar: once per element, below)
+            T* tg = sTg + n * 3;
+            tg[0] = Tw[0] * gx + Tw[3] * gy + Tw[5] * gz;
+            tg[1] = Tw[3] * gx + Tw[1] * gy + Tw[4] * gz;
+            tg[2] = Tw[5] * gx + Tw[4] * gy + Tw[2] * gz;
+          }
         }
       }
       __syncwarp();
@@ -378,15 +392,34 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
               for (int kk = 0; kk < 3; ++kk)
                 if (p >= 2 || kk >= ii) acc[p][ii * 3 + kk] = fma(ha[ii], sb[kk], acc[p][ii * 3 + kk]);
           }
-          if (bd.geonl) {   // kgstiff (src/kg1.f:16-110)
+          if (!kBbar && bd.geonl) {   // kgstiff (src/kg1.f:16-110)
             const T* tg = sTg + nb * 3;
-            const T gtg = kBbar ? sV[3 * na] * tg[0] + sV[3 * na + 1] * tg[1] + sV[3 * na + 2] * tg[2]
-                                : ax * tg[0] + ay * tg[1] + az * tg[2];
+            const T gtg = ax * tg[0] + ay * tg[1] + az * tg[2];
             acc[p][0] += gtg; acc[p][4] += gtg; acc[p][8] += gtg;
           }
         }
       }
       __syncwarp();
+    }
+  }
+  if (kBbar && bd.geonl) {
+    // kgstiff with the averaged derivatives (src/kg1.f:46-54): v_a^T T v_b
+    // per node pair with the element's stress sum T
+    if (active) {
+      T tsum[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) tsum[k] = sTg[k];
+#pragma unroll
+      for (int p = 0; p < 9; ++p) {
+        const int k = 4 * p + t;
+        const T* va = sV + 3 * pa[k];
+        const T* vb = sV + 3 * pb[k];
+        const T t0 = tsum[0] * vb[0] + tsum[3] * vb[1] + tsum[5] * vb[2];
+        const T t1 = tsum[3] * vb[0] + tsum[1] * vb[1] + tsum[4] * vb[2];
+        const T t2 = tsum[5] * vb[0] + tsum[4] * vb[1] + tsum[2] * vb[2];
+        const T gtg = va[0] * t0 + va[1] * t1 + va[2] * t2;
+        acc[p][0] += gtg; acc[p][4] += gtg; acc[p][8] += gtg;
+      }
     }
   }
 
