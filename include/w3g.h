@@ -190,6 +190,23 @@ int w3g_set_tangent_precision(w3g_context* ctx, int precision);
 int w3g_state_upload(w3g_context* ctx, const w3g_block_state* host);
 int w3g_state_download(w3g_context* ctx, const w3g_block_state* host);
 
+/*
+ * The element-block section of a WARP3D restart file (replaces, for a
+ * driver without WARP3D's own restart code, store_blocks as called by
+ * store, src/store.f:329-341, :915-1010; and its readers in src/reopen.f):
+ * Fortran sequential unformatted records (4-byte little-endian lengths) of
+ * history (state n) and cep per block, then urcs_n, rot_n1 of the geonl
+ * blocks, eps_n and element volumes, each array followed by the check
+ * record 2147483647 and each section after the first by one more.
+ * w3g_store_blocks writes the resident state (append = 1: at the end of an
+ * existing file); w3g_reopen_blocks reads it starting at byte `offset`,
+ * checks every record length and check record (W3G_EARG otherwise),
+ * uploads it with the n+1 arrays equal to the n arrays, as reopen does,
+ * and returns the offset after the section in *end_offset (may be NULL).
+ */
+int w3g_store_blocks(w3g_context* ctx, const char* path, int append);
+int w3g_reopen_blocks(w3g_context* ctx, const char* path, long long offset, long long* end_offset);
+
 /* ---- the hot path, host arrays ------------------------------------- */
 
 /* tanstf (src/tanstf.f:17): element tangent stiffnesses for all blocks.

@@ -153,6 +153,8 @@ PROTOTYPES = [
     ("w3g_set_tangent_precision", C.c_int, [_vp, C.c_int]),
     ("w3g_state_upload", C.c_int, [_vp, C.POINTER(BlockState)]),
     ("w3g_state_download", C.c_int, [_vp, C.POINTER(BlockState)]),
+    ("w3g_store_blocks", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("w3g_reopen_blocks", C.c_int, [_vp, C.c_char_p, C.c_longlong, C.POINTER(C.c_longlong)]),
     ("w3g_tanstf", C.c_int, [_vp, C.c_int, C.c_int, _d, _d, _d, C.POINTER(_d)]),
     ("w3g_recover", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _d, _d, _d, _d, C.POINTER(RecoverInfo)]),
     ("w3g_update", C.c_int, [_vp]),

@@ -96,6 +96,19 @@ class Engine:
         s = state.struct(names)
         abi.check(self.lib, self.lib.w3g_state_download(self.ctx, C.byref(s)))
 
+    # ---- restart records (store_blocks / reopen) ---------------------------
+    def store_blocks(self, path: str, append: bool = False):
+        """Writes the element-block section of a WARP3D restart file
+        (w3g_store_blocks: store_blocks' records, src/store.f:915)."""
+        abi.check(self.lib, self.lib.w3g_store_blocks(self.ctx, path.encode(), 1 if append else 0))
+
+    def reopen_blocks(self, path: str, offset: int = 0) -> int:
+        """Reads that section from byte `offset` (w3g_reopen_blocks); returns
+        the offset after it."""
+        end = C.c_longlong()
+        abi.check(self.lib, self.lib.w3g_reopen_blocks(self.ctx, path.encode(), offset, C.byref(end)))
+        return end.value
+
     # ---- hot path, host arrays --------------------------------------------
     def tanstf(self, step: int, it: int, c: np.ndarray, u: np.ndarray, du: np.ndarray, estiff_blocks=None):
         """estiff_blocks: a list of per-block (span, utsz) arrays, or one
