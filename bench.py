@@ -118,6 +118,8 @@ def parse():
     ap.add_argument("--study-formulation", default="disp", choices=["disp", "bbar", "small_bbar"],
                     help="brick formulation of the precision study: displacement (finite strain), b-bar, or "
                          "small-displacement b-bar")
+    ap.add_argument("--type-study", action="store_true",
+                    help="time each element type's tangent and recovery alone (hex20, tet10, hex8)")
     ap.add_argument("--batched-study", action="store_true",
                     help="instead of the bench line: Newton solves of the mixed-type bars, FP64 and FP32 tangent")
     ap.add_argument("--study-section", type=int, default=32, help="cells per side of the bars' section")
@@ -426,6 +428,52 @@ def bench_formulations(args, dev, local):
             # OpenMP threads on an Intel Mac (example_3_nonlinear/output_20C_temp)
             res["reference_published"] = {"value": 0.68e6, "tangent_elem_s": 1.54e6, "recovery_elem_s": 1.22e6,
                                           "unit": UNIT, "hardware": "Intel Mac, 10 OpenMP threads (ifort + MKL)"}
+        out[name] = res
+        eng.close()
+        del tc, tu, tdu, tifv
+        torch.cuda.empty_cache()
+    return out
+
+
+def type_study(args, dev):
+    """One Newton iteration's element work per element type alone, FP64 and
+    with the FP32 tangent: 40^3 20-node bricks, 40^3 x 6 10-node
+    tetrahedra, n^3 8-node bricks (jitter 0.05h, mm01, blocks of 128;
+    state after one step to 1% tension; CUDA events over 5 calls each)."""
+    import torch
+    from warp3d_gb300 import abi
+    from warp3d_gb300.engine import Engine
+    from warp3d_gb300.model import Bilinear, Model, cube_mesh, cube_mesh_hex20, cube_mesh_tet10
+    out = {}
+    for name, mesh, n, et in (("hex20", cube_mesh_hex20, 40, abi.ETYPE_Q3DISOP),
+                              ("tet10", cube_mesh_tet10, 40, abi.ETYPE_TET10),
+                              ("hex8", cube_mesh, args.n, abi.ETYPE_L3DISOP)):
+        coords, incid = mesh(n, jitter=0.05, seed=3)
+        model = Model(coords, incid, etype=et, materials=[Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)])
+        eng = Engine(model)
+        u1 = (np.diag([-0.005, -0.005, 0.01]) @ coords.T).T.ravel()
+        assert eng.recover(1, 1, False, model.c, np.zeros(model.nodof), u1, np.zeros(model.nodof))[0] == 0
+        eng.update()
+        du = (np.diag([-0.0005, -0.0005, 0.001]) @ coords.T).T.ravel()
+        tc, tu, tdu = (torch.from_numpy(a).to(dev) for a in (model.c, u1, du))
+        tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
+        res = {"elements": model.noelem}
+        for pname, prec in (("fp64", abi.TANGENT_FP64), ("fp32", abi.TANGENT_FP32)):
+            eng.set_precision(prec)
+            for _ in range(max(3, args.warmup)):
+                eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), 0)
+                eng.recover_dev(2, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), 0)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ev[0].record()
+            for _ in range(5):
+                eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), 0)
+            ev[1].record()
+            for _ in range(5):
+                eng.recover_dev(2, 1, False, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr(), 0)
+            ev[2].record()
+            torch.cuda.synchronize()
+            res[pname] = {"tangent_ms": ev[0].elapsed_time(ev[1]) / 5, "recover_ms": ev[1].elapsed_time(ev[2]) / 5}
         out[name] = res
         eng.close()
         del tc, tu, tdu, tifv
@@ -796,6 +844,9 @@ def main():
         return
     if args.batched_study:
         print(json.dumps({"batched_study": batched_study(args, dev)}))
+        return
+    if args.type_study:
+        print(json.dumps({"type_study": type_study(args, dev)}))
         return
 
     from warp3d_gb300 import abi
