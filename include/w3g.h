@@ -134,6 +134,12 @@ typedef struct w3g_model_desc {
   double dt;                    /* time increment of the load step       */
   double eps_bbar;              /* b-bar stabilization factor (0), the
                                    global eps_bbar, src/initst.f:537      */
+  int asymmetric_assembly;      /* "assembly asymmetric on" (main_data):
+                                   full (totdof*totdof, span) element
+                                   matrices, column-major per element
+                                   (gptns1.f bdbt_asym, tanstf.f:223-225),
+                                   mm10 tangents not symmetrized
+                                   (mm10_a.f:1165-1166); 8-node bricks */
 } w3g_model_desc;
 
 /*

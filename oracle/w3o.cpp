@@ -1026,6 +1026,7 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
         w3o::CrystalProps cp;
         const int e = B.felem - 1 + i;
         w3o::mm10_element_props(m->crystals[m->elem_crystal[e]], m->elem_angles + 3 * (size_t)e, cp);
+        cp.asymmetric = m->asymmetric_assembly;
         double hn[MM10_HIST], hn1[MM10_HIST], un[9], un1[9], dd[6], rr[9];
         for (int k = 0; k < MM10_HIST; ++k) { hn[k] = ehist[g](i, k); hn1[k] = ehist1[g](i, k); }
         for (int k = 0; k < 9; ++k) { un[k] = urcs_n[g](i, k); un1[k] = zero; rr[k] = rot[g](i, k); }
@@ -1159,9 +1160,13 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
 int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& B, const double* c,
                   const double* u, const double* du, double* estiff) {
   const int span = B.span, nnode = B.nnode, ngp = B.ngp, totdof = B.totdof, utsz = B.utsz;
+  // asymmetric assembly: full element matrices, ek_full(span, totdof**2)
+  // column-major (tanstf.f:223-225, gptns1.f:241-246 bdbt_asym)
+  const bool asym = m->asymmetric_assembly != 0;
+  const int nrow = asym ? totdof * totdof : utsz;
   const int* edest = m->edest[B.blk];
   const int* cdest = m->cdest[B.blk];
-  for (size_t k = 0; k < (size_t)utsz * span; ++k) estiff[k] = zero;
+  for (size_t k = 0; k < (size_t)nrow * span; ++k) estiff[k] = zero;
 
   // dptstf (src/dptstf.f:86-156)
   A2 ce(totdof), ue(totdof), due(totdof);
@@ -1206,7 +1211,7 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
                 volume.data());
   }
   if (bbar) vol_avg(span, vol, volume.data());
-  A2 ek(utsz);
+  A2 ek(nrow);
   ek.zero();
   A2 b(totdof * 6), bd(totdof * 6);
   b.zero(); bd.zero();
@@ -1316,12 +1321,22 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
         for (int kk = 1; kk <= 6; ++kk)
           BD(i, j, kk - 1) = CE(1, kk) * BB(i, j, 0) + CE(2, kk) * BB(i, j, 1) + CE(3, kk) * BB(i, j, 2) +
                              CE(4, kk) * BB(i, j, 3) + CE(5, kk) * BB(i, j, 4) + CE(6, kk) * BB(i, j, 5);
-    for (int j = 0; j < utsz; ++j) {
-      int row = icp_r[j] - 1, col = icp_c[j] - 1;
-      for (int i = 0; i < span; ++i)
-        ek(i, j) = ek(i, j) + BB(i, col, 0) * BD(i, row, 0) + BB(i, col, 1) * BD(i, row, 1) +
-                   BB(i, col, 2) * BD(i, row, 2) + BB(i, col, 3) * BD(i, row, 3) +
-                   BB(i, col, 4) * BD(i, row, 4) + BB(i, col, 5) * BD(i, row, 5);
+    if (asym) {   // bdbt_asym (src/gptns1.f:1513-1612): every (row, col)
+      int j = 0;
+      for (int col = 0; col < totdof; ++col)
+        for (int row = 0; row < totdof; ++row, ++j)
+          for (int i = 0; i < span; ++i)
+            ek(i, j) = ek(i, j) + BB(i, col, 0) * BD(i, row, 0) + BB(i, col, 1) * BD(i, row, 1) +
+                       BB(i, col, 2) * BD(i, row, 2) + BB(i, col, 3) * BD(i, row, 3) +
+                       BB(i, col, 4) * BD(i, row, 4) + BB(i, col, 5) * BD(i, row, 5);
+    } else {
+      for (int j = 0; j < utsz; ++j) {
+        int row = icp_r[j] - 1, col = icp_c[j] - 1;
+        for (int i = 0; i < span; ++i)
+          ek(i, j) = ek(i, j) + BB(i, col, 0) * BD(i, row, 0) + BB(i, col, 1) * BD(i, row, 1) +
+                     BB(i, col, 2) * BD(i, row, 2) + BB(i, col, 3) * BD(i, row, 3) +
+                     BB(i, col, 4) * BD(i, row, 4) + BB(i, col, 5) * BD(i, row, 5);
+      }
     }
 #undef BB
 #undef BD
@@ -1365,20 +1380,32 @@ int tangent_block(const w3g_model_desc* m, const w3g_block_state* s, const Blk& 
         int cp1 = enode * (enode - 1) / 2;
         int cp2 = (nnode + enode) * (nnode + enode - 1) / 2 + nnode;
         int cp3 = (2 * nnode + enode) * (2 * nnode + enode - 1) / 2 + 2 * nnode;
-        for (int j = 1; j <= enode; ++j)
+        for (int j = 1; j <= enode; ++j) {
+          if (asym) {   // kg1.f:112-178: (row j, col enode) and its mirror
+            for (int d = 0; d < 3; ++d) {
+              const int r = d * nnode + j, c = d * nnode + enode;   // 1-based
+              const int k = (c - 1) * totdof + r - 1, kt = (r - 1) * totdof + c - 1;
+              for (int i = 0; i < span; ++i) {
+                ek(i, k) = ek(i, k) + gtg(i, cp1 + j - 1);
+                if (r != c) ek(i, kt) = ek(i, kt) + gtg(i, cp1 + j - 1);
+              }
+            }
+            continue;
+          }
           for (int i = 0; i < span; ++i) {
             ek(i, cp1 + j - 1) = ek(i, cp1 + j - 1) + gtg(i, cp1 + j - 1);
             ek(i, cp2 + j - 1) = ek(i, cp2 + j - 1) + gtg(i, cp1 + j - 1);
             ek(i, cp3 + j - 1) = ek(i, cp3 + j - 1) + gtg(i, cp1 + j - 1);
           }
+        }
       }
     }
   }
   // rktstf_do_transpose + beta_fact (src/rktstf.f:160-172, :221-290)
   for (int i = 0; i < span; ++i)
-    for (int k = 0; k < utsz; ++k) estiff[(size_t)i * utsz + k] = ek(i, k);
+    for (int k = 0; k < nrow; ++k) estiff[(size_t)i * nrow + k] = ek(i, k);
   if (m->beta_fact != one)
-    for (size_t k = 0; k < (size_t)utsz * span; ++k) estiff[k] = m->beta_fact * estiff[k];
+    for (size_t k = 0; k < (size_t)nrow * span; ++k) estiff[k] = m->beta_fact * estiff[k];
   return 0;
 }
 

@@ -960,10 +960,12 @@ int mm10_point(const CrystalProps& p, int step, int iter, bool extrapolated_du, 
   double p_strain_ten_c[6] = {zero, zero, zero, zero, zero, zero};
   if (!(iter0off || no_load)) {
     tangent(p, np1, J);
-    double w[36];   // mm10_a_make_symm_1
-    for (int j = 0; j < 6; ++j)
-      for (int i = 0; i < 6; ++i) M6(w, i, j) = (M6(np1.tangent, i, j) + M6(np1.tangent, j, i)) * half;
-    for (int k = 0; k < 36; ++k) np1.tangent[k] = w[k];
+    if (!p.asymmetric) {   // mm10_a_make_symm_1 unless asymmetric assembly (mm10_a.f:1165-1166)
+      double w[36];
+      for (int j = 0; j < 6; ++j)
+        for (int i = 0; i < 6; ++i) M6(w, i, j) = (M6(np1.tangent, i, j) + M6(np1.tangent, j, i)) * half;
+      for (int k = 0; k < 36; ++k) np1.tangent[k] = w[k];
+    }
     update_rotation(p, np1, n);
     output(p, np1, n, p_strain_ten_c);
   }

@@ -29,6 +29,7 @@ struct CrystalProps {
   double rate_n, tau_y, tau_v, theta_0, voche_m, iD_v, k_0, burgers;
   double atol, atol1, rtol, rtol1;
   int miter;
+  int asymmetric = 0;            // asymmetric assembly: tangent left unsymmetrized
 };
 
 // builds the element's crystal properties from a crystal definition and

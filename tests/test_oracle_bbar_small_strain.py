@@ -214,3 +214,60 @@ def test_crystal_bbar_brick_runs_and_keeps_rigid_modes():
         for d in range(3):
             r = np.zeros((3, 8)); r[d] = 1.0
             assert np.max(np.abs(K @ r.ravel())) < 1e-10 * np.max(np.abs(K))
+
+
+# ---- asymmetric assembly ("assembly asymmetric on") -----------------------
+def _full(v, n):
+    return v.reshape(n, n).T      # column-major (totdof**2) -> K[row, col]
+
+
+@pytest.mark.parametrize("etype", [abi.ETYPE_L3DISOP, abi.ETYPE_Q3DISOP, abi.ETYPE_TET10])
+def test_asymmetric_assembly_of_a_symmetric_material_is_the_full_symmetric_matrix(etype):
+    out = {}
+    for asym in (False, True):
+        model, nxyz = make_model(n=2, jitter=0.1, etype=etype, asymmetric=asym, bbar=etype == abi.ETYPE_L3DISOP)
+        du = np.random.default_rng(3).normal(0.0, 1e-3, model.nodof)
+        ora, st, _ = _run(model, du)
+        assert st == 0
+        est = model.estiff_blocks()
+        assert ora.tanstf(1, 1, model.c, np.zeros(model.nodof), du, est) == 0
+        out[asym] = (model, est[0])
+    (m0, packed), (m1, full) = out[False], out[True]
+    n = m0.totdof
+    assert full.shape == (m1.noelem, n * n)
+    for e in range(m0.noelem):
+        K = _full(full[e], n)
+        assert rel_err(K, _unpack(packed[e], n)) < 1e-14
+
+
+def test_asymmetric_assembly_keeps_the_crystal_tangent_unsymmetric():
+    coords, incid = cube_mesh(2, jitter=0.05)
+    res = {}
+    for asym in (False, True):
+        model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(8, 3), asymmetric=asym)
+        ora = oracle.Oracle(model)
+        du = np.zeros(model.nodof)
+        top = np.isclose(model.coords[:, 2], 2.0)
+        du[3 * np.nonzero(top)[0] + 2] = 0.004                 # plastic in one increment
+        st, _ = ora.recover(1, 1, True, model.c, np.zeros(model.nodof), du, np.zeros(model.nodof))
+        assert st == 0
+        est = model.estiff_blocks()
+        assert ora.tanstf(1, 1, model.c, np.zeros(model.nodof), du, est) == 0
+        res[asym] = (ora.state, est[0], model)
+    (s0, k0, m0), (s1, k1, m1) = res[False], res[True]
+    # the update is the same; only the stored tangent (history 1-36) differs
+    assert np.array_equal(np.concatenate(s0.urcs_n1), np.concatenate(s1.urcs_n1))
+    h0, h1 = np.concatenate(s0.history1), np.concatenate(s1.history1)
+    assert np.array_equal(h0[..., 36:], h1[..., 36:])
+    D1 = h1[..., :36].reshape(-1, 6, 6)
+    assert np.max(np.abs(D1 - np.swapaxes(D1, 1, 2))) > 1e-8 * np.max(np.abs(D1))
+    assert np.allclose(0.5 * (D1 + np.swapaxes(D1, 1, 2)), h0[..., :36].reshape(-1, 6, 6), rtol=0, atol=1e-9 * np.max(np.abs(D1)))
+    asym = []
+    for e in range(m1.noelem):
+        K = _full(k1[e], 24)
+        asym.append(np.max(np.abs(K - K.T)) / np.max(np.abs(K)))
+        for d in range(3):                                   # rigid translations, both sides
+            r = np.zeros((3, 8)); r[d] = 1.0
+            assert np.max(np.abs(K @ r.ravel())) < 1e-10 * np.max(np.abs(K))
+            assert np.max(np.abs(r.ravel() @ K)) < 1e-10 * np.max(np.abs(K))
+    assert max(asym) > 1e-8            # the plastic points' tangents are not symmetric

@@ -95,6 +95,7 @@ class ModelDesc(C.Structure):
         ("elem_angles", C.POINTER(C.c_double)),
         ("dt", C.c_double),
         ("eps_bbar", C.c_double),
+        ("asymmetric_assembly", C.c_int),
     ]
 
 

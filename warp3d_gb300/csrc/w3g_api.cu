@@ -139,6 +139,11 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
 int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
   TangentArgs a = tangent_args(c, d_c, d_u, d_du);
   const int p = c->precision;
+  if (c->m.asym) {   // asymmetric assembly: full 8-node brick matrices
+    cudaError_t e = launch_tangent_full(c->m, a, p != W3G_TANGENT_FP64, st);
+    if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
+    return c->m.ttype_chunks[0] > 0 ? 1 : 0;
+  }
   const bool tc = p >= W3G_TANGENT_TF32;
   cudaError_t e = cudaSuccess;
   if (tc)
@@ -185,6 +190,7 @@ int enqueue_recover(w3g_context* c, const double* d_c, const double* d_u, const 
   a.params = c->s.params;
   a.beta_fact = c->m.beta_fact;
   a.bbar_beta = c->m.bbar_beta;
+  a.asym = c->m.asym;
   a.xtal = c->m.xtal;
   a.xtype = c->m.xtype;
   a.mm10_scr = c->s.mm10_scr;
@@ -251,10 +257,10 @@ int copy_estiff_range(w3g_context* c, double* const* estiff, int b0, int b1, cud
     const BlockDesc& bd = c->blocks[b];
     if (!estiff[b]) continue;
     int e = b;
-    size_t run = (size_t)bd.utsz * bd.span;
-    while (e + 1 < b1 && estiff[e + 1] && estiff[e + 1] == estiff[e] + (size_t)c->blocks[e].utsz * c->blocks[e].span) {
+    size_t run = (size_t)bd.ek_rows * bd.span;
+    while (e + 1 < b1 && estiff[e + 1] && estiff[e + 1] == estiff[e] + (size_t)c->blocks[e].ek_rows * c->blocks[e].span) {
       ++e;
-      run += (size_t)c->blocks[e].utsz * c->blocks[e].span;
+      run += (size_t)c->blocks[e].ek_rows * c->blocks[e].span;
     }
     CK(cudaMemcpyAsync(estiff[b], c->s.estiff + bd.estiff_off, run * sizeof(double), cudaMemcpyDeviceToHost, st));
     b = e;
@@ -328,7 +334,7 @@ int download_estiff32(w3g_context* c, double* const* estiff, cudaStream_t st) {
       const BlockDesc& bd = c->blocks[b];
       const float* src = f + bd.estiff_off;
       double* dst = estiff[b];
-      const size_t n = (size_t)bd.utsz * bd.span;
+      const size_t n = (size_t)bd.ek_rows * bd.span;
       for (size_t k = 0; k < n; ++k) dst[k] = src[k];
     }
   };
@@ -363,6 +369,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   m.qbar = md->qbar_flag ? 1 : 0;
   m.beta_fact = md->beta_fact;
   m.bbar_beta = (1.0 - md->eps_bbar) * (1.0 / 3.0);   // bmod.f: beta = (one - eps_stab)*third
+  m.asym = md->asymmetric_assembly ? 1 : 0;
 
   // ---- block table (elblks, iprops, lprops) ----
   std::vector<BlockDesc>& B = c->blocks;
@@ -390,6 +397,11 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     d.etype = ip[0]; d.nnode = ip[1]; d.ngp = ip[5]; d.mat = ip[24];
     d.totdof = d.nnode * ip[3];
     d.utsz = (d.totdof * d.totdof - d.totdof) / 2 + d.totdof;
+    d.ek_rows = md->asymmetric_assembly ? d.totdof * d.totdof : d.utsz;   // tanstf.f:223-225
+    if (md->asymmetric_assembly && d.etype != W3G_ETYPE_L3DISOP) {
+      delete c;
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": asymmetric assembly needs 8-node bricks");
+    }
     // b-bar is an option of the 8-node brick (elprp.f); other types ignore lprops(19)
     d.geonl = lp[17] != 0; d.bbar = lp[18] != 0 && d.etype == W3G_ETYPE_L3DISOP;
     // (etype, nnode, ngp, integration order) with a GPU path
@@ -448,7 +460,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     }
     gp += (long long)d.span * d.ngp;
     cep += 21LL * d.span * d.ngp;
-    est += (long long)d.utsz * d.span;
+    est += (long long)d.ek_rows * d.span;
     einf += (long long)d.totdof * d.span;
     geo += (long long)(3 * d.nnode + 1) * d.span * d.ngp;
     const int ts = type_slot(d.etype);
@@ -715,6 +727,8 @@ int w3g_destroy(w3g_context* c) {
 int w3g_set_tangent_precision(w3g_context* c, int precision) {
   if (!c) return fail(W3G_EARG, "null context");
   if (precision < W3G_TANGENT_FP64 || precision > W3G_TANGENT_BF16X3) return fail(W3G_EARG, "bad precision");
+  if (c->m.asym && precision >= W3G_TANGENT_TF32)
+    return fail(W3G_EUNSUPPORTED, "asymmetric assembly: FP64 and FP32 tangents only");
   CK(cudaSetDevice(c->device));
   if (precision != W3G_TANGENT_FP64 && !c->s.estiff32) {
     CK(dalloc(&c->s.estiff32, (size_t)c->m.estiff_total));
@@ -785,7 +799,7 @@ int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const doubl
   CK(cudaMemcpyAsync(c->s.d_c, hc, (size_t)c->m.ncoord * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->s.d_u, hu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->s.d_du, hdu, (size_t)c->m.nodof * sizeof(double), cudaMemcpyHostToDevice, st));
-  if (estiff && c->precision == W3G_TANGENT_FP64 && c->sched.mode == W3G_SCHED_PER_TYPE)
+  if (estiff && c->precision == W3G_TANGENT_FP64 && c->sched.mode == W3G_SCHED_PER_TYPE && !c->m.asym)
     return tanstf_overlapped(c, estiff, st);
   int r = run_tangent(c, c->s.d_c, c->s.d_u, c->s.d_du, st);
   if (r) return r;

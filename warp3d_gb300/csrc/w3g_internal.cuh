@@ -42,10 +42,11 @@ struct BlockDesc {
   int span;
   int felem;          // 0-based first element
   int etype, nnode, ngp, totdof, utsz, mat;
+  int ek_rows;        // rows of estiff per element: utsz, or totdof^2 (asymmetric assembly)
   int geonl, bbar;
   long long gp_off;     // sum of span*ngp over previous blocks
   long long cep_off;    // sum of 21*span*ngp
-  long long estiff_off; // sum of utsz*span
+  long long estiff_off; // sum of ek_rows*span
   long long einf_off;   // sum of totdof*span (also edest/cdest offset)
   long long geo_off;    // sum of (3*nnode+1)*span*ngp (undeformed-geometry cache)
   long long hist_off;   // sum of hist*span*ngp (material history)
@@ -153,6 +154,7 @@ struct DeviceModel {
   double beta_fact = 1.0;
   double bbar_beta = 1.0 / 3.0;    // bmod's beta = (1 - eps_bbar) / 3
   int has_bbar = 0;                // any 8-node brick block with b-bar
+  int asym = 0;                    // asymmetric assembly: full element matrices
   int nsm = 0;
   int nchunks = 0;                          // recovery work items (partials)
   int nrchunks = 0;                         // of these, items of the three element types
@@ -277,6 +279,7 @@ struct RecoverArgs {
   const IterParams* params;
   double beta_fact;
   double bbar_beta;          // (1 - eps_bbar) / 3
+  int asym;                  // asymmetric assembly: mm10 tangents not symmetrized
   // mm10 blocks
   const CrystalElem* xtal;   // noelem entries (mm10 elements)
   const CrystalType* xtype;
@@ -296,6 +299,9 @@ struct RecoverArgs {
 // (queue counters are reset inside)
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc,
                            int* counter, cudaStream_t s, bool skip_hex8 = false);
+// 8-node brick tangents as full matrices (asymmetric assembly), per-type
+// work items of type slot 0
+cudaError_t launch_tangent_full(const DeviceModel& m, const TangentArgs& a, bool fp32, cudaStream_t s);
 // per-type launches over explicit work-item ranges (first item, count per
 // type); returns the number of kernels launched through *launches
 cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bool fp32, const int* first,

@@ -756,10 +756,12 @@ __device__ bool mm10_gp(const RecoverArgs& a, const IterParams& p, int gp_index,
     }
     for (int k = 0; k < 36; ++k) tangent[k] = x.C[k];
     lu_solve(6, JJ, tangent, 6);
-    double w[36];   // mm10_a_make_symm_1
-    for (int j = 0; j < 6; ++j)
-      for (int r = 0; r < 6; ++r) w[r + 6 * j] = (tangent[r + 6 * j] + tangent[j + 6 * r]) * 0.5;
-    for (int k = 0; k < 36; ++k) tangent[k] = w[k];
+    if (!a.asym) {   // mm10_a_make_symm_1 unless asymmetric assembly (mm10_a.f:1165-1166)
+      double w[36];
+      for (int j = 0; j < 6; ++j)
+        for (int r = 0; r < 6; ++r) w[r + 6 * j] = (tangent[r + 6 * j] + tangent[j + 6 * r]) * 0.5;
+      for (int k = 0; k < 36; ++k) tangent[k] = w[k];
+    }
     // np1 is the full-step solve state (mm10_setup on the whole increment)
     // mm10_update_rotation: wbarp with the lattice spins np1%qs
     double tr[9], RW[9];

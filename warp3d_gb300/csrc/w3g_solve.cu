@@ -585,6 +585,7 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
   const DeviceModel& m = c->m;
   const int n = m.nodof;
   if (m.estiff_total >= INT_MAX) return w3g_fail(W3G_EUNSUPPORTED, "element stiffnesses exceed 2^31 values");
+  if (m.asym) return w3g_fail(W3G_EUNSUPPORTED, "the device assembly and PCG take symmetric element matrices");
   std::vector<int> ed(m.einf_total);
   std::vector<int> ifv_ptr(n + 1);
   std::vector<long long> ifv_src(m.einf_total);

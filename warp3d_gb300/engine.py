@@ -124,7 +124,7 @@ class Engine:
     def _contiguous_ptrs(self, buf: np.ndarray):
         m = self.model
         if not hasattr(self, "_estiff_off"):
-            sizes = np.array(m.spans, dtype=np.uintp) * np.array(m.block_utsz, dtype=np.uintp)
+            sizes = np.array(m.spans, dtype=np.uintp) * np.array(m.block_ek_rows, dtype=np.uintp)
             self._estiff_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uintp) * np.uintp(8)
             self._estiff_total = int(sizes.sum())
         if buf.dtype != np.float64 or not buf.flags.c_contiguous or buf.size != self._estiff_total:

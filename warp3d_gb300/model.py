@@ -310,7 +310,8 @@ class Model:
     never mix types, as in WARP3D)."""
 
     def __init__(self, coords, incid=None, *, parts=None, block_size=128, etype=abi.ETYPE_L3DISOP, geonl=True,
-                 bbar=False, qbar=True, materials=None, block_spans=None, angles=None, dt=1.0, eps_bbar=0.0):
+                 bbar=False, qbar=True, materials=None, block_spans=None, angles=None, dt=1.0, eps_bbar=0.0,
+                 asymmetric=False):
         if parts is None:
             parts = [Part(etype, np.asarray(incid), block_spans, materials)]
         self.coords = np.asarray(coords, dtype=np.float64)
@@ -318,6 +319,8 @@ class Model:
         self.block_size = block_size
         self.geonl, self.bbar, self.qbar = geonl, bbar, qbar
         self.eps_bbar = float(eps_bbar)
+        # "assembly asymmetric on": full column-major element matrices
+        self.asymmetric = bool(asymmetric)
         self.nnode = self.coords.shape[0]
         self.nodof = 3 * self.nnode
         self.ncoord = 3 * self.nnode
@@ -351,6 +354,9 @@ class Model:
         self.block_ngp = [ELEMENT_TYPES[t][1] for t in btype]
         self.block_totdof = [3 * n for n in self.block_nnode]
         self.block_utsz = [d * (d + 1) // 2 for d in self.block_totdof]
+        # rows of estiff_blocks(blk)%ptr: utsz, or totdof**2 with asymmetric
+        # assembly (src/tanstf.f:223-225)
+        self.block_ek_rows = [d * d if self.asymmetric else u for d, u in zip(self.block_totdof, self.block_utsz)]
         self._block_incid = bincid
         self.block_crystal = [isinstance(m, Crystal) for m in bmat]
         self.block_hist = [HIST_MM10 if cr else HIST_MM01 for cr in self.block_crystal]
@@ -372,6 +378,7 @@ class Model:
         self.nnode_el, self.ngp = ELEMENT_TYPES[t0][0], ELEMENT_TYPES[t0][1]
         self.totdof = 3 * self.nnode_el
         self.utsz = self.totdof * (self.totdof + 1) // 2
+        self.ek_rows = self.totdof * self.totdof if self.asymmetric else self.utsz
         self.incid = np.concatenate(bincid) if self.uniform else None
         self._tables()
 
@@ -439,13 +446,16 @@ class Model:
             d.elem_angles = self.elem_angles.ctypes.data_as(C.POINTER(C.c_double))
         d.dt = self.dt
         d.eps_bbar = self.eps_bbar
+        d.asymmetric_assembly = 1 if self.asymmetric else 0
         return d
 
     def new_state(self) -> "HostState":
         return HostState(self)
 
     def estiff_blocks(self):
-        return [np.zeros((s, u)) for s, u in zip(self.spans, self.block_utsz)]
+        """Per block (span, rows): the packed upper triangle (utsz), or with
+        asymmetric assembly the full matrix, column-major (totdof**2)."""
+        return [np.zeros((s, u)) for s, u in zip(self.spans, self.block_ek_rows)]
 
 
 def _ptrs(arrs):

@@ -37,14 +37,21 @@ class Assembler:
 
     def __init__(self, model):
         self.model = model
+        self.full = bool(getattr(model, "asymmetric", False))
         I, J, self.off = [], [], []
         pairs = {}
         for b in range(model.nelblk):
             td = model.block_totdof[b]
+            ed = model.edest[b].astype(np.int64) - 1          # (span, totdof)
+            if self.full:   # column-major full matrices: entry c*totdof + r is (r, c)
+                c, r = np.divmod(np.arange(td * td), td)
+                I.append(ed[:, r].ravel())
+                J.append(ed[:, c].ravel())
+                self.off.append(None)
+                continue
             if td not in pairs:
                 pairs[td] = upper_pairs(td)
             r, c = pairs[td]
-            ed = model.edest[b].astype(np.int64) - 1          # (span, totdof)
             gi, gj = ed[:, r], ed[:, c]
             off = r != c
             I += [gi.ravel(), gj[:, off].ravel()]
@@ -54,10 +61,11 @@ class Assembler:
         self.J = np.concatenate(J)
 
     def assemble(self, estiff_blocks) -> sp.csr_matrix:
-        """estiff_blocks: per block (span, utsz) element matrices."""
+        """estiff_blocks: per block (span, utsz) packed element matrices, or
+        (span, totdof**2) full ones with asymmetric assembly."""
         v = []
         for est, off in zip(estiff_blocks, self.off):
-            v += [est.ravel(), est[:, off].ravel()]
+            v += [est.ravel()] if off is None else [est.ravel(), est[:, off].ravel()]
         n = self.model.nodof
         K = sp.coo_matrix((np.concatenate(v), (self.I, self.J)), shape=(n, n)).tocsr()
         K.sum_duplicates()
