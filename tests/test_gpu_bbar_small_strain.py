@@ -125,12 +125,19 @@ def test_small_displacement_other_types(etype):
 
 
 def test_blocks_with_and_without_bbar():
-    model, nxyz = make_model(n=4, jitter=0.1, spans=[40, 24], bbar=True)
-    model.lprops[40:, 18] = 0            # second block: displacement brick
+    # ragged blocks (40, 23, 1), the middle one a displacement brick: the
+    # b-bar instantiations handle both kinds of block in one launch
+    model, nxyz = make_model(n=4, jitter=0.1, spans=[40, 23, 1], bbar=True)
+    model.lprops[40:63, 18] = 0
     ora, drv, du = loaded_state(model, nxyz, oracle.Oracle, steps=2, strain_per_step=0.0015)
-    eng, o2, errs = _recover_both(model, ora.state, 3, 1, drv.u, du)
-    errs["ke"] = _tangent_err(model, eng, o2, 3, 1, drv.u, du)
-    assert max(errs.values()) <= TOL, errs
+    for sched in (None, dict(mode=abi.SCHED_PERSISTENT, order=abi.ORDER_HEAVY_FIRST)):
+        eng, o2, errs = _recover_both(model, ora.state, 3, 1, drv.u, du, sched=sched)
+        errs["ke"] = _tangent_err(model, eng, o2, 3, 1, drv.u, du)
+        assert max(errs.values()) <= TOL, (sched, errs)
+        for prec, tol in [(abi.TANGENT_FP32, 1e-5), *TOL_TC.items()]:
+            eng.set_precision(prec)
+            err = _tangent_err(model, eng, o2, 3, 1, drv.u, du)
+            assert err <= tol, (sched, prec, err)
 
 
 @pytest.mark.parametrize("opts", [dict(bbar=True), dict(geonl=False, bbar=True)])
