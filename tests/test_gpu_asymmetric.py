@@ -1,9 +1,10 @@
 """Asymmetric assembly ("assembly asymmetric on"): full column-major
 element matrices (totdof², span) for 8-node bricks (gptns1.f bdbt_asym,
 kg1.f's asymmetric branch, tanstf.f:223-225) and mm10 tangents left
-unsymmetrized (mm10_a.f:1165-1166). The CUDA engine against the oracle at
-the plain path's 1e-12 (FP32: 1e-5); the tensor-core forms, other element
-types and the symmetric-only device solver are refused."""
+unsymmetrized (mm10_a.f:1165-1166); 20-node bricks and tetrahedra (mm01)
+through their packed items and an expansion. The CUDA engine against the
+oracle at the plain path's 1e-12 (FP32: 1e-5); the tensor-core forms and
+the symmetric-only device solver are refused."""
 import numpy as np
 import pytest
 
@@ -78,12 +79,40 @@ def test_crystal_full_unsymmetric_matrices():
     assert asym > 1e-8
 
 
+@pytest.mark.parametrize("etype,spans", [(abi.ETYPE_Q3DISOP, [5, 3]), (abi.ETYPE_TET10, [30, 18])])
+def test_other_types_full_matrices(etype, spans):
+    # 20-node bricks and tetrahedra (mm01): packed work items, expanded
+    model, nxyz = make_model(n=2, jitter=0.08, spans=spans, etype=etype, asymmetric=True)
+    tot = model.totdof
+    assert model.estiff_blocks()[0].shape == (spans[0], tot * tot)
+    ora, drv, du = loaded_state(model, nxyz, oracle.Oracle, steps=2, strain_per_step=0.0015)
+    eng, o2, errs, ko = _pair(model, ora.state, 3, 1, False, drv.u, du)
+    print(etype, {k: f"{v:.1e}" for k, v in errs.items()})
+    assert max(errs.values()) <= 1e-12, errs
+    eng.set_precision(abi.TANGENT_FP32)
+    kg = model.estiff_blocks()
+    eng.tanstf(3, 1, model.c, drv.u, du, kg)
+    assert max(rel_err(g, o, axis=1) for g, o in zip(kg, ko)) <= 1e-5
+
+
+def test_mixed_types_full_matrices():
+    from warp3d_gb300.model import Bilinear, Part, cube_mesh_hex20
+    c8, i8 = cube_mesh(2, jitter=0.05)
+    c20, i20 = cube_mesh_hex20(2, jitter=0.05)
+    # two disconnected parts: bricks, then 20-node bricks shifted aside
+    off = c8.shape[0]
+    coords = np.vstack([c8, c20 + np.array([5.0, 0.0, 0.0])])
+    mat = Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)
+    model = Model(coords, parts=[Part(abi.ETYPE_L3DISOP, i8, [8], [mat]),
+                                 Part(abi.ETYPE_Q3DISOP, i20 + off, [8], [mat])], asymmetric=True)
+    du = np.random.default_rng(4).normal(0.0, 1e-4, model.nodof)
+    state = model.new_state()
+    eng, o2, errs, ko = _pair(model, state, 1, 1, False, np.zeros(model.nodof), du)
+    assert max(errs.values()) <= 1e-12, errs
+
+
 def test_refusals():
     coords, incid = cube_mesh(2)
-    from warp3d_gb300.model import cube_mesh_hex20
-    c20, i20 = cube_mesh_hex20(1)
-    with pytest.raises(abi.W3GError):
-        _engine(Model(c20, i20, etype=abi.ETYPE_Q3DISOP, asymmetric=True))
     from warp3d_gb300.solver import DeviceCsr
     with pytest.raises(abi.W3GError):
         DeviceCsr(_engine(Model(coords, incid, asymmetric=True)))

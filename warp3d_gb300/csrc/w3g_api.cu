@@ -48,6 +48,7 @@ void free_all(w3g_context* c) {
                   s.geo, s.c_geo, s.geo_dirty,
                   s.hist, s.hist1, s.urcs_n, s.urcs_n1, s.eps_n, s.eps_n1, s.rot_n1, s.cep, s.estiff,
                   s.estiff32, s.einf, s.evol, s.partials, s.ifv_partials, s.status, s.d_info,
+                  m.blocks_packed, s.estiff_packed, s.estiff_packed32,
                   s.d_c, s.d_u, s.d_du, s.d_ifv};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -139,10 +140,25 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
 int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const double* d_du, cudaStream_t st) {
   TangentArgs a = tangent_args(c, d_c, d_u, d_du);
   const int p = c->precision;
-  if (c->m.asym) {   // asymmetric assembly: full 8-node brick matrices
-    cudaError_t e = launch_tangent_full(c->m, a, p != W3G_TANGENT_FP64, st);
+  if (c->m.asym) {   // asymmetric assembly: full matrices
+    const bool f32 = p != W3G_TANGENT_FP64;
+    cudaError_t e = launch_tangent_full(c->m, a, f32, st);   // 8-node bricks, any [D]
+    int n = c->m.ttype_chunks[0] > 0 ? 1 : 0;
+    if (e == cudaSuccess && c->m.packed_total > 0) {
+      // 20-node bricks and tetrahedra (mm01, symmetric [D]): packed into
+      // the scratch array, then expanded
+      TangentArgs ap = a;
+      ap.blocks = c->m.blocks_packed;
+      ap.estiff = f32 ? (void*)c->s.estiff_packed32 : (void*)c->s.estiff_packed;
+      int first[kNumTypes], count[kNumTypes], k = 0;
+      for (int t = 0; t < kNumTypes; ++t) { first[t] = c->m.ttype_chunk0[t]; count[t] = t == 0 ? 0 : c->m.ttype_chunks[t]; }
+      e = launch_tangent_ranges(c->m, ap, f32, first, count, st, &k);
+      n += k;
+      if (e == cudaSuccess) e = launch_expand_packed(c->m, a, ap.estiff, f32, st);
+      ++n;
+    }
     if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
-    return c->m.ttype_chunks[0] > 0 ? 1 : 0;
+    return n;
   }
   const bool tc = p >= W3G_TANGENT_TF32;
   cudaError_t e = cudaSuccess;
@@ -398,9 +414,9 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     d.totdof = d.nnode * ip[3];
     d.utsz = (d.totdof * d.totdof - d.totdof) / 2 + d.totdof;
     d.ek_rows = md->asymmetric_assembly ? d.totdof * d.totdof : d.utsz;   // tanstf.f:223-225
-    if (md->asymmetric_assembly && d.etype != W3G_ETYPE_L3DISOP) {
+    if (md->asymmetric_assembly && d.etype != W3G_ETYPE_L3DISOP && d.mat == W3G_MAT_CRYSTAL) {
       delete c;
-      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": asymmetric assembly needs 8-node bricks");
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": mm10 needs 8-node bricks");
     }
     // b-bar is an option of the 8-node brick (elprp.f); other types ignore lprops(19)
     d.geonl = lp[17] != 0; d.bbar = lp[18] != 0 && d.etype == W3G_ETYPE_L3DISOP;
@@ -515,6 +531,15 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     return fail(W3G_EARG, "blocks do not cover all elements");
   }
   m.ngp_total = gp; m.cep_total = cep; m.estiff_total = est; m.einf_total = einf; m.geo_total = geo;
+  // asymmetric assembly: packed offsets of the 20-node brick / tetrahedron
+  // blocks in the scratch array their matrices are expanded from
+  std::vector<BlockDesc> Bp(B);
+  if (m.asym)
+    for (int b = 0; b < md->nelblk; ++b)
+      if (B[b].etype != W3G_ETYPE_L3DISOP) {
+        Bp[b].estiff_off = m.packed_total;
+        m.packed_total += (long long)B[b].utsz * B[b].span;
+      }
   m.hist_total = hist;
   m.nchunks = (int)chunks.size();
 
@@ -644,6 +669,10 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(s.rot_n1, 9 * gp);
   AL(s.cep, cep);
   AL(s.estiff, est);
+  if (m.packed_total > 0) {
+    AL(m.blocks_packed, md->nelblk);
+    AL(s.estiff_packed, m.packed_total);
+  }
   AL(s.einf, einf);
   AL(s.evol, md->noelem);
   AL(s.geo, geo);
@@ -668,6 +697,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   cudaStream_t st = c->stream;
 #define UP(d, h, n) if (e == cudaSuccess) e = cudaMemcpyAsync(d, h, (size_t)(n) * sizeof(*(h)), cudaMemcpyHostToDevice, st)
   UP(m.blocks, B.data(), md->nelblk);
+  if (m.packed_total > 0) UP(m.blocks_packed, Bp.data(), md->nelblk);
   UP(m.chunks, chunks.data(), m.nchunks);
   UP(m.tchunks, tchunks.data(), m.ntchunks);
   UP(m.tcchunks, tcchunks.data(), m.ntcchunks);
@@ -734,6 +764,8 @@ int w3g_set_tangent_precision(w3g_context* c, int precision) {
     CK(dalloc(&c->s.estiff32, (size_t)c->m.estiff_total));
     CK(cudaMemsetAsync(c->s.estiff32, 0, (size_t)c->m.estiff_total * sizeof(float), c->stream));
   }
+  if (precision != W3G_TANGENT_FP64 && c->m.packed_total > 0 && !c->s.estiff_packed32)
+    CK(dalloc(&c->s.estiff_packed32, (size_t)c->m.packed_total));
   c->precision = precision;
   return 0;
 }

@@ -155,6 +155,11 @@ struct DeviceModel {
   double bbar_beta = 1.0 / 3.0;    // bmod's beta = (1 - eps_bbar) / 3
   int has_bbar = 0;                // any 8-node brick block with b-bar
   int asym = 0;                    // asymmetric assembly: full element matrices
+  // asymmetric assembly with 20-node bricks or tetrahedra (mm01, symmetric
+  // [D]): their packed matrices go to a scratch array first (block table
+  // with packed offsets), then are expanded to the full layout
+  BlockDesc* blocks_packed = nullptr;
+  long long packed_total = 0;
   int nsm = 0;
   int nchunks = 0;                          // recovery work items (partials)
   int nrchunks = 0;                         // of these, items of the three element types
@@ -201,6 +206,8 @@ struct DeviceState {
   double* cep = nullptr;     // cep_total
   double* estiff = nullptr;  // estiff_total (FP64 form)
   float* estiff32 = nullptr; // estiff_total (FP32 form), lazily allocated
+  double* estiff_packed = nullptr;   // packed_total (asymmetric assembly scratch)
+  float* estiff_packed32 = nullptr;  // the same for the FP32 form, lazily allocated
   double* einf = nullptr;    // einf_total
   double* evol = nullptr;    // noelem
   // undeformed geometry per GP (dN/dX, det[J0]) and the coordinates it
@@ -302,6 +309,11 @@ cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32
 // 8-node brick tangents as full matrices (asymmetric assembly), per-type
 // work items of type slot 0
 cudaError_t launch_tangent_full(const DeviceModel& m, const TangentArgs& a, bool fp32, cudaStream_t s);
+// asymmetric assembly of 20-node bricks and tetrahedra: the packed
+// matrices (written through m.blocks_packed into `packed`) expanded to the
+// full column-major layout of a.estiff
+cudaError_t launch_expand_packed(const DeviceModel& m, const TangentArgs& a, const void* packed, bool fp32,
+                                 cudaStream_t s);
 // per-type launches over explicit work-item ranges (first item, count per
 // type); returns the number of kernels launched through *launches
 cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bool fp32, const int* first,

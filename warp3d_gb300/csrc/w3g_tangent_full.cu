@@ -20,6 +20,11 @@
 //   store    the column-major matrix staged in shared memory, written with
 //            coalesced stores
 // The FP64 instantiation is the plain form, FP32 the precision form.
+//
+// 20-node bricks and tetrahedra under asymmetric assembly (mm01: a
+// symmetric [D]) take their usual packed work items, written to a scratch
+// array, and k_expand_packed mirrors each packed upper triangle into the
+// full column-major matrix.
 #include "w3g_tangent_items.cuh"
 
 namespace w3g {
@@ -233,7 +238,42 @@ __global__ void __launch_bounds__(32) k_tangent_full_hex8(TangentArgs a) {
   }
 }
 
+// full column-major matrices from packed upper triangles (column-packed,
+// pos = c(c+1)/2 + r for r <= c), one CTA per tangent work item
+template <class T>
+__global__ void __launch_bounds__(256) k_expand_packed(const Chunk* chunks, int chunk0, const BlockDesc* blocks,
+                                                      const BlockDesc* blocks_packed, const T* packed, T* full) {
+  const Chunk ch = chunks[chunk0 + blockIdx.x];
+  const BlockDesc bd = blocks[ch.blk];
+  const long long pbase = blocks_packed[ch.blk].estiff_off;
+  const int tot = bd.totdof, nn = tot * tot;
+  for (int e = 0; e < ch.n; ++e) {
+    const int i = ch.i0 + e;
+    const T* src = packed + pbase + (long long)i * bd.utsz;
+    T* dst = full + bd.estiff_off + (long long)i * nn;
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+      const int c = k / tot, r = k - c * tot;
+      const int lo = r < c ? r : c, hi = r < c ? c : r;
+      dst[k] = src[hi * (hi + 1) / 2 + lo];
+    }
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_expand_packed(const DeviceModel& m, const TangentArgs& a, const void* packed, bool fp32,
+                                 cudaStream_t s) {
+  const int n = m.ttype_chunks[1] + m.ttype_chunks[2];
+  if (n == 0) return cudaSuccess;
+  const int c0 = m.ttype_chunks[1] > 0 ? m.ttype_chunk0[1] : m.ttype_chunk0[2];
+  if (fp32)
+    k_expand_packed<float><<<n, 256, 0, s>>>(a.chunks, c0, m.blocks, m.blocks_packed, (const float*)packed,
+                                            (float*)a.estiff);
+  else
+    k_expand_packed<double><<<n, 256, 0, s>>>(a.chunks, c0, m.blocks, m.blocks_packed, (const double*)packed,
+                                             (double*)a.estiff);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_tangent_full(const DeviceModel& m, const TangentArgs& a, bool fp32, cudaStream_t s) {
   if (m.ttype_chunks[0] == 0) return cudaSuccess;
