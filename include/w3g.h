@@ -139,7 +139,8 @@ typedef struct w3g_model_desc {
                                    matrices, column-major per element
                                    (gptns1.f bdbt_asym, tanstf.f:223-225),
                                    mm10 tangents not symmetrized
-                                   (mm10_a.f:1165-1166); 8-node bricks */
+                                   (mm10_a.f:1165-1166); FP64 and FP32
+                                   tangent forms */
 } w3g_model_desc;
 
 /*
