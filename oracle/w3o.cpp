@@ -973,8 +973,12 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
       }
       for (int i = 0; i < span; ++i) dfn1_all[(size_t)g * MXVL + i] = dfn1[i];
     } else {
-      // rstgp2: det[J] of rknstr_sm_displ
-      for (int i = 0; i < span; ++i) det_j[g][i] = det_j_mid[g][i];
+      // rstgp2: det[J] of rknstr_sm_displ; drive_10_update sets the
+      // rotations of small-displacement blocks to identity (rstgp1.f:4415-4432)
+      for (int i = 0; i < span; ++i) {
+        det_j[g][i] = det_j_mid[g][i];
+        for (int k = 0; k < 9; ++k) rot[g](i, k) = (k % 4 == 0) ? one : zero;
+      }
     }
     // gtlsn1 (src/gtlsn1.f:25-85), with bmod for b-bar
     b.zero();
@@ -1433,7 +1437,6 @@ int w3o_tanstf(const w3g_model_desc* m, const w3g_block_state* s, int step, int 
   for (int blk = 0; blk < m->nelblk; ++blk) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
-    if (B.mat_type == W3G_MAT_CRYSTAL && !B.geonl) return W3G_EUNSUPPORTED;
   }
 #ifdef _OPENMP
   if (g_threads > 0) omp_set_num_threads(g_threads);
@@ -1459,11 +1462,10 @@ int w3o_recover(const w3g_model_desc* m, const w3g_block_state* s, int step, int
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
     if (B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL) return W3G_EUNSUPPORTED;
-    // mm10 is restated on the finite-strain path only. With b-bar WARP3D
-    // also scales F_n and F_n+1 to F-bar (gtmat1_make_fbar, gtmat1.f:145-151),
-    // but only UMATs read those (rstgp1.f:3786-3787): mm10 blocks take the
-    // b-bar strain increment, internal forces and tangent restated here.
-    if (B.mat_type == W3G_MAT_CRYSTAL && !B.geonl) return W3G_EUNSUPPORTED;
+    // With b-bar WARP3D also scales F_n and F_n+1 of mm10 blocks to F-bar
+    // (gtmat1_make_fbar, gtmat1.f:145-151), but only UMATs read those
+    // (rstgp1.f:3786-3787): mm10 blocks take the b-bar strain increment,
+    // internal forces and tangent restated here.
     if (B.mat_type == W3G_MAT_CRYSTAL && (!m->crystals || !m->elem_crystal || !m->elem_angles))
       return W3G_EARG;
   }

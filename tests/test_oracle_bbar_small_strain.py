@@ -187,15 +187,24 @@ def test_small_strain_uniaxial_closed_form(etype):
         assert np.max(np.abs(np.concatenate(st.urcs_n)[:, :, [0, 1, 3, 4, 5]])) < 1e-7 * sy
 
 
-@pytest.mark.parametrize("geonl,bbar", [(False, False), (False, True)])
-def test_crystal_blocks_need_the_finite_strain_path(geonl, bbar):
-    coords, incid = cube_mesh(1)
-    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(1, 3), geonl=geonl, bbar=bbar)
+@pytest.mark.parametrize("bbar", [False, True])
+def test_crystal_small_displacement_elastic_limit(bbar):
+    # mm10 on small-displacement blocks: identity rotations
+    # (drive_10_update, rstgp1.f:4415-4432), the increment B du; a small
+    # elastic increment gives sigma = C eps with the stored tangent C
+    coords, incid = cube_mesh(2, jitter=0.05)
+    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(8, 3), geonl=False, bbar=bbar)
     ora = oracle.Oracle(model)
-    z = np.zeros(model.nodof)
-    st, _ = ora.recover(1, 0, False, model.c, z, z, z.copy())
-    assert st == abi.EUNSUPPORTED
-    assert ora.tanstf(1, 0, model.c, z, z, model.estiff_blocks()) == abi.EUNSUPPORTED
+    du = np.random.default_rng(5).normal(0.0, 1e-7, model.nodof)
+    st, _ = ora.recover(1, 1, False, model.c, np.zeros(model.nodof), du, np.zeros(model.nodof))
+    assert st == 0
+    s1 = ora.state
+    eps = np.concatenate(s1.eps_n1).reshape(-1, 6)
+    sig = np.concatenate(s1.urcs_n1)[..., :6].reshape(-1, 6)
+    C = np.concatenate(s1.history1)[..., :36].reshape(-1, 6, 6)   # column-major -> C^T
+    pred = np.einsum("gji,gj->gi", C, eps)
+    assert rel_err(sig, pred) < 1e-6
+    assert np.array_equal(np.concatenate(s1.rot_n1), np.concatenate(model.new_state().rot_n1))
 
 
 def test_crystal_bbar_brick_runs_and_keeps_rigid_modes():

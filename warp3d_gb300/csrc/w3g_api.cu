@@ -456,13 +456,9 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
         }
       }
     }
-    if (d.mat == W3G_MAT_CRYSTAL && !d.geonl) {
-      // mm10 blocks with b-bar: WARP3D also forms F-bar (gtmat1_make_fbar),
-      // which only UMATs read (rstgp1.f:3786-3787); mm10 sees the b-bar
-      // strain increment, internal forces and tangent, as built here
-      delete c;
-      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": mm10 needs geonl");
-    }
+    // mm10 blocks with b-bar: WARP3D also forms F-bar (gtmat1_make_fbar),
+    // which only UMATs read (rstgp1.f:3786-3787); mm10 sees the b-bar
+    // strain increment, internal forces and tangent, as built here
     if (d.bbar) m.has_bbar = 1;
     d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf; d.geo_off = geo;
     d.hist = d.mat == W3G_MAT_CRYSTAL ? kHistMM10 : kHistMM01;

@@ -102,29 +102,39 @@ __global__ void __launch_bounds__(kRecoverThreads) k_mm10_kin(RecoverArgs a, int
   } else {
     for (int k = 0; k < 3 * NN; ++k) tg0[k] = geo[k];
   }
-  double th1[9], thh[9];
-  for (int k = 0; k < 9; ++k) { th1[k] = 0.0; thh[k] = 0.0; }
-  for (int n = 0; n < NN; ++n) {
-    const double tx = tg0[3 * n], ty = tg0[3 * n + 1], tz = tg0[3 * n + 2];
-    const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]), u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
-    const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
-                 uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
-    th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
-    th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
-    th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
-    thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
-    thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
-    thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+  // finite strain: gtmat1 in reference order; small displacement: no
+  // deformation gradient, rotations = identity (drive_10_update,
+  // rstgp1.f:4415-4432)
+  double F1[9], Fh[9], R1[9], Rh[9];
+  double dfn1 = 1.0, dfh = 1.0;
+  if (bd.geonl) {
+    double th1[9], thh[9];
+    for (int k = 0; k < 9; ++k) { th1[k] = 0.0; thh[k] = 0.0; }
+    for (int n = 0; n < NN; ++n) {
+      const double tx = tg0[3 * n], ty = tg0[3 * n + 1], tz = tg0[3 * n + 2];
+      const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]), u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
+      const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
+                   uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
+      th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
+      th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
+      th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
+      thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
+      thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
+      thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+    }
+    F1[0] = th1[0] + 1.0; F1[1] = th1[1]; F1[2] = th1[2]; F1[3] = th1[3]; F1[4] = th1[4] + 1.0;
+    F1[5] = th1[5]; F1[6] = th1[6]; F1[7] = th1[7]; F1[8] = th1[8] + 1.0;
+    Fh[0] = thh[0] + 1.0; Fh[1] = thh[1]; Fh[2] = thh[2]; Fh[3] = thh[3]; Fh[4] = thh[4] + 1.0;
+    Fh[5] = thh[5]; Fh[6] = thh[6]; Fh[7] = thh[7]; Fh[8] = thh[8] + 1.0;
+    dfn1 = det_ref(F1);
+    dfh = det_ref(Fh);
+    if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
+    else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
+    polar_rotation_ref(F1, R1);
+    polar_rotation_ref(Fh, Rh);
+  } else {
+    for (int k = 0; k < 9; ++k) F1[k] = Fh[k] = R1[k] = Rh[k] = (k % 4 == 0) ? 1.0 : 0.0;
   }
-  const double F1[9] = {th1[0] + 1.0, th1[1], th1[2], th1[3], th1[4] + 1.0, th1[5], th1[6], th1[7], th1[8] + 1.0};
-  const double Fh[9] = {thh[0] + 1.0, thh[1], thh[2], thh[3], thh[4] + 1.0, thh[5], thh[6], thh[7], thh[8] + 1.0};
-  const double dfn1 = det_ref(F1);
-  const double dfh = det_ref(Fh);
-  if (dfn1 <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 0, i));
-  else if (dfh <= 1.0e-20) atomicMin(a.status, bad_point_key(ch.blk, g, 1, i));
-  double R1[9], Rh[9];
-  polar_rotation_ref(F1, R1);
-  polar_rotation_ref(Fh, Rh);
   double dth[9], L[9];
   for (int k = 0; k < 9; ++k) dth[k] = 0.0;
   for (int n = 0; n < NN; ++n) {
@@ -164,7 +174,8 @@ __global__ void __launch_bounds__(kRecoverThreads) k_mm10_kin(RecoverArgs a, int
     ddt[0] += cb; ddt[1] += cb; ddt[2] += cb;
   }
   double uddt[6];
-  rotate_to_unrotated(Rh, ddt, uddt);
+  if (bd.geonl) rotate_to_unrotated(Rh, ddt, uddt);
+  else for (int k = 0; k < 6; ++k) uddt[k] = ddt[k];   // rstgp2: the increment as it is
   for (int k = 0; k < 6; ++k) a.eps_n1[gpi * 6 + k] = a.eps_n[gpi * 6 + k] + uddt[k];
   if (p.iter > 0 && bd.geonl)
     for (int k = 0; k < 9; ++k) a.rot_n1[gpi * 9 + k] = R1[k];
