@@ -87,6 +87,11 @@ TANGENT_BYTES_PER_ELEM = 8 * (21 * 8 + 24 + 48 + 18 * 8 + 300)
 TANGENT32_BYTES_PER_ELEM = TANGENT_BYTES_PER_ELEM - 4 * 300
 RECOVER_BYTES_PER_ELEM = 6016
 
+# precision forms of the tangent on the tensor cores, and the one the
+# headline "mixed" figure reports
+TC_FORMS = (("tf32", 2), ("bf16", 3), ("tf32x3", 4), ("bf16x3", 5))
+HEADLINE_FORM = "tf32"
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -105,6 +110,7 @@ def parse():
     ap.add_argument("--crystal-n", type=int, default=32, help="elements per cube edge of the mm10 workload")
     ap.add_argument("--no-solver", action="store_true", help="skip the device assembly / PCG measurement")
     ap.add_argument("--no-formulations", action="store_true", help="skip the b-bar / small-displacement lines")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks on sampled blocks")
     ap.add_argument("--precision-study", action="store_true",
                     help="instead of the bench line: Newton solves of the cube under every tangent precision form")
     ap.add_argument("--study-steps", type=int, default=20)
@@ -246,6 +252,12 @@ def bench_batched(args, dev, local):
                      "per_type_direct": {"value": ne / (ms_pt * 1e-3), "ms_per_step": ms_pt},
                      "gpu_launches": launches}
     out["mixed"]["speedup_vs_plain"] = out["plain_fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    if not args.no_parity:
+        # 16 blocks of each element type against the oracle, same state
+        eng.set_schedule(mode=abi.SCHED_PER_TYPE)
+        blocks = spread_blocks(model, 16, types=(abi.ETYPE_L3DISOP, abi.ETYPE_Q3DISOP, abi.ETYPE_TET10))
+        out["parity"] = parity_sample(eng, model, blocks, 2, 1, False, model.c, u1, du, p, stream,
+                                      precisions=(("fp32", abi.TANGENT_FP32), ("tf32", abi.TANGENT_TF32)))
     names = {abi.ETYPE_L3DISOP: "hex8", abi.ETYPE_Q3DISOP: "hex20", abi.ETYPE_TET10: "tet10"}
     res = {"workload": "mixed hex8/hex20/tet10 bars 64x64 cells in section, random blocks [16,128], "
                        "per-block yield U(250,550) MPa, jitter 0.05h, 1 Newton iteration = recovery + tangent",
@@ -345,6 +357,10 @@ def bench_crystal(args, dev, local, with_cpu):
     out["local_newton_iterations"] = {"min": int(its.min()), "mean": float(its.mean()), "max": int(its.max()),
                                       "p99": float(np.percentile(its, 99)),
                                       "histogram": {int(k): int(v) for k, v in enumerate(hist) if v}}
+    if not args.no_parity:
+        eng.set_schedule(mode=abi.SCHED_PER_TYPE, order=abi.ORDER_HEAVY_FIRST)
+        out["parity"] = parity_sample(eng, model, spread_blocks(model, 16), step + 1, 1, False, model.c, u, du, p,
+                                      stream, precisions=(("fp32", abi.TANGENT_FP32), ("tf32", abi.TANGENT_TF32)))
     if with_cpu:
         # CPU baseline leg: the oracle on the first 16 blocks (2,048
         # elements) of the same state
@@ -356,7 +372,7 @@ def bench_crystal(args, dev, local, with_cpu):
         sst = sub.new_state()
         for name in sst.NAMES:
             setattr(sst, name, [a.copy() for a in getattr(st, name)[:nb]])
-        ora = oracle.Oracle(sub, state=sst, threads=host_threads())
+        ora = oracle.Oracle(sub, state=sst, threads=host_threads(), fast=True)
         ifv = np.zeros(model.nodof)
         est = sub.estiff_blocks()
         t0 = time.perf_counter()
@@ -366,7 +382,8 @@ def bench_crystal(args, dev, local, with_cpu):
             ora.tanstf(step + 1, 1, model.c, u, du, est)
         t_cpu = (time.perf_counter() - t0) / reps
         out["cpu_baseline"] = {"value": sub.noelem / t_cpu, "unit": UNIT, "cores": host_threads(), "kind": "port",
-                               "sample": f"{sub.noelem} elements ({nb} blocks of 128) of the same state, {reps} iterations"}
+                               "sample": f"{sub.noelem} elements ({nb} blocks of 128) of the same state, {reps} iterations",
+                               "build": oracle.FAST_FLAGS}
     eng.close()
     return {"workload": f"{n}^3 hex8 l3disop geonl, mm10 fcc Voce (tau_y 90, tau_v 200, theta_0 500 MPa, n 20), "
                         "random orientations, state after 1% tension in 10 steps",
@@ -529,14 +546,180 @@ def load_traffic():
     return {}
 
 
-def cpu_baseline(model_n, nblocks, threads, reps=8):
-    """Times the oracle (CPU restatement, OpenMP over blocks) on the first
-    `nblocks` element blocks of the same workload: one recovery + one
-    tangent per rep, like a Newton iteration."""
+# ---- parity at the benchmark's own sizes ---------------------------------
+# The oracle (the CPU restatement, checker build) replays one Newton
+# iteration of element work on a sample of blocks of the benchmark model:
+# the sample blocks' state is read from the device before a GPU iteration,
+# the GPU iteration runs on the whole model, its outputs for the sample
+# blocks are read back, and the oracle runs the same iteration on a model
+# made of the sample blocks alone (same nodes, materials, orientations),
+# from the same state. Outside every timed region.
+
+PARITY_ARRAYS = ("urcs_n1", "eps_n1", "rot_n1", "history1", "cep", "einfvec", "element_vol")
+
+
+def sub_model(model, blocks):
+    """A model holding only `blocks` of `model` (one part per block, in the
+    given order) over the nodes they use, and that node map."""
+    from warp3d_gb300.model import Model, Part
+    incs = [model._block_incid[b] for b in blocks]
+    used = np.unique(np.concatenate([i.ravel() for i in incs]))
+    remap = -np.ones(model.nnode, dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    parts = [Part(model.block_etype[b], remap[model._block_incid[b]], [model.spans[b]], [model.block_material[b]])
+             for b in blocks]
+    angles = None
+    if model.crystals:
+        angles = np.concatenate([model.elem_angles[model.felem[b]:model.felem[b] + model.spans[b]] for b in blocks])
+    sub = Model(model.coords[used], parts=parts, geonl=model.geonl, bbar=model.bbar, qbar=model.qbar,
+                angles=angles, dt=model.dt, eps_bbar=model.eps_bbar, asymmetric=model.asymmetric)
+    dofs = (3 * used[:, None] + np.arange(3)[None, :]).ravel()
+    return sub, dofs
+
+
+def _scatter_struct(model, sub_state, blocks, names):
+    """BlockState of the full model whose block pointers point into
+    sub_state for `blocks` and are NULL elsewhere."""
+    from warp3d_gb300 import abi
+    st, keep = abi.BlockState(), []
+    for name in names:
+        addr = np.zeros(model.nelblk, dtype=np.uintp)
+        for k, b in enumerate(blocks):
+            addr[b] = getattr(sub_state, name)[k].__array_interface__["data"][0]
+        arr = (C.c_void_p * model.nelblk).from_buffer(addr)
+        keep.append((addr, arr))
+        setattr(st, name, C.cast(arr, C.POINTER(C.POINTER(C.c_double))))
+    return st, keep
+
+
+def _download_blocks(eng, model, sub, blocks, names):
+    from warp3d_gb300 import abi
+    state = sub.new_state()
+    st, keep = _scatter_struct(model, state, blocks, names)
+    abi.check(eng.lib, eng.lib.w3g_state_download(eng.ctx, C.byref(st)))
+    del keep
+    return state
+
+
+def _estiff_blocks(eng, model, blocks):
+    """Element stiffnesses of `blocks` from the device (FP64 or FP32, as the
+    engine's current precision form stores them), as float64 (span, rows)."""
+    import torch
+    from warp3d_gb300 import abi
+    torch.cuda.synchronize()
+    ptr, _ = eng.estiff_device()
+    f32 = eng.precision != abi.TANGENT_FP64
+    sizes = np.array(model.spans, dtype=np.int64) * np.array(model.block_ek_rows, dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    cudart = C.CDLL("libcudart.so")
+    out = []
+    for b in blocks:
+        a = np.empty((model.spans[b], model.block_ek_rows[b]), dtype=np.float32 if f32 else np.float64)
+        rc = cudart.cudaMemcpy(C.c_void_p(a.ctypes.data), C.c_void_p(ptr + int(offs[b]) * a.itemsize),
+                               C.c_size_t(a.nbytes), 2)
+        assert rc == 0, f"cudaMemcpy {rc}"
+        out.append(a.astype(np.float64))
+    return out
+
+
+def _ke_err(got, ref):
+    """max over elements of max|dKe| / max|Ke| (per-element relative)."""
+    worst = 0.0
+    for g, o in zip(got, ref):
+        den = np.max(np.abs(o), axis=1)
+        worst = max(worst, float(np.max(np.max(np.abs(g - o), axis=1) / np.where(den > 0, den, 1.0))))
+    return worst
+
+
+def parity_sample(eng, model, blocks, step, it, extrap, c, u, du, dptrs, stream, precisions=()):
+    """One GPU Newton iteration (recovery, then tangent) of the whole model
+    against the oracle on `blocks`; returns the max relative error per
+    output array, per-element for Ke, and for each precision form in
+    `precisions` ((name, code) pairs) its Ke error against the oracle's
+    FP64 Ke on the same blocks."""
+    import torch
+    import oracle
+    from warp3d_gb300 import abi
+    from warp3d_gb300.model import HostState
+    blocks = [int(b) for b in blocks]
+    sub, dofs = sub_model(model, blocks)
+    prec0 = eng.precision
+    eng.set_precision(abi.TANGENT_FP64)
+    pre = _download_blocks(eng, model, sub, blocks, HostState.NAMES)
+    d_c, d_u, d_du, d_ifv = dptrs
+    with torch.cuda.stream(stream):
+        eng.recover_dev(step, it, extrap, d_c, d_u, d_du, d_ifv, stream.cuda_stream)
+        eng.tanstf_dev(step, it, d_c, d_u, d_du, stream.cuda_stream)
+    torch.cuda.synchronize()
+    st_gpu, _ = eng.recover_info()
+    post = _download_blocks(eng, model, sub, blocks, PARITY_ARRAYS)
+    ke_gpu = _estiff_blocks(eng, model, blocks)
+    ora = oracle.Oracle(sub, state=pre, threads=host_threads())
+    ifv = np.zeros(sub.nodof)
+    st_ora, _ = ora.recover(step, it, extrap, sub.c, np.ascontiguousarray(u[dofs]), np.ascontiguousarray(du[dofs]),
+                            ifv)
+    ke_ora = sub.estiff_blocks()
+    ora.tanstf(step, it, sub.c, np.ascontiguousarray(u[dofs]), np.ascontiguousarray(du[dofs]), ke_ora)
+    res = {"blocks": len(blocks), "elements": sub.noelem, "status_gpu": int(st_gpu), "status_oracle": int(st_ora)}
+    for name in PARITY_ARRAYS:
+        g = np.concatenate([a.ravel() for a in getattr(post, name)])
+        o = np.concatenate([a.ravel() for a in getattr(ora.state, name)])
+        den = float(np.max(np.abs(o)))
+        res[name] = float(np.max(np.abs(g - o)) / den) if den > 0 else float(np.max(np.abs(g)))
+    res["estiff"] = _ke_err(ke_gpu, ke_ora)
+    res["max_fp64"] = max(res[k] for k in (*PARITY_ARRAYS, "estiff"))
+    if precisions:
+        res["estiff_precision_forms"] = {}
+        for name, code in precisions:
+            eng.set_precision(code)
+            with torch.cuda.stream(stream):
+                eng.tanstf_dev(step, it, d_c, d_u, d_du, stream.cuda_stream)
+            torch.cuda.synchronize()
+            res["estiff_precision_forms"][name] = _ke_err(_estiff_blocks(eng, model, blocks), ke_ora)
+    eng.set_precision(prec0)
+    return res
+
+
+def spread_blocks(model, k, types=None):
+    """k blocks spread evenly over the model (per element type if `types`)."""
+    if types is None:
+        return np.unique(np.linspace(0, model.nelblk - 1, k).round().astype(int)).tolist()
+    out = []
+    for t in types:
+        bs = [b for b in range(model.nelblk) if model.block_etype[b] == t]
+        if bs:
+            out += [bs[i] for i in np.unique(np.linspace(0, len(bs) - 1, k).round().astype(int))]
+    return out
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_baseline(model_n, nblocks, threads, reps=8, warmup=1):
+    """Times the oracle (CPU restatement, OpenMP over blocks, compiled with
+    multiply-add contraction as WARP3D's ifort -O3 build is) on the first
+    `nblocks` element blocks of the same workload (None: all of it): one
+    recovery + one tangent per rep, like a Newton iteration."""
     import oracle
     from warp3d_gb300.model import Bilinear, Model, cube_mesh
     coords, incid = cube_mesh(model_n, jitter=0.1, seed=12345)
-    ne = min(nblocks * 128, incid.shape[0])
+    ne = incid.shape[0] if nblocks is None else min(nblocks * 128, incid.shape[0])
     used = np.unique(incid[:ne])
     remap = -np.ones(coords.shape[0], dtype=np.int64)
     remap[used] = np.arange(len(used))
@@ -547,13 +730,14 @@ def cpu_baseline(model_n, nblocks, threads, reps=8):
     u1 = ((F1 - np.eye(3)) @ X.T).T.ravel()
     rng = np.random.Generator(np.random.PCG64(2024))
     du = ((np.diag([-0.0005, -0.0005, 0.001]) @ X.T).T + rng.normal(0.0, 2e-5, X.shape)).ravel()
-    ora = oracle.Oracle(sub, threads=threads, deterministic=False)
+    ora = oracle.Oracle(sub, threads=threads, deterministic=False, fast=True)
     ifv = np.zeros(sub.nodof)
     ora.recover(1, 1, False, sub.c, np.zeros(sub.nodof), u1, ifv)
     ora.update()
     est = [np.zeros((s, sub.utsz)) for s in sub.spans]
-    ora.recover(2, 1, False, sub.c, u1, du, ifv)          # warm-up
-    ora.tanstf(2, 1, sub.c, u1, du, est)
+    for _ in range(max(1, warmup)):
+        ora.recover(2, 1, False, sub.c, u1, du, ifv)
+        ora.tanstf(2, 1, sub.c, u1, du, est)
     t_rec = t_tan = 0.0
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -565,8 +749,11 @@ def cpu_baseline(model_n, nblocks, threads, reps=8):
         t_tan += t2 - t1
     t_rec /= reps
     t_tan /= reps
+    what = "all" if nblocks is None or ne == incid.shape[0] else "the first"
     return {"value": ne / (t_rec + t_tan), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{ne} elements ({nblocks} blocks of 128) of the {model_n}^3 workload, {reps} iterations",
+            "sample": f"{what} {ne} elements ({len(sub.spans)} blocks of 128) of the {model_n}^3 workload, "
+                      f"{reps} iterations after {max(1, warmup)} warm-up",
+            "cpu": cpu_model(), "build": oracle.FAST_FLAGS,
             "tangent_elem_per_s": ne / t_tan, "recovery_elem_per_s": ne / t_rec}
 
 
@@ -591,21 +778,26 @@ def whole_job_throughput(units_per_rank, ms_local, world, dist=None, device="cpu
 
 
 def reference_arm(args, rank, world):
+    """The reference's CPU path on the host cores: the oracle's contracted
+    build on the whole headline workload (all 262,144 elements at 64^3),
+    the same warm-up and timed step counts as the GPU arm."""
     if rank != 0:
         return
     threads = host_threads()
-    reps = max(1, min(args.steps, 8))
-    cb = cpu_baseline(args.n, args.cpu_sample_blocks, threads, reps=reps)
+    cb = cpu_baseline(args.n, None, threads, reps=args.steps, warmup=args.warmup)
+    ne = args.n ** 3
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-        "steps": reps, "warmup": 1, "ms_per_step": 1e3 * args.cpu_sample_blocks * 128 / cb["value"],
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * ne / cb["value"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.n}^3 hex8 l3disop geonl, mm01, blocks of 128 (bounded CPU sample)",
-                   "sample": cb["sample"]},
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "config": {"workload": f"{args.n}^3 hex8 l3disop geonl (jitter 0.1h), mm01 bilinear, blocks of 128, "
+                               f"1 Newton iteration = tangent + recovery",
+                   "elements": ne, "gauss_points": ne * 8, "sample": cb["sample"]},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "cpu", "build")},
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "WARP3D itself (Fortran + Intel MKL) cannot be built here; the reference arm times the "
-                "oracle, a C++ restatement of the same routines, OpenMP over blocks on all host threads",
+                "oracle, a C++ restatement of the same routines compiled with multiply-add contraction, "
+                "OpenMP over blocks on all host threads",
     }
     print(json.dumps(line), flush=True)
 
@@ -822,6 +1014,63 @@ def precision_study(args, dev):
     return out
 
 
+def _r(x, nd=4):
+    return None if x is None else float(f"{x:.{nd}g}")
+
+
+def summarize_mixed(mixed):
+    """Headline view of the precision forms: per form the tangent time and
+    the iteration's speed-up over plain FP64."""
+    if not mixed:
+        return None
+    out = {"value": _r(mixed["value"]), "speedup_vs_fp64": _r(mixed["speedup_vs_fp64"]),
+           "form": mixed.get("form", "fp32"), "dtype": mixed.get("dtype")}
+    forms = {"fp32": {"tangent_ms": _r(mixed["fp32"]["tangent_ms"]), "speedup": _r(mixed["fp32"]["speedup_vs_fp64"])}}
+    for k, v in (mixed.get("tensor_core") or {}).items():
+        forms[k] = {"tangent_ms": _r(v["tangent_ms"]), "speedup": _r(v["speedup_vs_fp64"]),
+                    "tangent_hbm_frac": _r(v.get("tangent_hbm_frac"))}
+    out["forms"] = forms
+    return out
+
+
+def compact_roofline(rf):
+    keep = ("bound", "kernel", "achieved", "peak", "unit", "frac", "traffic", "peak_source")
+    out = {k: rf[k] for k in keep if k in rf}
+    for k in ("tangent_tc", "recovery"):
+        if k in rf:
+            out[k] = rf[k]
+    return out
+
+
+def summarize_parity(p1, batched, crystal):
+    """Max relative error of every FP64 output array against the oracle,
+    per workload, and the precision forms' Ke error."""
+    def one(p):
+        if not p:
+            return None
+        d = {"elements": p["elements"], "max_fp64": _r(p["max_fp64"], 3),
+             "worst_array": max(PARITY_ARRAYS + ("estiff",), key=lambda k: p[k])}
+        if "estiff_precision_forms" in p:
+            d["ke_precision_forms"] = {k: _r(v, 3) for k, v in p["estiff_precision_forms"].items()}
+        return d
+    return {"config1_64cube": one(p1), "config3_batched": one((batched or {}).get("parity")),
+            "config4_crystal": one((crystal or {}).get("parity")), "tolerance_fp64": 1e-12}
+
+
+def summarize_leg(leg):
+    if not leg or "plain_fp64" not in leg:
+        return leg and {"error": leg.get("error")}
+    out = {"elements": leg.get("elements"), "plain_fp64": _r(leg["plain_fp64"]["value"]),
+           "plain_ms": _r(leg["plain_fp64"]["ms_per_step"])}
+    for k in ("mixed", "mixed_tf32", "mixed_tc"):
+        if k in leg:
+            out[k] = _r(leg[k]["value"])
+            out[k + "_speedup"] = _r(leg[k].get("speedup_vs_plain"))
+    if "cpu_baseline" in leg:
+        out["cpu_baseline"] = _r(leg["cpu_baseline"]["value"])
+    return out
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -908,23 +1157,40 @@ def main():
     ms64, tan64, rec64, launches64 = timed(abi.TANGENT_FP64)
     clocks = finish_clocks(clk, local)
     mixed = None
+    hbm = hbm_peak_gbs()
     if not args.no_mixed:
-        ms32, tan32, rec32, launches32 = timed(abi.TANGENT_FP32)
-        mixed = {"value": ne / (ms32 * 1e-3), "ms_per_step": ms32, "tangent_ms": tan32, "recovery_ms": rec32,
-                 "speedup_vs_fp64": ms64 / ms32, "dtype": "tangent fp32 (FMA), recovery fp64"}
+        def form(prec):
+            ms_p, tan_p, rec_p, launches_p = timed(prec)
+            gbs = TANGENT32_BYTES_PER_ELEM * ne / (tan_p * 1e-3) / 1e9
+            return {"value": ne / (ms_p * 1e-3), "ms_per_step": ms_p, "tangent_ms": tan_p, "recovery_ms": rec_p,
+                    "speedup_vs_fp64": ms64 / ms_p, "tangent_hbm_gbs": gbs,
+                    "tangent_hbm_frac": gbs / hbm if hbm else None, "gpu_launches": launches_p}
+        fp32 = form(abi.TANGENT_FP32)
         # tensor-core forms of the same tangent (tcgen05.mma), one
         # Newton iteration each (tangent + FP64 recovery)
-        tcf = {}
-        for name, prec in (("tf32", abi.TANGENT_TF32), ("bf16", abi.TANGENT_BF16),
-                           ("tf32x3", abi.TANGENT_TF32X3), ("bf16x3", abi.TANGENT_BF16X3)):
-            ms_p, tan_p, rec_p, _ = timed(prec)
-            tcf[name] = {"tangent_ms": tan_p, "ms_per_step": ms_p, "value": ne / (ms_p * 1e-3),
-                         "tangent_hbm_gbs": TANGENT32_BYTES_PER_ELEM * ne / (tan_p * 1e-3) / 1e9}
-        mixed["tensor_core"] = tcf
+        tcf = {name: form(prec) for name, prec in TC_FORMS}
+        head = tcf[HEADLINE_FORM]
+        mixed = {"value": head["value"], "ms_per_step": head["ms_per_step"], "tangent_ms": head["tangent_ms"],
+                 "recovery_ms": head["recovery_ms"], "speedup_vs_fp64": head["speedup_vs_fp64"],
+                 "form": HEADLINE_FORM,
+                 "dtype": f"tangent {HEADLINE_FORM} on the tensor cores (tcgen05.mma, FP32 accumulation), "
+                          "recovery fp64",
+                 "fp32": fp32, "tensor_core": tcf}
         eng.set_precision(abi.TANGENT_FP64)
 
     # whole-job throughput: max time over ranks
     value, t_step = whole_job_throughput(ne, ms64, world, dist, dev)
+
+    # parity of this workload against the oracle: 64 blocks spread over the
+    # mesh, one iteration from the same state; precision forms' Ke against
+    # the oracle's FP64 Ke on the same blocks
+    parity1 = None
+    if not args.no_parity and rank == 0:
+        forms = (("fp32", abi.TANGENT_FP32), ("tf32", abi.TANGENT_TF32), ("bf16", abi.TANGENT_BF16),
+                 ("tf32x3", abi.TANGENT_TF32X3), ("bf16x3", abi.TANGENT_BF16X3))
+        parity1 = parity_sample(eng, model, spread_blocks(model, 64), 2, 1, False, model.c, u1, du,
+                                (tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr()), stream,
+                                precisions=forms)
 
     # ---- e2e through the host-array C-ABI ----
     e2e = None
@@ -976,8 +1242,6 @@ def main():
                              "tflops_refdense_count": RECOVER_FLOP_PER_ELEM_REFDENSE * ne / (rec64 * 1e-3) / 1e12,
                              "hbm_gbs": RECOVER_BYTES_PER_ELEM * ne / (rec64 * 1e-3) / 1e9}}
     roofline["hbm_peak_gbs_measured"] = hbm_peak_gbs()
-    if mixed:
-        mixed["tangent_hbm_gbs"] = TANGENT32_BYTES_PER_ELEM * ne / (mixed["tangent_ms"] * 1e-3) / 1e9
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -1001,6 +1265,12 @@ def main():
         batched = bench_batched(args, dev, local)
 
     if rank == 0:
+        # the full record first, then the headline line (last line of the
+        # output) with compact summaries of every leg
+        details = {"details": {"mixed": mixed, "batched": batched, "crystal": crystal, "solver": solver,
+                               "formulations": formulations, "parity_config1": parity1, "roofline": roofline,
+                               "cpu_baseline": cb, "e2e": e2e}}
+        print(json.dumps(details), flush=True)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -1010,9 +1280,10 @@ def main():
                        "elements": ne, "gauss_points": ne * 8, "l2": "inputs ~3 GB per step > L2, no flush",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "tangent_ms": tan64, "recovery_ms": rec64,
-            "mixed": mixed, "e2e": e2e, "roofline": roofline, "cpu_baseline": cb, "clocks": clocks,
-            "gpu_launches": launches64, "batched": batched, "crystal": crystal, "solver": solver,
-            "formulations": formulations,
+            "mixed": summarize_mixed(mixed), "e2e": e2e, "roofline": compact_roofline(roofline),
+            "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches64,
+            "parity": summarize_parity(parity1, batched, crystal),
+            "batched": summarize_leg(batched), "crystal": summarize_leg(crystal),
         }
         print(json.dumps(line), flush=True)
     eng.close()

@@ -193,6 +193,18 @@ const char* w3g_last_error(void);
    its MMAs gave up (that tile's Ke is then NaN). */
 int w3g_set_tangent_precision(w3g_context* ctx, int precision);
 
+/* Bounded waits of the tensor-core tangent kernels (no WARP3D
+   counterpart). Every wait of a kernel for its own copies or MMAs gives up
+   after `polls` polls (default W3G_WAIT_LIMIT_DEFAULT; a negative value
+   restores it). A wait that gives up ends that CTA's work: no further MMA
+   is issued, its copies and MMAs still in flight are waited out (bounded)
+   before tensor memory is freed, the element matrices it did not finish
+   are NaN and w3g_tanstf returns W3G_EFATAL. With 0 every such wait gives
+   up at once, before the first MMA: a driver can exercise its handling of
+   that status without any fault on the GPU. */
+#define W3G_WAIT_LIMIT_DEFAULT (1ll << 22)
+int w3g_set_wait_limit(w3g_context* ctx, long long polls);
+
 /* ---- state transfer (restart, fixtures, output) -------------------- */
 int w3g_state_upload(w3g_context* ctx, const w3g_block_state* host);
 int w3g_state_download(w3g_context* ctx, const w3g_block_state* host);
@@ -379,9 +391,14 @@ int w3g_residual_norms_dev(w3g_csr* csr, const void* d_v, const void* d_fixed_ma
    elblks (3*nelblk) and totdof (nelblk) are host arrays.
    Allocates nothing: its scratch is a fixed static device array for at
    most W3G_NOALLOC_MAX_BLOCKS element blocks (larger models: W3G_EARG).
-   The first call on a device sets up the array's address and must come
-   before any stream capture. Calls share the array: calls that overlap
-   on the GPU race and must be serialised. Returns after the work ends. */
+   The first call on a device looks up the array's address and caches it
+   for the device's primary context (stale after cudaDeviceReset: do not
+   call again on that device afterwards). Every call copies the host
+   tables and waits for its work, so no call may be made while `stream`
+   is being captured (W3G_EARG). Calls share the array: calls that
+   overlap on the GPU race and must be serialised. edest entries outside
+   1..nodof are skipped and reported as W3G_EARG with the first block that
+   holds one. Returns after the work ends. */
 #define W3G_NOALLOC_MAX_BLOCKS 65536
 int w3g_assemble_ifv_noalloc(int nelblk, const int* elblks, const int* totdof,
                              int nodof, const double* d_einfvec,

@@ -18,21 +18,29 @@ from warp3d_gb300.model import HostState, Model, block_ptrs, dptr
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libw3o.so")
+# the same restatement compiled with multiply-add contraction: the timed CPU
+# baseline only (see build.sh), never a checker
+FAST_LIB_PATH = os.path.join(HERE, "_build", "libw3o_fast.so")
+FAST_FLAGS = "g++ -O3 -fopenmp -ffp-contract=fast -fno-math-errno -fno-trapping-math -funroll-loops"
 
-_lib = None
+_libs = {}
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("w3o.cpp", "w3o.h", "w3o_mm10.cpp", "w3o_mm10.h")]
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(map(os.path.getmtime, srcs)):
+    srcs = [os.path.join(HERE, f) for f in ("w3o.cpp", "w3o.h", "w3o_mm10.cpp", "w3o_mm10.h", "build.sh")]
+    newest = max(map(os.path.getmtime, srcs))
+    stale = any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (LIB_PATH, FAST_LIB_PATH))
+    if force or stale:
         subprocess.run(["sh", os.path.join(HERE, "build.sh")], check=True)
     return LIB_PATH
 
 
-def load() -> C.CDLL:
-    global _lib
-    if _lib is None:
-        lib = C.CDLL(build())
+def load(fast: bool = False) -> C.CDLL:
+    """The checker library, or with fast=True the contracted build that the
+    CPU baseline times."""
+    if fast not in _libs:
+        build()
+        lib = C.CDLL(FAST_LIB_PATH if fast else LIB_PATH)
         _d = C.POINTER(C.c_double)
         _pd = C.POINTER(_d)
         mp = C.POINTER(abi.ModelDesc)
@@ -47,16 +55,16 @@ def load() -> C.CDLL:
         lib.w3o_shape_derivs.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _d, _d, _d]
         lib.w3o_mm01_point.argtypes = [C.c_int, C.c_int] + [_d] * 11
         lib.w3o_mm10_point.argtypes = [C.POINTER(abi.Crystal), _d, C.c_int, C.c_int, C.c_int, C.c_double] + [_d] * 6
-        _lib = lib
-    return _lib
+        _libs[fast] = lib
+    return _libs[fast]
 
 
 class Oracle:
     """Same calls as warp3d_gb300.engine.Engine, on a HostState."""
 
     def __init__(self, model: Model, state: HostState | None = None, threads: int = 0,
-                 deterministic: bool = True):
-        self.lib = load()
+                 deterministic: bool = True, fast: bool = False):
+        self.lib = load(fast)
         self.model = model
         self.state = state if state is not None else model.new_state()
         self.desc = model.desc()

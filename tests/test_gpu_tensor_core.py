@@ -75,6 +75,60 @@ def test_tensor_core_tangent_plastic_state(plastic_hex8, precision):
     assert err <= TOL[precision]
 
 
+def _unpack(packed):
+    """(span, 300) packed upper triangles -> (span, 24, 24) symmetric."""
+    n = 24
+    iu = np.triu_indices(n)
+    # packed position of (i, j), i <= j: j (j + 1) / 2 + i
+    pos = iu[1] * (iu[1] + 1) // 2 + iu[0]
+    K = np.zeros((packed.shape[0], n, n))
+    K[:, iu[0], iu[1]] = packed[:, pos]
+    K[:, iu[1], iu[0]] = packed[:, pos]
+    return K
+
+
+@pytest.mark.parametrize("precision", ALL)
+def test_tensor_core_tangent_keeps_the_rigid_translations(plastic_hex8, precision):
+    """Ke t = 0 for the element's three rigid translations t. The gradient-
+    pair form rounds only the material point values and the constant
+    operator, whose node sums stay exactly zero, so what is left is the FP32
+    accumulation (the level of the FP32 CUDA-core kernel)."""
+    model, eng, ora, u, du = plastic_hex8
+    eng.set_precision(precision)
+    est = model.estiff_blocks()
+    eng.tanstf(4, 1, model.c, u, du, est)
+    eng.set_precision(abi.TANGENT_FP64)
+    worst = 0.0
+    for blk in est:
+        K = _unpack(blk)
+        scale = np.max(np.abs(K), axis=(1, 2))
+        for d in range(3):
+            t = np.zeros(24)
+            t[8 * d:8 * d + 8] = 1.0
+            worst = max(worst, float(np.max(np.max(np.abs(K @ t), axis=1) / scale)))
+    print(f"{NAMES[precision]} max |Ke t| / max |Ke| = {worst:.1e}")
+    assert worst <= 5e-6
+
+
+def test_tensor_core_wait_limit_zero_reports_efatal_without_a_fault(plastic_hex8):
+    """A wait limit of 0: every tile gives up before its first MMA, Ke is
+    NaN, w3g_tanstf returns W3G_EFATAL once; with the default limit the
+    next call is correct again."""
+    model, eng, ora, u, du = plastic_hex8
+    for precision in (abi.TANGENT_TF32, abi.TANGENT_BF16X3):
+        eng.set_precision(precision)
+        eng.set_wait_limit(0)
+        est = model.estiff_blocks()
+        with pytest.raises(abi.W3GError) as ei:
+            eng.tanstf(4, 1, model.c, u, du, est)
+        assert ei.value.code == abi.EFATAL
+        assert all(np.all(np.isnan(b)) for b in est)
+        assert eng.check_finite() > 0
+        eng.set_wait_limit(-1)
+        assert _tangent_err(model, eng, ora, 4, 1, u, du) <= TOL[precision]
+    eng.set_precision(abi.TANGENT_FP64)
+
+
 @pytest.mark.parametrize("precision", ALL)
 def test_tensor_core_tangent_linear_iteration_zero(plastic_hex8, precision):
     # iteration 0: no geometric term from the rotation update path, elastic D
@@ -87,7 +141,7 @@ def test_tensor_core_tangent_linear_iteration_zero(plastic_hex8, precision):
 
 def test_tensor_core_tangent_mixed_types():
     """8-node bricks on the tensor cores; 20-node bricks and tetrahedra
-    take the FP32 CUDA-core kernels in the same call."""
+    in the same call."""
     rng = np.random.Generator(np.random.PCG64(11))
     coords, parts, origins = mixed_mesh(
         [(abi.ETYPE_L3DISOP, 3), (abi.ETYPE_Q3DISOP, 2), (abi.ETYPE_TET10, 2)], ny=2, nz=3, jitter=0.05, seed=11)

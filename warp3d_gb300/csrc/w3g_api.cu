@@ -31,6 +31,11 @@ int fail(int code, const std::string& msg) {
       return fail(W3G_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
   } while (0)
 
+// trailing elements allocated beyond the arrays that 1-D bulk copies read
+// (cep, rot_n1, urcs_n1): a copy of a tile's slab is rounded out to 16-byte
+// boundaries and may read up to 8 bytes past the last element
+constexpr size_t kBulkPad = 4;
+
 template <class T>
 cudaError_t dalloc(T** p, size_t n) {
   if (n == 0) n = 1;
@@ -41,7 +46,7 @@ void free_all(w3g_context* c) {
   DeviceModel& m = c->m;
   DeviceState& s = c->s;
   if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
-  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.tcchunks, s.tc_timeout, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
+  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.tcchunks, m.tcgtiles, s.tc_timeout, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
                   m.cdest, m.mat, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
                   m.ifv_rowptr, m.ifv_src, s.params, s.counters, m.xtal, m.xtype, m.mm10_gp, s.mm10_scr,
                   s.mm10_iters, s.mm10_order, s.mm10_ident, s.mm10_bins,
@@ -132,6 +137,7 @@ TangentArgs tangent_args(w3g_context* c, const double* d_c, const double* d_u, c
   a.qbar = c->m.qbar;
   a.beta_fact = c->m.beta_fact;
   a.bbar_beta = c->m.bbar_beta;
+  a.wait_limit = c->wait_limit;
   return a;
 }
 
@@ -162,9 +168,12 @@ int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const 
   }
   const bool tc = p >= W3G_TANGENT_TF32;
   cudaError_t e = cudaSuccess;
-  if (tc)
-    e = launch_tangent_tc_hex8(c->m, a, p == W3G_TANGENT_BF16 || p == W3G_TANGENT_BF16X3,
-                               p == W3G_TANGENT_TF32X3 || p == W3G_TANGENT_BF16X3, c->s.tc_timeout, st);
+  if (tc) {
+    const bool bf16 = p == W3G_TANGENT_BF16 || p == W3G_TANGENT_BF16X3;
+    const bool split = p == W3G_TANGENT_TF32X3 || p == W3G_TANGENT_BF16X3;
+    e = launch_tangent_tcg_hex8(c->m, a, bf16, split, c->s.tc_timeout, st);
+    if (e == cudaSuccess) e = launch_tangent_tc_hex8(c->m, a, bf16, split, c->s.tc_timeout, st);
+  }
   if (e == cudaSuccess)
     e = launch_tangent(c->m, a, c->precision != W3G_TANGENT_FP64, c->sched, c->s.counters + 1, st, tc);
   if (e != cudaSuccess) return fail(W3G_ECUDA, std::string("tangent launch: ") + cudaGetErrorString(e));
@@ -496,11 +505,18 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   }
   m.ntchunks = (int)tchunks.size();
   c->h_tchunks = tchunks;
-  std::vector<Chunk> tcchunks;   // tensor-core tiles: 5 elements of an 8-node-brick block
-  for (int b = 0; b < md->nelblk; ++b)
-    if (B[b].etype == W3G_ETYPE_L3DISOP)
+  // tensor-core tiles of 8-node bricks: gradient-pair tiles of 16
+  // elements, b-bar blocks in tiles of 5 (the B-bar operand kernel)
+  std::vector<Chunk> tcchunks, tcgtiles;
+  for (int b = 0; b < md->nelblk; ++b) {
+    if (B[b].etype != W3G_ETYPE_L3DISOP) continue;
+    if (B[b].bbar)
       for (int i0 = 0; i0 < B[b].span; i0 += 5) tcchunks.push_back(Chunk{b, i0, std::min(5, B[b].span - i0), 0});
+    else
+      for (int i0 = 0; i0 < B[b].span; i0 += 16) tcgtiles.push_back(Chunk{b, i0, std::min(16, B[b].span - i0), 0});
+  }
   m.ntcchunks = (int)tcchunks.size();
+  m.ntcgtiles = (int)tcgtiles.size();
   m.nrchunks = (int)chunks.size();
   m.mm10_chunk0 = (int)chunks.size();
   m.mm10_chunks = (int)mm10_chunks.size();
@@ -630,6 +646,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(m.chunks, m.nchunks);
   AL(m.tchunks, m.ntchunks);
   AL(m.tcchunks, m.ntcchunks);
+  AL(m.tcgtiles, m.ntcgtiles);
   AL(s.tc_timeout, 1);
   for (int k = 0; k < 2; ++k) {
     AL(m.rorder[k], m.nrchunks);
@@ -659,11 +676,11 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(s.hist, hist);
   AL(s.hist1, hist);
   AL(s.urcs_n, 9 * gp);
-  AL(s.urcs_n1, 9 * gp);
+  AL(s.urcs_n1, 9 * gp + kBulkPad);
   AL(s.eps_n, 6 * gp);
   AL(s.eps_n1, 6 * gp);
-  AL(s.rot_n1, 9 * gp);
-  AL(s.cep, cep);
+  AL(s.rot_n1, 9 * gp + kBulkPad);
+  AL(s.cep, cep + kBulkPad);
   AL(s.estiff, est);
   if (m.packed_total > 0) {
     AL(m.blocks_packed, md->nelblk);
@@ -697,6 +714,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   UP(m.chunks, chunks.data(), m.nchunks);
   UP(m.tchunks, tchunks.data(), m.ntchunks);
   UP(m.tcchunks, tcchunks.data(), m.ntcchunks);
+  UP(m.tcgtiles, tcgtiles.data(), m.ntcgtiles);
   for (int k = 0; k < 2; ++k) {
     UP(m.rorder[k], rord[k].data(), m.nrchunks);
     UP(m.torder[k], tord[k].data(), m.ntchunks);
@@ -763,6 +781,12 @@ int w3g_set_tangent_precision(w3g_context* c, int precision) {
   if (precision != W3G_TANGENT_FP64 && c->m.packed_total > 0 && !c->s.estiff_packed32)
     CK(dalloc(&c->s.estiff_packed32, (size_t)c->m.packed_total));
   c->precision = precision;
+  return 0;
+}
+
+int w3g_set_wait_limit(w3g_context* c, long long polls) {
+  if (!c) return fail(W3G_EARG, "null context");
+  c->wait_limit = polls < 0 ? W3G_WAIT_LIMIT_DEFAULT : polls;
   return 0;
 }
 
@@ -842,7 +866,10 @@ int w3g_tanstf(w3g_context* c, int step, int iter, const double* hc, const doubl
   if (c->precision >= W3G_TANGENT_TF32) {
     int timeout = 0;
     CK(cudaMemcpy(&timeout, c->s.tc_timeout, sizeof(int), cudaMemcpyDeviceToHost));
-    if (timeout) return fail(W3G_EFATAL, "tensor-core tangent: MMA completion wait gave up (Ke set to NaN)");
+    if (timeout) {   // reported once: the flag starts clear for the next call
+      CK(cudaMemset(c->s.tc_timeout, 0, sizeof(int)));
+      return fail(W3G_EFATAL, "tensor-core tangent: a bounded wait gave up (Ke of the unfinished tiles set to NaN)");
+    }
   }
   return 0;
 }
@@ -946,7 +973,7 @@ int enqueue_iteration(w3g_context* c, int what, const double* d_c, const double*
 int ensure_graph(w3g_context* c, int what, const void* d_c, const void* d_u, const void* d_du, void* d_ifv) {
   IterationGraph& g = c->graph;
   if (g.exec && g.what == what && g.precision == c->precision && g.c == d_c && g.u == d_u && g.du == d_du &&
-      g.ifv == d_ifv && same_schedule(g.sched, c->sched))
+      g.ifv == d_ifv && same_schedule(g.sched, c->sched) && g.wait_limit == c->wait_limit)
     return 0;
   if (g.exec) {
     CK(cudaGraphExecDestroy(g.exec));
@@ -974,6 +1001,7 @@ int ensure_graph(w3g_context* c, int what, const void* d_c, const void* d_u, con
   g.precision = c->precision;
   g.c = d_c; g.u = d_u; g.du = d_du; g.ifv = d_ifv;
   g.sched = c->sched;
+  g.wait_limit = c->wait_limit;
   g.launches = n;
   return 0;
 }

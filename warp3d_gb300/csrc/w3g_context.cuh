@@ -14,6 +14,7 @@ struct IterationGraph {
   int what = 0, precision = -1;
   const void *c = nullptr, *u = nullptr, *du = nullptr, *ifv = nullptr;
   w3g::Schedule sched{};
+  long long wait_limit = 0;
   int launches = 0;
 };
 
@@ -23,6 +24,7 @@ struct w3g_context {
   w3g::DeviceModel m;
   w3g::DeviceState s;
   int precision = W3G_TANGENT_FP64;
+  long long wait_limit = W3G_WAIT_LIMIT_DEFAULT;   // bounded waits of the tensor-core kernels
   w3g::Schedule sched{W3G_SCHED_PER_TYPE, 0, 0, 1, 1, W3G_ORDER_HEAVY_FIRST};
   IterationGraph graph;
   int ifv_parts = 0;

@@ -180,8 +180,10 @@ struct DeviceModel {
   BlockDesc* blocks = nullptr;     // device
   Chunk* chunks = nullptr;         // device, recovery items grouped by type
   Chunk* tchunks = nullptr;        // device, tangent items grouped by type
-  Chunk* tcchunks = nullptr;       // device, tensor-core tangent tiles (8-node bricks, <= 5 elements)
+  Chunk* tcchunks = nullptr;       // device, tensor-core tangent tiles of b-bar 8-node bricks (<= 5 elements)
   int ntcchunks = 0;
+  Chunk* tcgtiles = nullptr;       // device, gradient-pair tensor-core tiles of the other 8-node bricks (<= 16)
+  int ntcgtiles = 0;
   // schedule orders of the work items (W3G_ORDER_BLOCKS, _HEAVY_FIRST)
   int* rorder[2] = {nullptr, nullptr};
   int* torder[2] = {nullptr, nullptr};
@@ -256,6 +258,7 @@ struct TangentArgs {
   int qbar;
   double beta_fact;
   double bbar_beta;      // (1 - eps_bbar) / 3
+  long long wait_limit;  // polls of every bounded wait in the tensor-core kernels (0: give up at once)
 };
 
 struct RecoverArgs {
@@ -318,10 +321,15 @@ cudaError_t launch_expand_packed(const DeviceModel& m, const TangentArgs& a, con
 // type); returns the number of kernels launched through *launches
 cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bool fp32, const int* first,
                                   const int* count, cudaStream_t s, int* launches);
-// precision forms on the tensor cores: 8-node bricks (w3g_tangent_tc.cu)
+// precision forms on the tensor cores: b-bar 8-node bricks
+// (w3g_tangent_tc.cu) and the other 8-node bricks, gradient-pair form
+// (w3g_tangent_tcg.cu)
 cudaError_t launch_tangent_tc_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
                                    int* tc_timeout, cudaStream_t s);
 cudaError_t init_tangent_tc_kernels();
+cudaError_t launch_tangent_tcg_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
+                                    int* tc_timeout, cudaStream_t s);
+cudaError_t init_tangent_tcg_kernels();
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, const Schedule& sc,
                            int* counter, cudaStream_t s);
 // launches of the element kernels under a schedule
@@ -339,6 +347,7 @@ cudaError_t init_mm10_kernels();
 inline cudaError_t init_kernels() {
   cudaError_t e = init_tangent_kernels();
   if (e == cudaSuccess) e = init_tangent_tc_kernels();
+  if (e == cudaSuccess) e = init_tangent_tcg_kernels();
   if (e == cudaSuccess) e = init_recover_kernels();
   return e == cudaSuccess ? init_mm10_kernels() : e;
 }

@@ -26,8 +26,17 @@
 //   * all calls share the one array and it keeps the last call's
 //     contents: calls whose work overlaps on the GPU (different streams
 //     or threads without ordering) race on it and must be serialised by
-//     the caller. The entry point rewrites every entry it reads, so no
-//     clearing between calls is needed; ifv is zeroed by the call.
+//     the caller. The entry point rewrites every entry it reads and
+//     clears the bad-index record first; ifv is zeroed by the call;
+//   * every call copies the caller's tables from host memory and waits
+//     for its work, so it must not be called while its stream is being
+//     captured into a graph (it refuses with W3G_EARG);
+//   * the cached address belongs to the device's primary context: after
+//     cudaDeviceReset on that device it is stale, and the process must
+//     not call this entry point on that device again;
+//   * edest entries outside 1..nodof are skipped (no write outside ifv)
+//     and the call returns W3G_EARG naming the first block holding one.
+#include <climits>
 #include <mutex>
 #include <string>
 #include <cuda_runtime.h>
@@ -45,6 +54,7 @@ struct NoallocScratch {
   int totdof[kMaxBlocks];
   long long einf_off[kMaxBlocks];
   double partial[kMaxBlocks];
+  int bad_block;      // smallest 0-based block with an edest entry outside 1..nodof, or INT_MAX
 };
 
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
@@ -53,9 +63,11 @@ static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 std::mutex g_mu;
 NoallocScratch* g_addr[64] = {};
 
-__global__ void k_zero(double* v, int n) {
+// zeroes ifv and clears the bad-index record of the previous call
+__global__ void k_zero(double* v, int n, NoallocScratch* s) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) v[k] = 0.0;
+  if (k == 0) s->bad_block = INT_MAX;
 }
 
 // einfvec offset of every block: exclusive prefix sum of span*totdof
@@ -81,7 +93,7 @@ __global__ void __launch_bounds__(kThreads) k_offsets(NoallocScratch* s, int nel
 
 // one CTA per element block; OpenMP-ATOMIC-style scatter as addifv does
 __global__ void __launch_bounds__(kThreads) k_scatter(NoallocScratch* s, const double* __restrict__ einf,
-                                                      const int* __restrict__ edest, double* ifv) {
+                                                      const int* __restrict__ edest, double* ifv, int nodof) {
   __shared__ double sw[kThreads / 32];
   const int b = blockIdx.x;
   const int span = s->elblks[3 * b], totdof = s->totdof[b];
@@ -92,7 +104,9 @@ __global__ void __launch_bounds__(kThreads) k_scatter(NoallocScratch* s, const d
     const int i = k % span;            // einfvec (span, totdof): k = j*span + i
     const int j = k / span;
     const double v = einf[off + k];
-    atomicAdd(&ifv[edest[off + (long long)i * totdof + j] - 1], v);
+    const int dof = edest[off + (long long)i * totdof + j];
+    if (dof >= 1 && dof <= nodof) atomicAdd(&ifv[dof - 1], v);
+    else atomicMin(&s->bad_block, b);   // skipped: never written outside ifv
     sa += fabs(v);
   }
   for (int o = 16; o > 0; o >>= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
@@ -135,6 +149,13 @@ extern "C" int w3g_assemble_ifv_noalloc(int nelblk, const int* elblks, const int
     return fail(W3G_EARG, std::to_string(nelblk) + " element blocks exceed the fixed scratch of " +
                               std::to_string(kMaxBlocks) + " blocks");
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+      return fail(W3G_EARG, "called while the stream is being captured (the call copies host tables and waits)");
+    }
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
     return fail(W3G_ECUDA, "no current CUDA device");
@@ -158,19 +179,24 @@ extern "C" int w3g_assemble_ifv_noalloc(int nelblk, const int* elblks, const int
       return fail(W3G_EARG, "bad span or totdof in block " + std::to_string(b + 1));
     }
   }
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemcpyAsync(s->elblks, elblks, sizeof(int) * 3 * nelblk, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(s->totdof, totdof, sizeof(int) * nelblk, cudaMemcpyHostToDevice, st);
+  int bad = INT_MAX;
   if (e == cudaSuccess) {
     k_offsets<<<1, kThreads, 0, st>>>(s, nelblk);
-    k_zero<<<(nodof + kThreads - 1) / kThreads, kThreads, 0, st>>>(d_ifv, nodof);
-    k_scatter<<<nelblk, kThreads, 0, st>>>(s, d_einfvec, d_edest, d_ifv);
+    k_zero<<<(nodof + kThreads - 1) / kThreads, kThreads, 0, st>>>(d_ifv, nodof, s);
+    k_scatter<<<nelblk, kThreads, 0, st>>>(s, d_einfvec, d_edest, d_ifv, nodof);
     k_sum_partials<<<1, kThreads, 0, st>>>(s, nelblk, d_sum_ifv);
     e = cudaGetLastError();
   }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, &s->bad_block, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     return fail(W3G_ECUDA, cudaGetErrorString(e));
+  }
+  if (bad != INT_MAX) {
+    return fail(W3G_EARG, "edest entry outside 1.." + std::to_string(nodof) + " in block " + std::to_string(bad + 1) +
+                              " (skipped; ifv lacks those contributions)");
   }
   return 0;
 }

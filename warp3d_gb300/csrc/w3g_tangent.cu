@@ -200,7 +200,7 @@ cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bo
 
 int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8) {
   if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) return m.ntchunks > 0 ? 1 : 0;
-  int n = skip_hex8 && m.ntcchunks > 0 ? 1 : 0;
+  int n = skip_hex8 ? (m.ntcchunks > 0 ? 1 : 0) + (m.ntcgtiles > 0 ? 1 : 0) : 0;
   for (int t = skip_hex8 ? 1 : 0; t < kNumTypes; ++t) n += m.ttype_chunks[t] > 0 ? 1 : 0;
   return n;
 }

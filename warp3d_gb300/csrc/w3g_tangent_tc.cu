@@ -61,7 +61,7 @@ constexpr int kThreads = 256;
 constexpr int kSubs = 6;               // threads per (element, Gauss point) in phase 1
 constexpr int kTmemCols = 128;
 constexpr int kKfStride = TOT + 1;     // padded row of the staged element matrices
-constexpr long long kWaitLimit = 1ll << 22;   // mbarrier polls before giving up
+constexpr long long kDrainLimit = 1ll << 26;  // polls waiting out MMAs in flight after a wait gave up
 
 template <bool kBF16>
 struct TcLayout {
@@ -455,7 +455,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
   __syncthreads();
 
   // ---- phase 3: MMA chain (one thread), completion on the mbarrier ----
-  if (tid == 0) {
+  // A wait limit of 0 gives up before any MMA is issued.
+  const bool issue = a.wait_limit > 0;
+  if (tid == 0 && issue) {
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t a0 = smem_u32(opA), b0 = smem_u32(opB);
     const uint32_t lo = 2 * L::kOpBytes;   // A_lo, B_lo follow A_hi, B_hi
@@ -472,18 +474,23 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
         smem_u32(&S.mbar)));
   }
-  // bounded wait on phase 0 of the mbarrier
+  // bounded wait on phase 0 of the mbarrier; after giving up, the MMAs
+  // that were issued may still be running: they are waited out (bounded)
+  // before tensor memory is read or freed
   {
-    uint32_t done = 0;
-    long long polls = 0;
-    while (!done && polls < kWaitLimit) {
-      asm volatile(
-          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
-          : "=r"(done)
-          : "r"(smem_u32(&S.mbar)));
-      ++polls;
+    auto poll = [&](long long limit) {
+      uint32_t done = 0;
+      for (long long polls = 0; !done && polls < limit; ++polls)
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_u32(&S.mbar)));
+      return done != 0;
+    };
+    if (!poll(a.wait_limit)) {
+      S.timeout = 1;
+      if (issue) poll(kDrainLimit);
     }
-    if (!done) S.timeout = 1;
   }
   asm volatile("tcgen05.fence::after_thread_sync;");
   __syncthreads();
@@ -494,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
   // by consecutive rows fall in distinct banks; operands are consumed
   float* kf = reinterpret_cast<float*>(opA);
   float* ke = reinterpret_cast<float*>(opA) + kTcElems * TOT * kKfStride;   // [kTcElems][UT]
-  if (warp < 4) {
+  if (warp < 4 && ok) {
     const int r = 32 * warp + lane;
     const int e = r / TOT, dr = r % TOT;
     // the 32-column TMEM chunks holding this warp's elements' columns

@@ -66,6 +66,12 @@ class Engine:
         except Exception:
             pass
 
+    def set_wait_limit(self, polls: int):
+        """Bound on the polls of every wait in the tensor-core kernels
+        (w3g_set_wait_limit; negative: the default). 0 makes them give up
+        before any MMA: w3g_tanstf then reports W3G_EFATAL with NaN Ke."""
+        abi.check(self.lib, self.lib.w3g_set_wait_limit(self.ctx, polls))
+
     def set_precision(self, precision: int):
         abi.check(self.lib, self.lib.w3g_set_tangent_precision(self.ctx, precision))
         self.precision = precision
