@@ -463,18 +463,21 @@ void tcomp1(int span, A2& theta, const double* nxi, const double* neta, const do
       T(i, j, 1) = G(2, 1) * nxi[j] + G(2, 2) * neta[j] + G(2, 3) * nzeta[j];
       T(i, j, 2) = G(3, 1) * nxi[j] + G(3, 2) * neta[j] + G(3, 3) * nzeta[j];
     }
+  // the accumulation theta = theta + thtemp*ue as one fused multiply-add
+  // per term (what an FMA-contracting Fortran build executes; the CUDA
+  // engine uses the same fused operations in the same order)
   int tpos1 = nnode, tpos2 = 2 * nnode;
   for (int j = 0; j < nnode; ++j)
     for (int i = 0; i < span; ++i) {
-      theta(i, 0) = theta(i, 0) + T(i, j, 0) * ue(i, j);
-      theta(i, 1) = theta(i, 1) + T(i, j, 0) * ue(i, tpos1 + j);
-      theta(i, 2) = theta(i, 2) + T(i, j, 0) * ue(i, tpos2 + j);
-      theta(i, 3) = theta(i, 3) + T(i, j, 1) * ue(i, j);
-      theta(i, 4) = theta(i, 4) + T(i, j, 1) * ue(i, tpos1 + j);
-      theta(i, 5) = theta(i, 5) + T(i, j, 1) * ue(i, tpos2 + j);
-      theta(i, 6) = theta(i, 6) + T(i, j, 2) * ue(i, j);
-      theta(i, 7) = theta(i, 7) + T(i, j, 2) * ue(i, tpos1 + j);
-      theta(i, 8) = theta(i, 8) + T(i, j, 2) * ue(i, tpos2 + j);
+      theta(i, 0) = std::fma(T(i, j, 0), ue(i, j), theta(i, 0));
+      theta(i, 1) = std::fma(T(i, j, 0), ue(i, tpos1 + j), theta(i, 1));
+      theta(i, 2) = std::fma(T(i, j, 0), ue(i, tpos2 + j), theta(i, 2));
+      theta(i, 3) = std::fma(T(i, j, 1), ue(i, j), theta(i, 3));
+      theta(i, 4) = std::fma(T(i, j, 1), ue(i, tpos1 + j), theta(i, 4));
+      theta(i, 5) = std::fma(T(i, j, 1), ue(i, tpos2 + j), theta(i, 5));
+      theta(i, 6) = std::fma(T(i, j, 2), ue(i, j), theta(i, 6));
+      theta(i, 7) = std::fma(T(i, j, 2), ue(i, tpos1 + j), theta(i, 7));
+      theta(i, 8) = std::fma(T(i, j, 2), ue(i, tpos2 + j), theta(i, 8));
     }
 }
 
@@ -489,10 +492,11 @@ int fcomp1(int span, A2& f, double* df, A2& theta) {
   }
   int bad = -1;
   for (int i = 0; i < span; ++i) {
-    double f1 = F(2, 2) * F(3, 3) - F(2, 3) * F(3, 2);
-    double f2 = F(2, 1) * F(3, 3) - F(2, 3) * F(3, 1);
-    double f3 = F(2, 1) * F(3, 2) - F(2, 2) * F(3, 1);
-    df[i] = F(1, 1) * f1 - F(1, 2) * f2 + F(1, 3) * f3;
+    // a*b - c*d as fma(a, b, -(c*d)); the cofactor sum left to right, fused
+    double f1 = std::fma(F(2, 2), F(3, 3), -(F(2, 3) * F(3, 2)));
+    double f2 = std::fma(F(2, 1), F(3, 3), -(F(2, 3) * F(3, 1)));
+    double f3 = std::fma(F(2, 1), F(3, 2), -(F(2, 2) * F(3, 1)));
+    df[i] = std::fma(F(1, 3), f3, std::fma(F(1, 1), f1, -(F(1, 2) * f2)));
     if (df[i] <= 1.0e-20 && bad < 0) bad = i;
   }
   return bad;
@@ -504,17 +508,20 @@ void evcmp1_new(int span, A2& c, A2& lamda) {
   for (int bel = 0; bel < span; ++bel) {
     double m11 = c(bel, 0), m12 = c(bel, 1), m13 = c(bel, 3);
     double m22 = c(bel, 2), m23 = c(bel, 4), m33 = c(bel, 5);
+    // the reference's expressions with each product-sum fused, left to
+    // right: a*b + c*d + e*f -> fma(e, f, fma(c, d, a*b)); x - a*b -> fma(-a, b, x)
     double de = m12 * m23;
     double dd = m12 * m12;
     double ee = m23 * m23;
     double ff = m13 * m13;
     double m = m11 + m22 + m33;
-    double c1 = (m11 * m22 + m11 * m33 + m22 * m33) - (dd + ee + ff);
-    double c0 = m33 * dd + m11 * ee + m22 * ff - m11 * m22 * m33 - two * m13 * de;
-    double p = m * m - three * c1;
-    double q = m * (p - onept5 * c1) - thirteenpt5 * c0;
+    double c1 = std::fma(m22, m33, std::fma(m11, m33, m11 * m22)) - (dd + ee + ff);
+    double c0 = std::fma(-(two * m13), de,
+                         std::fma(-(m11 * m22), m33, std::fma(m22, ff, std::fma(m11, ee, m33 * dd))));
+    double p = std::fma(m, m, -(three * c1));
+    double q = std::fma(m, p - onept5 * c1, -(thirteenpt5 * c0));
     double sqrtp = std::sqrt(std::fabs(p));
-    double phi = twentyseven * (quarter * c1 * c1 * (p - c1) + c0 * (q + sixpt75 * c0));
+    double phi = twentyseven * std::fma(quarter * c1 * c1, p - c1, c0 * std::fma(sixpt75, c0, q));
     phi = third * std::atan2(std::sqrt(std::fabs(phi)), q);
     double cphi = sqrtp * std::cos(phi);
     double sphi = iroot3 * sqrtp * std::sin(phi);
@@ -532,21 +539,25 @@ void evcmp1_new(int span, A2& c, A2& lamda) {
 // ivcmp1 + irscp1 + rtcmp1, src/gtmat1.f:691-735, 961-1130: [R] = [F][U]^-1
 void rtcmp1(int span, A2& f, double* const* rcol) {
   A2 c(6), cc(6), ev(3);
+  // three-term products sums fused left to right: fma(e, f, fma(c, d, a*b))
+  auto dot3 = [](double a, double b, double c2_, double d, double e, double f) {
+    return std::fma(e, f, std::fma(c2_, d, a * b));
+  };
   for (int i = 0; i < span; ++i) {
-    c(i, 0) = F(1, 1) * F(1, 1) + F(2, 1) * F(2, 1) + F(3, 1) * F(3, 1);
-    c(i, 1) = F(1, 1) * F(1, 2) + F(2, 1) * F(2, 2) + F(3, 1) * F(3, 2);
-    c(i, 2) = F(1, 2) * F(1, 2) + F(2, 2) * F(2, 2) + F(3, 2) * F(3, 2);
-    c(i, 3) = F(1, 1) * F(1, 3) + F(2, 1) * F(2, 3) + F(3, 1) * F(3, 3);
-    c(i, 4) = F(1, 2) * F(1, 3) + F(2, 2) * F(2, 3) + F(3, 2) * F(3, 3);
-    c(i, 5) = F(1, 3) * F(1, 3) + F(2, 3) * F(2, 3) + F(3, 3) * F(3, 3);
+    c(i, 0) = dot3(F(1, 1), F(1, 1), F(2, 1), F(2, 1), F(3, 1), F(3, 1));
+    c(i, 1) = dot3(F(1, 1), F(1, 2), F(2, 1), F(2, 2), F(3, 1), F(3, 2));
+    c(i, 2) = dot3(F(1, 2), F(1, 2), F(2, 2), F(2, 2), F(3, 2), F(3, 2));
+    c(i, 3) = dot3(F(1, 1), F(1, 3), F(2, 1), F(2, 3), F(3, 1), F(3, 3));
+    c(i, 4) = dot3(F(1, 2), F(1, 3), F(2, 2), F(2, 3), F(3, 2), F(3, 3));
+    c(i, 5) = dot3(F(1, 3), F(1, 3), F(2, 3), F(2, 3), F(3, 3), F(3, 3));
   }
   for (int i = 0; i < span; ++i) {
-    cc(i, 0) = c(i, 0) * c(i, 0) + c(i, 1) * c(i, 1) + c(i, 3) * c(i, 3);
-    cc(i, 1) = c(i, 0) * c(i, 1) + c(i, 1) * c(i, 2) + c(i, 3) * c(i, 4);
-    cc(i, 2) = c(i, 1) * c(i, 1) + c(i, 2) * c(i, 2) + c(i, 4) * c(i, 4);
-    cc(i, 3) = c(i, 0) * c(i, 3) + c(i, 1) * c(i, 4) + c(i, 3) * c(i, 5);
-    cc(i, 4) = c(i, 1) * c(i, 3) + c(i, 2) * c(i, 4) + c(i, 4) * c(i, 5);
-    cc(i, 5) = c(i, 3) * c(i, 3) + c(i, 4) * c(i, 4) + c(i, 5) * c(i, 5);
+    cc(i, 0) = dot3(c(i, 0), c(i, 0), c(i, 1), c(i, 1), c(i, 3), c(i, 3));
+    cc(i, 1) = dot3(c(i, 0), c(i, 1), c(i, 1), c(i, 2), c(i, 3), c(i, 4));
+    cc(i, 2) = dot3(c(i, 1), c(i, 1), c(i, 2), c(i, 2), c(i, 4), c(i, 4));
+    cc(i, 3) = dot3(c(i, 0), c(i, 3), c(i, 1), c(i, 4), c(i, 3), c(i, 5));
+    cc(i, 4) = dot3(c(i, 1), c(i, 3), c(i, 2), c(i, 4), c(i, 4), c(i, 5));
+    cc(i, 5) = dot3(c(i, 3), c(i, 3), c(i, 4), c(i, 4), c(i, 5), c(i, 5));
   }
   evcmp1_new(span, c, ev);
   for (int i = 0; i < span; ++i) {
@@ -554,29 +565,29 @@ void rtcmp1(int span, A2& f, double* const* rcol) {
   }
   for (int i = 0; i < span; ++i) {
     double iu = ev(i, 0) + ev(i, 1) + ev(i, 2);
-    double iiu = ev(i, 0) * ev(i, 1) + ev(i, 1) * ev(i, 2) + ev(i, 0) * ev(i, 2);
+    double iiu = std::fma(ev(i, 0), ev(i, 2), std::fma(ev(i, 1), ev(i, 2), ev(i, 0) * ev(i, 1)));
     double iiiu = ev(i, 0) * ev(i, 1) * ev(i, 2);
-    double a2 = one / (iiiu * (iu * iiu - iiiu));
-    double b2 = iu * iiu * iiu - iiiu * (iu * iu + iiu);
-    double c2 = -iiiu - iu * (iu * iu - two * iiu);
+    double a2 = one / (iiiu * std::fma(iu, iiu, -iiiu));
+    double b2 = std::fma(iu * iiu, iiu, -(iiiu * std::fma(iu, iu, iiu)));
+    double c2 = std::fma(-iu, std::fma(iu, iu, -(two * iiu)), -iiiu);
     double d2 = iu;
     double ui[6];
-    ui[0] = a2 * (b2 + c2 * c(i, 0) + d2 * cc(i, 0));
-    ui[1] = a2 * (c2 * c(i, 1) + d2 * cc(i, 1));
-    ui[2] = a2 * (b2 + c2 * c(i, 2) + d2 * cc(i, 2));
-    ui[3] = a2 * (c2 * c(i, 3) + d2 * cc(i, 3));
-    ui[4] = a2 * (c2 * c(i, 4) + d2 * cc(i, 4));
-    ui[5] = a2 * (b2 + c2 * c(i, 5) + d2 * cc(i, 5));
+    ui[0] = a2 * std::fma(d2, cc(i, 0), std::fma(c2, c(i, 0), b2));
+    ui[1] = a2 * std::fma(d2, cc(i, 1), c2 * c(i, 1));
+    ui[2] = a2 * std::fma(d2, cc(i, 2), std::fma(c2, c(i, 2), b2));
+    ui[3] = a2 * std::fma(d2, cc(i, 3), c2 * c(i, 3));
+    ui[4] = a2 * std::fma(d2, cc(i, 4), c2 * c(i, 4));
+    ui[5] = a2 * std::fma(d2, cc(i, 5), std::fma(c2, c(i, 5), b2));
 #define RR(a, b) rcol[(a - 1) + 3 * (b - 1)][i]
-    RR(1, 1) = F(1, 1) * ui[0] + F(1, 2) * ui[1] + F(1, 3) * ui[3];
-    RR(1, 2) = F(1, 1) * ui[1] + F(1, 2) * ui[2] + F(1, 3) * ui[4];
-    RR(1, 3) = F(1, 1) * ui[3] + F(1, 2) * ui[4] + F(1, 3) * ui[5];
-    RR(2, 1) = F(2, 1) * ui[0] + F(2, 2) * ui[1] + F(2, 3) * ui[3];
-    RR(2, 2) = F(2, 1) * ui[1] + F(2, 2) * ui[2] + F(2, 3) * ui[4];
-    RR(2, 3) = F(2, 1) * ui[3] + F(2, 2) * ui[4] + F(2, 3) * ui[5];
-    RR(3, 1) = F(3, 1) * ui[0] + F(3, 2) * ui[1] + F(3, 3) * ui[3];
-    RR(3, 2) = F(3, 1) * ui[1] + F(3, 2) * ui[2] + F(3, 3) * ui[4];
-    RR(3, 3) = F(3, 1) * ui[3] + F(3, 2) * ui[4] + F(3, 3) * ui[5];
+    RR(1, 1) = dot3(F(1, 1), ui[0], F(1, 2), ui[1], F(1, 3), ui[3]);
+    RR(1, 2) = dot3(F(1, 1), ui[1], F(1, 2), ui[2], F(1, 3), ui[4]);
+    RR(1, 3) = dot3(F(1, 1), ui[3], F(1, 2), ui[4], F(1, 3), ui[5]);
+    RR(2, 1) = dot3(F(2, 1), ui[0], F(2, 2), ui[1], F(2, 3), ui[3]);
+    RR(2, 2) = dot3(F(2, 1), ui[1], F(2, 2), ui[2], F(2, 3), ui[4]);
+    RR(2, 3) = dot3(F(2, 1), ui[3], F(2, 2), ui[4], F(2, 3), ui[5]);
+    RR(3, 1) = dot3(F(3, 1), ui[0], F(3, 2), ui[1], F(3, 3), ui[3]);
+    RR(3, 2) = dot3(F(3, 1), ui[1], F(3, 2), ui[2], F(3, 3), ui[4]);
+    RR(3, 3) = dot3(F(3, 1), ui[3], F(3, 2), ui[4], F(3, 3), ui[5]);
 #undef RR
   }
 }

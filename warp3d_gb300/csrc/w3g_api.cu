@@ -507,13 +507,18 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   c->h_tchunks = tchunks;
   // tensor-core tiles of 8-node bricks: gradient-pair tiles of 16
   // elements, b-bar blocks in tiles of 5 (the B-bar operand kernel)
-  std::vector<Chunk> tcchunks, tcgtiles;
+  std::vector<Chunk> tcchunks;
+  std::vector<TcgTile> tcgtiles;
   for (int b = 0; b < md->nelblk; ++b) {
-    if (B[b].etype != W3G_ETYPE_L3DISOP) continue;
-    if (B[b].bbar)
-      for (int i0 = 0; i0 < B[b].span; i0 += 5) tcchunks.push_back(Chunk{b, i0, std::min(5, B[b].span - i0), 0});
+    const BlockDesc& d = B[b];
+    if (d.etype != W3G_ETYPE_L3DISOP) continue;
+    if (d.bbar)
+      for (int i0 = 0; i0 < d.span; i0 += 5) tcchunks.push_back(Chunk{b, i0, std::min(5, d.span - i0), 0});
     else
-      for (int i0 = 0; i0 < B[b].span; i0 += 16) tcgtiles.push_back(Chunk{b, i0, std::min(16, B[b].span - i0), 0});
+      for (int i0 = 0; i0 < d.span; i0 += 16)
+        tcgtiles.push_back(TcgTile{i0, std::min(16, d.span - i0), d.span,
+                                   (d.geonl ? 1 : 0) | (d.mat == W3G_MAT_CRYSTAL ? 2 : 0), d.cep_off, d.gp_off,
+                                   d.estiff_off, d.einf_off, d.hist_off, 0});
   }
   m.ntcchunks = (int)tcchunks.size();
   m.ntcgtiles = (int)tcgtiles.size();

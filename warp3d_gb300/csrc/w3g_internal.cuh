@@ -63,6 +63,15 @@ struct Chunk {
   int type;   // type_slot of the block's element type
 };
 
+// one tile (up to 16 consecutive elements of a block) of the gradient-pair
+// tensor-core tangent, with the block fields the kernel reads resolved on
+// the host, so that a tile costs one 64-byte load
+struct TcgTile {
+  int i0, n, span, flags;     // flags: 1 = finite strain (geonl), 2 = mm10 ([D] from history1)
+  long long cep_off, gp_off, estiff_off, einf_off, hist_off, pad;
+};
+static_assert(sizeof(TcgTile) == 64, "TcgTile is one 64-byte record");
+
 // ---- mm10 crystal plasticity (w3g_mm10.cu) -----------------------------
 constexpr int kHistMM10 = 158;     // one fcc crystal, one hardening variable
 constexpr int kSlip = 12;          // fcc slip systems
@@ -182,7 +191,7 @@ struct DeviceModel {
   Chunk* tchunks = nullptr;        // device, tangent items grouped by type
   Chunk* tcchunks = nullptr;       // device, tensor-core tangent tiles of b-bar 8-node bricks (<= 5 elements)
   int ntcchunks = 0;
-  Chunk* tcgtiles = nullptr;       // device, gradient-pair tensor-core tiles of the other 8-node bricks (<= 16)
+  TcgTile* tcgtiles = nullptr;     // device, gradient-pair tensor-core tiles of the other 8-node bricks (<= 16)
   int ntcgtiles = 0;
   // schedule orders of the work items (W3G_ORDER_BLOCKS, _HEAVY_FIRST)
   int* rorder[2] = {nullptr, nullptr};

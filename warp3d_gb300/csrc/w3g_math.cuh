@@ -182,22 +182,39 @@ __device__ __forceinline__ void polar_rotation(const double* F, double* R) {
 }
 
 // ---------------------------------------------------------------------
-// Reference-order arithmetic for the finite-strain kinematics chain.
+// Fixed-order arithmetic for the finite-strain kinematics chain.
 //
 // WARP3D's polar decomposition (Cardano eigenvalues of C = F^T F, then
 // U^-1 from the invariants of U) is ill-conditioned when F is close to a
 // rotation: p = m^2 - 3 c1 cancels, and two evaluation orders of the same
-// formulas give rotations that differ by ~1e-9. To reproduce the
-// reference's rotations and strain increments to 1e-12, jacob1 (at t=0),
-// tcomp1, fcomp1 and the polar decomposition below evaluate every
-// expression in the reference's order with explicitly rounded
-// operations: no fused multiply-add, divisions where the reference
-// divides. The transcendental calls (atan2, cos, sin) are CUDA's.
+// formulas give rotations that differ by ~1e-9. To reproduce the oracle's
+// rotations and strain increments to 1e-12, jacob1 (at t=0), tcomp1,
+// fcomp1 and the polar decomposition below evaluate every expression in
+// one fixed order with explicitly rounded operations, the same order as
+// the oracle: jacob1 at t = 0 without fused multiply-add (computed once
+// and cached), the per-call chain with the reference's product sums fused
+// left to right (a*b + c*d + e*f -> fma(e, f, fma(c, d, a*b)), x - a*b ->
+// fma(-a, b, x)) -- what an FMA-contracting build of the Fortran executes
+// and two FP64 instructions in three fewer. Divisions stay where the
+// reference divides. The transcendental calls (atan2, cos, sin) are
+// CUDA's.
 // ---------------------------------------------------------------------
 __device__ __forceinline__ double rm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double ra(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double rs(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double rd(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
+// a*b + c*d + e*f, fused left to right
+__device__ __forceinline__ double dot3f(double a, double b, double c, double d, double e, double f) {
+  return fm(e, f, fm(c, d, rm(a, b)));
+}
+// one node's term of tcomp1 for both configurations: th += t * u (fused)
+__device__ __forceinline__ void tcomp1_node(double* th, double tx, double ty, double tz, double ux, double uy,
+                                            double uz) {
+  th[0] = fm(tx, ux, th[0]); th[1] = fm(tx, uy, th[1]); th[2] = fm(tx, uz, th[2]);
+  th[3] = fm(ty, ux, th[3]); th[4] = fm(ty, uy, th[4]); th[5] = fm(ty, uz, th[5]);
+  th[6] = fm(tz, ux, th[6]); th[7] = fm(tz, uy, th[7]); th[8] = fm(tz, uz, th[8]);
+}
 
 // jacob1 (src/gtmat1.f:382-480) in reference order; gama column-major.
 template <int NN>
@@ -234,40 +251,41 @@ __device__ __forceinline__ void grad_ref(const double* g, double p, double q, do
   tz = ra(ra(rm(g[2], p), rm(g[5], q)), rm(g[8], r));
 }
 
-// fcomp1 determinant (src/gtmat1.f:640-652)
+// fcomp1 determinant (src/gtmat1.f:640-652), fused as in the oracle
 __device__ __forceinline__ double det_ref(const double* F) {
-  double f1 = rs(rm(F[4], F[8]), rm(F[7], F[5]));
-  double f2 = rs(rm(F[1], F[8]), rm(F[7], F[2]));
-  double f3 = rs(rm(F[1], F[5]), rm(F[4], F[2]));
-  return ra(rs(rm(F[0], f1), rm(F[3], f2)), rm(F[6], f3));
+  double f1 = fm(F[4], F[8], -rm(F[7], F[5]));
+  double f2 = fm(F[1], F[8], -rm(F[7], F[2]));
+  double f3 = fm(F[1], F[5], -rm(F[4], F[2]));
+  return fm(F[6], f3, fm(F[0], f1, -rm(F[3], f2)));
 }
 
-// rtcmp1 + irscp1 + ivcmp1 + evcmp1_new in reference order
+// rtcmp1 + irscp1 + ivcmp1 + evcmp1_new (src/gtmat1.f:691-735, 961-1210),
+// the reference's expressions with the product sums fused as in the oracle
 __device__ __forceinline__ void polar_rotation_ref(const double* F, double* R) {
 #define FF(a, b) F[(a - 1) + 3 * (b - 1)]
   double c[6], cc[6];
-  c[0] = ra(ra(rm(FF(1, 1), FF(1, 1)), rm(FF(2, 1), FF(2, 1))), rm(FF(3, 1), FF(3, 1)));
-  c[1] = ra(ra(rm(FF(1, 1), FF(1, 2)), rm(FF(2, 1), FF(2, 2))), rm(FF(3, 1), FF(3, 2)));
-  c[2] = ra(ra(rm(FF(1, 2), FF(1, 2)), rm(FF(2, 2), FF(2, 2))), rm(FF(3, 2), FF(3, 2)));
-  c[3] = ra(ra(rm(FF(1, 1), FF(1, 3)), rm(FF(2, 1), FF(2, 3))), rm(FF(3, 1), FF(3, 3)));
-  c[4] = ra(ra(rm(FF(1, 2), FF(1, 3)), rm(FF(2, 2), FF(2, 3))), rm(FF(3, 2), FF(3, 3)));
-  c[5] = ra(ra(rm(FF(1, 3), FF(1, 3)), rm(FF(2, 3), FF(2, 3))), rm(FF(3, 3), FF(3, 3)));
-  cc[0] = ra(ra(rm(c[0], c[0]), rm(c[1], c[1])), rm(c[3], c[3]));
-  cc[1] = ra(ra(rm(c[0], c[1]), rm(c[1], c[2])), rm(c[3], c[4]));
-  cc[2] = ra(ra(rm(c[1], c[1]), rm(c[2], c[2])), rm(c[4], c[4]));
-  cc[3] = ra(ra(rm(c[0], c[3]), rm(c[1], c[4])), rm(c[3], c[5]));
-  cc[4] = ra(ra(rm(c[1], c[3]), rm(c[2], c[4])), rm(c[4], c[5]));
-  cc[5] = ra(ra(rm(c[3], c[3]), rm(c[4], c[4])), rm(c[5], c[5]));
+  c[0] = dot3f(FF(1, 1), FF(1, 1), FF(2, 1), FF(2, 1), FF(3, 1), FF(3, 1));
+  c[1] = dot3f(FF(1, 1), FF(1, 2), FF(2, 1), FF(2, 2), FF(3, 1), FF(3, 2));
+  c[2] = dot3f(FF(1, 2), FF(1, 2), FF(2, 2), FF(2, 2), FF(3, 2), FF(3, 2));
+  c[3] = dot3f(FF(1, 1), FF(1, 3), FF(2, 1), FF(2, 3), FF(3, 1), FF(3, 3));
+  c[4] = dot3f(FF(1, 2), FF(1, 3), FF(2, 2), FF(2, 3), FF(3, 2), FF(3, 3));
+  c[5] = dot3f(FF(1, 3), FF(1, 3), FF(2, 3), FF(2, 3), FF(3, 3), FF(3, 3));
+  cc[0] = dot3f(c[0], c[0], c[1], c[1], c[3], c[3]);
+  cc[1] = dot3f(c[0], c[1], c[1], c[2], c[3], c[4]);
+  cc[2] = dot3f(c[1], c[1], c[2], c[2], c[4], c[4]);
+  cc[3] = dot3f(c[0], c[3], c[1], c[4], c[3], c[5]);
+  cc[4] = dot3f(c[1], c[3], c[2], c[4], c[4], c[5]);
+  cc[5] = dot3f(c[3], c[3], c[4], c[4], c[5], c[5]);
   const double third = 1.0 / 3.0;
   double m11 = c[0], m12 = c[1], m13 = c[3], m22 = c[2], m23 = c[4], m33 = c[5];
   double de = rm(m12, m23), dd = rm(m12, m12), ee = rm(m23, m23), ff = rm(m13, m13);
   double m = ra(ra(m11, m22), m33);
-  double c1 = rs(ra(ra(rm(m11, m22), rm(m11, m33)), rm(m22, m33)), ra(ra(dd, ee), ff));
-  double c0 = rs(rs(ra(ra(rm(m33, dd), rm(m11, ee)), rm(m22, ff)), rm(rm(m11, m22), m33)), rm(rm(2.0, m13), de));
-  double p = rs(rm(m, m), rm(3.0, c1));
-  double q = rs(rm(m, rs(p, rm(1.5, c1))), rm(13.5, c0));
+  double c1 = rs(fm(m22, m33, fm(m11, m33, rm(m11, m22))), ra(ra(dd, ee), ff));
+  double c0 = fm(-rm(2.0, m13), de, fm(-rm(m11, m22), m33, fm(m22, ff, fm(m11, ee, rm(m33, dd)))));
+  double p = fm(m, m, -rm(3.0, c1));
+  double q = fm(m, rs(p, rm(1.5, c1)), -rm(13.5, c0));
   double sqrtp = sqrt(fabs(p));
-  double phi = rm(27.0, ra(rm(rm(rm(0.25, c1), c1), rs(p, c1)), rm(c0, ra(q, rm(6.75, c0)))));
+  double phi = rm(27.0, fm(rm(rm(0.25, c1), c1), rs(p, c1), rm(c0, fm(6.75, c0, q))));
   phi = rm(third, atan2(sqrt(fabs(phi)), q));
   const double iroot3 = 0.5773502691896258;    // 1/sqrt(3) rounded to double
   double cphi = rm(sqrtp, cos(phi));
@@ -281,27 +299,27 @@ __device__ __forceinline__ void polar_rotation_ref(const double* F, double* R) {
   if (e3 < e2) { double t = e2; e2 = e3; e3 = t; }
   double v1 = sqrt(e1), v2 = sqrt(e2), v3 = sqrt(e3);
   double iu = ra(ra(v1, v2), v3);
-  double iiu = ra(ra(rm(v1, v2), rm(v2, v3)), rm(v1, v3));
+  double iiu = fm(v1, v3, fm(v2, v3, rm(v1, v2)));
   double iiiu = rm(rm(v1, v2), v3);
-  double a2 = rd(1.0, rm(iiiu, rs(rm(iu, iiu), iiiu)));
-  double b2 = rs(rm(rm(iu, iiu), iiu), rm(iiiu, ra(rm(iu, iu), iiu)));
-  double c2 = rs(-iiiu, rm(iu, rs(rm(iu, iu), rm(2.0, iiu))));
+  double a2 = rd(1.0, rm(iiiu, fm(iu, iiu, -iiiu)));
+  double b2 = fm(rm(iu, iiu), iiu, -rm(iiiu, fm(iu, iu, iiu)));
+  double c2 = fm(-iu, fm(iu, iu, -rm(2.0, iiu)), -iiiu);
   double d2 = iu;
-  double ui0 = rm(a2, ra(ra(b2, rm(c2, c[0])), rm(d2, cc[0])));
-  double ui1 = rm(a2, ra(rm(c2, c[1]), rm(d2, cc[1])));
-  double ui2 = rm(a2, ra(ra(b2, rm(c2, c[2])), rm(d2, cc[2])));
-  double ui3 = rm(a2, ra(rm(c2, c[3]), rm(d2, cc[3])));
-  double ui4 = rm(a2, ra(rm(c2, c[4]), rm(d2, cc[4])));
-  double ui5 = rm(a2, ra(ra(b2, rm(c2, c[5])), rm(d2, cc[5])));
-  R[0] = ra(ra(rm(FF(1, 1), ui0), rm(FF(1, 2), ui1)), rm(FF(1, 3), ui3));
-  R[3] = ra(ra(rm(FF(1, 1), ui1), rm(FF(1, 2), ui2)), rm(FF(1, 3), ui4));
-  R[6] = ra(ra(rm(FF(1, 1), ui3), rm(FF(1, 2), ui4)), rm(FF(1, 3), ui5));
-  R[1] = ra(ra(rm(FF(2, 1), ui0), rm(FF(2, 2), ui1)), rm(FF(2, 3), ui3));
-  R[4] = ra(ra(rm(FF(2, 1), ui1), rm(FF(2, 2), ui2)), rm(FF(2, 3), ui4));
-  R[7] = ra(ra(rm(FF(2, 1), ui3), rm(FF(2, 2), ui4)), rm(FF(2, 3), ui5));
-  R[2] = ra(ra(rm(FF(3, 1), ui0), rm(FF(3, 2), ui1)), rm(FF(3, 3), ui3));
-  R[5] = ra(ra(rm(FF(3, 1), ui1), rm(FF(3, 2), ui2)), rm(FF(3, 3), ui4));
-  R[8] = ra(ra(rm(FF(3, 1), ui3), rm(FF(3, 2), ui4)), rm(FF(3, 3), ui5));
+  double ui0 = rm(a2, fm(d2, cc[0], fm(c2, c[0], b2)));
+  double ui1 = rm(a2, fm(d2, cc[1], rm(c2, c[1])));
+  double ui2 = rm(a2, fm(d2, cc[2], fm(c2, c[2], b2)));
+  double ui3 = rm(a2, fm(d2, cc[3], rm(c2, c[3])));
+  double ui4 = rm(a2, fm(d2, cc[4], rm(c2, c[4])));
+  double ui5 = rm(a2, fm(d2, cc[5], fm(c2, c[5], b2)));
+  R[0] = dot3f(FF(1, 1), ui0, FF(1, 2), ui1, FF(1, 3), ui3);
+  R[3] = dot3f(FF(1, 1), ui1, FF(1, 2), ui2, FF(1, 3), ui4);
+  R[6] = dot3f(FF(1, 1), ui3, FF(1, 2), ui4, FF(1, 3), ui5);
+  R[1] = dot3f(FF(2, 1), ui0, FF(2, 2), ui1, FF(2, 3), ui3);
+  R[4] = dot3f(FF(2, 1), ui1, FF(2, 2), ui2, FF(2, 3), ui4);
+  R[7] = dot3f(FF(2, 1), ui3, FF(2, 2), ui4, FF(2, 3), ui5);
+  R[2] = dot3f(FF(3, 1), ui0, FF(3, 2), ui1, FF(3, 3), ui3);
+  R[5] = dot3f(FF(3, 1), ui1, FF(3, 2), ui2, FF(3, 3), ui4);
+  R[8] = dot3f(FF(3, 1), ui3, FF(3, 2), ui4, FF(3, 3), ui5);
 #undef FF
 }
 

@@ -115,12 +115,8 @@ __global__ void __launch_bounds__(kRecoverThreads) k_mm10_kin(RecoverArgs a, int
       const double u1x = ra(ue[n], du[n]), u1y = ra(ue[NN + n], du[NN + n]), u1z = ra(ue[2 * NN + n], du[2 * NN + n]);
       const double uhx = ra(ue[n], rm(0.5, du[n])), uhy = ra(ue[NN + n], rm(0.5, du[NN + n])),
                    uhz = ra(ue[2 * NN + n], rm(0.5, du[2 * NN + n]));
-      th1[0] = ra(th1[0], rm(tx, u1x)); th1[1] = ra(th1[1], rm(tx, u1y)); th1[2] = ra(th1[2], rm(tx, u1z));
-      th1[3] = ra(th1[3], rm(ty, u1x)); th1[4] = ra(th1[4], rm(ty, u1y)); th1[5] = ra(th1[5], rm(ty, u1z));
-      th1[6] = ra(th1[6], rm(tz, u1x)); th1[7] = ra(th1[7], rm(tz, u1y)); th1[8] = ra(th1[8], rm(tz, u1z));
-      thh[0] = ra(thh[0], rm(tx, uhx)); thh[1] = ra(thh[1], rm(tx, uhy)); thh[2] = ra(thh[2], rm(tx, uhz));
-      thh[3] = ra(thh[3], rm(ty, uhx)); thh[4] = ra(thh[4], rm(ty, uhy)); thh[5] = ra(thh[5], rm(ty, uhz));
-      thh[6] = ra(thh[6], rm(tz, uhx)); thh[7] = ra(thh[7], rm(tz, uhy)); thh[8] = ra(thh[8], rm(tz, uhz));
+      tcomp1_node(th1, tx, ty, tz, u1x, u1y, u1z);
+      tcomp1_node(thh, tx, ty, tz, uhx, uhy, uhz);
     }
     F1[0] = th1[0] + 1.0; F1[1] = th1[1]; F1[2] = th1[2]; F1[3] = th1[3]; F1[4] = th1[4] + 1.0;
     F1[5] = th1[5]; F1[6] = th1[6]; F1[7] = th1[7]; F1[8] = th1[8] + 1.0;

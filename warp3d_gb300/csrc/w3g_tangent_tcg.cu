@@ -17,8 +17,9 @@
 // (r, s, gp), 64 x 72) with a per-element vector H (72 values per pair
 // (i,j)): Ke of every element of the model is one GEMM
 //   D[(e, ij), (a, b)] = sum_k H[(e, ij), k] M[(a, b), k],   K = 72,
-// run here as M = 128 rows (16 elements x 8 row slots, 6 used), N = 64,
-// on tcgen05.mma with an FP32 accumulator in tensor memory.
+// run here as M = 128 rows (8 row slots x 16 elements, row = slot*16 +
+// element, 6 slots used), N = 64, on tcgen05.mma with an FP32 accumulator
+// in tensor memory.
 //
 // Why this form: the per-element CUDA-core work shrinks to the Gauss-point
 // quantities ([D*] = [q][D][q]^T - Q-bar, Gamma, {T}, H: ~600 FP32 FMA per
@@ -72,7 +73,8 @@ constexpr int kSlots = 8;                    // A rows per element (6 pairs i <=
 constexpr int kM = kTile * kSlots;           // 128
 constexpr int kN = NN * NN;                  // 64 node pairs (a, b)
 constexpr int kKLive = 9 * NG;               // 72 = (r, s, gp)
-constexpr int kConsumers = 256;              // warps 0-7
+constexpr int kParts = 2;                    // threads per (element, Gauss point)
+constexpr int kConsumers = 128 * kParts;     // warps 0-7
 constexpr int kThreads = kConsumers + 32;    // + producer warp 8
 constexpr int kTmemCols = 64;
 constexpr long long kDrainLimit = 1ll << 26; // polls when waiting out copies / MMAs after an abort
@@ -116,8 +118,9 @@ static_assert(kTile * UT * 4 <= Form<true, false>::kOpA, "Ke staging must fit in
 
 struct TcgStatic {
   float dn[NG * 3 * NN + NG];          // dN/dxi per Gauss point (float) + weights
-  float x[kTile][TOT];                 // x(n+1) relative to node 1 of each element
+  float x[kTile][TOT + 1];             // x(n+1) relative to node 1 of each element (rows padded: banks)
   float dx[kTile * NG][21];            // [D*] lower triangle per (element, Gauss point): the two halves' rows
+  TcgTile hdr[3];                      // the tile in each stage, written by the producer before its arrival
   unsigned long long full[3], empty[3], mma;
   uint32_t tmem_base;
   // a bounded wait gave up: the producer's flag is written by the producer
@@ -213,21 +216,47 @@ __host__ __device__ constexpr int voigt(int i, int p) {
   return i == p ? i : (i + p == 1 ? 3 : (i + p == 3 ? 4 : 5));
 }
 
-// One half of the Gauss-point work of (element pe, point pg) of a tile:
-// Gamma, w det[J], the rows of [D*] = [q][D][q]^T - Q-bar this half owns
-// (H = 0: rows 0, 3, 5; H = 1: rows 1, 2, 4; the other half's rows come
-// through shared memory), {T}, and H^ij = Gamma^T X^ij Gamma for the half's
-// three pairs (H = 0: 00 01 02; H = 1: 11 12 22). Both halves reach the
-// same named barrier (the exchange) whether live or not.
+// row r of the 6 x 6 strain-rotation matrix [q] of getrm1 option 2
+// (gtmat1.f:803-846; the same entries as rotation_q2) from R, column-major:
+// rows 0-2 the normal components of R's rows a = r, rows 3-5 the pairs
+// (a, b) = (0, 1), (1, 2), (0, 2)
+__device__ __forceinline__ void q_row(const float* R, int r, float* o) {
+#define RX(i, j) R[(i) + 3 * (j)]
+  if (r < 3) {
+    const int x = r;
+    o[0] = RX(x, 0) * RX(x, 0); o[1] = RX(x, 1) * RX(x, 1); o[2] = RX(x, 2) * RX(x, 2);
+    o[3] = 2.f * RX(x, 0) * RX(x, 1); o[4] = 2.f * RX(x, 2) * RX(x, 1); o[5] = 2.f * RX(x, 0) * RX(x, 2);
+  } else {
+    const int x = r == 4 ? 1 : 0, y = r == 3 ? 1 : 2;
+    o[0] = RX(x, 0) * RX(y, 0); o[1] = RX(x, 1) * RX(y, 1); o[2] = RX(x, 2) * RX(y, 2);
+    o[3] = RX(x, 0) * RX(y, 1) + RX(y, 0) * RX(x, 1);
+    o[4] = RX(x, 1) * RX(y, 2) + RX(x, 2) * RX(y, 1);
+    o[5] = RX(x, 0) * RX(y, 2) + RX(x, 2) * RX(y, 0);
+  }
+#undef RX
+}
+
+// rows of [D*] formed by part H of a Gauss point's two threads: {0, 3, 5}
+// and {1, 2, 4} (11 and 10 lower-triangle entries)
+__host__ __device__ constexpr int row_of_part(int h, int jj) {
+  return h == 0 ? (jj == 0 ? 0 : jj == 1 ? 3 : 5) : (jj == 0 ? 1 : jj == 1 ? 2 : 4);
+}
+
+// One part (H = 0, 1) of the Gauss-point work of (element pe, point pg)
+// of a tile: Gamma, w det[J], the three rows of [D*] = [q][D][q]^T - Q-bar
+// this part owns (row_of_part; the other rows come from the other part
+// through shared memory), {T}, and H^ij = Gamma^T X^ij Gamma for the
+// part's three pairs (slots 3H .. 3H + 2 of 00 01 02 11 12 22), written
+// into the A operand. Both parts reach the same named barrier (the
+// exchange) whether their element is live or not.
 template <bool kBF16, bool kSplit, int H>
-__device__ __forceinline__ void point_h(const TangentArgs& a, const BlockDesc& bd, const Chunk& ch,
-                                        const unsigned char* st, TcgStatic& T, int pe, int pg, bool live,
-                                        unsigned char* opA) {
+__device__ __forceinline__ void point_h(const TangentArgs& a, const TcgTile& tl, const unsigned char* st,
+                                        TcgStatic& T, int pe, int pg, bool live, unsigned char* opA) {
   using F = Form<kBF16, kSplit>;
   const int item = pe * NG + pg;
   float gam[9], f = 0.f, Tw[6];
   if (live) {
-    const int i = ch.i0 + pe;
+    const int i = tl.i0 + pe;
     const float* dnx = T.dn + (pg * 3 + 0) * NN;
     const float* dne = T.dn + (pg * 3 + 1) * NN;
     const float* dnz = T.dn + (pg * 3 + 2) * NN;
@@ -237,38 +266,37 @@ __device__ __forceinline__ void point_h(const TangentArgs& a, const BlockDesc& b
     f = w * dj;
     // w det[J] [D], lower triangle row-wise (cep, or mm10 history1(1:36))
     float C[21];
-    if (bd.mat == W3G_MAT_CRYSTAL) {
-      const double* Hh = a.hist1 + bd.hist_off + ((long long)i * NG + pg) * kHistMM10;
+    if (tl.flags & 2) {
+      const double* Hh = a.hist1 + tl.hist_off + ((long long)i * NG + pg) * kHistMM10;
 #pragma unroll
       for (int r = 0, q = 0; r < 6; ++r)
 #pragma unroll
         for (int c = 0; c <= r; ++c, ++q) C[q] = f * (float)Hh[r + 6 * c];
     } else {
       const double* cp = reinterpret_cast<const double*>(
-          st + kStCep + pg * kCepSlab + pad_of(a.cep + bd.cep_off + ((long long)pg * bd.span + ch.i0) * 21));
+          st + kStCep + pg * kCepSlab + pad_of(a.cep + tl.cep_off + ((long long)pg * tl.span + tl.i0) * 21));
 #pragma unroll
       for (int q = 0; q < 21; ++q) C[q] = f * (float)cp[pe * 21 + q];
     }
-    if (bd.geonl) {
-      const long long g0 = (bd.gp_off + (long long)ch.i0 * NG) * 9;
+    if (tl.flags & 1) {
+      const long long g0 = (tl.gp_off + (long long)tl.i0 * NG) * 9;
       const double* rp = reinterpret_cast<const double*>(st + kStRot + pad_of(a.rot_n1 + g0)) + (pe * NG + pg) * 9;
       const double* up = reinterpret_cast<const double*>(st + kStUrcs + pad_of(a.urcs_n1 + g0)) + (pe * NG + pg) * 9;
-      float R[9], q[36], ur[6], cs[6];
+      float R[9], q[36], cs[6];
 #pragma unroll
       for (int m = 0; m < 9; ++m) R[m] = (float)rp[m];
 #pragma unroll
-      for (int m = 0; m < 6; ++m) ur[m] = (float)up[m];
-      rotation_q2<float>(R, q);
+      for (int r = 0; r < 6; ++r) q_row(R, r, q + 6 * r);
 #pragma unroll
       for (int r = 0; r < 6; ++r) {
         float v = 0.f;
 #pragma unroll
-        for (int m = 0; m < 6; ++m) v += q[6 * r + m] * ur[m];
+        for (int m = 0; m < 6; ++m) v += q[6 * r + m] * (float)up[m];
         cs[r] = v;                                   // Cauchy stress at n+1
       }
 #pragma unroll
       for (int jj = 0; jj < 3; ++jj) {
-        const int j = H == 0 ? (jj == 0 ? 0 : jj == 1 ? 3 : 5) : (jj == 0 ? 1 : jj == 1 ? 2 : 4);
+        const int j = row_of_part(H, jj);
         float tc[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
@@ -306,7 +334,7 @@ __device__ __forceinline__ void point_h(const TangentArgs& a, const BlockDesc& b
     } else {
 #pragma unroll
       for (int jj = 0; jj < 3; ++jj) {
-        const int j = H == 0 ? (jj == 0 ? 0 : jj == 1 ? 3 : 5) : (jj == 0 ? 1 : jj == 1 ? 2 : 4);
+        const int j = row_of_part(H, jj);
 #pragma unroll
         for (int c = 0; c <= j; ++c) T.dx[item][lw(j, c)] = C[lw(j, c)];
       }
@@ -314,15 +342,16 @@ __device__ __forceinline__ void point_h(const TangentArgs& a, const BlockDesc& b
       for (int m = 0; m < 6; ++m) Tw[m] = 0.f;
     }
   }
-  asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));   // both halves' rows of [D*] in T.dx
+  asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");   // both parts' rows of [D*] in T.dx
   if (!live) return;
   float Dl[21];
 #pragma unroll
   for (int z = 0; z < 21; ++z) Dl[z] = T.dx[item][z];
 #pragma unroll
   for (int pp = 0; pp < 3; ++pp) {
-    const int ii = H == 0 ? 0 : (pp == 2 ? 2 : 1);
-    const int jj = H == 0 ? pp : (pp == 0 ? 1 : 2);
+    const int slot = 3 * H + pp;            // pairs 00 01 02 11 12 22
+    const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+    const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
     float X[3][3];
 #pragma unroll
     for (int p = 0; p < 3; ++p)
@@ -338,8 +367,8 @@ __device__ __forceinline__ void point_h(const TangentArgs& a, const BlockDesc& b
 #pragma unroll
       for (int s2 = 0; s2 < 3; ++s2)
         Y[p][s2] = X[p][0] * gam[3 * s2] + X[p][1] * gam[3 * s2 + 1] + X[p][2] * gam[3 * s2 + 2];
-    // A operand row (element pe, slot 3H + pp), k = (r*3 + s)*8 + gp
-    const int row = pe * kSlots + 3 * H + pp;
+    // A operand row (slot, element pe), k = (r*3 + s)*8 + gp
+    const int row = slot * kTile + pe;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -350,7 +379,7 @@ __device__ __forceinline__ void point_h(const TangentArgs& a, const BlockDesc& b
 }
 
 template <bool kBF16, bool kSplit>
-__global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a, const Chunk* tiles, int ntiles,
+__global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a, const TcgTile* tiles, int ntiles,
                                                                    int* tc_timeout) {
   using F = Form<kBF16, kSplit>;
   constexpr int S = F::kStages;
@@ -403,19 +432,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
 
   if (warp == kConsumers / 32) {
     // ================= producer =================
+    constexpr int kPerLane = kTile * TOT / 32;   // 12 gathered dofs per lane and tile
+    TcgTile nxt = tiles[blockIdx.x];
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+      const TcgTile tl = nxt;
+      if (t + (int)gridDim.x < ntiles) nxt = tiles[t + gridDim.x];   // next tile's record, in flight meanwhile
+      // this tile's dof indices, all loads issued before the first copy
+      const long long dbase = tl.einf_off + (long long)tl.i0 * TOT;
+      const int nv = tl.n * TOT;
+      const bool geonl = tl.flags & 1;
+      int ci[kPerLane], ei[kPerLane];
+#pragma unroll
+      for (int j = 0; j < kPerLane; ++j) {
+        const int q = lane + 32 * j;
+        ci[j] = q < nv ? a.cdest[dbase + q] - 1 : 0;
+        ei[j] = q < nv && geonl ? a.edest[dbase + q] - 1 : 0;
+      }
       const int s = k % S, use = k / S;
       if (use > 0 && !wait_phase(&T.empty[s], (use - 1) & 1, limit, cabort)) {
         if (lane == 0) *pabort = 1;
         break;
       }
       if (*cabort) break;
-      const Chunk ch = tiles[t];
-      const BlockDesc bd = a.blocks[ch.blk];
       unsigned char* st = stages + s * kStage;
       const uint32_t bar = su32(&T.full[s]);
       if (lane == 0) {
+        T.hdr[s] = tl;   // published by the arrival below (release)
         uint32_t tx = 0;
         // byte total first (expect_tx must not trail the copies' completion)
         for (int pass = 0; pass < 2; ++pass) {
@@ -428,31 +471,31 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
             if (pass == 1) bulk_g2s(dst, (const void*)p16, bytes, bar);
             txc += bytes;
           };
-          if (bd.mat != W3G_MAT_CRYSTAL)
+          if (!(tl.flags & 2))
             for (int gp = 0; gp < NG; ++gp)
-              range(a.cep + bd.cep_off + ((long long)gp * bd.span + ch.i0) * 21, (long long)ch.n * 21,
+              range(a.cep + tl.cep_off + ((long long)gp * tl.span + tl.i0) * 21, (long long)tl.n * 21,
                     su32(st + kStCep + gp * kCepSlab));
-          if (bd.geonl) {
-            const long long g0 = (bd.gp_off + (long long)ch.i0 * NG) * 9;
-            range(a.rot_n1 + g0, (long long)ch.n * NG * 9, su32(st + kStRot));
-            range(a.urcs_n1 + g0, (long long)ch.n * NG * 9, su32(st + kStUrcs));
+          if (geonl) {
+            const long long g0 = (tl.gp_off + (long long)tl.i0 * NG) * 9;
+            range(a.rot_n1 + g0, (long long)tl.n * NG * 9, su32(st + kStRot));
+            range(a.urcs_n1 + g0, (long long)tl.n * NG * 9, su32(st + kStUrcs));
           }
           tx = txc;
         }
       }
       // gathers of the nodal values (u and du only for finite strain)
-      const long long dbase = bd.einf_off + (long long)ch.i0 * TOT;
-      const int nv = ch.n * TOT;
       double* xc = reinterpret_cast<double*>(st + kStXc);
       double* xu = reinterpret_cast<double*>(st + kStXu);
       double* xdu = reinterpret_cast<double*>(st + kStXdu);
-      for (int q = lane; q < nv; q += 32) {
-        const double* pc = a.c + (a.cdest[dbase + q] - 1);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(xc + q)), "l"(pc) : "memory");
-        if (bd.geonl) {
-          const int ed = a.edest[dbase + q] - 1;
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(xu + q)), "l"(a.u + ed) : "memory");
-          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(xdu + q)), "l"(a.du + ed) : "memory");
+#pragma unroll
+      for (int j = 0; j < kPerLane; ++j) {
+        const int q = lane + 32 * j;
+        if (q < nv) {
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(xc + q)), "l"(a.c + ci[j]) : "memory");
+          if (geonl) {
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(xu + q)), "l"(a.u + ei[j]) : "memory");
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(xdu + q)), "l"(a.du + ei[j]) : "memory");
+          }
         }
       }
       asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
@@ -460,27 +503,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
     }
   } else {
     // ================= consumers =================
-    // warps 0-3 and 4-7 take the two halves of every (element, Gauss
-    // point): the half is uniform over a warp
-    const int h = warp >> 2, item = (warp & 3) * 32 + lane;
-    const int pe = item >> 3, pg = item & 7;
+    // warps 0-3 and 4-7 take the two parts of every (element, Gauss
+    // point): the part is uniform over a warp. A warp holds 8 elements x 4
+    // Gauss points, lane = element (low 3 bits) + 8 x point, so that its
+    // stores into an A row slot (rows slot*16 + element) fall in 32
+    // distinct banks
+    const int h = warp >> 2;
+    const int pe = (lane & 7) + 8 * (warp & 1), pg = (lane >> 3) + 4 * ((warp >> 1) & 1);
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
       const int s = k % S;
-      const Chunk ch = tiles[t];
-      const BlockDesc bd = a.blocks[ch.blk];
       const unsigned char* st = stages + s * kStage;
       if (!wait_phase(&T.full[s], (k / S) & 1, limit, pabort)) *cabort = 1;
       // previous tile's Ke store must have read the staging (A region)
       if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (*cabort) break;
+      // the tile record, read from shared memory where needed; what the
+      // epilogue needs is copied before the stage (and record) is released
+      const TcgTile& tl = T.hdr[s];
+      const int tn = tl.n;
+      float* const out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)tl.i0 * UT;
       // element coordinates at n+1 relative to node 1
-      for (int q = tid; q < ch.n * TOT; q += kConsumers) {
+      for (int q = tid; q < tl.n * TOT; q += kConsumers) {
         const int e = q / TOT, d = q % TOT, q0 = e * TOT + (d / NN) * NN;
         const double* xc = reinterpret_cast<const double*>(st + kStXc);
         double v = xc[q], ref = xc[q0];
-        if (bd.geonl) {
+        if (tl.flags & 1) {
           const double* xu = reinterpret_cast<const double*>(st + kStXu);
           const double* xdu = reinterpret_cast<const double*>(st + kStXdu);
           v = v + xu[q] + xdu[q];
@@ -488,12 +537,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
         }
         T.x[e][d] = (float)(v - ref);
       }
-      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       // the Gauss-point work, written into the A operand (the previous
       // tile's MMAs are complete and its Ke store has read the region)
-      const bool live = pe < ch.n;
-      if (h == 0) point_h<kBF16, kSplit, 0>(a, bd, ch, st, T, pe, pg, live, opA);
-      else point_h<kBF16, kSplit, 1>(a, bd, ch, st, T, pe, pg, live, opA);
+      const bool live = pe < tl.n;
+      if (h == 0) point_h<kBF16, kSplit, 0>(a, tl, st, T, pe, pg, live, opA);
+      else point_h<kBF16, kSplit, 1>(a, tl, st, T, pe, pg, live, opA);
       if (kBF16) {   // the K padding (72..79) must be finite zeros: the staging reuses the region
         for (int row = tid; row < kM; row += kConsumers)
           for (int kk = kKLive; kk < F::kK; ++kk) {
@@ -502,19 +551,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
           }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (tid == 0) {
         // stage consumed: hand it back to the producer
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&T.empty[s])) : "memory");
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t a0 = su32(opA), b0 = su32(opB);
-#pragma unroll
+        // descriptors advanced in the start-address field (16-byte units):
+        // one k-step = two core matrices along K = 256 bytes
+        const uint64_t da = sdesc(su32(opA), F::kSBO), db = sdesc(su32(opB), F::kSBO);
+#pragma unroll 1
         for (int ks = 0; ks < F::kSteps; ++ks) {
-          const uint32_t o = ks * 256;   // two core matrices along K
-          mma<kBF16>(tmem, sdesc(a0 + o, F::kSBO), sdesc(b0 + o, F::kSBO), ks > 0);
+          const uint64_t o = (uint64_t)ks * (256 >> 4);
+          mma<kBF16>(tmem, da + o, db + o, ks > 0);
           if (kSplit) {
-            mma<kBF16>(tmem, sdesc(a0 + o, F::kSBO), sdesc(b0 + F::kOpB + o, F::kSBO), true);
-            mma<kBF16>(tmem, sdesc(a0 + F::kOpA + o, F::kSBO), sdesc(b0 + o, F::kSBO), true);
+            mma<kBF16>(tmem, da + o, db + o + (F::kOpB >> 4), true);
+            mma<kBF16>(tmem, da + o + (F::kOpA >> 4), db + o, true);
           }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -527,46 +578,50 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
         wait_phase(&T.mma, k & 1, kDrainLimit, nullptr);
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (*cabort) break;
       // accumulator -> packed Ke in the staging (the A region: the MMAs are done)
       {
         float* ke = reinterpret_cast<float*>(opA);
-        const int quad = warp & 3, half = warp >> 2;
-        const int row = 32 * quad + lane, e = row >> 3, slot = row & 7;
-        uint32_t v[32];
+        // warp w: lane quadrant w % 4, columns 32 * (w / 4) .. + 31
+        const bool ld_warp = warp < 8;
+        const int quad = warp & 3, half = (warp >> 2) & 1;
+        const int row = 32 * quad + lane, e = row & (kTile - 1), slot = row >> 4;
         const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(32 * half);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-              "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-              "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        // all accumulator reads done before the A region is overwritten
-        asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
-        if (slot < 6 && e < ch.n) {
+        if (ld_warp) {
           const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
           const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+          const bool keep = slot < 6 && e < tn;
           const float bf = (float)a.beta_fact;
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const int ab = 32 * half + c, an = ab >> 3, bn = ab & 7;
-            if (ii == jj && an > bn) continue;
-            const int d1 = ii * NN + an, d2 = jj * NN + bn;
-            ke[e * UT + d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[c]) * bf;
+          for (int p16 = 0; p16 < 2; ++p16) {
+            uint32_t v[16];   // the load and its wait in one statement
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                "tcgen05.wait::ld.sync.aligned;"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr + 16 * p16)
+                : "memory");
+            // the MMAs are complete: the staging may overwrite the A operand
+            if (keep) {
+#pragma unroll
+              for (int c = 0; c < 16; ++c) {
+                const int ab = 32 * half + 16 * p16 + c, an = ab >> 3, bn = ab & 7;
+                if (ii == jj && an > bn) continue;
+                const int d1 = ii * NN + an, d2 = jj * NN + bn;
+                ke[e * UT + d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[c]) * bf;
+              }
+            }
           }
         }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       {
-        float* out = reinterpret_cast<float*>(a.estiff) + bd.estiff_off + (long long)ch.i0 * UT;
-        const uint32_t bytes = (uint32_t)ch.n * UT * 4;
+        const uint32_t bytes = (uint32_t)tn * UT * 4;
         if (((uintptr_t)out & 15) == 0) {
           if (tid == 0) {
             asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(out), "r"(su32(opA)),
@@ -575,8 +630,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
           }
         } else {   // block offset not 16-byte aligned (after a block of another element type)
           const float* ke = reinterpret_cast<const float*>(opA);
-          for (int q = tid; q < ch.n * UT; q += kConsumers) out[q] = ke[q];
-          asm volatile("bar.sync 1, %0;" ::"n"(kConsumers));
+          for (int q = tid; q < tn * UT; q += kConsumers) out[q] = ke[q];
+          asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
         }
       }
       if (tid == 0) T.done = k + 1;
@@ -595,10 +650,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
     int q = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++q) {
       if (q < T.done) continue;
-      const Chunk ch = tiles[t];
-      const BlockDesc bd = a.blocks[ch.blk];
-      float* out = reinterpret_cast<float*>(a.estiff) + bd.estiff_off + (long long)ch.i0 * UT;
-      for (int z = tid; z < ch.n * UT; z += kThreads) out[z] = __int_as_float(0x7fc00000);
+      const TcgTile tl = tiles[t];
+      float* out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)tl.i0 * UT;
+      for (int z = tid; z < tl.n * UT; z += kThreads) out[z] = __int_as_float(0x7fc00000);
     }
   }
   if (warp == 0) {
