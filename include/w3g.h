@@ -64,7 +64,9 @@ extern "C" {
 
 /* Material models (iprops(25,elem)) */
 #define W3G_MAT_BILINEAR 1    /* mm01: bilinear Mises, mixed hardening */
+#define W3G_MAT_UMAT 8        /* Abaqus UMAT interface (drive_umat_update) */
 #define W3G_MAT_CRYSTAL 10    /* mm10: crystal plasticity */
+#define W3G_UMAT_NPROPS 50    /* UMAT properties per element (dmatprp(151:200)) */
 
 /* Status codes */
 #define W3G_OK 0
@@ -141,6 +143,11 @@ typedef struct w3g_model_desc {
                                    mm10 tangents not symmetrized
                                    (mm10_a.f:1165-1166); FP64 and FP32
                                    tangent forms */
+  /* UMAT elements (iprops(25) = 8) only; NULL otherwise */
+  const double* umat_props;     /* W3G_UMAT_NPROPS*noelem: the element's
+                                   material umat values as rknstr loads
+                                   them (local_work%umat_props,
+                                   src/rknstr.f:1528) */
 } w3g_model_desc;
 
 /*
@@ -192,6 +199,16 @@ const char* w3g_last_error(void);
    w3g_tanstf returns W3G_EFATAL if a tensor-core tile's bounded wait for
    its MMAs gave up (that tile's Ke is then NaN). */
 int w3g_set_tangent_precision(w3g_context* ctx, int precision);
+
+/* The UMAT compiled into the library describes itself as WARP3D's
+   umat_set_features does (src/user_routines_umat.f:35-66): info[0] =
+   state variables per material point (the history words of W3G_MAT_UMAT
+   blocks), info[1] = 21 symmetric [D] terms, info[2] = 0 when it returns
+   unrotated Cauchy stresses (1: Cauchy), info[3] = output states. The
+   device UMAT is an Abaqus-style routine (warp3d_gb300/csrc/w3g_umat.cuh);
+   a user UMAT replaces it there and the library is rebuilt, as WARP3D
+   links user_routines_umat.f into its executable. */
+int w3g_umat_features(int* info);
 
 /* Bounded waits of the tensor-core tangent kernels (no WARP3D
    counterpart). Every wait of a kernel for its own copies or MMAs gives up

@@ -27,7 +27,8 @@ _libs = {}
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("w3o.cpp", "w3o.h", "w3o_mm10.cpp", "w3o_mm10.h", "build.sh")]
+    srcs = [os.path.join(HERE, f) for f in ("w3o.cpp", "w3o.h", "w3o_mm10.cpp", "w3o_mm10.h", "w3o_umat.cpp",
+                                             "w3o_umat.h", "build.sh")]
     newest = max(map(os.path.getmtime, srcs))
     stale = any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (LIB_PATH, FAST_LIB_PATH))
     if force or stale:
@@ -55,6 +56,7 @@ def load(fast: bool = False) -> C.CDLL:
         lib.w3o_shape_derivs.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _d, _d, _d]
         lib.w3o_mm01_point.argtypes = [C.c_int, C.c_int] + [_d] * 11
         lib.w3o_mm10_point.argtypes = [C.POINTER(abi.Crystal), _d, C.c_int, C.c_int, C.c_int, C.c_double] + [_d] * 6
+        lib.w3o_umat_point.argtypes = [_d, C.c_int, C.c_int, C.c_int] + [_d] * 7
         _libs[fast] = lib
     return _libs[fast]
 
@@ -107,3 +109,23 @@ def mm01_points(step, e, nu, beta, hprime, yld, cgn, deps, history):
     # cep (span, 36) column-major with (r,c) -> r + 6c  -> [n, 6(c), 6(r)] -> transpose
     cep_m = cep.reshape(36, n).T.reshape(n, 6, 6).transpose(0, 2, 1)
     return cgn1.reshape(9, n).T, hist1.reshape(11, n).T, hist.reshape(11, n).T, cep_m
+
+
+def umat_point(props, step, it, extrapolated, urcs_n, eps_n, uddt, hist):
+    """One point of the UMAT path: (status, urcs_n1 (9), hist1 (20), [D] 6x6
+    symmetric in WARP3D order)."""
+    lib = load()
+    f = lambda a, n: np.ascontiguousarray(np.resize(np.asarray(a, dtype=np.float64), n))
+    pr = np.zeros(abi.UMAT_NPROPS)
+    pr[:len(props)] = props
+    un1, h1, c21 = np.zeros(9), np.zeros(abi.HIST_UMAT), np.zeros(21)
+    st = lib.w3o_umat_point(dptr(pr), step, it, 1 if extrapolated else 0, dptr(f(urcs_n, 9)), dptr(f(eps_n, 6)),
+                            dptr(f(uddt, 6)), dptr(f(hist, abi.HIST_UMAT)), dptr(un1), dptr(h1), dptr(c21))
+    D = np.zeros((6, 6))
+    k = 0
+    for r in range(6):
+        for c in range(r + 1):
+            D[r, c] = D[c, r] = c21[k]
+            k += 1
+    return st, un1, h1, D
+

@@ -17,10 +17,10 @@ set -e
 here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/_build"
 ${CXX:-g++} -O3 -fopenmp -ffp-contract=off -fPIC -shared -std=c++17 \
-    -o "$here/_build/libw3o.so" "$here/w3o.cpp" "$here/w3o_mm10.cpp" &
+    -o "$here/_build/libw3o.so" "$here/w3o.cpp" "$here/w3o_mm10.cpp" "$here/w3o_umat.cpp" &
 checker=$!
 ${CXX:-g++} -O3 -fopenmp -ffp-contract=fast -fno-math-errno -fno-trapping-math -funroll-loops -fPIC -shared \
-    -std=c++17 -o "$here/_build/libw3o_fast.so" "$here/w3o.cpp" "$here/w3o_mm10.cpp" &
+    -std=c++17 -o "$here/_build/libw3o_fast.so" "$here/w3o.cpp" "$here/w3o_mm10.cpp" "$here/w3o_umat.cpp" &
 timed=$!
 wait $checker
 wait $timed

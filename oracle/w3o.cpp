@@ -20,6 +20,7 @@
 
 #include "w3o.h"
 #include "w3o_mm10.h"
+#include "w3o_umat.h"
 
 #include <cmath>
 #include <cstdint>
@@ -38,7 +39,9 @@ constexpr int NSTR = 6;
 constexpr int NSTRS = 9;
 constexpr int MM01_HIST = 11;   // mm01_set_sizes, src/mm01.f:976-979
 constexpr int MM10_HIST = w3o::MM10_HIST;
-inline int hist_size(int mat_type) { return mat_type == W3G_MAT_CRYSTAL ? MM10_HIST : MM01_HIST; }
+inline int hist_size(int mat_type) {
+  return mat_type == W3G_MAT_CRYSTAL ? MM10_HIST : mat_type == W3G_MAT_UMAT ? w3o::UMAT_NSTATV : MM01_HIST;
+}
 
 int g_threads = 0;
 int g_deterministic = 1;
@@ -867,6 +870,7 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
   const int* cdest = m->cdest[B.blk];
   const int hist = hist_size(B.mat_type);
   const bool crystal = B.mat_type == W3G_MAT_CRYSTAL;
+  const bool umat = B.mat_type == W3G_MAT_UMAT;
 
   // dupstr: element displacements (src/drive_eps_sig_internal_forces.f:560)
   A2 ue(totdof), due(totdof);
@@ -1050,6 +1054,27 @@ RecOut recover_block(const w3g_model_desc* m, const w3g_block_state* s, const Bl
         if (st != 0) { out.status = W3G_LOCAL_FAIL; out.bad_elem = e + 1; return out; }
         for (int k = 0; k < MM10_HIST; ++k) ehist1[g](i, k) = hn1[k];
         for (int k = 0; k < 9; ++k) urcs_n1[g](i, k) = un1[k];
+      }
+    } else if (umat) {
+      // drive_umat_update (src/rstgp1.f:3476-4010); the [D] goes to cep
+      // already symmetrised (rstgp1_make_symmetric_store)
+      for (int i = 0; i < span; ++i) {
+        const int e = B.felem - 1 + i;
+        double hn[w3o::UMAT_NSTATV], hn1[w3o::UMAT_NSTATV], un[9], un1[9], en[6], dd[6], c21[21];
+        for (int k = 0; k < w3o::UMAT_NSTATV; ++k) { hn[k] = ehist[g](i, k); hn1[k] = ehist1[g](i, k); }
+        for (int k = 0; k < 9; ++k) un[k] = urcs_n[g](i, k);
+        const double* epn = s->eps_n[B.blk] + ((size_t)i * ngp + g) * NSTR;
+        for (int k = 0; k < 6; ++k) { en[k] = epn[k]; dd[k] = uddt(i, k); }
+        const bool cut = w3o::umat_drive(m->umat_props + (size_t)e * w3o::UMAT_NPROPS, step, iter, extrapolated_du,
+                                         un, en, dd, hn, w3o::UMAT_NSTATV, un1, hn1, c21);
+        if (cut) { out.status = W3G_LOCAL_FAIL; out.bad_elem = e + 1; return out; }
+        for (int k = 0; k < w3o::UMAT_NSTATV; ++k) ehist1[g](i, k) = hn1[k];
+        for (int k = 0; k < 9; ++k) urcs_n1[g](i, k) = un1[k];
+        for (int k = 0; k < 21; ++k) {
+          const int r = kLowerR[k] - 1, c = kLowerC[k] - 1;
+          cep(i, r + 6 * c) = c21[k];
+          cep(i, c + 6 * r) = c21[k];
+        }
       }
     } else if (nonlinear_update) {
       mm01(span, step, mv, cgn, cgn1, dep, ehist[g], ehist1[g], rtse[g]);
@@ -1472,7 +1497,9 @@ int w3o_recover(const w3g_model_desc* m, const w3g_block_state* s, int step, int
   for (int blk = 0; blk < m->nelblk; ++blk) {
     Blk B;
     if (!block_info(m, blk, B)) return W3G_EUNSUPPORTED;
-    if (B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL) return W3G_EUNSUPPORTED;
+    if (B.mat_type != W3G_MAT_BILINEAR && B.mat_type != W3G_MAT_CRYSTAL && B.mat_type != W3G_MAT_UMAT)
+      return W3G_EUNSUPPORTED;
+    if (B.mat_type == W3G_MAT_UMAT && !m->umat_props) return W3G_EARG;
     // With b-bar WARP3D also scales F_n and F_n+1 of mm10 blocks to F-bar
     // (gtmat1_make_fbar, gtmat1.f:145-151), but only UMATs read those
     // (rstgp1.f:3786-3787): mm10 blocks take the b-bar strain increment,

@@ -49,6 +49,10 @@ int w3o_mm01_point(int span, int step, const double* e, const double* nu,
 /* Hook for the single-point crystal tests: one mm10 update of one Gauss
    point (one crystal) as drive_10_update calls it. hist_n, hist_n1: 158
    values; urcs_n, urcs_n1: 9; uddt: 6; rot_n1: 9 (column-major). */
+/* one point of the UMAT path (drive_umat_update + the example UMAT) */
+int w3o_umat_point(const double* props, int step, int iter, int extrapolated_du, const double* urcs_n,
+                   const double* eps_n, const double* uddt, const double* hist, double* urcs_n1,
+                   double* hist1, double* cep21);
 int w3o_mm10_point(const w3g_crystal* crystal, const double* angles, int step, int iter,
                    int extrapolated_du, double dt, double* hist_n, double* hist_n1,
                    const double* urcs_n, double* urcs_n1, const double* uddt,

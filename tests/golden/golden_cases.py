@@ -19,7 +19,7 @@ import os
 import numpy as np
 
 from warp3d_gb300 import abi
-from warp3d_gb300.model import Bilinear, Crystal, HostState, Model, Part, cube_mesh, random_orientations
+from warp3d_gb300.model import Bilinear, Crystal, HostState, Model, Part, Umat, cube_mesh, random_orientations
 from warp3d_gb300.newton import NewtonDriver, uniaxial_bcs
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -40,6 +40,16 @@ def _mm01_case(etype, nxyz, spans, shear, dyld=25.0, **opts):
     from tests.helpers import MESHES
     coords, incid = MESHES[etype](nxyz[0], jitter=0.08, seed=31, n_xyz=nxyz)
     mats = [Bilinear.from_hprime(200000.0, 0.3, 400.0 + dyld * b, 2000.0) for b in range(len(spans))]
+    model = Model(coords, parts=[Part(etype, incid, spans, mats)], **opts)
+    return model, nxyz, {"strain": 0.0015, "shear": shear, "extrapolate": False}
+
+
+def _umat_case(etype, nxyz, spans, shear, **opts):
+    """Material model 8 with the library's UMAT (the reference's example,
+    Mises with linear kinematic hardening), one yield stress per block."""
+    from tests.helpers import MESHES
+    coords, incid = MESHES[etype](nxyz[0], jitter=0.08, seed=37, n_xyz=nxyz)
+    mats = [Umat((200000.0, 0.3, 400.0 + 25.0 * b, 2000.0, 0.0)) for b in range(len(spans))]
     model = Model(coords, parts=[Part(etype, incid, spans, mats)], **opts)
     return model, nxyz, {"strain": 0.0015, "shear": shear, "extrapolate": False}
 
@@ -67,6 +77,12 @@ CASES = {
     # differences of the internal forces to 1e-9)
     "hex8_mm10_bbar": lambda: _mm10_case(bbar=True),
     "tet10_mm01_small": lambda: _mm01_case(abi.ETYPE_TET10, (1, 1, 2), [7, 5], 0.0, dyld=0.0, geonl=False),
+    # material model 8 (UMAT): finite-strain bricks, small-displacement
+    # tetrahedra (one block: with two yield stresses on this 1 x 1 x 2
+    # tetrahedral mesh the kinematic hardening of this UMAT -- and of mm01
+    # with beta = 0 -- stalls the second step's Newton iterations)
+    "hex8_umat": lambda: _umat_case(abi.ETYPE_L3DISOP, (2, 2, 2), [5, 3], 0.001),
+    "tet10_umat_small": lambda: _umat_case(abi.ETYPE_TET10, (1, 1, 2), [12], 0.0, geonl=False),
 }
 
 
@@ -79,7 +95,9 @@ def model_spec(model: Model) -> dict:
         d[f"part{k}_incid"] = np.asarray(p.incid, dtype=np.int64)
         d[f"part{k}_spans"] = np.asarray(p.spans, dtype=np.int64)
     mats = model.block_material
-    if isinstance(mats[0], Crystal):
+    if isinstance(mats[0], Umat):
+        d["umat"] = np.array([m.values() for m in mats])
+    elif isinstance(mats[0], Crystal):
         d["crystal"] = np.array([float(getattr(mats[0], f)) for f in CRYSTAL_FIELDS])
         d["angles"] = np.asarray(model.elem_angles)
         d["dt"] = np.float64(model.dt)
@@ -101,7 +119,7 @@ def model_from(z) -> Model:
         return Model(z["coords"], p.incid, etype=p.etype, block_spans=p.spans, materials=[cr],
                      angles=z["angles"], dt=float(z["dt"]), geonl=bool(z["geonl"]), qbar=bool(z["qbar"]),
                      bbar=bool(z["bbar"]) if "bbar" in z else False)
-    mats = [Bilinear(*row) for row in z["bilinear"]]
+    mats = [Umat(tuple(row)) for row in z["umat"]] if "umat" in z else [Bilinear(*row) for row in z["bilinear"]]
     off = 0
     for p in parts:
         p.materials = mats[off:off + len(p.spans)]
@@ -185,7 +203,10 @@ def compare(z, model: Model, state: HostState, ifv, info, est) -> dict:
         for b in range(model.nelblk):
             g = got[b]
             w = z[f"out_{name}_{b}"]
-            if name in ("history", "history1") and not model.block_crystal[b]:
+            # mm01 packs an integer state into the low word of history word 4
+            # (a UMAT's history holds plain doubles there)
+            mm01 = not model.block_crystal[b] and not model.block_umat[b]
+            if name in ("history", "history1") and mm01:
                 gi = g[..., 3].copy().view(np.int64) & 0xFFFFFFFF
                 wi = w[..., 3].copy().view(np.int64) & 0xFFFFFFFF
                 errs[f"{name}_state_word"] = max(errs.get(f"{name}_state_word", 0.0),

@@ -53,3 +53,13 @@ def test_oracle_library_builds_and_exports():
     lib = oracle.load()
     for n in ("w3o_tanstf", "w3o_recover", "w3o_update", "w3o_mm01_point"):
         assert hasattr(lib, n)
+
+
+def test_umat_features_describe_the_compiled_umat():
+    """w3g_umat_features answers as WARP3D's umat_set_features does for the
+    UMAT compiled into the library (a host call: no kernel)."""
+    lib = C.CDLL(build.build())
+    lib.w3g_umat_features.argtypes = [C.POINTER(C.c_int)]
+    info = (C.c_int * 4)()
+    assert lib.w3g_umat_features(info) == 0
+    assert list(info) == [abi.HIST_UMAT, 21, 0, 14]

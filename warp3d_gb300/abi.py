@@ -18,7 +18,9 @@ ETYPE_Q3DISOP = 1
 ETYPE_L3DISOP = 2
 ETYPE_TET10 = 6
 MAT_BILINEAR = 1
+MAT_UMAT = 8
 MAT_CRYSTAL = 10
+UMAT_NPROPS = 50
 
 OK = 0
 STEP_CUT = 1
@@ -31,6 +33,7 @@ EFATAL = -5
 
 HIST_MM01 = 11
 HIST_MM10 = 158       # one fcc crystal, one hardening variable
+HIST_UMAT = 20        # state variables of the UMAT compiled into the library (w3g_umat_features)
 
 TANGENT_FP64 = 0
 TANGENT_FP32 = 1
@@ -97,6 +100,7 @@ class ModelDesc(C.Structure):
         ("dt", C.c_double),
         ("eps_bbar", C.c_double),
         ("asymmetric_assembly", C.c_int),
+        ("umat_props", C.POINTER(C.c_double)),
     ]
 
 
@@ -154,6 +158,7 @@ PROTOTYPES = [
     ("w3g_last_error", C.c_char_p, []),
     ("w3g_set_tangent_precision", C.c_int, [_vp, C.c_int]),
     ("w3g_set_wait_limit", C.c_int, [_vp, C.c_longlong]),
+    ("w3g_umat_features", C.c_int, [C.POINTER(C.c_int)]),
     ("w3g_state_upload", C.c_int, [_vp, C.POINTER(BlockState)]),
     ("w3g_state_download", C.c_int, [_vp, C.POINTER(BlockState)]),
     ("w3g_store_blocks", C.c_int, [_vp, C.c_char_p, C.c_int]),

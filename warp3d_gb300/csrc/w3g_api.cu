@@ -14,6 +14,7 @@
 using namespace w3g;
 
 #include "w3g_context.cuh"
+#include "w3g_umat.cuh"
 
 namespace {
 
@@ -47,7 +48,7 @@ void free_all(w3g_context* c) {
   DeviceState& s = c->s;
   if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
   void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.tcchunks, m.tcgtiles, s.tc_timeout, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
-                  m.cdest, m.mat, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
+                  m.cdest, m.mat, m.umat_props, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
                   m.ifv_rowptr, m.ifv_src, s.params, s.counters, m.xtal, m.xtype, m.mm10_gp, s.mm10_scr,
                   s.mm10_iters, s.mm10_order, s.mm10_ident, s.mm10_bins,
                   s.geo, s.c_geo, s.geo_dirty,
@@ -207,6 +208,7 @@ int enqueue_recover(w3g_context* c, const double* d_c, const double* d_u, const 
   a.rot_n1 = c->s.rot_n1;
   a.cep = c->s.cep;
   a.einf = c->s.einf;
+  a.umat_props = c->m.umat_props;
   a.evol = c->s.evol;
   a.partials = c->s.partials;
   a.status = c->s.status;
@@ -401,6 +403,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   B.resize(md->nelblk);
   long long gp = 0, cep = 0, est = 0, einf = 0, geo = 0, hist = 0;
   int expect_felem = 1, n_mm10_gp = 0;
+  bool any_umat = false;
   std::vector<Chunk> type_chunks[kNumTypes], ttype_chunks[kNumTypes], mm10_chunks;
   std::vector<int> mm10_gp;
   for (int b = 0; b < md->nelblk; ++b) {
@@ -438,9 +441,19 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": element type not supported");
     }
-    if (d.mat != W3G_MAT_BILINEAR && d.mat != W3G_MAT_CRYSTAL) {
+    if (d.mat != W3G_MAT_BILINEAR && d.mat != W3G_MAT_CRYSTAL && d.mat != W3G_MAT_UMAT) {
       delete c;
       return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": material model not supported");
+    }
+    if (d.mat == W3G_MAT_UMAT && !md->umat_props) {
+      delete c;
+      return fail(W3G_EARG, "block " + std::to_string(b + 1) + ": UMAT elements without umat_props");
+    }
+    // WARP3D hands a UMAT the F-bar gradients of b-bar bricks
+    // (gtmat1_make_fbar), which are not formed here
+    if (d.mat == W3G_MAT_UMAT && d.bbar) {
+      delete c;
+      return fail(W3G_EUNSUPPORTED, "block " + std::to_string(b + 1) + ": UMAT with b-bar");
     }
     if (d.mat == W3G_MAT_CRYSTAL) {
       if (d.etype != W3G_ETYPE_L3DISOP) {
@@ -470,7 +483,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     // strain increment, internal forces and tangent, as built here
     if (d.bbar) m.has_bbar = 1;
     d.gp_off = gp; d.cep_off = cep; d.estiff_off = est; d.einf_off = einf; d.geo_off = geo;
-    d.hist = d.mat == W3G_MAT_CRYSTAL ? kHistMM10 : kHistMM01;
+    d.hist = d.mat == W3G_MAT_CRYSTAL ? kHistMM10 : d.mat == W3G_MAT_UMAT ? kUmatNstatv : kHistMM01;
+    if (d.mat == W3G_MAT_UMAT) any_umat = true;
     d.hist_off = hist;
     d.mm10_off = d.mat == W3G_MAT_CRYSTAL ? n_mm10_gp : -1;
     hist += (long long)d.hist * d.span * d.ngp;
@@ -672,6 +686,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(m.edest, einf);
   AL(m.cdest, einf);
   AL(m.mat, md->noelem);
+  if (any_umat) AL(m.umat_props, (long long)W3G_UMAT_NPROPS * md->noelem);
   for (int t = 0; t < kNumTypes; ++t) {
     AL(m.dn[t], dnt[t].size());
     AL(m.dn32[t], dnt32[t].size());
@@ -727,6 +742,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   UP(m.edest, ed.data(), einf);
   UP(m.cdest, cd.data(), einf);
   UP(m.mat, mat.data(), md->noelem);
+  if (any_umat) UP(m.umat_props, md->umat_props, (long long)W3G_UMAT_NPROPS * md->noelem);
   if (n_mm10_gp > 0) {
     UP(m.xtal, xtal.data(), md->noelem);
     UP(m.xtype, xtype.data(), md->ncrystals);
@@ -786,6 +802,12 @@ int w3g_set_tangent_precision(w3g_context* c, int precision) {
   if (precision != W3G_TANGENT_FP64 && c->m.packed_total > 0 && !c->s.estiff_packed32)
     CK(dalloc(&c->s.estiff_packed32, (size_t)c->m.packed_total));
   c->precision = precision;
+  return 0;
+}
+
+int w3g_umat_features(int* info) {
+  if (!info) return fail(W3G_EARG, "null argument");
+  for (int k = 0; k < 4; ++k) info[k] = kUmatInfo[k];
   return 0;
 }
 

@@ -199,6 +199,7 @@ struct DeviceModel {
   int* edest = nullptr;            // device, concatenated (totdof, span)
   int* cdest = nullptr;
   MatProps* mat = nullptr;         // device, noelem
+  double* umat_props = nullptr;    // device, W3G_UMAT_NPROPS * noelem when the model has UMAT elements
   double* dn[kNumTypes] = {nullptr, nullptr, nullptr};   // device, fill_dn_table per type
   float* dn32[kNumTypes] = {nullptr, nullptr, nullptr};  // device, the same in float
   // deterministic ifv assembly: CSR over global dofs of einfvec indices
@@ -299,6 +300,7 @@ struct RecoverArgs {
   double beta_fact;
   double bbar_beta;          // (1 - eps_bbar) / 3
   int asym;                  // asymmetric assembly: mm10 tangents not symmetrized
+  const double* umat_props;  // UMAT elements: kUmatNprops per element (noelem entries), else null
   // mm10 blocks
   const CrystalElem* xtal;   // noelem entries (mm10 elements)
   const CrystalType* xtype;

@@ -36,14 +36,18 @@ __global__ void k_begin_recover(IterParams* params, unsigned long long* status, 
 __global__ void __launch_bounds__(kRecoverThreads) k_recover_hex8(RecoverArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const IterParams p = *a.params;
-  recover_item_hex8(a, p, a.chunk0 + blockIdx.x, smem);
+  const int cidx = a.chunk0 + blockIdx.x;
+  if (umat_chunk(a, cidx)) recover_item_gen<Hex8, 8, 8, true>(a, p, cidx, smem);
+  else recover_item_hex8(a, p, cidx, smem);
 }
 
 template <class E, int LPE, int EPC>
 __global__ void __launch_bounds__(kRecoverThreads) k_recover_type(RecoverArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const IterParams p = *a.params;
-  recover_item_gen<E, LPE, EPC>(a, p, a.chunk0 + blockIdx.x, smem);
+  const int cidx = a.chunk0 + blockIdx.x;
+  if (umat_chunk(a, cidx)) recover_item_gen<E, LPE, EPC, true>(a, p, cidx, smem);
+  else recover_item_gen<E, LPE, EPC>(a, p, cidx, smem);
 }
 
 // persistent: the CTA takes q.grain queue entries at a time
@@ -60,10 +64,20 @@ __global__ void __launch_bounds__(kRecoverThreads) k_recover_persistent(RecoverA
     const int w1 = min(w0 + q.grain, q.nitems);
     for (int w = w0; w < w1; ++w) {
       const int cidx = q.items[w];
+      const bool um = umat_chunk(a, cidx);
       switch (a.chunks[cidx].type) {
-        case 0: recover_item_hex8(a, p, cidx, smem); break;
-        case 1: recover_item_gen<Hex20, 32, 2>(a, p, cidx, smem); break;
-        default: recover_item_gen<Tet10, 4, 16>(a, p, cidx, smem); break;
+        case 0:
+          if (um) recover_item_gen<Hex8, 8, 8, true>(a, p, cidx, smem);
+          else recover_item_hex8(a, p, cidx, smem);
+          break;
+        case 1:
+          if (um) recover_item_gen<Hex20, 32, 2, true>(a, p, cidx, smem);
+          else recover_item_gen<Hex20, 32, 2>(a, p, cidx, smem);
+          break;
+        default:
+          if (um) recover_item_gen<Tet10, 4, 16, true>(a, p, cidx, smem);
+          else recover_item_gen<Tet10, 4, 16>(a, p, cidx, smem);
+          break;
       }
       __syncthreads();   // the next item reuses the shared memory
     }

@@ -25,8 +25,44 @@
 #include "w3g_internal.cuh"
 #include "w3g_elem.cuh"
 #include "w3g_math.cuh"
+#include "w3g_umat.cuh"
 
 namespace w3g {
+
+// drive_umat_update at one Gauss point (w3g_umat.cuh): state at n and
+// history from the blocked arrays, history at n+1 written when iter > 0,
+// F at n from the undeformed gradients (identity for small displacement).
+// A UMAT asking for a smaller load step (pnewdt < 1) sets the step-cut key
+// of a failed material update (WARP3D's material_cut_step).
+template <int NN>
+__device__ __forceinline__ void umat_gauss_point(const RecoverArgs& a, const IterParams& p, int blk,
+                                                 const BlockDesc& bd, int i, int g, long long gpi, const double* tg0,
+                                                 const double* ue, const double* F1, const double* uddt,
+                                                 double* cgn1, double* cep21) {
+  double fn[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, f1[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (bd.geonl) {
+    double th[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int n = 0; n < NN; ++n)
+      tcomp1_node(th, tg0[3 * n], tg0[3 * n + 1], tg0[3 * n + 2], ue[n], ue[NN + n], ue[2 * NN + n]);
+    for (int k = 0; k < 9; ++k) { fn[k] = th[k] + ((k % 4 == 0) ? 1.0 : 0.0); f1[k] = F1[k]; }
+  }
+  const long long hoff = bd.hist_off + ((long long)i * bd.ngp + g) * kUmatNstatv;
+  double hist1[kUmatNstatv];
+  // at iteration 0 the recovery is nonlinear exactly when du is extrapolated
+  const bool cut = umat_point(a.umat_props + (long long)(bd.felem + i) * kUmatNprops, p.step, p.iter,
+                              p.iter == 0 && p.nonlinear, a.dt, bd.felem + i + 1, g + 1, a.urcs_n + gpi * 9,
+                              a.eps_n + gpi * 6, uddt, a.hist + hoff, fn, f1, cgn1, hist1, cep21);
+  if (p.iter > 0)
+    for (int k = 0; k < kUmatNstatv; ++k) a.hist1[hoff + k] = hist1[k];
+  if (cut) atomicMin(a.status, bad_point_key(blk, g, 2, i));
+}
+
+// the chunk belongs to a block of material model 8 (UMAT): its elements
+// take the kUmat instantiation of recover_item_gen, so that the mm01 items
+// carry no UMAT code
+__device__ __forceinline__ bool umat_chunk(const RecoverArgs& a, int cidx) {
+  return a.blocks[a.chunks[cidx].blk].mat == W3G_MAT_UMAT;
+}
 
 // shared memory of one recovery item of element type E, EPC elements
 template <class E, int EPC>
@@ -364,7 +400,9 @@ __device__ __noinline__ void recover_item_hex8(const RecoverArgs& a, const IterP
 }  // namespace hex8r
 using hex8r::recover_item_hex8;
 
-template <class E, int LPE, int EPC>
+// kUmat: the instantiation for blocks of material model 8 (UMAT); the
+// others run mm01
+template <class E, int LPE, int EPC, bool kUmat = false>
 __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterParams& p, int cidx,
                                                  unsigned char* smem) {
   constexpr int NN = E::NN, NG = E::NG, TOT = E::TOTDOF;
@@ -506,9 +544,13 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
     for (int k = 0; k < 9; ++k) cgn[k] = a.urcs_n[gpi * 9 + k];
 #pragma unroll
     for (int k = 0; k < 6; ++k) eps1[k] = a.eps_n[gpi * 6 + k] + uddt[k];
+    if constexpr (!kUmat) {
 #pragma unroll
-    for (int k = 0; k < 11; ++k) hist[k] = a.hist[hoff + k];
-    if (p.nonlinear) {
+      for (int k = 0; k < 11; ++k) hist[k] = a.hist[hoff + k];
+    }
+    if constexpr (kUmat) {   // drive_umat_update
+      umat_gauss_point<NN>(a, p, ch.blk, bd, i, g, gpi, tg0, ue, F1, uddt, cgn1, cep21);
+    } else if (p.nonlinear) {
       const double alpha11_first = a.hist[bd.hist_off + (long long)g * kHistMM01 + 10];
       mm01_point(mp, p.step, cgn, uddt, hist, alpha11_first, cgn1, hist1, cep21);
     } else {
@@ -541,8 +583,10 @@ __device__ __noinline__ void recover_item_gen(const RecoverArgs& a, const IterPa
 #pragma unroll
         for (int k = 0; k < 9; ++k) a.rot_n1[gpi * 9 + k] = R1[k];
       }
+      if constexpr (!kUmat) {
 #pragma unroll
-      for (int k = 0; k < 11; ++k) a.hist1[hoff + k] = hist1[k];
+        for (int k = 0; k < 11; ++k) a.hist1[hoff + k] = hist1[k];
+      }
     }
 
     // element forces f_a = P dN_a/dX, P = wf det[J_{n+1}] [T] F1^-T

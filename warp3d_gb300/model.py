@@ -32,6 +32,7 @@ from . import abi
 
 HIST_MM01 = abi.HIST_MM01
 HIST_MM10 = abi.HIST_MM10
+HIST_UMAT = abi.HIST_UMAT
 NSTR = 6
 NSTRS = 9
 
@@ -82,6 +83,22 @@ class Bilinear:
         with np.errstate(all="ignore"):
             h = np.float32(np.float32(e * et) / np.float32(e - et))
         return {7: e, 8: np.float32(self.nu), 14: np.float32(self.beta), 15: h, 23: np.float32(self.yld)}
+
+
+@dataclass
+class Umat:
+    """WARP3D material model 8, the Abaqus UMAT interface, with the UMAT
+    compiled into the library (the reference's example: Mises plasticity
+    with linear kinematic hardening). ``props`` are the material's umat
+    values (dmatprp(151:200), up to 50); the example reads E, nu, yield
+    stress, H' and the thermal expansion coefficient."""
+
+    props: tuple = (200000.0, 0.3, 400.0, 2000.0, 0.0)
+
+    def values(self) -> np.ndarray:
+        v = np.zeros(abi.UMAT_NPROPS)
+        v[:len(self.props)] = self.props
+        return v
 
 
 @dataclass
@@ -359,7 +376,9 @@ class Model:
         self.block_ek_rows = [d * d if self.asymmetric else u for d, u in zip(self.block_totdof, self.block_utsz)]
         self._block_incid = bincid
         self.block_crystal = [isinstance(m, Crystal) for m in bmat]
-        self.block_hist = [HIST_MM10 if cr else HIST_MM01 for cr in self.block_crystal]
+        self.block_umat = [isinstance(m, Umat) for m in bmat]
+        self.block_hist = [HIST_MM10 if cr else HIST_UMAT if um else HIST_MM01
+                           for cr, um in zip(self.block_crystal, self.block_umat)]
         self.dt = float(dt)
         self.crystals = []
         self.elem_crystal = np.full(self.noelem, -1, dtype=np.int32)
@@ -388,6 +407,9 @@ class Model:
         self.props = np.zeros((ne, abi.MXELPR), dtype=np.float32)
         self.iprops = np.zeros((ne, abi.MXELPR), dtype=np.int32)
         self.lprops = np.zeros((ne, abi.MXELPR), dtype=np.int32)
+        # umat values per element (rknstr's local_work%umat_props); only
+        # passed when the model has UMAT blocks
+        self.umat_props = np.zeros((ne, abi.UMAT_NPROPS)) if any(self.block_umat) else None
         self.edest = []
         for b in range(self.nelblk):
             f, s, t = self.felem[b], self.spans[b], self.block_etype[b]
@@ -400,7 +422,8 @@ class Model:
             self.iprops[rows, 4] = order
             self.iprops[rows, 5] = ngp
             mat = self.block_material[b]
-            self.iprops[rows, 24] = abi.MAT_CRYSTAL if isinstance(mat, Crystal) else abi.MAT_BILINEAR
+            self.iprops[rows, 24] = (abi.MAT_CRYSTAL if isinstance(mat, Crystal) else
+                                     abi.MAT_UMAT if isinstance(mat, Umat) else abi.MAT_BILINEAR)
             self.iprops[rows, 37] = 1
             self.lprops[rows, 17] = 1 if self.geonl else 0
             # b-bar is an option of the 8-node brick only (elprp.f sets
@@ -409,6 +432,8 @@ class Model:
             if isinstance(mat, Crystal):
                 self.props[rows, 6] = np.float32(mat.e)
                 self.props[rows, 7] = np.float32(mat.nu)
+            elif isinstance(mat, Umat):
+                self.umat_props[rows] = mat.values()
             else:
                 for k, v in mat.props_values().items():
                     self.props[rows, k - 1] = v
@@ -447,6 +472,8 @@ class Model:
         d.dt = self.dt
         d.eps_bbar = self.eps_bbar
         d.asymmetric_assembly = 1 if self.asymmetric else 0
+        if self.umat_props is not None:
+            d.umat_props = self.umat_props.ctypes.data_as(C.POINTER(C.c_double))
         return d
 
     def new_state(self) -> "HostState":
