@@ -246,8 +246,19 @@ def bench_batched(args, dev, local):
         t1 = time.perf_counter()
         sched, tuned_ms = eng.autotune(2, 1, False, *p, sh, reps=2)
         t_tune = time.perf_counter() - t1
+        # the single persistent launch per kernel against per-type launches,
+        # each replayed from its graph (the autotuner's choice is among them
+        # or a persistent variant with another occupancy or grain)
+        table = {}
+        for label, kw in (("per_type", dict(mode=abi.SCHED_PER_TYPE)),
+                          ("persistent_heavy_first", dict(mode=abi.SCHED_PERSISTENT, order=abi.ORDER_HEAVY_FIRST)),
+                          ("persistent_block_order", dict(mode=abi.SCHED_PERSISTENT, order=abi.ORDER_BLOCKS))):
+            eng.set_schedule(**kw)
+            table[label] = round(time_graph()[0], 4)
+        eng.set_schedule(**sched)
         ms, launches = time_graph()
         out[name] = {"value": ne / (ms * 1e-3), "ms_per_step": ms, "schedule": sched,
+                     "schedules_ms": table,
                      "autotune_best_ms": tuned_ms, "autotune_s": t_tune,
                      "per_type_direct": {"value": ne / (ms_pt * 1e-3), "ms_per_step": ms_pt},
                      "gpu_launches": launches}

@@ -396,6 +396,14 @@ int w3g_pcg_dev(w3g_csr* csr, const void* d_fixed_mask, const void* d_b,
 int w3g_residual_norms_dev(w3g_csr* csr, const void* d_v, const void* d_fixed_mask,
                            void* d_out, void* stream);
 
+/* d_out[0] = sum over the free dofs of a_i b_i (device doubles), one
+   deterministic device reduction: the s-value of the line search
+   (mnralg_ls_get_s, src/mnralg.f:1135-1158, s = -sum res idu over the
+   unconstrained dofs) with a = -res (the internal forces under
+   displacement control) and b = the Newton correction idu. */
+int w3g_free_dot_dev(w3g_csr* csr, const void* d_a, const void* d_b, const void* d_fixed_mask,
+                     void* d_out, void* stream);
+
 /* ---- internal-force assembly without device allocation --------------
    No counterpart in the reference. For callers that cannot allocate
    device memory -- a Fortran code whose device arrays come from a pool or

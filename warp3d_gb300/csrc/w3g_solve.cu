@@ -465,6 +465,26 @@ __global__ void __launch_bounds__(kThreads) k_norms_fin(const double* partials, 
   }
 }
 
+// sum over the free dofs of a_i b_i: the line search's s-value of mnralg_ls
+// (s = -sum res idu, src/mnralg.f:1135-1158) with a = -res; per-CTA partials
+// in a fixed order
+__global__ void __launch_bounds__(kThreads) k_dot_free(int n, const double* __restrict__ a,
+                                                       const double* __restrict__ b,
+                                                       const unsigned char* __restrict__ fixed, double* partials) {
+  __shared__ double sh[kWarps];
+  double t = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (!fixed[i]) t += a[i] * b[i];
+  t = block_sum(t, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(kThreads) k_dot_fin(const double* partials, int nparts, double* out) {
+  __shared__ double sh[kWarps];
+  const double t = sum_partials(partials, nparts, 1, 0, sh);
+  if (threadIdx.x == 0) out[0] = t;
+}
+
 }  // namespace
 
 struct w3g_csr {
@@ -694,7 +714,7 @@ int w3g_csr_create(w3g_context* c, w3g_csr** out) {
   al(&s->q, n);
   al(&s->dinv, n);
   if (triplet) al(&s->binv, 3 * (size_t)n);
-  al(&s->partials, 4 * (size_t)s->grid);   // PCG partials, then the norms' partials
+  al(&s->partials, 5 * (size_t)s->grid);   // PCG partials, the norms' partials, the free dot's
   al(&s->sc, 1);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming);
@@ -835,6 +855,19 @@ int w3g_residual_norms_dev(w3g_csr* s, const void* d_v, const void* d_fixed, voi
   double* part = s->partials + 2 * (size_t)s->grid;
   k_norms<<<s->grid, kThreads, 0, st>>>(s->n, (const double*)d_v, (const unsigned char*)d_fixed, part);
   k_norms_fin<<<1, kThreads, 0, st>>>(part, s->grid, (double*)d_out);
+  CKS(cudaGetLastError());
+  return 0;
+}
+
+int w3g_free_dot_dev(w3g_csr* s, const void* d_a, const void* d_b, const void* d_fixed, void* d_out,
+                     void* stream) {
+  if (!s || !d_a || !d_b || !d_fixed || !d_out) return w3g_fail(W3G_EARG, "null argument");
+  CKS(cudaSetDevice(s->ctx->device));
+  cudaStream_t st = (cudaStream_t)stream;
+  double* part = s->partials + 4 * (size_t)s->grid;
+  k_dot_free<<<s->grid, kThreads, 0, st>>>(s->n, (const double*)d_a, (const double*)d_b,
+                                           (const unsigned char*)d_fixed, part);
+  k_dot_fin<<<1, kThreads, 0, st>>>(part, s->grid, (double*)d_out);
   CKS(cudaGetLastError());
   return 0;
 }

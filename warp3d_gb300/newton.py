@@ -8,7 +8,9 @@ so that the engine can be exercised end to end on synthetic problems:
                extrapolated previous increment elsewhere), recovery with
                iter = 0, tangent (mnralg.f:249-402)
   iteration i  solve K d = r on the free dofs, du += d, recovery with
-               iter = i, residual test, new tangent (mnralg.f:435-569)
+               iter = i, residual test, new tangent (mnralg.f:435-569);
+               with line search, du = du0 + alpha d with alpha from
+               mnralg_ls (mnralg.f:758-914)
   converged    update n+1 -> n, u += du (update.f:73-94)
 
 Displacement-controlled problems only (no applied loads): the residual on
@@ -72,9 +74,39 @@ class Assembler:
         return K
 
 
+# line-search defaults of WARP3D's input (indypm.f:1278-1283) and the
+# r-reduction fraction of mnralg_ls (mnralg.f:802)
+LS_RHO, LS_SLACK_TOL, LS_MIN_STEP, LS_MAX_STEP, LS_REDUCE = 0.7, 0.5, 0.01, 1.0, 0.9
+
+
+def line_search(s0: float, trial, rho: float = LS_RHO, slack_tol: float = LS_SLACK_TOL,
+                alpha_min: float = LS_MIN_STEP, alpha_max: float = LS_MAX_STEP, reduce: float = LS_REDUCE):
+    """The step-length search of mnralg_ls (src/mnralg.f:758-914) for a
+    Newton correction idu with s0 = -res.idu < 0 over the free dofs.
+    trial(alpha) sets du = du0 + alpha idu, recomputes the internal forces
+    (mnralg_ls_update_res) and returns s(alpha); the search backtracks
+    alpha = rho alpha from alpha_max until |s / s0| < slack_tol, and falls
+    back to alpha = 1 (recomputing there) when the ratio stops falling by
+    `reduce` or alpha drops below alpha_min. Returns (alpha, trials)."""
+    alpha, ell, r_prev = alpha_max, 1, None
+    while True:
+        r = abs(trial(alpha) / s0)
+        if r < slack_tol:
+            return alpha, ell
+        if ell >= 2 and r > reduce * r_prev:     # ratio not decreasing: full step
+            trial(1.0)
+            return 1.0, ell + 1
+        r_prev = r
+        alpha = rho * alpha                      # simple backtrack
+        if alpha < alpha_min:
+            trial(1.0)
+            return 1.0, ell + 1
+        ell += 1
+
+
 class NewtonDriver:
     def __init__(self, model, engine, fixed: np.ndarray, tol: float = 1e-8, maxit: int = 25,
-                 extrapolate: bool = False):
+                 extrapolate: bool = False, line_search: bool = False):
         self.model = model
         self.engine = engine
         self.fixed = np.asarray(fixed, dtype=np.int64)
@@ -87,7 +119,9 @@ class NewtonDriver:
         self.du_prev = None
         self.ifv = np.zeros(model.nodof)
         self.estiff = model.estiff_blocks()
+        self.line_search = line_search
         self.history = []   # (step, iterations, residual list)
+        self.alphas = []    # (step, [accepted step length per iteration]) with line search
 
     def _tangent(self, step, it, du):
         self.engine.tanstf(step, it, self.model.c, self.u, du, self.estiff)
@@ -104,15 +138,29 @@ class NewtonDriver:
         if st != 0:
             raise RuntimeError(f"step {step}: recovery requested a step cut at iteration 0")
         K = self._tangent(step, 0, du)
-        res_hist = []
+        res_hist, alphas = [], []
         for it in range(1, self.maxit + 1):
             r = -self.ifv[self.free]
             Kff = K[self.free][:, self.free].tocsc()
             d = spla.spsolve(Kff, r)
-            du[self.free] += d
-            st, _ = self.engine.recover(step, it, extrap, m.c, self.u, du, self.ifv)
-            if st != 0:
-                raise RuntimeError(f"step {step}: step cut requested at iteration {it}")
+
+            def trial(alpha, du0=du.copy(), it=it):
+                du[:] = du0
+                du[self.free] += alpha * d if alpha != 1.0 else d
+                st, _ = self.engine.recover(step, it, extrap, m.c, self.u, du, self.ifv)
+                if st != 0:
+                    raise RuntimeError(f"step {step}: step cut requested at iteration {it}")
+                return float(np.dot(self.ifv[self.free], d))   # s = -res.idu, res = -ifv
+
+            # mnralg_ls: s0 from the residual the correction was solved for;
+            # s0 >= 0 (or no line search) takes the full step
+            s0 = float(np.dot(self.ifv[self.free], d))
+            if self.line_search and s0 < 0.0:
+                alpha, _ = line_search(s0, trial)
+            else:
+                alpha = 1.0
+                trial(1.0)
+            alphas.append(alpha)
             rn = np.linalg.norm(self.ifv[self.free])
             scale = max(np.linalg.norm(self.ifv), 1e-300)
             res_hist.append(rn / scale)
@@ -125,6 +173,7 @@ class NewtonDriver:
         self.u += du
         self.du_prev = du
         self.history.append((step, len(res_hist), res_hist))
+        self.alphas.append((step, alphas))
         return res_hist
 
 

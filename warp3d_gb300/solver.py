@@ -12,7 +12,8 @@ gradient on the free dofs.
 of mnralg, src/mnralg.f:249-569) with every vector on the device: the
 element path, the assembly, the solve and the convergence norms (cvtest,
 src/cvtest.f:20) run there; per iteration the host reads only the
-recovery status, the solver's iteration count and two norms. PyTorch
+recovery status, the solver's iteration count and two norms (and, with
+the line search of mnralg_ls, one s-value per trial step length). PyTorch
 provides the device vectors and the few vector updates of the driver.
 """
 from __future__ import annotations
@@ -79,6 +80,10 @@ class DeviceCsr:
     def residual_norms(self, d_v: int, d_fixed: int, d_out: int, stream: int = 0):
         abi.check(self.lib, self.lib.w3g_residual_norms_dev(self.h, d_v, d_fixed, d_out, stream or None))
 
+    def free_dot(self, d_a: int, d_b: int, d_fixed: int, d_out: int, stream: int = 0):
+        """d_out[0] = sum over the free dofs of a_i b_i (w3g_free_dot_dev)."""
+        abi.check(self.lib, self.lib.w3g_free_dot_dev(self.h, d_a, d_b, d_fixed, d_out, stream or None))
+
 
 class IncrementFailed(RuntimeError):
     """A (sub-)increment did not converge, or its recovery or solve asked
@@ -132,7 +137,7 @@ class DeviceNewtonDriver:
     def __init__(self, model, engine, fixed, tol: float = 1e-8, maxit: int = 25, extrapolate: bool = False,
                  lin_rtol: float = 1e-10, lin_maxit: int = 50000, device: int = 0, csr: DeviceCsr | None = None,
                  adaptive: bool = False, adaptive_step1: bool = False, adapt_divisions: int = 4,
-                 adapt_min_fact: float = 1.0 / 16.0):
+                 adapt_min_fact: float = 1.0 / 16.0, line_search: bool = False):
         import torch
         self.torch = torch
         self.model = model
@@ -152,6 +157,9 @@ class DeviceNewtonDriver:
         self.mask = torch.zeros(n, dtype=torch.uint8, device=dev)
         self.mask[self.fixed_idx] = 1
         self.norms = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.sval = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.line_search = line_search
+        self.alphas = []        # (step, [accepted step length per iteration]) with line search
         self.csr = csr if csr is not None else DeviceCsr(engine)   # the pattern is the model's: shareable
         self.history = []       # (step, iterations, relative residuals) per converged increment
         self.lin_history = []   # (step, [PCG iterations per Newton iteration])
@@ -188,7 +196,8 @@ class DeviceNewtonDriver:
         else:
             self.du.zero_()
         self.du[self.fixed_idx] = imp[self.fixed_idx]
-        res_hist, lin = [], []
+        res_hist, lin, alphas = [], [], []
+        self.alphas_last = alphas
         self.trace = []
         if self._recover(step, 0, extrap) != 0:
             raise IncrementFailed(f"step {step}: recovery requested a step cut at iteration 0")
@@ -201,9 +210,7 @@ class DeviceNewtonDriver:
             if st == abi.PCG_BREAKDOWN:
                 raise IncrementFailed(f"step {step}: tangent not positive definite on the free dofs "
                                        f"(iteration {it})")
-            self.du += self.d
-            if self._recover(step, it, extrap) != 0:
-                raise IncrementFailed(f"step {step}: step cut requested at iteration {it}")
+            alphas.append(self._search(step, it, extrap))
             self.csr.residual_norms(self.ifv.data_ptr(), self.mask.data_ptr(), self.norms.data_ptr())
             rf, ra = self.norms.cpu().numpy()
             rn, scale = float(np.sqrt(rf)), max(float(np.sqrt(ra)), 1e-300)
@@ -213,6 +220,32 @@ class DeviceNewtonDriver:
                 return res_hist, lin
             self._tangent(step, it)
         raise IncrementFailed(f"step {step}: no convergence in {self.maxit} iterations: {res_hist}")
+
+    def _s_value(self) -> float:
+        """s = -res.idu over the free dofs (res = -ifv), one device reduction."""
+        self.csr.free_dot(self.ifv.data_ptr(), self.d.data_ptr(), self.mask.data_ptr(), self.sval.data_ptr())
+        return float(self.sval.item())
+
+    def _search(self, step, it, extrap) -> float:
+        """du += alpha d with alpha from mnralg_ls (newton.line_search), the
+        internal forces recomputed for the accepted length; returns alpha."""
+        from .newton import line_search
+
+        def trial(alpha, du0=self.du.clone()):
+            self.du.copy_(du0)
+            if alpha == 1.0:
+                self.du += self.d
+            else:
+                self.du.add_(self.d, alpha=alpha)
+            if self._recover(step, it, extrap) != 0:
+                raise IncrementFailed(f"step {step}: step cut requested at iteration {it}")
+            return self._s_value()
+
+        s0 = self._s_value() if self.line_search else 0.0
+        if self.line_search and s0 < 0.0:
+            return line_search(s0, trial)[0]
+        trial(1.0)
+        return 1.0
 
     def step(self, step: int, imposed: np.ndarray):
         """imposed: full-length vector; its values on fixed dofs are the
@@ -233,6 +266,7 @@ class DeviceNewtonDriver:
             self.frac_prev = f
             self.history.append((step, len(res_hist), res_hist))
             self.lin_history.append((step, lin))
+            self.alphas.append((step, list(self.alphas_last)))
             self.fractions.append(f)
             out.extend(res_hist)
 
