@@ -117,6 +117,8 @@ def parse():
     ap.add_argument("--study-strain", type=float, default=0.02)
     ap.add_argument("--study-forms", default="fp64,fp32,tf32,bf16,tf32x3,bf16x3")
     ap.add_argument("--study-maxit", type=int, default=25)
+    ap.add_argument("--study-forcing", default="fixed", choices=["fixed", "ew"],
+                    help="PCG tolerance per Newton iteration: fixed 1e-10, or Eisenstat-Walker forcing terms")
     ap.add_argument("--study-lin-maxit", type=int, default=50000)
     ap.add_argument("--study-no-extrapolate", action="store_true",
                     help="start every step from zero instead of the scaled previous increment")
@@ -897,7 +899,8 @@ def newton_forms(args, model, fixed, topz, nz, names, eng, csr):
         eng.upload(initial)
         drv = DeviceNewtonDriver(model, eng, fixed, tol=1e-8, maxit=args.study_maxit, lin_rtol=1e-10,
                                  lin_maxit=args.study_lin_maxit, csr=csr, extrapolate=not args.study_no_extrapolate,
-                                 adaptive=not args.study_no_adaptive, adaptive_step1=True)
+                                 adaptive=not args.study_no_adaptive, adaptive_step1=True,
+                                 forcing=args.study_forcing)
         rec = {"steps": [], "failed": None}
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -958,7 +961,9 @@ def batched_study(args, dev):
                         f"[16,128], per-block yield U(250,550) MPa; uniaxial {100 * args.study_strain:g}% in "
                         f"{args.study_steps} steps",
             "elements": model.noelem, "blocks": model.nelblk, "dofs": model.nodof, "csr_nnz": csr.nnz,
-            "setup_s": setup_s, "newton_tol": 1e-8, "pcg_rtol": 1e-10, "forms": forms}
+            "setup_s": setup_s, "newton_tol": 1e-8,
+            "pcg_rtol": 1e-10 if args.study_forcing == "fixed" else "Eisenstat-Walker (gamma 0.9, eta_max 0.1)",
+            "forms": forms}
 
 
 def precision_study(args, dev):

@@ -47,3 +47,14 @@ def test_not_adaptive_raises_at_once():
     with pytest.raises(RuntimeError):
         run_subdivided(attempt, False)
     assert len(seen) == 1
+
+
+def test_eisenstat_walker_forcing_terms():
+    from warp3d_gb300.solver import EW_ETA_MAX, ew_forcing
+    # quadratic in the residual ratio, capped at eta_max
+    assert ew_forcing(0.1, 1e-2, 1e-1, 1e-12) == pytest.approx(0.9 * 1e-2)
+    assert ew_forcing(0.1, 0.9, 1.0, 1e-12) == EW_ETA_MAX
+    # safeguard: a sudden drop after a loose solve keeps gamma eta^2
+    assert ew_forcing(0.5, 1e-6, 1.0, 1e-12) == pytest.approx(0.9 * 0.25 if 0.9 * 0.25 < EW_ETA_MAX else EW_ETA_MAX)
+    # never tighter than reaching the Newton target needs
+    assert ew_forcing(1e-3, 1e-7, 1e-3, 1e-8) == pytest.approx(0.05)

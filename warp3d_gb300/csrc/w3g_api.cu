@@ -33,8 +33,9 @@ int fail(int code, const std::string& msg) {
   } while (0)
 
 // trailing elements allocated beyond the arrays that 1-D bulk copies read
-// (cep, rot_n1, urcs_n1): a copy of a tile's slab is rounded out to 16-byte
-// boundaries and may read up to 8 bytes past the last element
+// (cep, rot_n1, urcs_n1; edest, cdest): a copy of a tile's slab is rounded
+// out to 16-byte boundaries and may read up to 12 bytes past the last
+// element
 constexpr size_t kBulkPad = 4;
 
 template <class T>
@@ -683,8 +684,8 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
     AL(s.mm10_ident, n_mm10_gp);
     AL(s.mm10_bins, 128);
   }
-  AL(m.edest, einf);
-  AL(m.cdest, einf);
+  AL(m.edest, einf + kBulkPad);   // int arrays: 16 bytes of slack for the tiles' index-slab copies
+  AL(m.cdest, einf + kBulkPad);
   AL(m.mat, md->noelem);
   if (any_umat) AL(m.umat_props, (long long)W3G_UMAT_NPROPS * md->noelem);
   for (int t = 0; t < kNumTypes; ++t) {

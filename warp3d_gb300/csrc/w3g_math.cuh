@@ -181,6 +181,34 @@ __device__ __forceinline__ void polar_rotation(const double* F, double* R) {
 #undef FF
 }
 
+// double -> float, rounded to nearest even, on the integer pipes. GB300's
+// FP64 pipe (which also executes the F2F conversion) retires 2 lanes per
+// clock and SM, a warp-wide conversion costs ~64 issue cycles of its SM
+// sub-partition; this sequence of ~12 integer operations costs ~1. From
+// the IEEE 754 binary64 / binary32 layouts: the float keeps the top 23 of
+// the 52 mantissa bits, the 29 dropped bits decide the rounding (ties to
+// even), a carry out of the mantissa moves into the exponent. Magnitudes
+// below the smallest normal float become 0 and above the largest become
+// infinity (also for infinite and NaN inputs), which the element inputs
+// (stresses, rotations, material matrices) never reach.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const int e = (int)((hi >> 20) & 0x7FFu) - (1023 - 127);
+  const unsigned m = __funnelshift_l(lo, hi, 3) & 0x7FFFFFu;
+  const unsigned rest = lo & 0x1FFFFFFFu;
+  unsigned r = ((unsigned)e << 23) + m;
+  r += (rest > 0x10000000u) | ((rest == 0x10000000u) & (m & 1u));
+  r = e <= 0 ? 0u : (e >= 255 || r >= 0x7F800000u ? 0x7F800000u : r);
+  return __uint_as_float((hi & 0x80000000u) | r);
+}
+
+// a double input in the arithmetic type of a kernel: unchanged for double,
+// d2f_rn for float (the same value as a float conversion in the normal
+// range, without the FP64 pipe)
+template <class T> __device__ __forceinline__ T from_f64(double x);
+template <> __device__ __forceinline__ double from_f64<double>(double x) { return x; }
+template <> __device__ __forceinline__ float from_f64<float>(double x) { return d2f_rn(x); }
+
 // ---------------------------------------------------------------------
 // Fixed-order arithmetic for the finite-strain kinematics chain.
 //

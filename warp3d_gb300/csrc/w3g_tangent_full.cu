@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(32) k_tangent_full_hex8(TangentArgs a) {
           ref = ref + a.u[e0] + a.du[e0];
         }
       }
-      S.x[lane] = (T)(v - ref);
+      S.x[lane] = from_f64<T>(v - ref);
     }
     __syncwarp();
     // ---- phase 1: one Gauss point per lane ----
@@ -96,13 +96,13 @@ __global__ void __launch_bounds__(32) k_tangent_full_hex8(TangentArgs a) {
 #pragma unroll
         for (int r = 0; r < 6; ++r)
 #pragma unroll
-          for (int c = 0; c < 6; ++c) Dl[r * 6 + c] = f * (T)h1[r + 6 * c];
+          for (int c = 0; c < 6; ++c) Dl[r * 6 + c] = f * from_f64<T>(h1[r + 6 * c]);
       } else {                           // extract_D_symmetric
         const double* cp = a.cep + bd.cep_off + ((long long)gp * bd.span + i) * 21;
 #pragma unroll
         for (int r = 0; r < 6; ++r)
 #pragma unroll
-          for (int c = 0; c < 6; ++c) Dl[r * 6 + c] = f * (T)cp[low(r, c)];
+          for (int c = 0; c < 6; ++c) Dl[r * 6 + c] = f * from_f64<T>(cp[low(r, c)]);
       }
       T* D = S.D[gp];
       T* Tw = S.Tw[gp];
@@ -110,9 +110,9 @@ __global__ void __launch_bounds__(32) k_tangent_full_hex8(TangentArgs a) {
         const long long gpi = bd.gp_off + (long long)i * NG + gp;
         T R[9], q[36], ur[6], cs[6];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) R[k] = (T)a.rot_n1[gpi * 9 + k];
+        for (int k = 0; k < 9; ++k) R[k] = from_f64<T>(a.rot_n1[gpi * 9 + k]);
 #pragma unroll
-        for (int k = 0; k < 6; ++k) ur[k] = (T)a.urcs_n1[gpi * 9 + k];
+        for (int k = 0; k < 6; ++k) ur[k] = from_f64<T>(a.urcs_n1[gpi * 9 + k]);
         rotation_q2<T>(R, q);
         qmply<T>(q, ur, cs);
 #pragma unroll

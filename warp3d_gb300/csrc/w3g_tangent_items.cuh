@@ -55,11 +55,11 @@ __device__ __forceinline__ void load_D21(const TangentArgs& a, const BlockDesc& 
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-      for (int c = 0; c <= r; ++c) C[k++] = f * (T)h1[r + 6 * c];
+      for (int c = 0; c <= r; ++c) C[k++] = f * from_f64<T>(h1[r + 6 * c]);
   } else {
     const double* cp = a.cep + bd.cep_off + ((long long)gp * bd.span + i) * 21;
 #pragma unroll
-    for (int k = 0; k < 21; ++k) C[k] = f * (T)cp[k];
+    for (int k = 0; k < 21; ++k) C[k] = f * from_f64<T>(cp[k]);
   }
 }
 
@@ -209,7 +209,7 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
           int eidx = a.edest[dbase + d * NN + node] - 1;
           v = v + a.u[eidx] + a.du[eidx];
         }
-        E[d * NN + node] = (T)(v - ref[d]);
+        E[d * NN + node] = from_f64<T>(v - ref[d]);
       }
     }
   }
@@ -253,10 +253,10 @@ __device__ __noinline__ void tangent_item_hex8(const TangentArgs& a, int cidx, u
         T R[9], q[36], ur[6], cs[6];
         const double* rp = a.rot_n1 + (gpbase + gp) * 9;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) R[k] = (T)rp[k];
+        for (int k = 0; k < 9; ++k) R[k] = from_f64<T>(rp[k]);
         const double* up = a.urcs_n1 + (gpbase + gp) * 9;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) ur[k] = (T)up[k];
+        for (int k = 0; k < 6; ++k) ur[k] = from_f64<T>(up[k]);
         rotation_q2<T>(R, q);
         qmply<T>(q, ur, cs);
         // [D*] = [q][D][q]^T, lower triangle, row by row (ctran1)
@@ -520,7 +520,7 @@ __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cid
           int eidx = a.edest[dbase + d * NN + node] - 1;
           v = v + a.u[eidx] + a.du[eidx];
         }
-        E[d * NN + node] = (float)(v - ref[d]);
+        E[d * NN + node] = d2f_rn(v - ref[d]);
       }
     }
   }
@@ -559,10 +559,10 @@ __device__ __noinline__ void tangent_item_hex8_f32(const TangentArgs& a, int cid
         float R[9], q[36], ur[6], cs[6];
         const double* rp = a.rot_n1 + (gpbase + gp) * 9;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) R[k] = (float)rp[k];
+        for (int k = 0; k < 9; ++k) R[k] = d2f_rn(rp[k]);
         const double* up = a.urcs_n1 + (gpbase + gp) * 9;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) ur[k] = (float)up[k];
+        for (int k = 0; k < 6; ++k) ur[k] = d2f_rn(up[k]);
         rotation_q2<float>(R, q);
         qmply<float>(q, ur, cs);
 #pragma unroll
@@ -806,7 +806,7 @@ __device__ __noinline__ void tangent_item_gen(const TangentArgs& a, int cidx, un
       for (int d = 0; d < 3; ++d) {
         double v = a.c[a.cdest[dbase + d * NN + node] - 1];
         if (bd.geonl) { const int e = a.edest[dbase + d * NN + node] - 1; v = v + a.u[e] + a.du[e]; }
-        Eb[d * NN + node] = (T)(v - ref[d]);
+        Eb[d * NN + node] = from_f64<T>(v - ref[d]);
       }
     }
   }
@@ -828,16 +828,16 @@ __device__ __noinline__ void tangent_item_gen(const TangentArgs& a, int cidx, un
     T C[21];
     const double* cp = a.cep + bd.cep_off + ((long long)gp * bd.span + i) * 21;
 #pragma unroll
-    for (int k = 0; k < 21; ++k) C[k] = f * (T)cp[k];
+    for (int k = 0; k < 21; ++k) C[k] = f * from_f64<T>(cp[k]);
     T* D = sD + gp * 21;
     T* Tw = sT + gp * 6;
     const long long gpi = bd.gp_off + (long long)i * NG + gp;
     if (bd.geonl) {
       T R[9], q[36], ur[6], cs[6];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) R[k] = (T)a.rot_n1[gpi * 9 + k];
+      for (int k = 0; k < 9; ++k) R[k] = from_f64<T>(a.rot_n1[gpi * 9 + k]);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) ur[k] = (T)a.urcs_n1[gpi * 9 + k];
+      for (int k = 0; k < 6; ++k) ur[k] = from_f64<T>(a.urcs_n1[gpi * 9 + k]);
       rotation_q2<T>(R, q);
       qmply<T>(q, ur, cs);
 #pragma unroll

@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
         ref = ref + a.u[e0] + a.du[e0];
         v = v + a.u[e1] + a.du[e1];
       }
-      S.x[e][dn] = (float)(v - ref);
+      S.x[e][dn] = d2f_rn(v - ref);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -276,18 +276,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_tangent_tc_hex8(TangentArgs a, 
       for (int k = sub; k < 21; k += kSubs) {
         int r = 0, c = k;
         while (c > r) { c -= r + 1; ++r; }   // k = r(r+1)/2 + c, c <= r
-        S.u.p1.C[pe][pgp][k] = f * (float)H[r + 6 * c];
+        S.u.p1.C[pe][pgp][k] = f * d2f_rn(H[r + 6 * c]);
       }
     } else {
       const long long cb = bd.cep_off + ((long long)pgp * bd.span + i) * 21;
-      for (int k = sub; k < 21; k += kSubs) S.u.p1.C[pe][pgp][k] = f * (float)a.cep[cb + k];
+      for (int k = sub; k < 21; k += kSubs) S.u.p1.C[pe][pgp][k] = f * d2f_rn(a.cep[cb + k]);
     }
     if (bd.geonl) {
       // R and the unrotated stress: each value loaded and converted once
       const long long gpi = bd.gp_off + (long long)i * NG + pgp;
-      S.u.p1.R[pe][pgp][sub] = (float)a.rot_n1[gpi * 9 + sub];
-      if (sub < 3) S.u.p1.R[pe][pgp][sub + 6] = (float)a.rot_n1[gpi * 9 + sub + 6];
-      S.u.p1.ur[pe][pgp][sub] = (float)a.urcs_n1[gpi * 9 + sub];
+      S.u.p1.R[pe][pgp][sub] = d2f_rn(a.rot_n1[gpi * 9 + sub]);
+      if (sub < 3) S.u.p1.R[pe][pgp][sub + 6] = d2f_rn(a.rot_n1[gpi * 9 + sub + 6]);
+      S.u.p1.ur[pe][pgp][sub] = d2f_rn(a.urcs_n1[gpi * 9 + sub]);
     }
   }
   __syncthreads();

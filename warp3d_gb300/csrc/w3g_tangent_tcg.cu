@@ -29,12 +29,15 @@
 // trilinear brick dN_b/dxi_s at a Gauss point changes sign, and only sign,
 // between the two nodes mirrored in xi_s, and round-to-nearest is odd, so
 // every column sum over b of the rounded M is exactly zero. Rounding H only
-// perturbs the material point values, which keeps that property too; what
-// remains is the FP32 accumulation (as in the FP32 CUDA-core kernel), so
-// no projection onto the translation-free matrices is needed.
+// perturbs the material point values, which keeps that property too, as
+// long as the diagonal pairs' H^ii stay exactly symmetric after rounding
+// (only the upper triangle of Ke is stored, the lower one is its mirror):
+// they are formed for r <= s and written to both positions. What remains
+// is the FP32 accumulation (as in the FP32 CUDA-core kernel), so no
+// projection onto the translation-free matrices is needed.
 //
 // The kernel is persistent (one CTA per SM) and pipelined:
-//   warp 8 (producer)  per tile, into a ring of shared-memory stages:
+//   warp 24 (producer) per tile, into a ring of shared-memory stages:
 //                      1-D bulk copies (cp.async.bulk, completion counted
 //                      in bytes on the stage's mbarrier) of the tile's
 //                      contiguous slabs -- cep (21, span, ngp) for each of
@@ -42,15 +45,27 @@
 //                      span) -- and 8-byte cp.async gathers of the nodal
 //                      coordinates, u and du through cdest/edest, which
 //                      arrive on the same mbarrier
-//   warps 0-7          per tile: two threads per (element, Gauss point)
-//   (consumers)        form Gamma, [D*], {T} and H^ij (three pairs each)
-//                      into the A operand (K-major, no swizzle); thread 0
-//                      issues the MMA chain (M is built once per CTA as
-//                      the B operand); the accumulator is read with
+//   warps 0-23         per tile: six threads per (element, Gauss point),
+//   (consumers)        k = 0..5, in three phases separated by CTA
+//                      barriers, the point's intermediates in shared
+//                      memory (one float per point and quantity, points
+//                      consecutive: conflict-free): (1) k = 0 forms Gamma
+//                      and w det[J]; every k converts a share of cep to
+//                      float and forms row k of the strain rotation [q]
+//                      and {T}_k; (2) k forms row k of [D*] = [q][D][q]^T -
+//                      Q-bar (lower triangle); (3) k forms H^ij = Gamma^T
+//                      X^ij Gamma of pair k (00 01 02 11 12 22) into the A
+//                      operand (K-major, no swizzle); thread 0 issues the
+//                      MMA chain (M is built once per CTA as the B
+//                      operand); warps 0-15 read the accumulator with
 //                      tcgen05.ld, each element's packed upper triangle
 //                      (utsz, span layout, setup.f:265-275) is staged in
 //                      shared memory and written with one bulk copy to
-//                      global memory (cp.async.bulk.global.shared::cta)
+//                      global memory (cp.async.bulk.global.shared::cta).
+//                      Six short threads per point instead of two long
+//                      ones: 24 warps hide the arithmetic and shared-
+//                      memory latencies that 8 warps at 168 registers
+//                      could not
 // Every wait is bounded (TangentArgs::wait_limit polls). A wait that gives
 // up sets the CTA's abort flag: no further MMA is issued, the copies still
 // in flight are waited for (again bounded), the tiles not finished get NaN
@@ -73,9 +88,10 @@ constexpr int kSlots = 8;                    // A rows per element (6 pairs i <=
 constexpr int kM = kTile * kSlots;           // 128
 constexpr int kN = NN * NN;                  // 64 node pairs (a, b)
 constexpr int kKLive = 9 * NG;               // 72 = (r, s, gp)
-constexpr int kParts = 2;                    // threads per (element, Gauss point)
-constexpr int kConsumers = 128 * kParts;     // warps 0-7
-constexpr int kThreads = kConsumers + 32;    // + producer warp 8
+constexpr int kRows = 6;                     // threads per (element, Gauss point)
+constexpr int kPoints = kTile * NG;          // 128 (element, Gauss point) per tile
+constexpr int kConsumers = kPoints * kRows;  // 768: warps 0-23
+constexpr int kThreads = kConsumers + 32;    // + producer warp 24
 constexpr int kTmemCols = 64;
 constexpr long long kDrainLimit = 1ll << 26; // polls when waiting out copies / MMAs after an abort
 
@@ -93,6 +109,18 @@ constexpr int kStXdu = kStXu + kTile * TOT * 8;
 constexpr int kStage = kStXdu + kTile * TOT * 8;  // 49312
 static_assert(kStage % 128 == 0 || kStage % 16 == 0, "stage alignment");
 
+// per-point intermediates in shared memory, [quantity][point] floats
+constexpr int kPtGam = 0;                 // Gamma (9)
+constexpr int kPtF = kPtGam + 9;          // w det[J]
+constexpr int kPtT = kPtF + 1;            // Cauchy stress at n+1 (6)
+constexpr int kPtC = kPtT + 6;            // cep (21), unscaled
+constexpr int kPtD = kPtC + 21;           // [D*] lower triangle (21), with w det[J]
+constexpr int kPtTw = kPtD + 21;          // w det[J] {T} (6)
+constexpr int kPtR = kPtTw + 6;           // R at n+1, column-major (9)
+constexpr int kPtU = kPtR + 9;            // unrotated stress urcs_n1 (6)
+constexpr int kPtN = kPtU + 6;            // 79 quantities
+constexpr int kPtBytes = kPtN * kPoints * 4;
+
 template <bool kBF16, bool kSplit>
 struct Form {
   static constexpr int kBytes = kBF16 ? 2 : 4;
@@ -104,10 +132,11 @@ struct Form {
   static constexpr int kSteps = kK / kKStep;
   static constexpr int kOpA = kM * kK * kBytes;                   // one A operand
   static constexpr int kOpB = kN * kK * kBytes;                   // one B operand
-  static constexpr int kStages = (kSplit && !kBF16) ? 2 : 3;
+  static constexpr int kStages = (kSplit && !kBF16) ? 1 : 2;
   static constexpr int kOffB = 0;
   static constexpr int kOffA = kOffB + (kSplit ? 2 : 1) * kOpB;
-  static constexpr int kOffStage = kOffA + (kSplit ? 2 : 1) * kOpA;
+  static constexpr int kOffPt = kOffA + (kSplit ? 2 : 1) * kOpA;
+  static constexpr int kOffStage = kOffPt + kPtBytes;
   static constexpr int kSmem = kOffStage + kStages * kStage;
   // byte offset of (row, k) in a K-major no-swizzle operand
   __device__ static __forceinline__ int off(int row, int k) {
@@ -119,15 +148,18 @@ static_assert(kTile * UT * 4 <= Form<true, false>::kOpA, "Ke staging must fit in
 struct TcgStatic {
   float dn[NG * 3 * NN + NG];          // dN/dxi per Gauss point (float) + weights
   float x[kTile][TOT + 1];             // x(n+1) relative to node 1 of each element (rows padded: banks)
-  float dx[kTile * NG][21];            // [D*] lower triangle per (element, Gauss point): the two halves' rows
-  TcgTile hdr[3];                      // the tile in each stage, written by the producer before its arrival
-  unsigned long long full[3], empty[3], mma;
+  alignas(16) TcgTile hdr[2];          // the tile in each stage, copied in with the stage's data
+  // the producer's dof-index slabs (cdest, edest) of two tiles: the next
+  // tile's are copied in while this one's gathers are issued
+  alignas(16) int idx[2][2][kTile * TOT + 4];
+  unsigned long long full[2], empty[2], mma, ibar[2];
   uint32_t tmem_base;
   // a bounded wait gave up: the producer's flag is written by the producer
   // only, the consumers' only by consumers before a named barrier, so that
   // every consumer takes the same branch after that barrier
   int pabort, cabort;
   int issued;                          // tiles whose copies the producer issued
+  int ifetch, iwait;                   // index slabs requested / waited for by the producer
   int done;                            // tiles the consumers finished (Ke stored)
 };
 
@@ -178,22 +210,28 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
 // leading bytes of a 1-D bulk copy started at the 16-byte boundary below p
 __device__ __forceinline__ uint32_t pad_of(const double* p) { return (uint32_t)((uintptr_t)p & 15); }
 
+// float -> TF32 (round to nearest, ties away from zero: add half a unit of
+// the 10-bit mantissa to the magnitude bits, drop the low 13) and -> BF16
+// (round to nearest even: the upper 16 bits after adding 0x7FFF plus the
+// lowest kept bit), on the integer pipes; finite inputs (the operand
+// values) only. The conversion instructions run on GB300's narrow
+// conversion pipe, at a small fraction of the integer rate.
+__device__ __forceinline__ uint32_t tf32_bits(float v) { return (__float_as_uint(v) + 0x1000u) & 0xFFFFE000u; }
+__device__ __forceinline__ uint16_t bf16_bits(float v) {
+  const uint32_t u = __float_as_uint(v);
+  return (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+}
+
 template <bool kBF16>
 __device__ __forceinline__ void put(unsigned char* op, int o, float v) {
-  if (kBF16) *reinterpret_cast<__nv_bfloat16*>(op + o) = __float2bfloat16_rn(v);
-  else {
-    uint32_t t;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
-    *reinterpret_cast<uint32_t*>(op + o) = t;
-  }
+  if (kBF16) *reinterpret_cast<uint16_t*>(op + o) = bf16_bits(v);
+  else *reinterpret_cast<uint32_t*>(op + o) = tf32_bits(v);
 }
 
 template <bool kBF16>
 __device__ __forceinline__ float round_in(float v) {
-  if (kBF16) return __bfloat162float(__float2bfloat16_rn(v));
-  uint32_t t;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(v));
-  return __uint_as_float(t);
+  if (kBF16) return __uint_as_float((uint32_t)bf16_bits(v) << 16);
+  return __uint_as_float(tf32_bits(v));
 }
 
 // one value of an operand (and its low part for the split forms)
@@ -236,145 +274,236 @@ __device__ __forceinline__ void q_row(const float* R, int r, float* o) {
 #undef RX
 }
 
-// rows of [D*] formed by part H of a Gauss point's two threads: {0, 3, 5}
-// and {1, 2, 4} (11 and 10 lower-triangle entries)
-__host__ __device__ constexpr int row_of_part(int h, int jj) {
-  return h == 0 ? (jj == 0 ? 0 : jj == 1 ? 3 : 5) : (jj == 0 ? 1 : jj == 1 ? 2 : 4);
+// row of lower-triangle index q (q = r (r + 1) / 2 + c, c <= r)
+__host__ __device__ constexpr int lw_row(int q) { return q < 1 ? 0 : q < 3 ? 1 : q < 6 ? 2 : q < 10 ? 3 : q < 15 ? 4 : 5; }
+
+// the point's quantity q in the per-point arrays
+__device__ __forceinline__ float& pv(float* pt, int q, int p) { return pt[q * kPoints + p]; }
+
+// Phase 1 of the Gauss-point work of point p = (element e, Gauss point gp)
+// of a tile, thread k = 0..5 of the point: k < 3 forms row k of the
+// Jacobian [J]; every k converts its share of the point's double inputs to
+// float, each value once: cep entries 4k .. 4k+3 (mm10: history1(1:36))
+// and, with finite strain, R entries k and k + 6 and urcs_n1 entry k.
+template <int k>
+__device__ __forceinline__ void tcg_phase1(const TangentArgs& a, const TcgTile& tl, const unsigned char* st,
+                                           const TcgStatic& T, float* pt, int p, int e, int gp) {
+  const int i = tl.i0 + e;
+  if constexpr (k < 3) {   // row k of [J] = sum_a dN_a/dxi_k x_a (into the [D*] slots, free until phase 2)
+    const float* dn = T.dn + (gp * 3 + k) * NN;
+    float j0 = 0.f, j1 = 0.f, j2 = 0.f;
+#pragma unroll
+    for (int n = 0; n < NN; ++n) {
+      const float w = dn[n];
+      j0 += w * T.x[e][n];
+      j1 += w * T.x[e][NN + n];
+      j2 += w * T.x[e][2 * NN + n];
+    }
+    pv(pt, kPtD + 3 * k, p) = j0;
+    pv(pt, kPtD + 3 * k + 1, p) = j1;
+    pv(pt, kPtD + 3 * k + 2, p) = j2;
+  }
+  constexpr int q0 = 4 * k, q1 = q0 + 4 < 21 ? q0 + 4 : 21;
+  if (tl.flags & 2) {
+    const double* Hh = a.hist1 + tl.hist_off + ((long long)i * NG + gp) * kHistMM10;
+#pragma unroll
+    for (int q = q0; q < q1; ++q) pv(pt, kPtC + q, p) = d2f_rn(Hh[lw_row(q) + 6 * (q - lw_row(q) * (lw_row(q) + 1) / 2)]);
+  } else {
+    const double* cp = reinterpret_cast<const double*>(
+        st + kStCep + gp * kCepSlab + pad_of(a.cep + tl.cep_off + ((long long)gp * tl.span + tl.i0) * 21)) + e * 21;
+#pragma unroll
+    for (int q = q0; q < q1; ++q) pv(pt, kPtC + q, p) = d2f_rn(cp[q]);
+  }
+  if (tl.flags & 1) {
+    const long long g0 = (tl.gp_off + (long long)tl.i0 * NG) * 9;
+    const double* rp = reinterpret_cast<const double*>(st + kStRot + pad_of(a.rot_n1 + g0)) + (e * NG + gp) * 9;
+    const double* up = reinterpret_cast<const double*>(st + kStUrcs + pad_of(a.urcs_n1 + g0)) + (e * NG + gp) * 9;
+    pv(pt, kPtR + k, p) = d2f_rn(rp[k]);
+    if constexpr (k + 6 < 9) pv(pt, kPtR + k + 6, p) = d2f_rn(rp[k + 6]);
+    pv(pt, kPtU + k, p) = d2f_rn(up[k]);
+  }
 }
 
-// One part (H = 0, 1) of the Gauss-point work of (element pe, point pg)
-// of a tile: Gamma, w det[J], the three rows of [D*] = [q][D][q]^T - Q-bar
-// this part owns (row_of_part; the other rows come from the other part
-// through shared memory), {T}, and H^ij = Gamma^T X^ij Gamma for the
-// part's three pairs (slots 3H .. 3H + 2 of 00 01 02 11 12 22), written
-// into the A operand. Both parts reach the same named barrier (the
-// exchange) whether their element is live or not.
-template <bool kBF16, bool kSplit, int H>
-__device__ __forceinline__ void point_h(const TangentArgs& a, const TcgTile& tl, const unsigned char* st,
-                                        TcgStatic& T, int pe, int pg, bool live, unsigned char* opA) {
-  using F = Form<kBF16, kSplit>;
-  const int item = pe * NG + pg;
-  float gam[9], f = 0.f, Tw[6];
-  if (live) {
-    const int i = tl.i0 + pe;
-    const float* dnx = T.dn + (pg * 3 + 0) * NN;
-    const float* dne = T.dn + (pg * 3 + 1) * NN;
-    const float* dnz = T.dn + (pg * 3 + 2) * NN;
-    const float w = T.dn[NG * 3 * NN + pg];
-    float dj;
-    jacobian_inverse<NN, float>(dnx, dne, dnz, T.x[pe], T.x[pe] + NN, T.x[pe] + 2 * NN, gam, dj);
-    f = w * dj;
-    // w det[J] [D], lower triangle row-wise (cep, or mm10 history1(1:36))
-    float C[21];
-    if (tl.flags & 2) {
-      const double* Hh = a.hist1 + tl.hist_off + ((long long)i * NG + pg) * kHistMM10;
+// row r of [q] (q_row) from R in the per-point arrays
+template <int r>
+__device__ __forceinline__ void q_row_pt(float* pt, int p, float* o) {
+  constexpr int x = r < 3 ? r : (r == 4 ? 1 : 0), y = r < 3 ? r : (r == 3 ? 1 : 2);
+  float R[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int r = 0, q = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c <= r; ++c, ++q) C[q] = f * (float)Hh[r + 6 * c];
-    } else {
-      const double* cp = reinterpret_cast<const double*>(
-          st + kStCep + pg * kCepSlab + pad_of(a.cep + tl.cep_off + ((long long)pg * tl.span + tl.i0) * 21));
-#pragma unroll
-      for (int q = 0; q < 21; ++q) C[q] = f * (float)cp[pe * 21 + q];
-    }
-    if (tl.flags & 1) {
-      const long long g0 = (tl.gp_off + (long long)tl.i0 * NG) * 9;
-      const double* rp = reinterpret_cast<const double*>(st + kStRot + pad_of(a.rot_n1 + g0)) + (pe * NG + pg) * 9;
-      const double* up = reinterpret_cast<const double*>(st + kStUrcs + pad_of(a.urcs_n1 + g0)) + (pe * NG + pg) * 9;
-      float R[9], q[36], cs[6];
-#pragma unroll
-      for (int m = 0; m < 9; ++m) R[m] = (float)rp[m];
-#pragma unroll
-      for (int r = 0; r < 6; ++r) q_row(R, r, q + 6 * r);
-#pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        float v = 0.f;
-#pragma unroll
-        for (int m = 0; m < 6; ++m) v += q[6 * r + m] * (float)up[m];
-        cs[r] = v;                                   // Cauchy stress at n+1
-      }
-#pragma unroll
-      for (int jj = 0; jj < 3; ++jj) {
-        const int j = row_of_part(H, jj);
-        float tc[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-          float v = 0.f;
-#pragma unroll
-          for (int m = 0; m < 6; ++m) v += q[6 * j + m] * C[lw(m, c)];
-          tc[c] = v;
-        }
-#pragma unroll
-        for (int c = 0; c <= j; ++c) {
-          float v = 0.f;
-#pragma unroll
-          for (int m = 0; m < 6; ++m) v += tc[m] * q[6 * c + m];
-          if (a.qbar) {   // Q-bar terms of row j (ctran1 with qbar)
-            const float xx = cs[0], yy = cs[1], zz = cs[2], xy = cs[3], yz = cs[4], xz = cs[5];
-            const float hw = 0.5f * f;
-            if (j == 0 && c == 0) v -= 2.f * xx * f;
-            if (j == 1 && c == 1) v -= 2.f * yy * f;
-            if (j == 2 && c == 2) v -= 2.f * zz * f;
-            if (j == 3 && (c == 0 || c == 1)) v -= xy * f;
-            if (j == 3 && c == 3) v -= hw * (xx + yy);
-            if (j == 4 && (c == 1 || c == 2)) v -= yz * f;
-            if (j == 4 && c == 3) v -= f * xz;
-            if (j == 4 && c == 4) v -= hw * (yy + zz);
-            if (j == 5 && (c == 0 || c == 2)) v -= xz * f;
-            if (j == 5 && c == 3) v -= f * yz;
-            if (j == 5 && c == 4) v -= f * xy;
-            if (j == 5 && c == 5) v -= hw * (xx + zz);
-          }
-          T.dx[item][lw(j, c)] = v;
-        }
-      }
-#pragma unroll
-      for (int m = 0; m < 6; ++m) Tw[m] = cs[m] * f;
-    } else {
-#pragma unroll
-      for (int jj = 0; jj < 3; ++jj) {
-        const int j = row_of_part(H, jj);
-#pragma unroll
-        for (int c = 0; c <= j; ++c) T.dx[item][lw(j, c)] = C[lw(j, c)];
-      }
-#pragma unroll
-      for (int m = 0; m < 6; ++m) Tw[m] = 0.f;
-    }
+  for (int j = 0; j < 3; ++j) {   // the rows of R that row r of [q] uses
+    R[x + 3 * j] = pv(pt, kPtR + x + 3 * j, p);
+    if (y != x) R[y + 3 * j] = pv(pt, kPtR + y + 3 * j, p);
   }
-  asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");   // both parts' rows of [D*] in T.dx
-  if (!live) return;
-  float Dl[21];
+  q_row(R, r, o);
+}
+
+// Phase 2a, thread k of the point: k = 0 inverts [J] into Gamma and forms
+// w det[J] (cofactor inverse, as jacobian_inverse); with finite strain
+// every k forms the Cauchy stress component {T}_k = [q]_k {urcs_n1}.
+template <int k>
+__device__ __forceinline__ void tcg_phase2a(const TcgStatic& T, float* pt, int p, int gp, bool geonl) {
+  if constexpr (k == 0) {
+    const float j11 = pv(pt, kPtD + 0, p), j12 = pv(pt, kPtD + 1, p), j13 = pv(pt, kPtD + 2, p);
+    const float j21 = pv(pt, kPtD + 3, p), j22 = pv(pt, kPtD + 4, p), j23 = pv(pt, kPtD + 5, p);
+    const float j31 = pv(pt, kPtD + 6, p), j32 = pv(pt, kPtD + 7, p), j33 = pv(pt, kPtD + 8, p);
+    const float c1 = j22 * j33 - j23 * j32, c2 = j21 * j33 - j23 * j31, c3 = j21 * j32 - j22 * j31;
+    const float dj = j11 * c1 - j12 * c2 + j13 * c3, rdj = 1.f / dj;
+    pv(pt, kPtGam + 0, p) = c1 * rdj;
+    pv(pt, kPtGam + 1, p) = -c2 * rdj;
+    pv(pt, kPtGam + 2, p) = c3 * rdj;
+    pv(pt, kPtGam + 3, p) = (j32 * j13 - j12 * j33) * rdj;
+    pv(pt, kPtGam + 4, p) = (j11 * j33 - j31 * j13) * rdj;
+    pv(pt, kPtGam + 5, p) = (j12 * j31 - j11 * j32) * rdj;
+    pv(pt, kPtGam + 6, p) = (j12 * j23 - j13 * j22) * rdj;
+    pv(pt, kPtGam + 7, p) = (j13 * j21 - j11 * j23) * rdj;
+    pv(pt, kPtGam + 8, p) = (j11 * j22 - j12 * j21) * rdj;
+    pv(pt, kPtF, p) = T.dn[NG * 3 * NN + gp] * dj;
+  }
+  if (geonl) {
+    float o[6];
+    q_row_pt<k>(pt, p, o);
+    float t = 0.f;
 #pragma unroll
-  for (int z = 0; z < 21; ++z) Dl[z] = T.dx[item][z];
+    for (int m = 0; m < 6; ++m) t += o[m] * pv(pt, kPtU + m, p);
+    pv(pt, kPtT + k, p) = t;
+  }
+}
+
+// Q-bar entry (j, c), c <= j, of ctran1 with qbar, without the factor
+// w det[J], from the Cauchy stress (xx yy zz xy yz xz)
+template <int J, int Cc>
+__device__ __forceinline__ float qbar_entry(float* pt, int p) {
+  constexpr int q = lw(J, Cc);
+  auto t = [&](int m) { return pv(pt, kPtT + m, p); };
+  if constexpr (q == 0) return 2.f * t(0);
+  if constexpr (q == 2) return 2.f * t(1);
+  if constexpr (q == 5) return 2.f * t(2);
+  if constexpr (q == 6 || q == 7 || q == 19) return t(3);
+  if constexpr (q == 11 || q == 12 || q == 18) return t(4);
+  if constexpr (q == 13 || q == 15 || q == 17) return t(5);
+  if constexpr (q == 9) return 0.5f * (t(0) + t(1));
+  if constexpr (q == 14) return 0.5f * (t(1) + t(2));
+  if constexpr (q == 20) return 0.5f * (t(0) + t(2));
+  return 0.f;
+}
+
+template <int J>
+__device__ __forceinline__ float qbar_entry_dispatch(int c, float* pt, int p) {
+  switch (c) {
+    case 0: return qbar_entry<J, 0>(pt, p);
+    case 1: return qbar_entry<J, 1>(pt, p);
+    case 2: return qbar_entry<J, 2>(pt, p);
+    case 3: return qbar_entry<J, 3>(pt, p);
+    case 4: return qbar_entry<J, 4>(pt, p);
+    default: return qbar_entry<J, 5>(pt, p);
+  }
+}
+
+__device__ __forceinline__ void q_row_dispatch(int c, float* pt, int p, float* o) {
+  switch (c) {
+    case 0: q_row_pt<0>(pt, p, o); break;
+    case 1: q_row_pt<1>(pt, p, o); break;
+    case 2: q_row_pt<2>(pt, p, o); break;
+    case 3: q_row_pt<3>(pt, p, o); break;
+    case 4: q_row_pt<4>(pt, p, o); break;
+    default: q_row_pt<5>(pt, p, o); break;
+  }
+}
+
+// Phase 2, thread J of the point: row J of w det[J] [D*] = [q][D][q]^T -
+// Q-bar (lower triangle, columns c <= J), and w det[J] {T}_J; without
+// finite strain [D*] = [D] and no {T}.
+template <int J>
+__device__ __forceinline__ void tcg_phase2(const TangentArgs& a, int flags, float* pt, int p) {
+  const float f = pv(pt, kPtF, p);
+  if (flags & 1) {
+    // the rows of [q] this thread needs are formed from R in registers
+    // (cheaper than reading them from shared memory six times over)
+    float qj[6], tc[6];
+    q_row_pt<J>(pt, p, qj);
 #pragma unroll
-  for (int pp = 0; pp < 3; ++pp) {
-    const int slot = 3 * H + pp;            // pairs 00 01 02 11 12 22
-    const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
-    const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
-    float X[3][3];
+    for (int c = 0; c < 6; ++c) {
+      float v = 0.f;
 #pragma unroll
-    for (int p = 0; p < 3; ++p)
+      for (int m = 0; m < 6; ++m) v += qj[m] * pv(pt, kPtC + lw(m, c), p);
+      tc[c] = v;
+    }
 #pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        float v = Dl[lw(voigt(ii, p), voigt(jj, q))];
-        if (ii == jj) v += Tw[voigt(p, q)];
-        X[p][q] = v;
-      }
-    float Y[3][3];
+    for (int c = 0; c <= J; ++c) {
+      float qc[6];
+      q_row_dispatch(c, pt, p, qc);
+      float v = 0.f;
 #pragma unroll
-    for (int p = 0; p < 3; ++p)
+      for (int m = 0; m < 6; ++m) v += tc[m] * qc[m];
+      v *= f;
+      if (a.qbar) v -= f * qbar_entry_dispatch<J>(c, pt, p);
+      pv(pt, kPtD + lw(J, c), p) = v;
+    }
+    pv(pt, kPtTw + J, p) = pv(pt, kPtT + J, p) * f;
+  } else {
 #pragma unroll
-      for (int s2 = 0; s2 < 3; ++s2)
-        Y[p][s2] = X[p][0] * gam[3 * s2] + X[p][1] * gam[3 * s2 + 1] + X[p][2] * gam[3 * s2 + 2];
-    // A operand row (slot, element pe), k = (r*3 + s)*8 + gp
-    const int row = slot * kTile + pe;
+    for (int c = 0; c <= J; ++c) pv(pt, kPtD + lw(J, c), p) = f * pv(pt, kPtC + lw(J, c), p);
+    pv(pt, kPtTw + J, p) = 0.f;
+  }
+}
+
+// per pair slot (00 01 02 11 12 22) and entry (r, q) of X^ij: the per-point
+// array holding [D*](v(i,r), v(j,q)), and for i = j the one holding
+// {T}[r][q] (w det[J] {T}, Voigt index v(r, q))
+struct PairIdx {
+  unsigned char d[6][9], tw[9];
+};
+__host__ __device__ constexpr PairIdx make_pair_idx() {
+  PairIdx t{};
+  for (int sl = 0; sl < 6; ++sl) {
+    const int ii = sl < 3 ? 0 : (sl < 5 ? 1 : 2), jj = sl < 3 ? sl : (sl == 3 ? 1 : 2);
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) t.d[sl][3 * r + q] = (unsigned char)(kPtD + lw(voigt(ii, r), voigt(jj, q)));
+  }
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) t.tw[3 * r + q] = (unsigned char)(kPtTw + voigt(r, q));
+  return t;
+}
+__constant__ PairIdx c_pair = make_pair_idx();
+
+// Phase 3, thread `slot` of the point: H^ij = Gamma^T X^ij Gamma for pair
+// slot of 00 01 02 11 12 22, X^ij[r][q] = [D*](v(i,r), v(j,q)) + delta_ij
+// {T}[r][q], into A operand row (slot, element e), k = (r*3 + s)*8 + gp.
+// One code path for the six pairs (indices from a table): specialised
+// copies let the compiler hoist the union of their loads and spill.
+template <bool kBF16, bool kSplit>
+__device__ __forceinline__ void tcg_phase3(float* pt, int p, int e, int gp, int slot, unsigned char* opA) {
+  using F = Form<kBF16, kSplit>;
+  const bool diag = slot == 0 || slot == 3 || slot == 5;
+  float gam[9], X[9];
+#pragma unroll
+  for (int m = 0; m < 9; ++m) gam[m] = pv(pt, kPtGam + m, p);
+#pragma unroll
+  for (int m = 0; m < 9; ++m) {
+    float v = pv(pt, c_pair.d[slot][m], p);
+    if (diag) v += pv(pt, c_pair.tw[m], p);
+    X[m] = v;
+  }
+  const int row = slot * kTile + e;
+  // one column s of H at a time: y = X Gamma_s, H[r][s] = Gamma_r . y. For
+  // i = j, H is symmetric: only r <= s is formed and written to both (r, s)
+  // and (s, r), so that the rounded operand stays exactly symmetric --
+  // otherwise an entry and its mirror can round to different TF32 / BF16
+  // values, and the packed upper triangle (mirrored below the diagonal)
+  // loses the exact rigid-translation null space of the node sums
+#pragma unroll
+  for (int s2 = 0; s2 < 3; ++s2) {
+    float y[3];
 #pragma unroll
     for (int r = 0; r < 3; ++r)
+      y[r] = X[3 * r] * gam[3 * s2] + X[3 * r + 1] * gam[3 * s2 + 1] + X[3 * r + 2] * gam[3 * s2 + 2];
 #pragma unroll
-      for (int s2 = 0; s2 < 3; ++s2)
-        put_split<kBF16, kSplit>(opA, F::kOpA, F::off(row, (3 * r + s2) * 8 + pg),
-                                 gam[3 * r] * Y[0][s2] + gam[3 * r + 1] * Y[1][s2] + gam[3 * r + 2] * Y[2][s2]);
+    for (int r = 0; r < 3; ++r) {
+      if (diag && r > s2) continue;
+      const float h = gam[3 * r] * y[0] + gam[3 * r + 1] * y[1] + gam[3 * r + 2] * y[2];
+      put_split<kBF16, kSplit>(opA, F::kOpA, F::off(row, (3 * r + s2) * 8 + gp), h);
+      if (diag && r < s2) put_split<kBF16, kSplit>(opA, F::kOpA, F::off(row, (3 * s2 + r) * 8 + gp), h);
+    }
   }
 }
 
@@ -404,11 +533,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&T.empty[s])), "r"(1));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&T.mma)), "r"(1));
+    for (int b = 0; b < 2; ++b)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&T.ibar[b])), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;");
     T.pabort = 0;
     T.cabort = 0;
     T.issued = 0;
     T.done = 0;
+    T.ifetch = 0;
+    T.iwait = 0;
   }
   for (int k = tid; k < NG * 3 * NN + NG; k += kThreads) T.dn[k] = a.dn32[0][k];
   // the constant operator M (B operand): row a*8 + b, k = (r*3 + s)*8 + gp,
@@ -432,22 +565,55 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
 
   if (warp == kConsumers / 32) {
     // ================= producer =================
+    // The dof indices of the tile after this one are bulk-copied into
+    // shared memory (T.idx, on T.ibar) while this tile's gathers are
+    // issued, so that no gather waits for an index load from DRAM; the
+    // consumers get the tile record by a cp.async into the stage header,
+    // on the stage's mbarrier. Index slab copies start at the 16-byte
+    // boundary below the slab (the arrays carry 16 bytes of slack at the
+    // end); `off` is the slab's first index within the copy.
     constexpr int kPerLane = kTile * TOT / 32;   // 12 gathered dofs per lane and tile
-    TcgTile nxt = tiles[blockIdx.x];
+    auto fetch_idx = [&](int t, int b) -> int {  // lane 0: returns the offset of the slab in T.idx[b]
+      const TcgTile* r = tiles + t;
+      const long long dbase = r->einf_off + (long long)r->i0 * TOT;
+      const int nv = r->n * TOT;
+      const bool fs = r->flags & 1;
+      const uintptr_t pc = (uintptr_t)(a.cdest + dbase), pe_ = (uintptr_t)(a.edest + dbase);
+      const uintptr_t pc16 = pc & ~(uintptr_t)15, pe16 = pe_ & ~(uintptr_t)15;
+      const uint32_t bytes = (uint32_t)(((pc - pc16) + nv * 4 + 15) & ~15ull);   // same offset for both arrays
+      const uint32_t bar = su32(&T.ibar[b]);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(fs ? 2 * bytes : bytes)
+                   : "memory");
+      // the slab's previous contents were read (generic proxy) by the
+      // gathers of two tiles ago; order those reads before the copy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_g2s(su32(&T.idx[b][0][0]), (const void*)pc16, bytes, bar);
+      if (fs) bulk_g2s(su32(&T.idx[b][1][0]), (const void*)pe16, bytes, bar);
+      T.ifetch += 1;
+      return (int)((pc - pc16) >> 2);
+    };
+    int off_next = 0;
+    if (lane == 0) off_next = fetch_idx(blockIdx.x, 0);
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
-      const TcgTile tl = nxt;
-      if (t + (int)gridDim.x < ntiles) nxt = tiles[t + gridDim.x];   // next tile's record, in flight meanwhile
-      // this tile's dof indices, all loads issued before the first copy
-      const long long dbase = tl.einf_off + (long long)tl.i0 * TOT;
-      const int nv = tl.n * TOT;
-      const bool geonl = tl.flags & 1;
+      const int b = k & 1;
+      const int off = __shfl_sync(0xffffffffu, off_next, 0);
+      const int nv = tiles[t].n * TOT;   // the record line is in cache: read for the index copy
+      const bool geonl = tiles[t].flags & 1;
+      if (!wait_phase(&T.ibar[b], (k >> 1) & 1, limit, cabort)) {
+        if (lane == 0) *pabort = 1;
+        break;
+      }
+      if (lane == 0) T.iwait = k + 1;
+      // the next tile's indices, in flight while this tile is issued (the
+      // other slab's indices were consumed by the previous tile's gathers)
+      if (lane == 0 && t + (int)gridDim.x < ntiles) off_next = fetch_idx(t + gridDim.x, b ^ 1);
       int ci[kPerLane], ei[kPerLane];
 #pragma unroll
       for (int j = 0; j < kPerLane; ++j) {
         const int q = lane + 32 * j;
-        ci[j] = q < nv ? a.cdest[dbase + q] - 1 : 0;
-        ei[j] = q < nv && geonl ? a.edest[dbase + q] - 1 : 0;
+        ci[j] = q < nv ? T.idx[b][0][off + q] - 1 : 0;
+        ei[j] = q < nv && geonl ? T.idx[b][1][off + q] - 1 : 0;
       }
       const int s = k % S, use = k / S;
       if (use > 0 && !wait_phase(&T.empty[s], (use - 1) & 1, limit, cabort)) {
@@ -458,7 +624,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
       unsigned char* st = stages + s * kStage;
       const uint32_t bar = su32(&T.full[s]);
       if (lane == 0) {
-        T.hdr[s] = tl;   // published by the arrival below (release)
+        const TcgTile tl = tiles[t];   // the record line is in cache (fetched one tile ago)
+        // the record into the stage header, complete when the stage is
+        for (int c = 0; c < 4; ++c)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(su32(&T.hdr[s]) + 16 * c),
+                       "l"(reinterpret_cast<const char*>(tiles + t) + 16 * c) : "memory");
         uint32_t tx = 0;
         // byte total first (expect_tx must not trail the copies' completion)
         for (int pass = 0; pass < 2; ++pass) {
@@ -503,13 +673,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
     }
   } else {
     // ================= consumers =================
-    // warps 0-3 and 4-7 take the two parts of every (element, Gauss
-    // point): the part is uniform over a warp. A warp holds 8 elements x 4
-    // Gauss points, lane = element (low 3 bits) + 8 x point, so that its
-    // stores into an A row slot (rows slot*16 + element) fall in 32
-    // distinct banks
-    const int h = warp >> 2;
-    const int pe = (lane & 7) + 8 * (warp & 1), pg = (lane >> 3) + 4 * ((warp >> 1) & 1);
+    // warp w: thread k = w % 6 of points p = lane + 32 (w / 6); point p is
+    // (element (lane & 7) + 8 (g & 1), Gauss point (lane >> 3) + 4 (g >> 1))
+    // with g = w / 6, so that the 32 lanes of a warp write their A operand
+    // values (rows slot*16 + element, k = .. + Gauss point) into 32
+    // distinct banks and read the per-point arrays consecutively
+    const int g = warp / kRows, kr = warp % kRows;
+    const int p = lane + 32 * g, pe = (lane & 7) + 8 * (g & 1), pg = (lane >> 3) + 4 * (g >> 1);
+    float* pt = reinterpret_cast<float*>(smem + F::kOffPt);
     int k = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
       const int s = k % S;
@@ -519,13 +690,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
       if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
       asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (*cabort) break;
-      // the tile record, read from shared memory where needed; what the
-      // epilogue needs is copied before the stage (and record) is released
-      const TcgTile& tl = T.hdr[s];
+      // the tile record (the stage, record included, is handed back to the
+      // producer once phase 1 has read it)
+      const TcgTile tl = T.hdr[s];
       const int tn = tl.n;
       float* const out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)tl.i0 * UT;
       // element coordinates at n+1 relative to node 1
-      for (int q = tid; q < tl.n * TOT; q += kConsumers) {
+      for (int q = tid; q < tn * TOT; q += kConsumers) {
         const int e = q / TOT, d = q % TOT, q0 = e * TOT + (d / NN) * NN;
         const double* xc = reinterpret_cast<const double*>(st + kStXc);
         double v = xc[q], ref = xc[q0];
@@ -535,26 +706,59 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
           v = v + xu[q] + xdu[q];
           ref = ref + xu[q0] + xdu[q0];
         }
-        T.x[e][d] = (float)(v - ref);
+        T.x[e][d] = d2f_rn(v - ref);
       }
       asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
-      // the Gauss-point work, written into the A operand (the previous
-      // tile's MMAs are complete and its Ke store has read the region)
-      const bool live = pe < tl.n;
-      if (h == 0) point_h<kBF16, kSplit, 0>(a, tl, st, T, pe, pg, live, opA);
-      else point_h<kBF16, kSplit, 1>(a, tl, st, T, pe, pg, live, opA);
-      if (kBF16) {   // the K padding (72..79) must be finite zeros: the staging reuses the region
-        for (int row = tid; row < kM; row += kConsumers)
-          for (int kk = kKLive; kk < F::kK; ++kk) {
-            put<kBF16>(opA, F::off(row, kk), 0.f);
-            if (kSplit) put<kBF16>(opA + F::kOpA, F::off(row, kk), 0.f);
-          }
+      const bool live = pe < tn;
+      if (live) {
+        switch (kr) {
+          case 0: tcg_phase1<0>(a, tl, st, T, pt, p, pe, pg); break;
+          case 1: tcg_phase1<1>(a, tl, st, T, pt, p, pe, pg); break;
+          case 2: tcg_phase1<2>(a, tl, st, T, pt, p, pe, pg); break;
+          case 3: tcg_phase1<3>(a, tl, st, T, pt, p, pe, pg); break;
+          case 4: tcg_phase1<4>(a, tl, st, T, pt, p, pe, pg); break;
+          default: tcg_phase1<5>(a, tl, st, T, pt, p, pe, pg); break;
+        }
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
+      // stage consumed: hand it back to the producer
+      if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&T.empty[s])) : "memory");
+      if (live) {
+        const bool geonl = tl.flags & 1;
+        switch (kr) {
+          case 0: tcg_phase2a<0>(T, pt, p, pg, geonl); break;
+          case 1: tcg_phase2a<1>(T, pt, p, pg, geonl); break;
+          case 2: tcg_phase2a<2>(T, pt, p, pg, geonl); break;
+          case 3: tcg_phase2a<3>(T, pt, p, pg, geonl); break;
+          case 4: tcg_phase2a<4>(T, pt, p, pg, geonl); break;
+          default: tcg_phase2a<5>(T, pt, p, pg, geonl); break;
+        }
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
+      if (live) {
+        switch (kr) {
+          case 0: tcg_phase2<0>(a, tl.flags, pt, p); break;
+          case 1: tcg_phase2<1>(a, tl.flags, pt, p); break;
+          case 2: tcg_phase2<2>(a, tl.flags, pt, p); break;
+          case 3: tcg_phase2<3>(a, tl.flags, pt, p); break;
+          case 4: tcg_phase2<4>(a, tl.flags, pt, p); break;
+          default: tcg_phase2<5>(a, tl.flags, pt, p); break;
+        }
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
+      // H into the A operand (the previous tile's MMAs are complete and its
+      // Ke store has read the region)
+      if (live) tcg_phase3<kBF16, kSplit>(pt, p, pe, pg, kr, opA);
+      if constexpr (kBF16) {   // the K padding (72..79) must be finite zeros: the staging reuses the region
+        for (int z = tid; z < kM * (F::kK - kKLive); z += kConsumers) {
+          const int row = z / (F::kK - kKLive), kk = kKLive + z % (F::kK - kKLive);
+          put<kBF16>(opA, F::off(row, kk), 0.f);
+          if (kSplit) put<kBF16>(opA + F::kOpA, F::off(row, kk), 0.f);
+        }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (tid == 0) {
-        // stage consumed: hand it back to the producer
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&T.empty[s])) : "memory");
         asm volatile("tcgen05.fence::after_thread_sync;");
         // descriptors advanced in the start-address field (16-byte units):
         // one k-step = two core matrices along K = 256 bytes
@@ -580,44 +784,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
       asm volatile("tcgen05.fence::after_thread_sync;");
       asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (*cabort) break;
-      // accumulator -> packed Ke in the staging (the A region: the MMAs are done)
-      {
+      // accumulator -> packed Ke in the staging (the A region: the MMAs are
+      // done). Warp w < 16 reads TMEM lane quadrant w % 4 (the quadrant a
+      // warp may access), columns 16 (w / 4) .. + 15
+      if (warp < 16) {
         float* ke = reinterpret_cast<float*>(opA);
-        // warp w: lane quadrant w % 4, columns 32 * (w / 4) .. + 31
-        const bool ld_warp = warp < 8;
-        const int quad = warp & 3, half = (warp >> 2) & 1;
+        const int quad = warp & 3, cq = warp >> 2;
         const int row = 32 * quad + lane, e = row & (kTile - 1), slot = row >> 4;
-        const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(32 * half);
-        if (ld_warp) {
-          const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
-          const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
-          const bool keep = slot < 6 && e < tn;
-          const float bf = (float)a.beta_fact;
+        const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(16 * cq);
+        const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+        const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+        const bool keep = slot < 6 && e < tn;
+        const float bf = (float)a.beta_fact;
+        uint32_t v[16];   // the load and its wait in one statement
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            "tcgen05.wait::ld.sync.aligned;"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr)
+            : "memory");
+        if (keep) {
 #pragma unroll
-          for (int p16 = 0; p16 < 2; ++p16) {
-            uint32_t v[16];   // the load and its wait in one statement
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-                "tcgen05.wait::ld.sync.aligned;"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15])
-                : "r"(taddr + 16 * p16)
-                : "memory");
-            // the MMAs are complete: the staging may overwrite the A operand
-            if (keep) {
-#pragma unroll
-              for (int c = 0; c < 16; ++c) {
-                const int ab = 32 * half + 16 * p16 + c, an = ab >> 3, bn = ab & 7;
-                if (ii == jj && an > bn) continue;
-                const int d1 = ii * NN + an, d2 = jj * NN + bn;
-                ke[e * UT + d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[c]) * bf;
-              }
-            }
+          for (int c = 0; c < 16; ++c) {
+            const int ab = 16 * cq + c, an = ab >> 3, bn = ab & 7;
+            if (ii == jj && an > bn) continue;
+            const int d1 = ii * NN + an, d2 = jj * NN + bn;
+            ke[e * UT + d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[c]) * bf;
           }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       {
@@ -644,6 +841,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
     // not take, then NaN for every tile of this CTA not finished
     if (tid == 0) {
       for (int q = T.done; q < T.issued; ++q) wait_phase(&T.full[q % S], (q / S) & 1, kDrainLimit, nullptr);
+      for (int q = T.iwait; q < T.ifetch; ++q) wait_phase(&T.ibar[q & 1], (q >> 1) & 1, kDrainLimit, nullptr);
       atomicExch(tc_timeout, 1);
     }
     __syncthreads();

@@ -85,6 +85,26 @@ class DeviceCsr:
         abi.check(self.lib, self.lib.w3g_free_dot_dev(self.h, d_a, d_b, d_fixed, d_out, stream or None))
 
 
+# Eisenstat-Walker forcing terms (choice 2, gamma = 0.9, exponent 2) for the
+# inexact Newton solves: the linear solve of each iteration only needs to
+# be as accurate as the Newton iteration can use; the convergence test is
+# on the true residual of the recovery either way
+EW_ETA_MAX, EW_GAMMA = 0.1, 0.9
+
+
+def ew_forcing(eta_prev: float, rn: float, rn_prev: float, target: float) -> float:
+    """Next relative tolerance of the linear solve: gamma (rn / rn_prev)^2,
+    not below gamma eta_prev^2 when that is still large (safeguard against
+    a sudden drop), at most EW_ETA_MAX, and no tighter than what reaching
+    the Newton target `target` from rn needs."""
+    eta = EW_GAMMA * (rn / rn_prev) ** 2
+    sg = EW_GAMMA * eta_prev ** 2
+    if sg > 0.1:
+        eta = max(eta, sg)
+    eta = min(eta, EW_ETA_MAX)
+    return max(eta, 0.5 * target / rn)
+
+
 class IncrementFailed(RuntimeError):
     """A (sub-)increment did not converge, or its recovery or solve asked
     for a smaller step."""
@@ -137,13 +157,16 @@ class DeviceNewtonDriver:
     def __init__(self, model, engine, fixed, tol: float = 1e-8, maxit: int = 25, extrapolate: bool = False,
                  lin_rtol: float = 1e-10, lin_maxit: int = 50000, device: int = 0, csr: DeviceCsr | None = None,
                  adaptive: bool = False, adaptive_step1: bool = False, adapt_divisions: int = 4,
-                 adapt_min_fact: float = 1.0 / 16.0, line_search: bool = False):
+                 adapt_min_fact: float = 1.0 / 16.0, line_search: bool = False, forcing: str = "fixed"):
         import torch
         self.torch = torch
         self.model = model
         self.engine = engine
         self.tol, self.maxit, self.extrapolate = tol, maxit, extrapolate
         self.lin_rtol, self.lin_maxit = lin_rtol, lin_maxit
+        if forcing not in ("fixed", "ew"):
+            raise ValueError("forcing must be 'fixed' or 'ew'")
+        self.forcing = forcing
         self.adaptive, self.adaptive_step1 = adaptive, adaptive_step1
         self.adapt_divisions, self.adapt_min_fact = adapt_divisions, adapt_min_fact
         dev = torch.device("cuda", device)
@@ -202,9 +225,11 @@ class DeviceNewtonDriver:
         if self._recover(step, 0, extrap) != 0:
             raise IncrementFailed(f"step {step}: recovery requested a step cut at iteration 0")
         self._tangent(step, 0)
+        eta, rn_prev = EW_ETA_MAX, None
         for it in range(1, self.maxit + 1):
+            rtol = self.lin_rtol if self.forcing == "fixed" else max(self.lin_rtol, eta)
             st, nits, rel = self.csr.pcg(self.mask.data_ptr(), self.ifv.data_ptr(), -1.0, self.d.data_ptr(),
-                                         self.lin_rtol, self.lin_maxit)
+                                         rtol, self.lin_maxit)
             lin.append(nits)
             self.trace.append([st, nits, rel, None])
             if st == abi.PCG_BREAKDOWN:
@@ -218,6 +243,9 @@ class DeviceNewtonDriver:
             self.trace[-1][3] = rn / scale
             if rn <= self.tol * scale:
                 return res_hist, lin
+            if self.forcing == "ew" and rn_prev is not None:
+                eta = ew_forcing(eta, rn, rn_prev, self.tol * scale)
+            rn_prev = rn
             self._tangent(step, it)
         raise IncrementFailed(f"step {step}: no convergence in {self.maxit} iterations: {res_hist}")
 
