@@ -119,6 +119,8 @@ def parse():
     ap.add_argument("--study-maxit", type=int, default=25)
     ap.add_argument("--study-forcing", default="fixed", choices=["fixed", "ew"],
                     help="PCG tolerance per Newton iteration: fixed 1e-10, or Eisenstat-Walker forcing terms")
+    ap.add_argument("--study-eta-max", type=float, default=1e-4, help="largest Eisenstat-Walker tolerance")
+    ap.add_argument("--study-save-u", default=None, help="directory for each form's final displacements (.npy)")
     ap.add_argument("--study-lin-maxit", type=int, default=50000)
     ap.add_argument("--study-no-extrapolate", action="store_true",
                     help="start every step from zero instead of the scaled previous increment")
@@ -467,7 +469,7 @@ def bench_formulations(args, dev, local):
 
 def type_study(args, dev):
     """One Newton iteration's element work per element type alone, FP64 and
-    with the FP32 tangent: 40^3 20-node bricks, 40^3 x 6 10-node
+    with the FP32 tangent (and for bricks the tensor-core tangents): 40^3 20-node bricks, 40^3 x 6 10-node
     tetrahedra, n^3 8-node bricks (jitter 0.05h, mm01, blocks of 128;
     state after one step to 1% tension; CUDA events over 5 calls each)."""
     import torch
@@ -488,7 +490,11 @@ def type_study(args, dev):
         tc, tu, tdu = (torch.from_numpy(a).to(dev) for a in (model.c, u1, du))
         tifv = torch.zeros(model.nodof, dtype=torch.float64, device=dev)
         res = {"elements": model.noelem}
-        for pname, prec in (("fp64", abi.TANGENT_FP64), ("fp32", abi.TANGENT_FP32)):
+        forms = [("fp64", abi.TANGENT_FP64), ("fp32", abi.TANGENT_FP32)]
+        if et != abi.ETYPE_TET10:   # bricks: the tensor-core forms too
+            forms += [("tf32", abi.TANGENT_TF32), ("bf16", abi.TANGENT_BF16), ("tf32x3", abi.TANGENT_TF32X3),
+                      ("bf16x3", abi.TANGENT_BF16X3)]
+        for pname, prec in forms:
             eng.set_precision(prec)
             for _ in range(max(3, args.warmup)):
                 eng.tanstf_dev(2, 1, tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), 0)
@@ -900,7 +906,7 @@ def newton_forms(args, model, fixed, topz, nz, names, eng, csr):
         drv = DeviceNewtonDriver(model, eng, fixed, tol=1e-8, maxit=args.study_maxit, lin_rtol=1e-10,
                                  lin_maxit=args.study_lin_maxit, csr=csr, extrapolate=not args.study_no_extrapolate,
                                  adaptive=not args.study_no_adaptive, adaptive_step1=True,
-                                 forcing=args.study_forcing)
+                                 forcing=args.study_forcing, eta_max=args.study_eta_max)
         rec = {"steps": [], "failed": None}
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -928,6 +934,9 @@ def newton_forms(args, model, fixed, topz, nz, names, eng, csr):
         rec["mean_newton_per_step"] = float(np.mean(its)) if its else None
         rec["pcg_total"] = int(sum(sum(x["pcg"]) for x in rec["steps"]))
         u = drv.u
+        if args.study_save_u:
+            os.makedirs(args.study_save_u, exist_ok=True)
+            np.save(os.path.join(args.study_save_u, f"u_{name}.npy"), u)
         if name == "fp64":
             u_ref = u
             end_state = model.new_state()
@@ -962,7 +971,8 @@ def batched_study(args, dev):
                         f"{args.study_steps} steps",
             "elements": model.noelem, "blocks": model.nelblk, "dofs": model.nodof, "csr_nnz": csr.nnz,
             "setup_s": setup_s, "newton_tol": 1e-8,
-            "pcg_rtol": 1e-10 if args.study_forcing == "fixed" else "Eisenstat-Walker (gamma 0.9, eta_max 0.1)",
+            "pcg_rtol": 1e-10 if args.study_forcing == "fixed" else
+            f"Eisenstat-Walker (gamma 0.9, eta_max {args.study_eta_max:g}, floor 1e-10)",
             "forms": forms}
 
 

@@ -264,6 +264,20 @@ int w3g_recover(w3g_context* ctx, int step, int iter, int extrapolated_du,
 /* update (src/update.f:73-94): history, strains, stresses n+1 -> n. */
 int w3g_update(w3g_context* ctx);
 
+/* How w3g_update moves the converged state to n. W3G_UPDATE_COPY (the
+   default) copies n+1 into n, as WARP3D's update does, so both hold the
+   same values afterwards. W3G_UPDATE_SWAP exchanges the n and n+1 arrays
+   instead (no copy): n then holds the converged state and n+1 the state
+   of the step before, until the next recovery overwrites it -- except the
+   history of crystal-plasticity (mm10) blocks, which is copied back into
+   n+1 because their local solve starts from it. Every array the recovery
+   and tangent read is the same in both modes, so results are bitwise
+   identical; only a download of the n+1 arrays between an update and the
+   next recovery differs. */
+#define W3G_UPDATE_COPY 0
+#define W3G_UPDATE_SWAP 1
+int w3g_set_update_mode(w3g_context* ctx, int mode);
+
 /* ---- the hot path, device-resident arrays --------------------------
    Same work as above on device pointers (c, u, du, ifv of type double*
    on ctx's device) enqueued on `stream` (a cudaStream_t, or NULL for the

@@ -140,8 +140,8 @@ def test_tensor_core_tangent_linear_iteration_zero(plastic_hex8, precision):
 
 
 def test_tensor_core_tangent_mixed_types():
-    """8-node bricks on the tensor cores; 20-node bricks and tetrahedra
-    in the same call."""
+    """8-node and 20-node bricks on the tensor cores, tetrahedra on the
+    CUDA cores, in the same call."""
     rng = np.random.Generator(np.random.PCG64(11))
     coords, parts, origins = mixed_mesh(
         [(abi.ETYPE_L3DISOP, 3), (abi.ETYPE_Q3DISOP, 2), (abi.ETYPE_TET10, 2)], ny=2, nz=3, jitter=0.05, seed=11)
@@ -156,7 +156,7 @@ def test_tensor_core_tangent_mixed_types():
         err = _tangent_err(model, eng, ora, 4, 1, u, du)
         print(f"mixed {NAMES[precision]} tangent rel err {err:.2e}")
         assert err <= TOL[precision]
-        # tensor-core bricks + 20-node + tetrahedra kernels
+        # 8-node and 20-node tensor-core kernels + the tetrahedra items
         assert eng.last_launch_count() == 3
 
 
@@ -249,4 +249,70 @@ def test_tensor_core_tangent_in_a_graph_replay_equals_direct_launch(plastic_hex8
                               tifv.data_ptr(), stream)
         torch.cuda.synchronize()
         assert np.array_equal(ke(), direct)
+    eng.set_precision(abi.TANGENT_FP64)
+
+
+# the 20-node bricks' tensor-core kernel always splits both operands (the
+# 27-point rule keeps no exact translation null space under one rounding):
+# split-form accuracy for every request
+TOL20 = {abi.TANGENT_TF32: 1e-5, abi.TANGENT_BF16: 1e-4, abi.TANGENT_TF32X3: 1e-5, abi.TANGENT_BF16X3: 1e-4}
+
+
+@pytest.fixture(scope="module")
+def plastic_hex20():
+    rng = np.random.Generator(np.random.PCG64(21))
+    coords, parts, origins = mixed_mesh([(abi.ETYPE_Q3DISOP, 3)], ny=2, nz=3, jitter=0.05, seed=21)
+    plist = [Part(et, inc, random_spans(inc.shape[0], rng, 1, 9),
+                  [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)]) for et, inc in parts]
+    model = Model(coords, parts=plist)
+    return (model,) + _loaded(model, (3, 2, 3), origins=origins)
+
+
+def _unpack20(packed):
+    n = 60
+    iu = np.triu_indices(n)
+    pos = iu[1] * (iu[1] + 1) // 2 + iu[0]
+    K = np.zeros((packed.shape[0], n, n))
+    K[:, iu[0], iu[1]] = packed[:, pos]
+    K[:, iu[1], iu[0]] = packed[:, pos]
+    return K
+
+
+@pytest.mark.parametrize("precision", ALL)
+def test_tensor_core_tangent_hex20(plastic_hex20, precision):
+    """20-node bricks (27 Gauss points, ragged blocks) on the tensor cores:
+    every element matrix against the FP64 oracle, and the rigid
+    translations kept to the FP32 accumulation level."""
+    model, eng, ora, u, du = plastic_hex20
+    eng.set_precision(precision)
+    err = _tangent_err(model, eng, ora, 4, 1, u, du)
+    assert eng.last_launch_count() == 1   # the 20-node tensor-core kernel alone
+    est = model.estiff_blocks()
+    eng.tanstf(4, 1, model.c, u, du, est)
+    eng.set_precision(abi.TANGENT_FP64)
+    worst = 0.0
+    for blk in est:
+        K = _unpack20(blk)
+        scale = np.max(np.abs(K), axis=(1, 2))
+        for d in range(3):
+            t = np.zeros(60)
+            t[20 * d:20 * d + 20] = 1.0
+            worst = max(worst, float(np.max(np.max(np.abs(K @ t), axis=1) / scale)))
+    print(f"hex20 {NAMES[precision]} tangent rel err {err:.2e}, max |Ke t| / max |Ke| = {worst:.1e}")
+    assert err <= TOL20[precision]
+    assert worst <= 5e-6
+
+
+def test_tensor_core_hex20_wait_limit_zero_reports_efatal(plastic_hex20):
+    model, eng, ora, u, du = plastic_hex20
+    eng.set_precision(abi.TANGENT_TF32)
+    eng.set_wait_limit(0)
+    est = model.estiff_blocks()
+    with pytest.raises(abi.W3GError) as exc:
+        eng.tanstf(4, 1, model.c, u, du, est)
+    assert exc.value.code == abi.EFATAL
+    assert all(np.all(np.isnan(b)) for b in est)
+    # the context stays usable: the next call with the default limit is right
+    eng.set_wait_limit(-1)
+    assert _tangent_err(model, eng, ora, 4, 1, u, du) <= TOL20[abi.TANGENT_TF32]
     eng.set_precision(abi.TANGENT_FP64)

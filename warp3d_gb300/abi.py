@@ -30,6 +30,8 @@ EUNSUPPORTED = -2
 ECUDA = -3
 ENOMEM = -4
 EFATAL = -5
+UPDATE_COPY = 0
+UPDATE_SWAP = 1
 
 HIST_MM01 = 11
 HIST_MM10 = 158       # one fcc crystal, one hardening variable
@@ -158,6 +160,7 @@ PROTOTYPES = [
     ("w3g_last_error", C.c_char_p, []),
     ("w3g_set_tangent_precision", C.c_int, [_vp, C.c_int]),
     ("w3g_set_wait_limit", C.c_int, [_vp, C.c_longlong]),
+    ("w3g_set_update_mode", C.c_int, [_vp, C.c_int]),
     ("w3g_umat_features", C.c_int, [C.POINTER(C.c_int)]),
     ("w3g_state_upload", C.c_int, [_vp, C.POINTER(BlockState)]),
     ("w3g_state_download", C.c_int, [_vp, C.POINTER(BlockState)]),

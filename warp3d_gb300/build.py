@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libw3g.so")
-SOURCES = ["w3g_api.cu", "w3g_tangent.cu", "w3g_tangent_tc.cu", "w3g_tangent_tcg.cu", "w3g_recover.cu", "w3g_mm10.cu",
+SOURCES = ["w3g_api.cu", "w3g_tangent.cu", "w3g_tangent_tc.cu", "w3g_tangent_tcg.cu", "w3g_tangent_tc20.cu", "w3g_recover.cu", "w3g_mm10.cu",
            "w3g_solve.cu",
            "w3g_peak.cu", "w3g_noalloc.cu", "w3g_restart.cu",
            "w3g_tangent_full.cu"]

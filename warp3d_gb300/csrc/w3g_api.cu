@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 #include <algorithm>
 #include <thread>
@@ -48,7 +49,7 @@ void free_all(w3g_context* c) {
   DeviceModel& m = c->m;
   DeviceState& s = c->s;
   if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
-  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.tcchunks, m.tcgtiles, s.tc_timeout, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
+  void* ptrs[] = {m.blocks, m.chunks, m.tchunks, m.tcchunks, m.tcgtiles, m.tc20tiles, s.tc_timeout, m.rorder[0], m.rorder[1], m.torder[0], m.torder[1], m.edest,
                   m.cdest, m.mat, m.umat_props, m.dn[0], m.dn[1], m.dn[2], m.dn32[0], m.dn32[1], m.dn32[2],
                   m.ifv_rowptr, m.ifv_src, s.params, s.counters, m.xtal, m.xtype, m.mm10_gp, s.mm10_scr,
                   s.mm10_iters, s.mm10_order, s.mm10_ident, s.mm10_bins,
@@ -175,6 +176,7 @@ int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const 
     const bool split = p == W3G_TANGENT_TF32X3 || p == W3G_TANGENT_BF16X3;
     e = launch_tangent_tcg_hex8(c->m, a, bf16, split, c->s.tc_timeout, st);
     if (e == cudaSuccess) e = launch_tangent_tc_hex8(c->m, a, bf16, split, c->s.tc_timeout, st);
+    if (e == cudaSuccess) e = launch_tangent_tc_hex20(c->m, a, bf16, c->s.tc_timeout, st);
   }
   if (e == cudaSuccess)
     e = launch_tangent(c->m, a, c->precision != W3G_TANGENT_FP64, c->sched, c->s.counters + 1, st, tc);
@@ -535,8 +537,18 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
                                    (d.geonl ? 1 : 0) | (d.mat == W3G_MAT_CRYSTAL ? 2 : 0), d.cep_off, d.gp_off,
                                    d.estiff_off, d.einf_off, d.hist_off, 0});
   }
+  // tensor-core records of 20-node bricks: up to 8 consecutive elements
+  std::vector<TcgTile> tc20tiles;
+  for (int b = 0; b < md->nelblk; ++b) {
+    const BlockDesc& d = B[b];
+    if (d.etype != W3G_ETYPE_Q3DISOP) continue;
+    for (int i0 = 0; i0 < d.span; i0 += 8)
+      tc20tiles.push_back(TcgTile{i0, std::min(8, d.span - i0), d.span, d.geonl ? 1 : 0, d.cep_off, d.gp_off,
+                                  d.estiff_off, d.einf_off, d.hist_off, 0});
+  }
   m.ntcchunks = (int)tcchunks.size();
   m.ntcgtiles = (int)tcgtiles.size();
+  m.ntc20tiles = (int)tc20tiles.size();
   m.nrchunks = (int)chunks.size();
   m.mm10_chunk0 = (int)chunks.size();
   m.mm10_chunks = (int)mm10_chunks.size();
@@ -667,6 +679,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   AL(m.tchunks, m.ntchunks);
   AL(m.tcchunks, m.ntcchunks);
   AL(m.tcgtiles, m.ntcgtiles);
+  AL(m.tc20tiles, m.ntc20tiles);
   AL(s.tc_timeout, 1);
   for (int k = 0; k < 2; ++k) {
     AL(m.rorder[k], m.nrchunks);
@@ -736,6 +749,7 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
   UP(m.tchunks, tchunks.data(), m.ntchunks);
   UP(m.tcchunks, tcchunks.data(), m.ntcchunks);
   UP(m.tcgtiles, tcgtiles.data(), m.ntcgtiles);
+  UP(m.tc20tiles, tc20tiles.data(), m.ntc20tiles);
   for (int k = 0; k < 2; ++k) {
     UP(m.rorder[k], rord[k].data(), m.nrchunks);
     UP(m.torder[k], tord[k].data(), m.ntchunks);
@@ -809,6 +823,13 @@ int w3g_set_tangent_precision(w3g_context* c, int precision) {
 int w3g_umat_features(int* info) {
   if (!info) return fail(W3G_EARG, "null argument");
   for (int k = 0; k < 4; ++k) info[k] = kUmatInfo[k];
+  return 0;
+}
+
+int w3g_set_update_mode(w3g_context* c, int mode) {
+  if (!c) return fail(W3G_EARG, "null context");
+  if (mode != W3G_UPDATE_COPY && mode != W3G_UPDATE_SWAP) return fail(W3G_EARG, "unknown update mode");
+  c->update_mode = mode;
   return 0;
 }
 
@@ -931,6 +952,30 @@ int w3g_update(w3g_context* c) {
   CK(cudaSetDevice(c->device));
   const long long gp = c->m.ngp_total;
   cudaStream_t st = c->stream;
+  if (c->update_mode == W3G_UPDATE_SWAP) {
+    CK(cudaStreamSynchronize(st));   // no kernel of this context may still use the arrays
+    std::swap(c->s.hist, c->s.hist1);
+    std::swap(c->s.eps_n, c->s.eps_n1);
+    std::swap(c->s.urcs_n, c->s.urcs_n1);
+    // the mm10 local solve starts from history1: its blocks keep n+1 = n
+    // (runs of consecutive mm10 blocks copied together)
+    const auto& B = c->blocks;
+    for (size_t b = 0; b < B.size();) {
+      if (B[b].mat != W3G_MAT_CRYSTAL) { ++b; continue; }
+      const long long off = B[b].hist_off;
+      long long n = 0;
+      for (; b < B.size() && B[b].mat == W3G_MAT_CRYSTAL; ++b) n += (long long)B[b].hist * B[b].span * B[b].ngp;
+      CK(cudaMemcpyAsync(c->s.hist1 + off, c->s.hist + off, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice,
+                         st));
+    }
+    // the cached iteration graph holds the exchanged pointers
+    if (c->graph.exec) {
+      CK(cudaGraphExecDestroy(c->graph.exec));
+      c->graph.exec = nullptr;
+    }
+    CK(cudaStreamSynchronize(st));
+    return 0;
+  }
   CK(cudaMemcpyAsync(c->s.hist, c->s.hist1, (size_t)c->m.hist_total * sizeof(double), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(c->s.eps_n, c->s.eps_n1, (size_t)6 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(c->s.urcs_n, c->s.urcs_n1, (size_t)9 * gp * sizeof(double), cudaMemcpyDeviceToDevice, st));

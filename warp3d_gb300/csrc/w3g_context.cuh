@@ -25,6 +25,7 @@ struct w3g_context {
   w3g::DeviceState s;
   int precision = W3G_TANGENT_FP64;
   long long wait_limit = W3G_WAIT_LIMIT_DEFAULT;   // bounded waits of the tensor-core kernels
+  int update_mode = W3G_UPDATE_COPY;
   w3g::Schedule sched{W3G_SCHED_PER_TYPE, 0, 0, 1, 1, W3G_ORDER_HEAVY_FIRST};
   IterationGraph graph;
   int ifv_parts = 0;

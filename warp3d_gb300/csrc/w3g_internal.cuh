@@ -193,6 +193,8 @@ struct DeviceModel {
   int ntcchunks = 0;
   TcgTile* tcgtiles = nullptr;     // device, gradient-pair tensor-core tiles of the other 8-node bricks (<= 16)
   int ntcgtiles = 0;
+  TcgTile* tc20tiles = nullptr;    // device, tensor-core records of 20-node bricks (<= 8 elements)
+  int ntc20tiles = 0;
   // schedule orders of the work items (W3G_ORDER_BLOCKS, _HEAVY_FIRST)
   int* rorder[2] = {nullptr, nullptr};
   int* torder[2] = {nullptr, nullptr};
@@ -318,8 +320,10 @@ struct RecoverArgs {
 // ---- kernel launchers (defined in the .cu files) -----------------------
 // element kernels of one call: per-type launches or one persistent launch
 // (queue counters are reset inside)
+// (tc: the tensor-core kernels take the 8- and 20-node bricks, per-type
+// launches of the tetrahedra only)
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc,
-                           int* counter, cudaStream_t s, bool skip_hex8 = false);
+                           int* counter, cudaStream_t s, bool tc = false);
 // 8-node brick tangents as full matrices (asymmetric assembly), per-type
 // work items of type slot 0
 cudaError_t launch_tangent_full(const DeviceModel& m, const TangentArgs& a, bool fp32, cudaStream_t s);
@@ -341,10 +345,15 @@ cudaError_t init_tangent_tc_kernels();
 cudaError_t launch_tangent_tcg_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
                                     int* tc_timeout, cudaStream_t s);
 cudaError_t init_tangent_tcg_kernels();
+// the 20-node bricks on the tensor cores (w3g_tangent_tc20.cu), split
+// operands always
+cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
+                                    cudaStream_t s);
+cudaError_t init_tangent_tc20_kernels();
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, const Schedule& sc,
                            int* counter, cudaStream_t s);
 // launches of the element kernels under a schedule
-int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8 = false);
+int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool tc = false);
 int recover_kernel_launches(const DeviceModel& m, const Schedule& sc);
 // mm10 recovery of the crystal-plasticity items (kinematics, local
 // solves from a work queue sorted by the last iteration counts, forces)
@@ -359,6 +368,7 @@ inline cudaError_t init_kernels() {
   cudaError_t e = init_tangent_kernels();
   if (e == cudaSuccess) e = init_tangent_tc_kernels();
   if (e == cudaSuccess) e = init_tangent_tcg_kernels();
+  if (e == cudaSuccess) e = init_tangent_tc20_kernels();
   if (e == cudaSuccess) e = init_recover_kernels();
   return e == cudaSuccess ? init_mm10_kernels() : e;
 }

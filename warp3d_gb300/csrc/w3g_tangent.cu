@@ -119,10 +119,10 @@ int occupancy(bool bbar) { return std::max(1, g_occ[sizeof(T) == 4][bbar ? 1 : 0
 
 template <class T>
 cudaError_t launch(const DeviceModel& m, const TangentArgs& a, const Schedule& sc, int* counter, cudaStream_t s,
-                   bool skip_hex8) {
+                   bool tc) {
   cudaError_t e = cudaSuccess;
   const bool bb = m.has_bbar != 0;
-  if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) {
+  if (sc.mode == W3G_SCHED_PERSISTENT && !tc) {
     const int occ = occupancy<T>(bb);
     const int per_sm = sc.tangent_ctas_per_sm > 0 ? std::min(sc.tangent_ctas_per_sm, occ) : occ;
     const int grain = std::max(1, sc.tangent_grain);
@@ -133,12 +133,12 @@ cudaError_t launch(const DeviceModel& m, const TangentArgs& a, const Schedule& s
     k_tangent_persistent<T><<<grid, kTangentThreads, tangent_smem<T>(bb), s>>>(a, q);
     return cudaGetLastError();
   }
-  if (m.ttype_chunks[0] > 0 && !skip_hex8) {
+  if (m.ttype_chunks[0] > 0 && !tc) {
     TangentArgs h = a;
     h.chunk0 = m.ttype_chunk0[0];
     k_tangent_hex8<T><<<m.ttype_chunks[0], kTangentThreads, hex8_smem<T>(bb), s>>>(h);
   }
-  if (m.ttype_chunks[1] > 0) {
+  if (m.ttype_chunks[1] > 0 && !tc) {   // with the tensor-core forms, 20-node bricks have their kernel
     TangentArgs h = a;
     h.chunk0 = m.ttype_chunk0[1];
     k_tangent_type<Hex20, 32, 1, T><<<m.ttype_chunks[1], kTangentThreads, sizeof(TangentSmemGen<Hex20, 1, T>), s>>>(h);
@@ -198,17 +198,20 @@ cudaError_t launch_tangent_ranges(const DeviceModel& m, const TangentArgs& a, bo
               : launch_ranges<double>(m, a, first, count, s, launches);
 }
 
-int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool skip_hex8) {
-  if (sc.mode == W3G_SCHED_PERSISTENT && !skip_hex8) return m.ntchunks > 0 ? 1 : 0;
-  int n = skip_hex8 ? (m.ntcchunks > 0 ? 1 : 0) + (m.ntcgtiles > 0 ? 1 : 0) : 0;
-  for (int t = skip_hex8 ? 1 : 0; t < kNumTypes; ++t) n += m.ttype_chunks[t] > 0 ? 1 : 0;
+int tangent_kernel_launches(const DeviceModel& m, const Schedule& sc, bool tc) {
+  if (sc.mode == W3G_SCHED_PERSISTENT && !tc) return m.ntchunks > 0 ? 1 : 0;
+  if (tc)
+    return (m.ntcchunks > 0 ? 1 : 0) + (m.ntcgtiles > 0 ? 1 : 0) + (m.ntc20tiles > 0 ? 1 : 0) +
+           (m.ttype_chunks[2] > 0 ? 1 : 0);
+  int n = 0;
+  for (int t = 0; t < kNumTypes; ++t) n += m.ttype_chunks[t] > 0 ? 1 : 0;
   return n;
 }
 
 cudaError_t launch_tangent(const DeviceModel& m, const TangentArgs& a, bool fp32, const Schedule& sc, int* counter,
-                           cudaStream_t s, bool skip_hex8) {
+                           cudaStream_t s, bool tc) {
   if (m.ntchunks == 0) return cudaSuccess;
-  return fp32 ? launch<float>(m, a, sc, counter, s, skip_hex8) : launch<double>(m, a, sc, counter, s, skip_hex8);
+  return fp32 ? launch<float>(m, a, sc, counter, s, tc) : launch<double>(m, a, sc, counter, s, tc);
 }
 
 }  // namespace w3g

@@ -1,0 +1,442 @@
+// w3g_tangent_tc20.cu -- precision forms of the 20-node brick tangent on the
+// fifth-generation tensor cores.
+//
+// WARP3D's material and geometric stiffness of a q3disop element (gptns1.f
+// bdbtgen :1628, kg1.f :16) is, per pair of displacement components
+// i <= j and nodes a, b,
+//   Ke_ij[a][b] = sum_gp n_a^T H^ij_gp n_b,   H^ij = Gamma^T X^ij Gamma,
+// with n_a = dN_a/dxi at the Gauss point, Gamma = J^-1 and X^ij[p][q] =
+// [D*](v(i,p), v(j,q)) + delta_ij {T}[p][q] (the same point quantities as
+// the 8-node brick's gradient-pair kernel). Splitting the node sums,
+//   Ke_ij[a][b] = sum_{gp,r} n_a[r](gp) Y[(ij,b), (gp,r)],
+//   Y[(ij,b), (gp,r)] = sum_s H^ij_gp[r][s] n_b[s](gp),
+// every element's tangent is ONE product of its Y (120 rows (pair, node b)
+// x K = 81 (Gauss point, r)) with the CONSTANT operator N_A[a, (gp, r)] =
+// n_a[r](gp) of the element type: an MMA of M = 128 (120 used), N = 32 (20
+// used), K = 81 (padded to 88 for TF32, 96 for BF16), FP32 accumulation in
+// 32 TMEM columns. The CUDA cores form the Gauss-point quantities and Y
+// (~1,900 multiply-adds per point, against ~8,000 for B^T D* B + G^T T G).
+//
+// Operand precision: rounding N_A to TF32 or BF16 does NOT keep the exact
+// rigid-translation null space here (the 27-point rule has no mirror
+// symmetry of dN/dxi between nodes), and a rounded Y breaks the node sums
+// of the columns. So both operands are always split, x = hi + lo in the
+// input format, and the product is hi*hi + hi*lo + lo*hi (three MMAs): the
+// TF32 and TF32x3 requests both give TF32x3 accuracy on these elements,
+// BF16 and BF16x3 BF16x3 accuracy, with the translation null space kept to
+// the FP32 accumulation level.
+//
+// One CTA of 6 warps per record of up to 8 elements of a block, elements in
+// turn, two (BF16) or one (TF32) CTAs per SM:
+//   (0) the element's coordinates at n+1 relative to its node 1 (cdest /
+//       edest gathers);
+//   (1)-(3) warp k = thread k of every Gauss point (lane = point):
+//       [J] rows and the float conversion of cep, R, urcs_n1 (each value
+//       once); Gamma, w det J, {T}; row k of w det J [D*]; H of pair k
+//       (exactly symmetric for i = j) into shared memory;
+//   (4) threads 0-119, one per row (pair, node b): the 81 values of Y,
+//       split and written into the A operand (K-major, no swizzle);
+//   (5) thread 0 issues the 3 x K/k-step MMAs and commits to an mbarrier;
+//   (6) warps 0-3 read the accumulator (tcgen05.ld, each warp its lane
+//       quadrant), scale by beta_fact and scatter each element's packed
+//       upper triangle (utsz = 1830, setup.f:265-275) into shared memory,
+//       stored coalesced as FP32.
+// The one wait (for the MMAs) is bounded by TangentArgs::wait_limit; a wait
+// that gives up drains the MMAs (bounded), fills NaN Ke for every element of
+// the CTA not finished and sets the timeout flag (W3G_EFATAL). A limit of 0
+// gives up before the first MMA is issued.
+#include <cstdint>
+#include "w3g_internal.cuh"
+#include "w3g_elem.cuh"
+#include "w3g_math.cuh"
+#include "w3g_tc_common.cuh"
+
+namespace w3g {
+
+namespace {
+
+using namespace tc;
+
+constexpr int NN = Hex20::NN, NG = Hex20::NG, TOT = Hex20::TOTDOF, UT = Hex20::UTSZ;
+constexpr int kPts = 32;                 // point slots per quantity (27 used)
+constexpr int kThreads = 6 * 32;         // warp k = thread k of every Gauss point
+constexpr int kM = 128;                  // MMA rows: (pair, node b), 120 used
+constexpr int kCols = 32;                // MMA columns: node a, 20 used
+constexpr int kKLive = 3 * NG;           // 81: (Gauss point, r)
+constexpr int kRowsLive = 6 * NN;        // 120
+constexpr int kTmemCols = 32;
+constexpr long long kDrainLimit = 1ll << 26;
+
+template <bool kBF16>
+struct Op {
+  static constexpr int kBytes = kBF16 ? 2 : 4;
+  static constexpr int kPerCore = 16 / kBytes;              // K values per core-matrix row
+  static constexpr int kKStep = kBF16 ? 16 : 8;
+  static constexpr int kK = (kKLive + kKStep - 1) / kKStep * kKStep;   // 96 / 88
+  static constexpr int kSteps = kK / kKStep;
+  static constexpr int kSBO = (kK / kPerCore) * 128;       // next 8-row group
+  static constexpr int kOpA = kM * kK * kBytes;             // hi part; the lo part follows
+  static constexpr int kOpB = kCols * kK * kBytes;
+  static constexpr int kOffB = 0;
+  static constexpr int kOffA = kOffB + 2 * kOpB;
+  static constexpr int kSmem = kOffA + 2 * kOpA;
+  // byte offset of (row, k) in a K-major no-swizzle operand
+  __device__ static __forceinline__ int off(int row, int k) {
+    return (row >> 3) * kSBO + (k / kPerCore) * 128 + (row & 7) * 16 + (k % kPerCore) * kBytes;
+  }
+};
+
+struct Tc20Static {
+  float dn[NG * 3 * NN + NG];          // dN/dxi per Gauss point (float) + weights
+  float x[TOT];                        // x(n+1) relative to node 1
+  float pt[kPtN * kPts];               // per-point intermediates
+  float H[NG][6][9];                   // H^ij per point and pair
+  float ke[UT];                        // the element's packed Ke
+  unsigned long long mma;
+  uint32_t tmem_base;
+  int abort;                           // a wait gave up (written before a barrier)
+  int fail_t, fail_e;                  // record and element it gave up at
+};
+
+// instruction descriptor: FP32 accumulator, A/B K-major, M = 128, N = 32
+template <bool kBF16>
+__host__ __device__ constexpr uint32_t idesc20() {
+  return (1u << 4) | ((kBF16 ? 1u : 2u) << 7) | ((kBF16 ? 1u : 2u) << 10) | ((uint32_t)(kCols >> 3) << 17) |
+         ((uint32_t)(kM >> 4) << 24);
+}
+
+template <bool kBF16>
+__device__ __forceinline__ void mma20(uint32_t tmem, uint64_t da, uint64_t db, bool acc) {
+  const uint32_t id = idesc20<kBF16>(), a = acc ? 1u : 0u;
+  if (kBF16)
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                 ::"r"(tmem), "l"(da), "l"(db), "r"(id), "r"(a));
+  else
+    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}"
+                 ::"r"(tmem), "l"(da), "l"(db), "r"(id), "r"(a));
+}
+
+__device__ __forceinline__ float& pv20(float* pt, int q, int g) { return pv<kPts>(pt, q, g); }
+
+// Phase 1, thread k of Gauss point g of element i: k < 3 forms row k of
+// [J] (into the [D*] slots); every k converts its share of the point's
+// double inputs to float: cep entries 4k .. 4k+3 and, with finite strain,
+// R entries k and k + 6 and urcs_n1 entry k.
+template <int k>
+__device__ __forceinline__ void tc20_phase1(const TangentArgs& a, const TcgTile& tl, int i, Tc20Static& T, int g) {
+  float* pt = T.pt;
+  if constexpr (k < 3) {
+    const float* dn = T.dn + (g * 3 + k) * NN;
+    float j0 = 0.f, j1 = 0.f, j2 = 0.f;
+#pragma unroll
+    for (int n = 0; n < NN; ++n) {
+      const float w = dn[n];
+      j0 += w * T.x[n];
+      j1 += w * T.x[NN + n];
+      j2 += w * T.x[2 * NN + n];
+    }
+    pv20(pt, kPtD + 3 * k, g) = j0;
+    pv20(pt, kPtD + 3 * k + 1, g) = j1;
+    pv20(pt, kPtD + 3 * k + 2, g) = j2;
+  }
+  constexpr int q0 = 4 * k, q1 = q0 + 4 < 21 ? q0 + 4 : 21;
+  const double* cp = a.cep + tl.cep_off + ((long long)g * tl.span + i) * 21;
+#pragma unroll
+  for (int q = q0; q < q1; ++q) pv20(pt, kPtC + q, g) = d2f_rn(cp[q]);
+  if (tl.flags & 1) {
+    const long long gpi = tl.gp_off + (long long)i * NG + g;
+    const double* rp = a.rot_n1 + gpi * 9;
+    pv20(pt, kPtR + k, g) = d2f_rn(rp[k]);
+    if constexpr (k + 6 < 9) pv20(pt, kPtR + k + 6, g) = d2f_rn(rp[k + 6]);
+    pv20(pt, kPtU + k, g) = d2f_rn(a.urcs_n1[gpi * 9 + k]);
+  }
+}
+
+// Phase 3, thread `slot` of point g: H^ij = Gamma^T X^ij Gamma for pair
+// slot (00 01 02 11 12 22); for i = j only r <= s is formed and mirrored,
+// so that H^ii is exactly symmetric.
+__device__ __forceinline__ void tc20_phase3(Tc20Static& T, int g, int slot) {
+  float* pt = T.pt;
+  const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+  const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+  const bool diag = ii == jj;
+  float gam[9], X[9];
+#pragma unroll
+  for (int m = 0; m < 9; ++m) gam[m] = pv20(pt, kPtGam + m, g);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      float v = pv20(pt, kPtD + lw(voigt(ii, r), voigt(jj, q)), g);
+      if (diag) v += pv20(pt, kPtTw + voigt(r, q), g);
+      X[3 * r + q] = v;
+    }
+  float* h = T.H[g][slot];
+#pragma unroll
+  for (int s2 = 0; s2 < 3; ++s2) {
+    float y[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      y[r] = X[3 * r] * gam[3 * s2] + X[3 * r + 1] * gam[3 * s2 + 1] + X[3 * r + 2] * gam[3 * s2 + 2];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      if (diag && r > s2) continue;
+      const float v = gam[3 * r] * y[0] + gam[3 * r + 1] * y[1] + gam[3 * r + 2] * y[2];
+      h[3 * r + s2] = v;
+      if (diag && r < s2) h[3 * s2 + r] = v;
+    }
+  }
+}
+
+// the split parts of v in the input format: hi = round(v), lo = round(v - hi)
+template <bool kBF16>
+__device__ __forceinline__ void put_hilo(unsigned char* op, int op_bytes, int o, float v) {
+  const float hi = round_in<kBF16>(v);
+  put<kBF16>(op, o, hi);
+  put<kBF16>(op + op_bytes, o, v - hi);
+}
+
+template <bool kBF16>
+__global__ void __launch_bounds__(kThreads) k_tangent_tc_hex20(TangentArgs a, const TcgTile* tiles, int ntiles,
+                                                                int* tc_timeout) {
+  using O = Op<kBF16>;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* opB = smem + O::kOffB;
+  unsigned char* opA = smem + O::kOffA;
+  __shared__ Tc20Static T;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long limit = a.wait_limit;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&T.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&T.mma)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    T.abort = 0;
+    T.fail_t = -1;
+    T.fail_e = 0;
+  }
+  const double* dnd = a.dn[Hex20::SLOT];
+  for (int k = tid; k < NG * 3 * NN + NG; k += kThreads) T.dn[k] = (float)dnd[k];
+  // the constant operator N_A (B operand): row a, k = gp*3 + r, hi and lo
+  // parts of the double value; rows a >= 20 and k >= 81 zero
+  for (int idx = tid; idx < kCols * O::kK; idx += kThreads) {
+    const int row = idx / O::kK, k = idx % O::kK;
+    double v = 0.0;
+    if (row < NN && k < kKLive) v = dnd[k * NN + row];   // k = gp*3 + r
+    const float hi = round_in<kBF16>((float)v);
+    put<kBF16>(opB, O::off(row, k), hi);
+    put<kBF16>(opB + O::kOpB, O::off(row, k), (float)(v - (double)hi));
+  }
+  // A rows 120..127 and the K padding stay zero (finite) for every element
+  for (int idx = tid; idx < kM * O::kK; idx += kThreads) {
+    const int row = idx / O::kK, k = idx % O::kK;
+    if (row >= kRowsLive || k >= kKLive) {
+      put<kBF16>(opA, O::off(row, k), 0.f);
+      put<kBF16>(opA + O::kOpA, O::off(row, k), 0.f);
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = T.tmem_base;
+  const float bf = (float)a.beta_fact;
+  const int g = lane, kr = warp;   // phases 1-3: Gauss point, thread of the point
+  unsigned q = 0;                  // MMA chains issued (mbarrier phase)
+
+  for (int t = blockIdx.x; t < ntiles && !T.abort; t += gridDim.x) {
+    const TcgTile tl = tiles[t];
+    for (int e = 0; e < tl.n; ++e) {
+      const int i = tl.i0 + e;
+      // (0) coordinates at n+1 relative to node 1
+      if (tid < TOT) {
+        const long long dbase = tl.einf_off + (long long)i * TOT;
+        const int d0 = (tid / NN) * NN;
+        double v = a.c[a.cdest[dbase + tid] - 1], ref = a.c[a.cdest[dbase + d0] - 1];
+        if (tl.flags & 1) {
+          const int e1 = a.edest[dbase + tid] - 1, e0 = a.edest[dbase + d0] - 1;
+          v = v + a.u[e1] + a.du[e1];
+          ref = ref + a.u[e0] + a.du[e0];
+        }
+        T.x[tid] = d2f_rn(v - ref);
+      }
+      __syncthreads();
+      // (1) [J] rows, conversions
+      if (g < NG) {
+        switch (kr) {
+          case 0: tc20_phase1<0>(a, tl, i, T, g); break;
+          case 1: tc20_phase1<1>(a, tl, i, T, g); break;
+          case 2: tc20_phase1<2>(a, tl, i, T, g); break;
+          case 3: tc20_phase1<3>(a, tl, i, T, g); break;
+          case 4: tc20_phase1<4>(a, tl, i, T, g); break;
+          default: tc20_phase1<5>(a, tl, i, T, g); break;
+        }
+      }
+      __syncthreads();
+      // (2a) Gamma, w det J, {T}
+      if (g < NG) {
+        const float w = T.dn[NG * 3 * NN + g];
+        const bool geonl = tl.flags & 1;
+        switch (kr) {
+          case 0: pt_phase2a<0, kPts>(T.pt, g, w, geonl); break;
+          case 1: pt_phase2a<1, kPts>(T.pt, g, w, geonl); break;
+          case 2: pt_phase2a<2, kPts>(T.pt, g, w, geonl); break;
+          case 3: pt_phase2a<3, kPts>(T.pt, g, w, geonl); break;
+          case 4: pt_phase2a<4, kPts>(T.pt, g, w, geonl); break;
+          default: pt_phase2a<5, kPts>(T.pt, g, w, geonl); break;
+        }
+      }
+      __syncthreads();
+      // (2) rows of w det J [D*]
+      if (g < NG) {
+        const bool qb = a.qbar != 0;
+        switch (kr) {
+          case 0: pt_phase2<0, kPts>(qb, tl.flags, T.pt, g); break;
+          case 1: pt_phase2<1, kPts>(qb, tl.flags, T.pt, g); break;
+          case 2: pt_phase2<2, kPts>(qb, tl.flags, T.pt, g); break;
+          case 3: pt_phase2<3, kPts>(qb, tl.flags, T.pt, g); break;
+          case 4: pt_phase2<4, kPts>(qb, tl.flags, T.pt, g); break;
+          default: pt_phase2<5, kPts>(qb, tl.flags, T.pt, g); break;
+        }
+      }
+      __syncthreads();
+      // (3) H per point and pair
+      if (g < NG) tc20_phase3(T, g, kr);
+      __syncthreads();
+      // (4) Y into the A operand: thread = row (pair, node b); the previous
+      // element's MMAs are complete (waited for below)
+      if (tid < kRowsLive) {
+        const int slot = tid / NN, b = tid % NN;
+        for (int gp = 0; gp < NG; ++gp) {
+          const float* h = T.H[gp][slot];
+          const float n0 = T.dn[(gp * 3 + 0) * NN + b], n1 = T.dn[(gp * 3 + 1) * NN + b],
+                      n2 = T.dn[(gp * 3 + 2) * NN + b];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            put_hilo<kBF16>(opA, O::kOpA, O::off(tid, gp * 3 + r), h[3 * r] * n0 + h[3 * r + 1] * n1 + h[3 * r + 2] * n2);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (limit == 0) {   // give up before any MMA (the status path without a fault)
+        if (tid == 0) { T.abort = 1; T.fail_t = t; T.fail_e = e; }
+        __syncthreads();
+        break;
+      }
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint64_t da = sdesc(su32(opA), O::kSBO), db = sdesc(su32(opB), O::kSBO);
+        const uint64_t dal = da + (O::kOpA >> 4), dbl = db + (O::kOpB >> 4);
+#pragma unroll 1
+        for (int ks = 0; ks < O::kSteps; ++ks) {
+          const uint64_t o = (uint64_t)ks * (256 >> 4);   // one k-step = two core matrices along K
+          mma20<kBF16>(tmem, da + o, db + o, ks > 0);
+          mma20<kBF16>(tmem, da + o, dbl + o, true);
+          mma20<kBF16>(tmem, dal + o, db + o, true);
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            su32(&T.mma)) : "memory");
+      }
+      if (!wait_phase(&T.mma, q & 1, limit, nullptr)) {
+        // the MMAs may still be running: wait them out before tensor memory
+        // is read or freed
+        T.abort = 1;
+        wait_phase(&T.mma, q & 1, kDrainLimit, nullptr);
+      }
+      ++q;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      __syncthreads();
+      if (T.abort) {
+        if (tid == 0) { T.fail_t = t; T.fail_e = e; }
+        __syncthreads();
+        break;
+      }
+      // (6) accumulator -> packed Ke: warp w < 4 reads lane quadrant w
+      if (warp < 4) {
+        const int row = 32 * warp + lane;
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+            "tcgen05.wait::ld.sync.aligned;"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr), "r"(taddr + 16)
+            : "memory");
+        if (row < kRowsLive) {
+          const int slot = row / NN, b = row % NN;
+          const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+          const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+          const int d2 = jj * NN + b;
+#pragma unroll
+          for (int an = 0; an < NN; ++an) {
+            if (ii == jj && an > b) continue;
+            const int d1 = ii * NN + an;
+            T.ke[d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[an]) * bf;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      float* out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)i * UT;
+      for (int z = tid; z < UT; z += kThreads) out[z] = T.ke[z];
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  if (T.abort) {
+    // NaN for every element of this CTA's records from the one it gave up at
+    if (tid == 0) atomicExch(tc_timeout, 1);
+    for (int t = T.fail_t; t >= 0 && t < ntiles; t += gridDim.x) {
+      const TcgTile tl = tiles[t];
+      const int e0 = t == T.fail_t ? T.fail_e : 0;
+      float* out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)(tl.i0 + e0) * UT;
+      for (long long z = tid; z < (long long)(tl.n - e0) * UT; z += kThreads) out[z] = __int_as_float(0x7fc00000);
+    }
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+template <bool kBF16>
+cudaError_t set_attr20() {
+  return cudaFuncSetAttribute(k_tangent_tc_hex20<kBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Op<kBF16>::kSmem);
+}
+
+static_assert(Op<false>::kSmem + sizeof(Tc20Static) <= 227 * 1024, "TF32 form exceeds shared memory");
+static_assert(Op<true>::kSmem + sizeof(Tc20Static) <= 227 * 1024, "BF16 form exceeds shared memory");
+static_assert(Op<false>::kOffA % 16 == 0 && Op<true>::kOffA % 16 == 0, "operands must be 16-byte aligned");
+static_assert(UT * 4 <= 8 * 1024, "Ke staging");
+
+}  // namespace
+
+cudaError_t init_tangent_tc20_kernels() {
+  cudaError_t e = set_attr20<false>();
+  return e == cudaSuccess ? set_attr20<true>() : e;
+}
+
+cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
+                                    cudaStream_t s) {
+  if (m.ntc20tiles == 0) return cudaSuccess;
+  // as many CTAs as fit (1-2 per SM by shared memory), records taken in turn
+  const int per_sm = bf16 ? 2 : 1;
+  const int grid = m.ntc20tiles < m.nsm * per_sm ? m.ntc20tiles : m.nsm * per_sm;
+  if (bf16)
+    k_tangent_tc_hex20<true><<<grid, kThreads, Op<true>::kSmem, s>>>(a, m.tc20tiles, m.ntc20tiles, tc_timeout);
+  else
+    k_tangent_tc_hex20<false><<<grid, kThreads, Op<false>::kSmem, s>>>(a, m.tc20tiles, m.ntc20tiles, tc_timeout);
+  return cudaGetLastError();
+}
+
+}  // namespace w3g

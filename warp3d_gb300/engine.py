@@ -72,6 +72,12 @@ class Engine:
         before any MMA: w3g_tanstf then reports W3G_EFATAL with NaN Ke."""
         abi.check(self.lib, self.lib.w3g_set_wait_limit(self.ctx, polls))
 
+    def set_update_mode(self, mode: int):
+        """abi.UPDATE_COPY (WARP3D's copies n+1 -> n) or abi.UPDATE_SWAP
+        (the n and n+1 arrays exchanged; mm10 history copied back), see
+        w3g_set_update_mode."""
+        abi.check(self.lib, self.lib.w3g_set_update_mode(self.ctx, mode))
+
     def set_precision(self, precision: int):
         abi.check(self.lib, self.lib.w3g_set_tangent_precision(self.ctx, precision))
         self.precision = precision

@@ -92,16 +92,18 @@ class DeviceCsr:
 EW_ETA_MAX, EW_GAMMA = 0.1, 0.9
 
 
-def ew_forcing(eta_prev: float, rn: float, rn_prev: float, target: float) -> float:
+def ew_forcing(eta_prev: float, rn: float, rn_prev: float, target: float, eta_max: float = EW_ETA_MAX) -> float:
     """Next relative tolerance of the linear solve: gamma (rn / rn_prev)^2,
     not below gamma eta_prev^2 when that is still large (safeguard against
-    a sudden drop), at most EW_ETA_MAX, and no tighter than what reaching
-    the Newton target `target` from rn needs."""
+    a sudden drop), at most eta_max, and no tighter than what reaching the
+    Newton target `target` from rn needs. Problems whose Newton iterations
+    converge only linearly (an inexact tangent) need a small eta_max: with
+    0.1 the 100k-element mixed bars diverge in their first step."""
     eta = EW_GAMMA * (rn / rn_prev) ** 2
     sg = EW_GAMMA * eta_prev ** 2
     if sg > 0.1:
         eta = max(eta, sg)
-    eta = min(eta, EW_ETA_MAX)
+    eta = min(eta, eta_max)
     return max(eta, 0.5 * target / rn)
 
 
@@ -157,7 +159,8 @@ class DeviceNewtonDriver:
     def __init__(self, model, engine, fixed, tol: float = 1e-8, maxit: int = 25, extrapolate: bool = False,
                  lin_rtol: float = 1e-10, lin_maxit: int = 50000, device: int = 0, csr: DeviceCsr | None = None,
                  adaptive: bool = False, adaptive_step1: bool = False, adapt_divisions: int = 4,
-                 adapt_min_fact: float = 1.0 / 16.0, line_search: bool = False, forcing: str = "fixed"):
+                 adapt_min_fact: float = 1.0 / 16.0, line_search: bool = False, forcing: str = "fixed",
+                 eta_max: float = EW_ETA_MAX):
         import torch
         self.torch = torch
         self.model = model
@@ -166,7 +169,7 @@ class DeviceNewtonDriver:
         self.lin_rtol, self.lin_maxit = lin_rtol, lin_maxit
         if forcing not in ("fixed", "ew"):
             raise ValueError("forcing must be 'fixed' or 'ew'")
-        self.forcing = forcing
+        self.forcing, self.eta_max = forcing, eta_max
         self.adaptive, self.adaptive_step1 = adaptive, adaptive_step1
         self.adapt_divisions, self.adapt_min_fact = adapt_divisions, adapt_min_fact
         dev = torch.device("cuda", device)
@@ -225,7 +228,7 @@ class DeviceNewtonDriver:
         if self._recover(step, 0, extrap) != 0:
             raise IncrementFailed(f"step {step}: recovery requested a step cut at iteration 0")
         self._tangent(step, 0)
-        eta, rn_prev = EW_ETA_MAX, None
+        eta, rn_prev = self.eta_max, None
         for it in range(1, self.maxit + 1):
             rtol = self.lin_rtol if self.forcing == "fixed" else max(self.lin_rtol, eta)
             st, nits, rel = self.csr.pcg(self.mask.data_ptr(), self.ifv.data_ptr(), -1.0, self.d.data_ptr(),
@@ -244,7 +247,7 @@ class DeviceNewtonDriver:
             if rn <= self.tol * scale:
                 return res_hist, lin
             if self.forcing == "ew" and rn_prev is not None:
-                eta = ew_forcing(eta, rn, rn_prev, self.tol * scale)
+                eta = ew_forcing(eta, rn, rn_prev, self.tol * scale, self.eta_max)
             rn_prev = rn
             self._tangent(step, it)
         raise IncrementFailed(f"step {step}: no convergence in {self.maxit} iterations: {res_hist}")
