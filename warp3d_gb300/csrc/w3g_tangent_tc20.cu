@@ -59,13 +59,22 @@ using namespace tc;
 
 constexpr int NN = Hex20::NN, NG = Hex20::NG, TOT = Hex20::TOTDOF, UT = Hex20::UTSZ;
 constexpr int kPts = 32;                 // point slots per quantity (27 used)
-constexpr int kThreads = 6 * 32;         // warp k = thread k of every Gauss point
+constexpr int kThreads = 8 * 32;         // warps 0-5: thread k of every Gauss point; 6-7: prefetch
 constexpr int kM = 128;                  // MMA rows: (pair, node b), 120 used
 constexpr int kCols = 32;                // MMA columns: node a, 20 used
 constexpr int kKLive = 3 * NG;           // 81: (Gauss point, r)
 constexpr int kRowsLive = 6 * NN;        // 120
 constexpr int kTmemCols = 32;
 constexpr long long kDrainLimit = 1ll << 26;
+
+// an element's inputs, prefetched by warps 6-7 while the element before is
+// processed (8-byte cp.async: gathered nodal values, the 27 cep rows, the
+// element's contiguous R and stress slabs)
+struct Tc20Inputs {
+  double c[TOT], u[TOT], du[TOT];
+  double cep[NG * 21];
+  double rot[NG * 9], urcs[NG * 9];
+};
 
 template <bool kBF16>
 struct Op {
@@ -74,16 +83,25 @@ struct Op {
   static constexpr int kKStep = kBF16 ? 16 : 8;
   static constexpr int kK = (kKLive + kKStep - 1) / kKStep * kKStep;   // 96 / 88
   static constexpr int kSteps = kK / kKStep;
-  static constexpr int kSBO = (kK / kPerCore) * 128;       // next 8-row group
-  static constexpr int kOpA = kM * kK * kBytes;             // hi part; the lo part follows
-  static constexpr int kOpB = kCols * kK * kBytes;
+  // next 8-row group: 16 bytes more than the group's K extent, so that the
+  // stores of 32 consecutive rows fall into distinct banks
+  static constexpr int kSBO = (kK / kPerCore) * 128 + 16;
+  static constexpr int kOpA = (kM / 8) * kSBO;              // hi part; the lo part follows
+  static constexpr int kOpB = (kCols / 8) * kSBO;
   static constexpr int kOffB = 0;
   static constexpr int kOffA = kOffB + 2 * kOpB;
-  static constexpr int kSmem = kOffA + 2 * kOpA;
+  static constexpr int kOffIn = kOffA + 2 * kOpA;           // two Tc20Inputs: this and the next element
+  static constexpr int kSmem = kOffIn + 2 * (int)sizeof(Tc20Inputs);
   // byte offset of (row, k) in a K-major no-swizzle operand
   __device__ static __forceinline__ int off(int row, int k) {
     return (row >> 3) * kSBO + (k / kPerCore) * 128 + (row & 7) * 16 + (k % kPerCore) * kBytes;
   }
+};
+
+// where an element of the CTA's sequence lives
+struct Tc20Elem {
+  long long cep_off, gp_off, estiff_off, einf_off;
+  int i, span, flags, pad;
 };
 
 struct Tc20Static {
@@ -91,11 +109,11 @@ struct Tc20Static {
   float x[TOT];                        // x(n+1) relative to node 1
   float pt[kPtN * kPts];               // per-point intermediates
   float H[NG][6][9];                   // H^ij per point and pair
-  float ke[UT];                        // the element's packed Ke
+  float ke[UT];                        // packed Ke of the element in the epilogue
   unsigned long long mma;
   uint32_t tmem_base;
   int abort;                           // a wait gave up (written before a barrier)
-  int fail_t, fail_e;                  // record and element it gave up at
+  int fail_n;                          // sequence index of the first element not stored
 };
 
 // instruction descriptor: FP32 accumulator, A/B K-major, M = 128, N = 32
@@ -118,12 +136,12 @@ __device__ __forceinline__ void mma20(uint32_t tmem, uint64_t da, uint64_t db, b
 
 __device__ __forceinline__ float& pv20(float* pt, int q, int g) { return pv<kPts>(pt, q, g); }
 
-// Phase 1, thread k of Gauss point g of element i: k < 3 forms row k of
-// [J] (into the [D*] slots); every k converts its share of the point's
-// double inputs to float: cep entries 4k .. 4k+3 and, with finite strain,
-// R entries k and k + 6 and urcs_n1 entry k.
+// Phase 1, thread k of Gauss point g: k < 3 forms row k of [J] (into the
+// [D*] slots); every k converts its share of the point's staged double
+// inputs to float: cep entries 4k .. 4k+3 and, with finite strain, R
+// entries k and k + 6 and urcs_n1 entry k.
 template <int k>
-__device__ __forceinline__ void tc20_phase1(const TangentArgs& a, const TcgTile& tl, int i, Tc20Static& T, int g) {
+__device__ __forceinline__ void tc20_phase1(const Tc20Inputs& in, bool geonl, Tc20Static& T, int g) {
   float* pt = T.pt;
   if constexpr (k < 3) {
     const float* dn = T.dn + (g * 3 + k) * NN;
@@ -140,15 +158,12 @@ __device__ __forceinline__ void tc20_phase1(const TangentArgs& a, const TcgTile&
     pv20(pt, kPtD + 3 * k + 2, g) = j2;
   }
   constexpr int q0 = 4 * k, q1 = q0 + 4 < 21 ? q0 + 4 : 21;
-  const double* cp = a.cep + tl.cep_off + ((long long)g * tl.span + i) * 21;
 #pragma unroll
-  for (int q = q0; q < q1; ++q) pv20(pt, kPtC + q, g) = d2f_rn(cp[q]);
-  if (tl.flags & 1) {
-    const long long gpi = tl.gp_off + (long long)i * NG + g;
-    const double* rp = a.rot_n1 + gpi * 9;
-    pv20(pt, kPtR + k, g) = d2f_rn(rp[k]);
-    if constexpr (k + 6 < 9) pv20(pt, kPtR + k + 6, g) = d2f_rn(rp[k + 6]);
-    pv20(pt, kPtU + k, g) = d2f_rn(a.urcs_n1[gpi * 9 + k]);
+  for (int q = q0; q < q1; ++q) pv20(pt, kPtC + q, g) = d2f_rn(in.cep[g * 21 + q]);
+  if (geonl) {
+    pv20(pt, kPtR + k, g) = d2f_rn(in.rot[g * 9 + k]);
+    if constexpr (k + 6 < 9) pv20(pt, kPtR + k + 6, g) = d2f_rn(in.rot[g * 9 + k + 6]);
+    pv20(pt, kPtU + k, g) = d2f_rn(in.urcs[g * 9 + k]);
   }
 }
 
@@ -196,13 +211,62 @@ __device__ __forceinline__ void put_hilo(unsigned char* op, int op_bytes, int o,
   put<kBF16>(op + op_bytes, o, v - hi);
 }
 
+// the CTA's elements in sequence: records blockIdx.x, blockIdx.x + grid, ...
+// and their elements in turn; advances (t, e) and fills the descriptor
+__device__ __forceinline__ bool tc20_next(const TcgTile* tiles, int ntiles, int& t, int& e, Tc20Elem& d) {
+  while (t < ntiles) {
+    const TcgTile r = tiles[t];
+    if (e < r.n) {
+      d.cep_off = r.cep_off; d.gp_off = r.gp_off; d.estiff_off = r.estiff_off; d.einf_off = r.einf_off;
+      d.i = r.i0 + e; d.span = r.span; d.flags = r.flags;
+      ++e;
+      return true;
+    }
+    t += gridDim.x;
+    e = 0;
+  }
+  return false;
+}
+
+// warps 6-7 (64 threads, index p): the element's inputs into `in`, 8-byte
+// cp.async (the completion is waited for by the same threads)
+__device__ __forceinline__ void tc20_prefetch(const TangentArgs& a, const Tc20Elem& d, Tc20Inputs& in, int p) {
+  const long long dbase = d.einf_off + (long long)d.i * TOT;
+  const bool geonl = d.flags & 1;
+  for (int q = p; q < TOT; q += 64) {
+    const int ci = a.cdest[dbase + q] - 1;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(in.c + q)), "l"(a.c + ci) : "memory");
+    if (geonl) {
+      const int ei = a.edest[dbase + q] - 1;
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(in.u + q)), "l"(a.u + ei) : "memory");
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(in.du + q)), "l"(a.du + ei) : "memory");
+    }
+  }
+  for (int q = p; q < NG * 21; q += 64) {
+    const int g = q / 21, m = q % 21;
+    const double* src = a.cep + d.cep_off + ((long long)g * d.span + d.i) * 21 + m;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(in.cep + q)), "l"(src) : "memory");
+  }
+  if (geonl) {
+    const long long g0 = (d.gp_off + (long long)d.i * NG) * 9;
+    for (int q = p; q < NG * 9; q += 64) {
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(in.rot + q)), "l"(a.rot_n1 + g0 + q)
+                   : "memory");
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(su32(in.urcs + q)), "l"(a.urcs_n1 + g0 + q)
+                   : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 template <bool kBF16>
-__global__ void __launch_bounds__(kThreads) k_tangent_tc_hex20(TangentArgs a, const TcgTile* tiles, int ntiles,
+__global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(TangentArgs a, const TcgTile* tiles, int ntiles,
                                                                 int* tc_timeout) {
   using O = Op<kBF16>;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* opB = smem + O::kOffB;
   unsigned char* opA = smem + O::kOffA;
+  Tc20Inputs* inb = reinterpret_cast<Tc20Inputs*>(smem + O::kOffIn);
   __shared__ Tc20Static T;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long limit = a.wait_limit;
@@ -216,8 +280,7 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex20(TangentArgs a, co
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&T.mma)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;");
     T.abort = 0;
-    T.fail_t = -1;
-    T.fail_e = 0;
+    T.fail_n = -1;
   }
   const double* dnd = a.dn[Hex20::SLOT];
   for (int k = tid; k < NG * 3 * NN + NG; k += kThreads) T.dn[k] = (float)dnd[k];
@@ -239,6 +302,14 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex20(TangentArgs a, co
       put<kBF16>(opA + O::kOpA, O::off(row, k), 0.f);
     }
   }
+  // the first element's inputs
+  int nt = blockIdx.x, ne = 0;   // position of the next element in the sequence
+  Tc20Elem cur, prev{}, nxt;
+  bool have = tc20_next(tiles, ntiles, nt, ne, cur);
+  if (have && warp >= 6) {
+    tc20_prefetch(a, cur, inb[0], tid - 192);
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -246,116 +317,168 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex20(TangentArgs a, co
   const uint32_t tmem = T.tmem_base;
   const float bf = (float)a.beta_fact;
   const int g = lane, kr = warp;   // phases 1-3: Gauss point, thread of the point
-  unsigned q = 0;                  // MMA chains issued (mbarrier phase)
 
-  for (int t = blockIdx.x; t < ntiles && !T.abort; t += gridDim.x) {
-    const TcgTile tl = tiles[t];
-    for (int e = 0; e < tl.n; ++e) {
-      const int i = tl.i0 + e;
-      // (0) coordinates at n+1 relative to node 1
-      if (tid < TOT) {
-        const long long dbase = tl.einf_off + (long long)i * TOT;
-        const int d0 = (tid / NN) * NN;
-        double v = a.c[a.cdest[dbase + tid] - 1], ref = a.c[a.cdest[dbase + d0] - 1];
-        if (tl.flags & 1) {
-          const int e1 = a.edest[dbase + tid] - 1, e0 = a.edest[dbase + d0] - 1;
-          v = v + a.u[e1] + a.du[e1];
-          ref = ref + a.u[e0] + a.du[e0];
-        }
-        T.x[tid] = d2f_rn(v - ref);
+  // element n: its point phases overlap the MMAs of element n - 1, whose
+  // epilogue follows; then Y of n into the A operand and its MMAs
+  int n = 0;
+  for (; have; ++n) {
+    const Tc20Inputs& in = inb[n & 1];
+    const bool more = tc20_next(tiles, ntiles, nt, ne, nxt);
+    if (more && warp >= 6) tc20_prefetch(a, nxt, inb[(n + 1) & 1], tid - 192);
+    // (0) coordinates at n+1 relative to node 1
+    if (tid < TOT) {
+      const int d0 = (tid / NN) * NN;
+      double v = in.c[tid], ref = in.c[d0];
+      if (cur.flags & 1) {
+        v = v + in.u[tid] + in.du[tid];
+        ref = ref + in.u[d0] + in.du[d0];
       }
-      __syncthreads();
-      // (1) [J] rows, conversions
-      if (g < NG) {
-        switch (kr) {
-          case 0: tc20_phase1<0>(a, tl, i, T, g); break;
-          case 1: tc20_phase1<1>(a, tl, i, T, g); break;
-          case 2: tc20_phase1<2>(a, tl, i, T, g); break;
-          case 3: tc20_phase1<3>(a, tl, i, T, g); break;
-          case 4: tc20_phase1<4>(a, tl, i, T, g); break;
-          default: tc20_phase1<5>(a, tl, i, T, g); break;
-        }
+      T.x[tid] = d2f_rn(v - ref);
+    }
+    __syncthreads();
+    // (1) [J] rows, conversions
+    const bool geonl = cur.flags & 1;
+    if (warp < 6 && g < NG) {
+      switch (kr) {
+        case 0: tc20_phase1<0>(in, geonl, T, g); break;
+        case 1: tc20_phase1<1>(in, geonl, T, g); break;
+        case 2: tc20_phase1<2>(in, geonl, T, g); break;
+        case 3: tc20_phase1<3>(in, geonl, T, g); break;
+        case 4: tc20_phase1<4>(in, geonl, T, g); break;
+        default: tc20_phase1<5>(in, geonl, T, g); break;
       }
-      __syncthreads();
-      // (2a) Gamma, w det J, {T}
-      if (g < NG) {
-        const float w = T.dn[NG * 3 * NN + g];
-        const bool geonl = tl.flags & 1;
-        switch (kr) {
-          case 0: pt_phase2a<0, kPts>(T.pt, g, w, geonl); break;
-          case 1: pt_phase2a<1, kPts>(T.pt, g, w, geonl); break;
-          case 2: pt_phase2a<2, kPts>(T.pt, g, w, geonl); break;
-          case 3: pt_phase2a<3, kPts>(T.pt, g, w, geonl); break;
-          case 4: pt_phase2a<4, kPts>(T.pt, g, w, geonl); break;
-          default: pt_phase2a<5, kPts>(T.pt, g, w, geonl); break;
-        }
+    }
+    __syncthreads();
+    // (2a) Gamma, w det J, {T}
+    if (warp < 6 && g < NG) {
+      const float w = T.dn[NG * 3 * NN + g];
+      switch (kr) {
+        case 0: pt_phase2a<0, kPts>(T.pt, g, w, geonl); break;
+        case 1: pt_phase2a<1, kPts>(T.pt, g, w, geonl); break;
+        case 2: pt_phase2a<2, kPts>(T.pt, g, w, geonl); break;
+        case 3: pt_phase2a<3, kPts>(T.pt, g, w, geonl); break;
+        case 4: pt_phase2a<4, kPts>(T.pt, g, w, geonl); break;
+        default: pt_phase2a<5, kPts>(T.pt, g, w, geonl); break;
       }
-      __syncthreads();
-      // (2) rows of w det J [D*]
-      if (g < NG) {
-        const bool qb = a.qbar != 0;
-        switch (kr) {
-          case 0: pt_phase2<0, kPts>(qb, tl.flags, T.pt, g); break;
-          case 1: pt_phase2<1, kPts>(qb, tl.flags, T.pt, g); break;
-          case 2: pt_phase2<2, kPts>(qb, tl.flags, T.pt, g); break;
-          case 3: pt_phase2<3, kPts>(qb, tl.flags, T.pt, g); break;
-          case 4: pt_phase2<4, kPts>(qb, tl.flags, T.pt, g); break;
-          default: pt_phase2<5, kPts>(qb, tl.flags, T.pt, g); break;
-        }
+    }
+    __syncthreads();
+    // (2) rows of w det J [D*]
+    if (warp < 6 && g < NG) {
+      const bool qb = a.qbar != 0;
+      switch (kr) {
+        case 0: pt_phase2<0, kPts>(qb, cur.flags, T.pt, g); break;
+        case 1: pt_phase2<1, kPts>(qb, cur.flags, T.pt, g); break;
+        case 2: pt_phase2<2, kPts>(qb, cur.flags, T.pt, g); break;
+        case 3: pt_phase2<3, kPts>(qb, cur.flags, T.pt, g); break;
+        case 4: pt_phase2<4, kPts>(qb, cur.flags, T.pt, g); break;
+        default: pt_phase2<5, kPts>(qb, cur.flags, T.pt, g); break;
       }
-      __syncthreads();
-      // (3) H per point and pair
-      if (g < NG) tc20_phase3(T, g, kr);
-      __syncthreads();
-      // (4) Y into the A operand: thread = row (pair, node b); the previous
-      // element's MMAs are complete (waited for below)
-      if (tid < kRowsLive) {
-        const int slot = tid / NN, b = tid % NN;
-        for (int gp = 0; gp < NG; ++gp) {
-          const float* h = T.H[gp][slot];
-          const float n0 = T.dn[(gp * 3 + 0) * NN + b], n1 = T.dn[(gp * 3 + 1) * NN + b],
-                      n2 = T.dn[(gp * 3 + 2) * NN + b];
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-            put_hilo<kBF16>(opA, O::kOpA, O::off(tid, gp * 3 + r), h[3 * r] * n0 + h[3 * r + 1] * n1 + h[3 * r + 2] * n2);
-        }
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-      if (limit == 0) {   // give up before any MMA (the status path without a fault)
-        if (tid == 0) { T.abort = 1; T.fail_t = t; T.fail_e = e; }
-        __syncthreads();
-        break;
-      }
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint64_t da = sdesc(su32(opA), O::kSBO), db = sdesc(su32(opB), O::kSBO);
-        const uint64_t dal = da + (O::kOpA >> 4), dbl = db + (O::kOpB >> 4);
-#pragma unroll 1
-        for (int ks = 0; ks < O::kSteps; ++ks) {
-          const uint64_t o = (uint64_t)ks * (256 >> 4);   // one k-step = two core matrices along K
-          mma20<kBF16>(tmem, da + o, db + o, ks > 0);
-          mma20<kBF16>(tmem, da + o, dbl + o, true);
-          mma20<kBF16>(tmem, dal + o, db + o, true);
-        }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            su32(&T.mma)) : "memory");
-      }
-      if (!wait_phase(&T.mma, q & 1, limit, nullptr)) {
+    }
+    __syncthreads();
+    // (3) H per point and pair
+    if (warp < 6 && g < NG) tc20_phase3(T, g, kr);
+    // the next element's inputs have landed (read after the loop's next barrier)
+    if (warp >= 6) asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    // (6) of element n - 1: its MMAs done, accumulator -> packed Ke -> global
+    if (n > 0) {
+      if (!wait_phase(&T.mma, (n - 1) & 1, limit, nullptr)) {
         // the MMAs may still be running: wait them out before tensor memory
         // is read or freed
         T.abort = 1;
-        wait_phase(&T.mma, q & 1, kDrainLimit, nullptr);
+        wait_phase(&T.mma, (n - 1) & 1, kDrainLimit, nullptr);
       }
-      ++q;
       asm volatile("tcgen05.fence::after_thread_sync;");
       __syncthreads();
       if (T.abort) {
-        if (tid == 0) { T.fail_t = t; T.fail_e = e; }
-        __syncthreads();
+        if (tid == 0) T.fail_n = n - 1;
         break;
       }
-      // (6) accumulator -> packed Ke: warp w < 4 reads lane quadrant w
+      if (warp < 4) {   // warp w reads lane quadrant w
+        const int row = 32 * warp + lane;
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+            "tcgen05.wait::ld.sync.aligned;"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr), "r"(taddr + 16)
+            : "memory");
+        if (row < kRowsLive) {
+          const int slot = row / NN, b = row % NN;
+          const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+          const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+          const int d2 = jj * NN + b;
+#pragma unroll
+          for (int an = 0; an < NN; ++an) {
+            if (ii == jj && an > b) continue;
+            const int d1 = ii * NN + an;
+            T.ke[d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[an]) * bf;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      float* out = reinterpret_cast<float*>(a.estiff) + prev.estiff_off + (long long)prev.i * UT;
+      for (int z = tid; z < UT; z += kThreads) out[z] = T.ke[z];
+    }
+    // (4) Y of element n into the A operand (element n - 1's MMAs are
+    // complete): 240 threads, one per row (pair, node b) and half of the
+    // Gauss points
+    if (tid < 2 * kRowsLive) {
+      const int row = tid % kRowsLive, half = tid / kRowsLive;
+      const int slot = row / NN, b = row % NN;
+      const int g0 = half ? 14 : 0, g1 = half ? NG : 14;
+#pragma unroll 2
+      for (int gp = g0; gp < g1; ++gp) {
+        const float* h = T.H[gp][slot];
+        const float n0 = T.dn[(gp * 3 + 0) * NN + b], n1 = T.dn[(gp * 3 + 1) * NN + b],
+                    n2 = T.dn[(gp * 3 + 2) * NN + b];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          put_hilo<kBF16>(opA, O::kOpA, O::off(row, gp * 3 + r), h[3 * r] * n0 + h[3 * r + 1] * n1 + h[3 * r + 2] * n2);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (limit == 0) {   // give up before any MMA (the status path without a fault)
+      if (tid == 0) { T.abort = 1; T.fail_n = n; }
+      break;
+    }
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint64_t da = sdesc(su32(opA), O::kSBO), db = sdesc(su32(opB), O::kSBO);
+      const uint64_t dal = da + (O::kOpA >> 4), dbl = db + (O::kOpB >> 4);
+#pragma unroll 1
+      for (int ks = 0; ks < O::kSteps; ++ks) {
+        const uint64_t o = (uint64_t)ks * (256 >> 4);   // one k-step = two core matrices along K
+        mma20<kBF16>(tmem, da + o, db + o, ks > 0);
+        mma20<kBF16>(tmem, da + o, dbl + o, true);
+        mma20<kBF16>(tmem, dal + o, db + o, true);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          su32(&T.mma)) : "memory");
+    }
+    prev = cur;
+    cur = nxt;
+    have = more;
+  }
+  // the last element's epilogue
+  if (!T.abort && n > 0) {
+    if (!wait_phase(&T.mma, (n - 1) & 1, limit, nullptr)) {
+      T.abort = 1;
+      wait_phase(&T.mma, (n - 1) & 1, kDrainLimit, nullptr);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    __syncthreads();
+    if (T.abort) {
+      if (tid == 0) T.fail_n = n - 1;
+    } else {
       if (warp < 4) {
         const int row = 32 * warp + lane;
         const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
@@ -386,20 +509,21 @@ __global__ void __launch_bounds__(kThreads) k_tangent_tc_hex20(TangentArgs a, co
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
-      float* out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)i * UT;
+      float* out = reinterpret_cast<float*>(a.estiff) + prev.estiff_off + (long long)prev.i * UT;
       for (int z = tid; z < UT; z += kThreads) out[z] = T.ke[z];
-      __syncthreads();
     }
   }
+  if (warp >= 6) asm volatile("cp.async.wait_all;" ::: "memory");   // no copy outlives the CTA
   __syncthreads();
   if (T.abort) {
-    // NaN for every element of this CTA's records from the one it gave up at
+    // NaN for every element of the CTA's sequence from the first one not stored
     if (tid == 0) atomicExch(tc_timeout, 1);
-    for (int t = T.fail_t; t >= 0 && t < ntiles; t += gridDim.x) {
-      const TcgTile tl = tiles[t];
-      const int e0 = t == T.fail_t ? T.fail_e : 0;
-      float* out = reinterpret_cast<float*>(a.estiff) + tl.estiff_off + (long long)(tl.i0 + e0) * UT;
-      for (long long z = tid; z < (long long)(tl.n - e0) * UT; z += kThreads) out[z] = __int_as_float(0x7fc00000);
+    int t = blockIdx.x, e = 0, k = 0;
+    Tc20Elem d;
+    while (tc20_next(tiles, ntiles, t, e, d)) {
+      if (k++ < T.fail_n) continue;
+      float* out = reinterpret_cast<float*>(a.estiff) + d.estiff_off + (long long)d.i * UT;
+      for (int z = tid; z < UT; z += kThreads) out[z] = __int_as_float(0x7fc00000);
     }
   }
   if (warp == 0) {
@@ -417,6 +541,8 @@ cudaError_t set_attr20() {
 static_assert(Op<false>::kSmem + sizeof(Tc20Static) <= 227 * 1024, "TF32 form exceeds shared memory");
 static_assert(Op<true>::kSmem + sizeof(Tc20Static) <= 227 * 1024, "BF16 form exceeds shared memory");
 static_assert(Op<false>::kOffA % 16 == 0 && Op<true>::kOffA % 16 == 0, "operands must be 16-byte aligned");
+static_assert(Op<false>::kOffIn % 16 == 0 && Op<true>::kOffIn % 16 == 0, "staging must be 16-byte aligned");
+static_assert(2 * (Op<true>::kSmem + sizeof(Tc20Static)) <= 226 * 1024, "two BF16 CTAs per SM");
 static_assert(UT * 4 <= 8 * 1024, "Ke staging");
 
 }  // namespace
