@@ -418,6 +418,25 @@ int w3g_residual_norms_dev(w3g_csr* csr, const void* d_v, const void* d_fixed_ma
 int w3g_free_dot_dev(w3g_csr* csr, const void* d_a, const void* d_b, const void* d_fixed_mask,
                      void* d_out, void* stream);
 
+/* One Newton iteration of a device-resident driver as ONE CUDA graph (the
+   body of mnralg's iteration loop, src/mnralg.f:435-569, with the solve of
+   drive_assemble_solve): the solve of K_ff d = -ifv_f by Jacobi-PCG as a
+   device-side loop (a conditional graph node over batches of 16 CG
+   iterations: no host round trip inside the solve), d_d = d, du += d, the
+   element work at the new du (recovery for (step, iter), then the tangent
+   for the next iteration; the context's precision and schedule), the
+   assembly of K and cvtest's two norms of the new ifv into d_norms (2
+   device doubles). The host waits once, for the scalars returned here:
+   the PCG's iteration count and relative residual, the recovery's status
+   (0, or 1/2 = step cut as w3g_recover) and the norms (norms[0] = ||ifv_f||^2,
+   norms[1] = ||ifv||^2, host). The graph is built on the first call and
+   rebuilt when a pointer, the precision, the schedule or the wait limit
+   changes. Returns 0, W3G_PCG_MAXIT or W3G_PCG_BREAKDOWN as w3g_pcg_dev. */
+int w3g_newton_iteration_dev(w3g_csr* csr, int step, int iter, int extrapolated_du, const void* d_c,
+                             const void* d_u, void* d_du, void* d_ifv, const void* d_fixed_mask, void* d_d,
+                             double rtol, int maxit, void* d_norms, void* stream, int* pcg_iters,
+                             double* pcg_relres, int* recover_status, double* norms);
+
 /* ---- internal-force assembly without device allocation --------------
    No counterpart in the reference. For callers that cannot allocate
    device memory -- a Fortran code whose device arrays come from a pool or

@@ -157,3 +157,45 @@ def test_device_newton_adaptive_subdivision():
     steps = [h[0] for h in drv.history]
     for s in (1, 2):
         assert abs(sum(f for f, t in zip(drv.fractions, steps) if t == s) - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["hex8", "mixed"])
+@pytest.mark.parametrize("forcing", ["fixed", "ew"])
+def test_newton_iteration_graph_equals_step_by_step(kind, forcing):
+    """One graph per Newton iteration (w3g_newton_iteration_dev: the PCG as
+    a device-side conditional loop, du += d, recovery, tangent, assembly,
+    norms) against the same loop driven call by call: the same kernels in
+    the same order, so iteration counts, PCG counts and displacements are
+    bitwise equal; with the FP32 tangent too (the mixed model)."""
+    from warp3d_gb300.solver import DeviceNewtonDriver
+    if kind == "hex8":
+        n = 5
+        coords, incid = cube_mesh(n, jitter=0.1)
+        mk = lambda: Model(coords, incid)
+        nxyz, origins, strain, prec = (n, n, n), None, 0.01, abi.TANGENT_FP64
+    else:
+        coords, parts, origins = mixed_mesh(
+            [(abi.ETYPE_L3DISOP, 3), (abi.ETYPE_Q3DISOP, 2), (abi.ETYPE_TET10, 2)], ny=2, nz=2, jitter=0.05, seed=5)
+        rng = np.random.Generator(np.random.PCG64(5))
+        spans = [random_spans(inc.shape[0], rng, 1, 9) for _, inc in parts]
+        mk = lambda: Model(coords, parts=[Part(et, inc, sp, [Bilinear.from_hprime(200000.0, 0.3, 400.0, 2000.0)])
+                                          for (et, inc), sp in zip(parts, spans)])
+        nxyz, strain, prec = (3, 2, 2), 0.004, abi.TANGENT_FP32
+    runs = []
+    for graph in (False, True):
+        model = mk()
+        eng = _engine(model)
+        eng.set_precision(prec)
+        fixed, topz = uniaxial_bcs(model, nxyz, origins=origins)
+        drv = DeviceNewtonDriver(model, eng, fixed, tol=1e-8, maxit=40, lin_rtol=1e-10, extrapolate=True,
+                                 forcing=forcing, eta_max=1e-3, graph=graph)
+        for s in range(1, 4):
+            imp = np.zeros(model.nodof)
+            imp[topz] = strain * nxyz[2] / 3
+            drv.step(s, imp)
+        runs.append((drv, eng))
+    (a, _), (b, eb) = runs
+    print("newton", [h[1] for h in a.history], "pcg", [l for _, l in a.lin_history])
+    assert [h[1] for h in a.history] == [h[1] for h in b.history]
+    assert [l for _, l in a.lin_history] == [l for _, l in b.lin_history]
+    assert np.array_equal(a.u, b.u)

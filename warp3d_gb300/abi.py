@@ -194,6 +194,9 @@ PROTOTYPES = [
                               C.POINTER(C.c_double)]),
     ("w3g_residual_norms_dev", C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     ("w3g_free_dot_dev", C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    ("w3g_newton_iteration_dev", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
+                                          C.c_int, _vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     ("w3g_timers_get", C.c_int, [_vp, C.POINTER(Timers)]),
     ("w3g_timers_reset", C.c_int, [_vp]),
     ("w3g_check_finite", C.c_int, [_vp, C.POINTER(C.c_longlong)]),

@@ -1114,6 +1114,21 @@ int w3g_get_schedule(w3g_context* c, w3g_schedule* sched) {
   return 0;
 }
 
+}  // extern "C"
+
+namespace w3g {
+int enqueue_element_iteration(w3g_context* c, int what, const double* d_c, const double* d_u, const double* d_du,
+                              double* d_ifv, cudaStream_t st) {
+  return enqueue_iteration(c, what, d_c, d_u, d_du, d_ifv, st);
+}
+int enqueue_begin_recover(w3g_context* c, int step, int iter, int extrapolated_du, cudaStream_t st) {
+  return begin_recover(c, step, iter, extrapolated_du, st);
+}
+const w3g_recover_info* device_recover_info(const w3g_context* c) { return c->s.d_info; }
+}  // namespace w3g
+
+extern "C" {
+
 int w3g_iteration_dev(w3g_context* c, int step, int iter, int extrapolated_du, int what, const void* d_c,
                       const void* d_u, const void* d_du, void* d_ifv, void* stream) {
   if (!c || !d_c || !d_u || !d_du) return fail(W3G_EARG, "null argument");

@@ -372,6 +372,13 @@ inline cudaError_t init_kernels() {
   if (e == cudaSuccess) e = init_recover_kernels();
   return e == cudaSuccess ? init_mm10_kernels() : e;
 }
+// one Newton iteration's element work (recovery and/or tangent, the
+// W3G_ITER_* bits) enqueued on a stream, capturable; the iteration scalars
+// are set by enqueue_begin_recover (not capturable: its arguments change)
+int enqueue_element_iteration(w3g_context* c, int what, const double* d_c, const double* d_u, const double* d_du,
+                              double* d_ifv, cudaStream_t st);
+int enqueue_begin_recover(w3g_context* c, int step, int iter, int extrapolated_du, cudaStream_t st);
+const w3g_recover_info* device_recover_info(const w3g_context* c);
 // resident CTAs per SM of the persistent kernels
 int persistent_tangent_occupancy(const DeviceModel& m, bool fp32);
 int persistent_recover_occupancy();

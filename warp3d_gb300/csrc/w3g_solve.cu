@@ -485,6 +485,61 @@ __global__ void __launch_bounds__(kThreads) k_dot_fin(const double* partials, in
   if (threadIdx.x == 0) out[0] = t;
 }
 
+// ---- one Newton iteration as one graph (w3g_newton_iteration_dev) ----
+// the solve's tolerance and iteration limit, written before each launch
+struct NewtonParams {
+  double rtol;
+  int maxit, pad;
+};
+
+// k_pcg_init_fin with the tolerance read from the device
+__global__ void __launch_bounds__(kThreads) k_pcg_init_fin_p(const double* partials, int nparts,
+                                                             const NewtonParams* prm, PcgScal* sc) {
+  __shared__ double sh[kWarps];
+  const double rz = sum_partials(partials, nparts, 2, 0, sh);
+  const double rr = sum_partials(partials, nparts, 2, 1, sh);
+  if (threadIdx.x == 0) {
+    const double rtol = prm->rtol;
+    sc->rz = rz;
+    sc->rr = rr;
+    sc->bb = rr;
+    sc->tol2 = rtol * rtol * rr;
+    sc->alpha = sc->beta = sc->pap = 0.0;
+    sc->iters = 0;
+    sc->breakdown = 0;
+    sc->done = rr <= sc->tol2 ? 1 : 0;
+  }
+}
+
+// the loop condition of the device-side CG loop: another batch while the
+// solve is neither converged nor broken down and below the iteration limit
+// (every batch that runs advances iters, so the loop ends)
+__global__ void k_pcg_cond(const PcgScal* sc, const NewtonParams* prm, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, (!sc->done && sc->iters < prm->maxit) ? 1u : 0u);
+}
+
+__global__ void __launch_bounds__(kThreads) k_add(int n, const double* __restrict__ x, double* __restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] += x[i];
+}
+
+// the pinned host side of one launch: parameters in, scalars out
+struct NewtonHost {
+  NewtonParams prm;
+  PcgScal sc;
+  w3g_recover_info info;
+  double norms[2];
+};
+
+// what the Newton-iteration graph was built for
+struct NewtonKey {
+  const void *c = nullptr, *u = nullptr, *du = nullptr, *ifv = nullptr, *fixed = nullptr, *d = nullptr,
+             *norms = nullptr;
+  int precision = -1;
+  w3g::Schedule sched{};
+  long long wait_limit = 0;
+  bool triplet = false;
+};
+
 }  // namespace
 
 struct w3g_csr {
@@ -507,6 +562,12 @@ struct w3g_csr {
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   cudaGraphExec_t batch = nullptr;
   const void* graph_fixed = nullptr;   // mask the batch graph was captured with
+  // one Newton iteration as one graph
+  cudaGraphExec_t newton = nullptr;
+  NewtonKey newton_key;
+  cudaStream_t stream2 = nullptr;      // captures the CG loop body
+  NewtonParams* d_prm = nullptr;
+  NewtonHost* h_newton = nullptr;      // pinned
 };
 
 namespace {
@@ -520,6 +581,10 @@ namespace {
 
 void csr_free(w3g_csr* m) {
   if (m->batch) cudaGraphExecDestroy(m->batch);
+  if (m->newton) cudaGraphExecDestroy(m->newton);
+  if (m->stream2) cudaStreamDestroy(m->stream2);
+  if (m->d_prm) cudaFree(m->d_prm);
+  if (m->h_newton) cudaFreeHost(m->h_newton);
   void* ptrs[] = {m->rowptr, m->colind, m->diag, m->cptr, m->csrc, m->val, m->x, m->r, m->z, m->p, m->q,
                   m->dinv, m->binv, m->partials, m->sc};
   for (void* p : ptrs)
@@ -527,6 +592,37 @@ void csr_free(w3g_csr* m) {
   if (m->ev_in) cudaEventDestroy(m->ev_in);
   if (m->ev_out) cudaEventDestroy(m->ev_out);
   if (m->stream) cudaStreamDestroy(m->stream);
+}
+
+// the CG set-up of w3g_pcg_dev (preconditioner, x = 0, r, z, p, partials)
+void enqueue_pcg_init(w3g_csr* s, const unsigned char* fixed, const double* b, double b_scale, cudaStream_t st) {
+  const int n = s->n, G = s->grid;
+  if (s->triplet) {
+    k_binv<<<G, kThreads, 0, st>>>(n / 3, s->diag, s->val, fixed, s->binv);
+    k_pcg_init3<<<G, kThreads, 0, st>>>(n / 3, fixed, b, b_scale, s->binv, s->x, s->r, s->z, s->p, s->partials);
+  } else {
+    k_dinv<<<G, kThreads, 0, st>>>(n, s->diag, s->val, fixed, s->dinv);
+    k_pcg_init<<<G, kThreads, 0, st>>>(n, fixed, b, b_scale, s->dinv, s->x, s->r, s->z, s->p, s->partials);
+  }
+}
+
+// `count` CG iterations (each a no-op once the solve is done)
+void enqueue_pcg_iterations(w3g_csr* s, const unsigned char* fixed, int count, cudaStream_t st) {
+  const int n = s->n, G = s->grid;
+  for (int it = 0; it < count; ++it) {
+    const int GS = s->triplet ? s->grid_spmv : s->grid_spmv_rows;
+    if (s->triplet)
+      k_spmv3<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+    else
+      k_spmv<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
+    k_alpha<<<1, kThreads, 0, st>>>(s->partials, GS, s->sc);
+    if (s->triplet)
+      k_update3<<<G, kThreads, 0, st>>>(n / 3, s->binv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
+    else
+      k_update<<<G, kThreads, 0, st>>>(n, s->dinv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
+    k_beta<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
+    k_pupdate<<<G, kThreads, 0, st>>>(n, s->z, s->p, s->sc);
+  }
 }
 
 // the part of the pattern built by one host thread: rows [r0, r1)
@@ -593,6 +689,113 @@ int grid_for(int device) {
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   return std::max(1, sms) * 8;
+}
+
+}  // namespace
+
+namespace {
+
+// The Newton-iteration graph: the CG solve of K d = -ifv as a device-side
+// loop (a conditional while node over batches of kBatch iterations, the
+// condition set by k_pcg_cond: no host round trip per batch), then d = x,
+// du += d, the element work of the next iteration (recovery at du, then the
+// tangent; the caller launches k_begin_recover before the graph), the
+// assembly of K and the residual norms.
+int build_newton_graph(w3g_csr* s, const NewtonKey& k) {
+  w3g_context* c = s->ctx;
+  if (!s->stream2) CKS(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
+  if (!s->d_prm) CKS(cudaMalloc(&s->d_prm, sizeof(NewtonParams)));
+  if (!s->h_newton) CKS(cudaMallocHost(&s->h_newton, sizeof(NewtonHost)));
+  if (s->newton) {
+    CKS(cudaGraphExecDestroy(s->newton));
+    s->newton = nullptr;
+  }
+  const int n = s->n, G = s->grid;
+  const unsigned char* fixed = (const unsigned char*)k.fixed;
+  cudaStream_t cs = s->stream;
+  CKS(cudaStreamSynchronize(cs));
+  CKS(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t g = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &g, nullptr, nullptr, nullptr);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, 0);
+  if (e == cudaSuccess) {
+    enqueue_pcg_init(s, fixed, (const double*)k.ifv, -1.0, cs);
+    k_pcg_init_fin_p<<<1, kThreads, 0, cs>>>(s->partials, G, s->d_prm, s->sc);
+    k_pcg_cond<<<1, 1, 0, cs>>>(s->sc, s->d_prm, h);
+    e = cudaGetLastError();
+  }
+  // the loop node after what is captured so far; capture continues after it
+  cudaGraphNode_t wnode = nullptr;
+  cudaGraph_t body = nullptr;
+  if (e == cudaSuccess) {
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e == cudaSuccess) {
+      cudaGraphNodeParams prm{};
+      prm.type = cudaGraphNodeTypeConditional;
+      prm.conditional.handle = h;
+      prm.conditional.type = cudaGraphCondTypeWhile;
+      prm.conditional.size = 1;
+      e = cudaGraphAddNode(&wnode, g, deps, nullptr, nd, &prm);
+      if (e == cudaSuccess) body = prm.conditional.phGraph_out[0];
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+  // the loop body, captured into the node's graph from the second stream
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(s->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    enqueue_pcg_iterations(s, fixed, kBatch, s->stream2);
+    k_pcg_cond<<<1, 1, 0, s->stream2>>>(s->sc, s->d_prm, h);
+    e = cudaGetLastError();
+    cudaGraph_t bo = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s->stream2, &bo);
+    if (e == cudaSuccess) e = e2;
+  }
+  int nel = 0;
+  if (e == cudaSuccess) {
+    e = cudaMemcpyAsync((void*)k.d, s->x, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, cs);
+    k_add<<<G, kThreads, 0, cs>>>(n, s->x, (double*)k.du);
+    nel = w3g::enqueue_element_iteration(c, W3G_ITER_RECOVER | W3G_ITER_TANGENT, (const double*)k.c,
+                                         (const double*)k.u, (const double*)k.du, (double*)k.ifv, cs);
+    const int grid = (int)std::min<long long>((s->nnz + kThreads - 1) / kThreads, 16LL * G);
+    if (c->precision == W3G_TANGENT_FP64)
+      k_assemble<double><<<std::max(1, grid), kThreads, 0, cs>>>(s->nnz, s->cptr, s->csrc, c->s.estiff, s->val);
+    else
+      k_assemble<float><<<std::max(1, grid), kThreads, 0, cs>>>(s->nnz, s->cptr, s->csrc, c->s.estiff32, s->val);
+    double* part = s->partials + 2 * (size_t)G;
+    k_norms<<<G, kThreads, 0, cs>>>(n, (const double*)k.ifv, fixed, part);
+    k_norms_fin<<<1, kThreads, 0, cs>>>(part, G, (double*)k.norms);
+    if (e == cudaSuccess) e = cudaGetLastError();
+  }
+  cudaGraph_t gout = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(cs, &gout);
+  if (nel < 0) {
+    if (gout) cudaGraphDestroy(gout);
+    return nel;   // the element path's own error (message set)
+  }
+  if (e == cudaSuccess) e = ee;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&s->newton, gout, 0);
+  if (gout) cudaGraphDestroy(gout);
+  if (e != cudaSuccess) {
+    s->newton = nullptr;
+    return w3g_fail(W3G_ECUDA, std::string("newton iteration graph: ") + cudaGetErrorString(e));
+  }
+  s->newton_key = k;
+  return 0;
+}
+
+bool same_key(const NewtonKey& a, const NewtonKey& b) {
+  return a.c == b.c && a.u == b.u && a.du == b.du && a.ifv == b.ifv && a.fixed == b.fixed && a.d == b.d &&
+         a.norms == b.norms && a.precision == b.precision && a.wait_limit == b.wait_limit &&
+         a.triplet == b.triplet && a.sched.mode == b.sched.mode &&
+         a.sched.recover_ctas_per_sm == b.sched.recover_ctas_per_sm &&
+         a.sched.tangent_ctas_per_sm == b.sched.tangent_ctas_per_sm &&
+         a.sched.recover_grain == b.sched.recover_grain && a.sched.tangent_grain == b.sched.tangent_grain &&
+         a.sched.order == b.sched.order;
 }
 
 }  // namespace
@@ -792,15 +995,7 @@ int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale
   // ordered after the caller's stream
   CKS(cudaEventRecord(s->ev_in, (cudaStream_t)stream));
   CKS(cudaStreamWaitEvent(st, s->ev_in, 0));
-  if (s->triplet) {
-    k_binv<<<G, kThreads, 0, st>>>(n / 3, s->diag, s->val, fixed, s->binv);
-    k_pcg_init3<<<G, kThreads, 0, st>>>(n / 3, fixed, (const double*)d_b, b_scale, s->binv, s->x, s->r, s->z, s->p,
-                                        s->partials);
-  } else {
-    k_dinv<<<G, kThreads, 0, st>>>(n, s->diag, s->val, fixed, s->dinv);
-    k_pcg_init<<<G, kThreads, 0, st>>>(n, fixed, (const double*)d_b, b_scale, s->dinv, s->x, s->r, s->z, s->p,
-                                     s->partials);
-  }
+  enqueue_pcg_init(s, fixed, (const double*)d_b, b_scale, st);
   k_pcg_init_fin<<<1, kThreads, 0, st>>>(s->partials, G, rtol, s->sc);
   CKS(cudaGetLastError());
   if (!s->batch || s->graph_fixed != d_fixed) {
@@ -808,20 +1003,7 @@ int w3g_pcg_dev(w3g_csr* s, const void* d_fixed, const void* d_b, double b_scale
     s->batch = nullptr;
     cudaGraph_t g;
     CKS(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int it = 0; it < kBatch; ++it) {
-      const int GS = s->triplet ? s->grid_spmv : s->grid_spmv_rows;
-      if (s->triplet)
-        k_spmv3<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
-      else
-        k_spmv<<<GS, kThreads, 0, st>>>(n, s->rowptr, s->colind, s->val, fixed, s->p, s->q, s->partials, s->sc);
-      k_alpha<<<1, kThreads, 0, st>>>(s->partials, GS, s->sc);
-      if (s->triplet)
-        k_update3<<<G, kThreads, 0, st>>>(n / 3, s->binv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
-      else
-        k_update<<<G, kThreads, 0, st>>>(n, s->dinv, s->x, s->r, s->z, s->p, s->q, s->partials, s->sc);
-      k_beta<<<1, kThreads, 0, st>>>(s->partials, G, s->sc);
-      k_pupdate<<<G, kThreads, 0, st>>>(n, s->z, s->p, s->sc);
-    }
+    enqueue_pcg_iterations(s, fixed, kBatch, st);
     CKS(cudaStreamEndCapture(st, &g));
     cudaError_t e = cudaGraphInstantiate(&s->batch, g, 0);
     cudaGraphDestroy(g);
@@ -870,6 +1052,49 @@ int w3g_free_dot_dev(w3g_csr* s, const void* d_a, const void* d_b, const void* d
   k_dot_fin<<<1, kThreads, 0, st>>>(part, s->grid, (double*)d_out);
   CKS(cudaGetLastError());
   return 0;
+}
+
+int w3g_newton_iteration_dev(w3g_csr* s, int step, int iter, int extrapolated_du, const void* d_c,
+                             const void* d_u, void* d_du, void* d_ifv, const void* d_fixed, void* d_d, double rtol,
+                             int maxit, void* d_norms, void* stream, int* pcg_iters, double* pcg_relres,
+                             int* recover_status, double* norms) {
+  if (!s || !d_c || !d_u || !d_du || !d_ifv || !d_fixed || !d_d || !d_norms)
+    return w3g_fail(W3G_EARG, "null argument");
+  if (maxit < 0 || !(rtol >= 0.0)) return w3g_fail(W3G_EARG, "bad rtol / maxit");
+  w3g_context* c = s->ctx;
+  CKS(cudaSetDevice(c->device));
+  NewtonKey k;
+  k.c = d_c; k.u = d_u; k.du = d_du; k.ifv = d_ifv; k.fixed = d_fixed; k.d = d_d; k.norms = d_norms;
+  k.precision = c->precision;
+  k.sched = c->sched;
+  k.wait_limit = c->wait_limit;
+  k.triplet = s->triplet;
+  if (!s->newton || !same_key(k, s->newton_key)) {
+    const int r = build_newton_graph(s, k);
+    if (r) return r;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  NewtonHost* hh = s->h_newton;
+  hh->prm.rtol = rtol;
+  hh->prm.maxit = maxit;
+  CKS(cudaMemcpyAsync(s->d_prm, &hh->prm, sizeof(NewtonParams), cudaMemcpyHostToDevice, st));
+  int r = w3g::enqueue_begin_recover(c, step, iter, extrapolated_du, st);
+  if (r) return r;
+  CKS(cudaGraphLaunch(s->newton, st));
+  CKS(cudaMemcpyAsync(&hh->sc, s->sc, sizeof(PcgScal), cudaMemcpyDeviceToHost, st));
+  CKS(cudaMemcpyAsync(&hh->info, w3g::device_recover_info(c), sizeof(w3g_recover_info), cudaMemcpyDeviceToHost,
+                      st));
+  CKS(cudaMemcpyAsync(hh->norms, d_norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  if (pcg_iters) *pcg_iters = hh->sc.iters;
+  if (pcg_relres) *pcg_relres = hh->sc.bb > 0.0 ? std::sqrt(hh->sc.rr / hh->sc.bb) : 0.0;
+  if (recover_status) *recover_status = hh->info.material_cut_step;
+  if (norms) {
+    norms[0] = hh->norms[0];
+    norms[1] = hh->norms[1];
+  }
+  if (hh->sc.breakdown) return W3G_PCG_BREAKDOWN;
+  return (hh->sc.rr <= hh->sc.tol2) ? 0 : W3G_PCG_MAXIT;
 }
 
 int w3g_csr_set_node_blocks(w3g_csr* s, int enable) {

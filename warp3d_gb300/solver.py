@@ -80,6 +80,20 @@ class DeviceCsr:
     def residual_norms(self, d_v: int, d_fixed: int, d_out: int, stream: int = 0):
         abi.check(self.lib, self.lib.w3g_residual_norms_dev(self.h, d_v, d_fixed, d_out, stream or None))
 
+    def newton_iteration(self, step: int, it: int, extrap: bool, d_c: int, d_u: int, d_du: int, d_ifv: int,
+                         d_fixed: int, d_d: int, rtol: float, maxit: int, d_norms: int, stream: int = 0):
+        """One Newton iteration as one graph (w3g_newton_iteration_dev):
+        solve, du += d, recovery, tangent, assembly, norms. Returns (PCG
+        status, PCG iterations, relative residual, recovery status,
+        ||ifv_f||^2, ||ifv||^2)."""
+        its, rel, rst = C.c_int(), C.c_double(), C.c_int()
+        nrm = (C.c_double * 2)()
+        st = self.lib.w3g_newton_iteration_dev(self.h, step, it, 1 if extrap else 0, d_c, d_u, d_du, d_ifv, d_fixed,
+                                               d_d, rtol, maxit, d_norms, stream or None, C.byref(its),
+                                               C.byref(rel), C.byref(rst), nrm)
+        abi.check(self.lib, st, allow=(abi.OK, abi.PCG_MAXIT, abi.PCG_BREAKDOWN))
+        return st, its.value, rel.value, rst.value, nrm[0], nrm[1]
+
     def free_dot(self, d_a: int, d_b: int, d_fixed: int, d_out: int, stream: int = 0):
         """d_out[0] = sum over the free dofs of a_i b_i (w3g_free_dot_dev)."""
         abi.check(self.lib, self.lib.w3g_free_dot_dev(self.h, d_a, d_b, d_fixed, d_out, stream or None))
@@ -160,7 +174,7 @@ class DeviceNewtonDriver:
                  lin_rtol: float = 1e-10, lin_maxit: int = 50000, device: int = 0, csr: DeviceCsr | None = None,
                  adaptive: bool = False, adaptive_step1: bool = False, adapt_divisions: int = 4,
                  adapt_min_fact: float = 1.0 / 16.0, line_search: bool = False, forcing: str = "fixed",
-                 eta_max: float = EW_ETA_MAX):
+                 eta_max: float = EW_ETA_MAX, graph: bool = False):
         import torch
         self.torch = torch
         self.model = model
@@ -170,6 +184,9 @@ class DeviceNewtonDriver:
         if forcing not in ("fixed", "ew"):
             raise ValueError("forcing must be 'fixed' or 'ew'")
         self.forcing, self.eta_max = forcing, eta_max
+        # one graph per Newton iteration (w3g_newton_iteration_dev); the line
+        # search needs the host between its trial step lengths
+        self.graph = graph and not line_search
         self.adaptive, self.adaptive_step1 = adaptive, adaptive_step1
         self.adapt_divisions, self.adapt_min_fact = adapt_divisions, adapt_min_fact
         dev = torch.device("cuda", device)
@@ -231,6 +248,29 @@ class DeviceNewtonDriver:
         eta, rn_prev = self.eta_max, None
         for it in range(1, self.maxit + 1):
             rtol = self.lin_rtol if self.forcing == "fixed" else max(self.lin_rtol, eta)
+            if self.graph:
+                # solve, du += d, recovery, norms and the next tangent in one graph
+                c, u, du = self._ptrs()
+                st, nits, rel, rst, rf, ra = self.csr.newton_iteration(
+                    step, it, extrap, c, u, du, self.ifv.data_ptr(), self.mask.data_ptr(), self.d.data_ptr(), rtol,
+                    self.lin_maxit, self.norms.data_ptr())
+                lin.append(nits)
+                self.trace.append([st, nits, rel, None])
+                if st == abi.PCG_BREAKDOWN:
+                    raise IncrementFailed(f"step {step}: tangent not positive definite on the free dofs "
+                                          f"(iteration {it})")
+                if rst != 0:
+                    raise IncrementFailed(f"step {step}: step cut requested at iteration {it}")
+                alphas.append(1.0)
+                rn, scale = float(np.sqrt(rf)), max(float(np.sqrt(ra)), 1e-300)
+                res_hist.append(rn / scale)
+                self.trace[-1][3] = rn / scale
+                if rn <= self.tol * scale:
+                    return res_hist, lin
+                if self.forcing == "ew" and rn_prev is not None:
+                    eta = ew_forcing(eta, rn, rn_prev, self.tol * scale, self.eta_max)
+                rn_prev = rn
+                continue
             st, nits, rel = self.csr.pcg(self.mask.data_ptr(), self.ifv.data_ptr(), -1.0, self.d.data_ptr(),
                                          rtol, self.lin_maxit)
             lin.append(nits)
