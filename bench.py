@@ -1094,6 +1094,12 @@ def summarize_leg(leg):
             out[k + "_speedup"] = _r(leg[k].get("speedup_vs_plain"))
     if "cpu_baseline" in leg:
         out["cpu_baseline"] = _r(leg["cpu_baseline"]["value"])
+    # the batching form: the single persistent launch against per-type
+    # launches (graph replays, ms per iteration) and the autotuner's pick
+    for k in ("plain_fp64", "mixed"):
+        if isinstance(leg.get(k), dict) and "schedules_ms" in leg[k]:
+            out[k + "_schedules_ms"] = leg[k]["schedules_ms"]
+            out[k + "_tuned_mode"] = leg[k].get("schedule", {}).get("mode")
     return out
 
 
