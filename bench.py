@@ -406,7 +406,7 @@ def bench_crystal(args, dev, local, with_cpu):
             "timed_increment": f"{0.1 * h_last:.3f}% axial strain (+ noise 1e-7)", **out}
 
 
-# other formulations of the same brick, timed on the config-1 mesh and
+# other formulations of the same brick, timed on the 64^3 cube's mesh and
 # state: WARP3D's default l3disop (b-bar, finite strain) and the
 # small-displacement b-bar brick of its published 18,081-element model
 FORMULATIONS = {"bbar": dict(bbar=True), "small_bbar": dict(geonl=False, bbar=True)}
@@ -1079,8 +1079,8 @@ def summarize_parity(p1, batched, crystal):
         if "estiff_precision_forms" in p:
             d["ke_precision_forms"] = {k: _r(v, 3) for k, v in p["estiff_precision_forms"].items()}
         return d
-    return {"config1_64cube": one(p1), "config3_batched": one((batched or {}).get("parity")),
-            "config4_crystal": one((crystal or {}).get("parity")), "tolerance_fp64": 1e-12}
+    return {"hex8_64cube": one(p1), "mixed_1m_batched": one((batched or {}).get("parity")),
+            "mm10_32cube": one((crystal or {}).get("parity")), "tolerance_fp64": 1e-12}
 
 
 def summarize_leg(leg):
@@ -1300,7 +1300,7 @@ def main():
         # the full record first, then the headline line (last line of the
         # output) with compact summaries of every leg
         details = {"details": {"mixed": mixed, "batched": batched, "crystal": crystal, "solver": solver,
-                               "formulations": formulations, "parity_config1": parity1, "roofline": roofline,
+                               "formulations": formulations, "parity_hex8_64cube": parity1, "roofline": roofline,
                                "cpu_baseline": cb, "e2e": e2e}}
         print(json.dumps(details), flush=True)
         line = {
