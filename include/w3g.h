@@ -82,8 +82,9 @@ extern "C" {
 #define W3G_TANGENT_FP64 0    /* plain form: everything FP64            */
 #define W3G_TANGENT_FP32 1    /* Ke in FP32 (CUDA-core FP32 FMA)        */
 #define W3G_TANGENT_TF32 2    /* B^T D B on the tensor cores, TF32 operands,
-                                 FP32 accumulation, Ke stored FP32 (8-node
-                                 bricks; other types as W3G_TANGENT_FP32) */
+                                 FP32 accumulation, Ke stored FP32 (8- and
+                                 20-node bricks; tetrahedra as
+                                 W3G_TANGENT_FP32)                       */
 #define W3G_TANGENT_BF16 3    /* the same with BF16 operands             */
 #define W3G_TANGENT_TF32X3 4  /* TF32 with split operands (x = hi + lo,
                                  three MMAs): near-FP32 Ke accuracy       */
@@ -194,10 +195,12 @@ const char* w3g_last_error(void);
 /* Selects the precision form of the tangent (W3G_TANGENT_*). Every form
    but FP64 writes Ke as float into a separate device array; w3g_tanstf then
    widens to double only when host estiff pointers are given. The tensor-
-   core forms (TF32, BF16, and their split X3 variants) cover 8-node bricks;
-   20-node bricks and tetrahedra take the FP32 kernels in the same call.
-   w3g_tanstf returns W3G_EFATAL if a tensor-core tile's bounded wait for
-   its MMAs gave up (that tile's Ke is then NaN). */
+   core forms (TF32, BF16, and their split X3 variants) cover 8-node and
+   20-node bricks, each element matrix with the rigid translations
+   projected out after the accumulation (BF16 requests take the split
+   operands on 20-node bricks); tetrahedra take the FP32 kernel in the
+   same call. w3g_tanstf returns W3G_EFATAL if a tensor-core tile's
+   bounded wait for its MMAs gave up (that tile's Ke is then NaN). */
 int w3g_set_tangent_precision(w3g_context* ctx, int precision);
 
 /* The UMAT compiled into the library describes itself as WARP3D's

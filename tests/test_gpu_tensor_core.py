@@ -89,10 +89,10 @@ def _unpack(packed):
 
 @pytest.mark.parametrize("precision", ALL)
 def test_tensor_core_tangent_keeps_the_rigid_translations(plastic_hex8, precision):
-    """Ke t = 0 for the element's three rigid translations t. The gradient-
-    pair form rounds only the material point values and the constant
-    operator, whose node sums stay exactly zero, so what is left is the FP32
-    accumulation (the level of the FP32 CUDA-core kernel)."""
+    """Ke t = 0 for the element's three rigid translations t. The kernel
+    projects the translations out of every node-pair block after the
+    accumulation (whose error has a mean along them), so what is left is
+    the FP32 rounding of the projected entries."""
     model, eng, ora, u, du = plastic_hex8
     eng.set_precision(precision)
     est = model.estiff_blocks()
@@ -107,7 +107,51 @@ def test_tensor_core_tangent_keeps_the_rigid_translations(plastic_hex8, precisio
             t[8 * d:8 * d + 8] = 1.0
             worst = max(worst, float(np.max(np.max(np.abs(K @ t), axis=1) / scale)))
     print(f"{NAMES[precision]} max |Ke t| / max |Ke| = {worst:.1e}")
-    assert worst <= 5e-6
+    assert worst <= 1e-6
+
+
+@pytest.fixture(scope="module")
+def plastic_hex8_many_tiles():
+    """20^3 elements in random blocks of 1..128: 562 tiles over the 152
+    CTAs, so every CTA runs its pipeline over several tiles (the small
+    models give each CTA about one). The state: one recovery from the
+    virgin state over an affine increment (0.4% axial, 0.15% shear) with
+    noise, which yields most of the mesh."""
+    spans = random_spans(8000, np.random.Generator(np.random.PCG64(3)), lo=1, hi=128)
+    model, _ = make_model(n=20, jitter=0.1, spans=spans)
+    c = model.coords
+    du = np.zeros(model.nodof)
+    du[2::3] = 0.004 * c[:, 2]
+    du[0::3] = 0.0015 * c[:, 2]
+    du += np.random.Generator(np.random.PCG64(11)).normal(0.0, 2e-4, model.nodof)
+    u = np.zeros(model.nodof)
+    ora = oracle.Oracle(model)
+    eng = _engine(model)
+    ifv = np.zeros(model.nodof)
+    st, info = ora.recover(2, 2, False, model.c, u, du, ifv.copy())
+    assert st == 0 and info.plastic_work > 0.0
+    assert eng.recover(2, 2, False, model.c, u, du, ifv)[0] == 0
+    return model, eng, ora, u, du
+
+
+@pytest.mark.parametrize("precision", ALL)
+def test_tensor_core_tangent_several_tiles_per_cta(plastic_hex8_many_tiles, precision):
+    model, eng, ora, u, du = plastic_hex8_many_tiles
+    eng.set_precision(precision)
+    err = _tangent_err(model, eng, ora, 2, 2, u, du)
+    est = model.estiff_blocks()
+    eng.tanstf(2, 2, model.c, u, du, est)
+    eng.set_precision(abi.TANGENT_FP64)
+    worst = 0.0
+    for blk in est:
+        K = _unpack(blk)
+        scale = np.max(np.abs(K), axis=(1, 2))
+        for d in range(3):
+            t = np.zeros(24)
+            t[8 * d:8 * d + 8] = 1.0
+            worst = max(worst, float(np.max(np.max(np.abs(K @ t), axis=1) / scale)))
+    print(f"{NAMES[precision]} 8000 elements: rel err {err:.2e}, max |Ke t| / max |Ke| = {worst:.1e}")
+    assert err <= TOL[precision] and worst <= 1e-6
 
 
 def test_tensor_core_wait_limit_zero_reports_efatal_without_a_fault(plastic_hex8):
@@ -252,10 +296,9 @@ def test_tensor_core_tangent_in_a_graph_replay_equals_direct_launch(plastic_hex8
     eng.set_precision(abi.TANGENT_FP64)
 
 
-# the 20-node bricks' tensor-core kernel always splits both operands (the
-# 27-point rule keeps no exact translation null space under one rounding):
-# split-form accuracy for every request
-TOL20 = {abi.TANGENT_TF32: 1e-5, abi.TANGENT_BF16: 1e-4, abi.TANGENT_TF32X3: 1e-5, abi.TANGENT_BF16X3: 1e-4}
+# the 20-node bricks' tensor-core kernel: TF32 rounds the operands once,
+# TF32X3 splits them, and both BF16 requests take the split operands
+TOL20 = {abi.TANGENT_TF32: 2e-3, abi.TANGENT_BF16: 1e-4, abi.TANGENT_TF32X3: 1e-5, abi.TANGENT_BF16X3: 1e-4}
 
 
 @pytest.fixture(scope="module")
@@ -282,7 +325,8 @@ def _unpack20(packed):
 def test_tensor_core_tangent_hex20(plastic_hex20, precision):
     """20-node bricks (27 Gauss points, ragged blocks) on the tensor cores:
     every element matrix against the FP64 oracle, and the rigid
-    translations kept to the FP32 accumulation level."""
+    translations (projected out in the epilogue) at the FP32 rounding
+    level."""
     model, eng, ora, u, du = plastic_hex20
     eng.set_precision(precision)
     err = _tangent_err(model, eng, ora, 4, 1, u, du)
@@ -300,7 +344,7 @@ def test_tensor_core_tangent_hex20(plastic_hex20, precision):
             worst = max(worst, float(np.max(np.max(np.abs(K @ t), axis=1) / scale)))
     print(f"hex20 {NAMES[precision]} tangent rel err {err:.2e}, max |Ke t| / max |Ke| = {worst:.1e}")
     assert err <= TOL20[precision]
-    assert worst <= 5e-6
+    assert worst <= 1e-6
 
 
 def test_tensor_core_hex20_wait_limit_zero_reports_efatal(plastic_hex20):

@@ -176,7 +176,7 @@ int enqueue_tangent(w3g_context* c, const double* d_c, const double* d_u, const 
     const bool split = p == W3G_TANGENT_TF32X3 || p == W3G_TANGENT_BF16X3;
     e = launch_tangent_tcg_hex8(c->m, a, bf16, split, c->s.tc_timeout, st);
     if (e == cudaSuccess) e = launch_tangent_tc_hex8(c->m, a, bf16, split, c->s.tc_timeout, st);
-    if (e == cudaSuccess) e = launch_tangent_tc_hex20(c->m, a, bf16, c->s.tc_timeout, st);
+    if (e == cudaSuccess) e = launch_tangent_tc_hex20(c->m, a, bf16, split, c->s.tc_timeout, st);
   }
   if (e == cudaSuccess)
     e = launch_tangent(c->m, a, c->precision != W3G_TANGENT_FP64, c->sched, c->s.counters + 1, st, tc);

@@ -345,10 +345,9 @@ cudaError_t init_tangent_tc_kernels();
 cudaError_t launch_tangent_tcg_hex8(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
                                     int* tc_timeout, cudaStream_t s);
 cudaError_t init_tangent_tcg_kernels();
-// the 20-node bricks on the tensor cores (w3g_tangent_tc20.cu), split
-// operands always
-cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
-                                    cudaStream_t s);
+// the 20-node bricks on the tensor cores (w3g_tangent_tc20.cu)
+cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
+                                    int* tc_timeout, cudaStream_t s);
 cudaError_t init_tangent_tc20_kernels();
 cudaError_t launch_recover(const DeviceModel& m, const RecoverArgs& a, double* c_geo, const Schedule& sc,
                            int* counter, cudaStream_t s);

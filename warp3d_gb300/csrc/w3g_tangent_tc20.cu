@@ -17,17 +17,19 @@
 // 32 TMEM columns. The CUDA cores form the Gauss-point quantities and Y
 // (~1,900 multiply-adds per point, against ~8,000 for B^T D* B + G^T T G).
 //
-// Operand precision: rounding N_A to TF32 or BF16 does NOT keep the exact
-// rigid-translation null space here (the 27-point rule has no mirror
-// symmetry of dN/dxi between nodes), and a rounded Y breaks the node sums
-// of the columns. So both operands are always split, x = hi + lo in the
-// input format, and the product is hi*hi + hi*lo + lo*hi (three MMAs): the
-// TF32 and TF32x3 requests both give TF32x3 accuracy on these elements,
-// BF16 and BF16x3 BF16x3 accuracy, with the translation null space kept to
-// the FP32 accumulation level.
+// Operand precision: rounding N_A or Y to TF32 or BF16 does NOT keep the
+// exact rigid-translation null space here (the 27-point rule has no mirror
+// symmetry of dN/dxi between nodes), and the tensor cores' FP32
+// accumulation adds an error with a mean along the translations; the
+// epilogue therefore projects the translations out of every node-pair
+// block, which leaves them at the FP32 rounding level whatever the operand
+// rounding. TF32 requests round both operands once (one MMA per k-step);
+// TF32x3 splits them, x = hi + lo in the input format, and accumulates
+// hi*hi + hi*lo + lo*hi (three MMAs); BF16 and BF16x3 requests both take
+// the split operands (see launch_tangent_tc_hex20).
 //
-// One CTA of 6 warps per record of up to 8 elements of a block, elements in
-// turn, two (BF16) or one (TF32) CTAs per SM:
+// One CTA of 8 warps per record of up to 8 elements of a block, elements in
+// turn, two CTAs per SM (one for TF32x3, by shared memory):
 //   (0) the element's coordinates at n+1 relative to its node 1 (cdest /
 //       edest gathers);
 //   (1)-(3) warp k = thread k of every Gauss point (lane = point):
@@ -38,9 +40,10 @@
 //       split and written into the A operand (K-major, no swizzle);
 //   (5) thread 0 issues the 3 x K/k-step MMAs and commits to an mbarrier;
 //   (6) warps 0-3 read the accumulator (tcgen05.ld, each warp its lane
-//       quadrant), scale by beta_fact and scatter each element's packed
-//       upper triangle (utsz = 1830, setup.f:265-275) into shared memory,
-//       stored coalesced as FP32.
+//       quadrant) into shared memory; the rigid translations are projected
+//       out of every node-pair block, scaled by beta_fact and the packed
+//       upper triangle (utsz = 1830, setup.f:265-275) stored coalesced as
+//       FP32.
 // The one wait (for the MMAs) is bounded by TangentArgs::wait_limit; a wait
 // that gives up drains the MMAs (bounded), fills NaN Ke for every element of
 // the CTA not finished and sets the timeout flag (W3G_EFATAL). A limit of 0
@@ -76,7 +79,7 @@ struct Tc20Inputs {
   double rot[NG * 9], urcs[NG * 9];
 };
 
-template <bool kBF16>
+template <bool kBF16, bool kSplit>
 struct Op {
   static constexpr int kBytes = kBF16 ? 2 : 4;
   static constexpr int kPerCore = 16 / kBytes;              // K values per core-matrix row
@@ -86,11 +89,13 @@ struct Op {
   // next 8-row group: 16 bytes more than the group's K extent, so that the
   // stores of 32 consecutive rows fall into distinct banks
   static constexpr int kSBO = (kK / kPerCore) * 128 + 16;
-  static constexpr int kOpA = (kM / 8) * kSBO;              // hi part; the lo part follows
+  static constexpr int kOpA = (kM / 8) * kSBO;              // hi part; the lo part follows (split)
   static constexpr int kOpB = (kCols / 8) * kSBO;
+  static constexpr int kParts = kSplit ? 2 : 1;
+  static constexpr int kPerSm = (kBF16 || !kSplit) ? 2 : 1;   // CTAs per SM (shared memory)
   static constexpr int kOffB = 0;
-  static constexpr int kOffA = kOffB + 2 * kOpB;
-  static constexpr int kOffIn = kOffA + 2 * kOpA;           // two Tc20Inputs: this and the next element
+  static constexpr int kOffA = kOffB + kParts * kOpB;
+  static constexpr int kOffIn = kOffA + kParts * kOpA;           // two Tc20Inputs: this and the next element
   static constexpr int kSmem = kOffIn + 2 * (int)sizeof(Tc20Inputs);
   // byte offset of (row, k) in a K-major no-swizzle operand
   __device__ static __forceinline__ int off(int row, int k) {
@@ -203,14 +208,6 @@ __device__ __forceinline__ void tc20_phase3(Tc20Static& T, int g, int slot) {
   }
 }
 
-// the split parts of v in the input format: hi = round(v), lo = round(v - hi)
-template <bool kBF16>
-__device__ __forceinline__ void put_hilo(unsigned char* op, int op_bytes, int o, float v) {
-  const float hi = round_in<kBF16>(v);
-  put<kBF16>(op, o, hi);
-  put<kBF16>(op + op_bytes, o, v - hi);
-}
-
 // the CTA's elements in sequence: records blockIdx.x, blockIdx.x + grid, ...
 // and their elements in turn; advances (t, e) and fills the descriptor
 __device__ __forceinline__ bool tc20_next(const TcgTile* tiles, int ntiles, int& t, int& e, Tc20Elem& d) {
@@ -259,10 +256,85 @@ __device__ __forceinline__ void tc20_prefetch(const TangentArgs& a, const Tc20El
   asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-template <bool kBF16>
-__global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(TangentArgs a, const TcgTile* tiles, int ntiles,
-                                                                int* tc_timeout) {
-  using O = Op<kBF16>;
+// accumulator of one element -> packed Ke in T.ke, with the rigid
+// translations projected out of every node-pair block: K' = P S P,
+// P = I - 11^T / 20, S the block as stored (a diagonal block's upper
+// triangle mirrored). The tensor cores' FP32 accumulation is not
+// sign-symmetric, so its error has a mean along the translations, the same
+// in every element, which the soft modes of a yielded mesh do not
+// tolerate; the exact Ke has these null vectors, so the projection only
+// removes error. raw: shared memory free during the epilogue (the start
+// of the A operand: the element's MMAs are done; the next element's Y
+// rewrites every value of the live rows, K padding included) for the 120
+// accumulator rows (pair, node b) x node a, then the row and column sums
+// of each pair.
+// Every thread of the CTA takes part (two barriers).
+__device__ __forceinline__ void tc20_epilogue(uint32_t tmem, int warp, int lane, int tid, Tc20Static& T, float* raw,
+                                              float bf) {
+  constexpr int kLd = NN + 1;            // odd row stride: a warp's 32 rows in distinct banks
+  float* sums = raw + kRowsLive * kLd;   // per pair slot: r_a (20), c_b (20)
+  if (warp < 4) {   // warp w reads lane quadrant w
+    const int row = 32 * warp + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
+    uint32_t v[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+          "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+          "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr), "r"(taddr + 16)
+        : "memory");
+    if (row < kRowsLive) {
+#pragma unroll
+      for (int an = 0; an < NN; ++an) raw[row * kLd + an] = __uint_as_float(v[an]);
+    }
+  }
+  __syncthreads();
+  // K_ab of pair slot p sits in row (p, b), column a
+  if (tid < 6 * 2 * NN) {
+    const int slot = tid / (2 * NN), q = tid % (2 * NN);
+    const bool diag = slot == 0 || slot == 3 || slot == 5;
+    const float* r = raw + slot * NN * kLd;
+    float acc = 0.f;
+#pragma unroll 4
+    for (int t = 0; t < NN; ++t) {
+      const int an = q < NN ? q : t, b = q < NN ? t : q - NN;
+      acc += diag && an > b ? r[an * kLd + b] : r[b * kLd + an];
+    }
+    sums[slot * 2 * NN + q] = acc;
+  }
+  __syncthreads();
+  if (warp < 4) {
+    const int row = 32 * warp + lane;
+    if (row < kRowsLive) {
+      const int slot = row / NN, b = row % NN;
+      const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+      const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+      const int d2 = jj * NN + b;
+      const float* sm = sums + slot * 2 * NN;
+      float tot = 0.f;
+#pragma unroll
+      for (int t = 0; t < NN; ++t) tot += sm[t];
+      const float cb = sm[NN + b] - 0.05f * tot;
+#pragma unroll
+      for (int an = 0; an < NN; ++an) {
+        if (ii == jj && an > b) continue;
+        const int d1 = ii * NN + an;
+        const float kp = raw[row * kLd + an] - 0.05f * (sm[an] + cb);
+        T.ke[d2 * (d2 + 1) / 2 + d1] = kp * bf;
+      }
+    }
+  }
+}
+
+template <bool kBF16, bool kSplit>
+__global__ void __launch_bounds__(kThreads, Op<kBF16, kSplit>::kPerSm) k_tangent_tc_hex20(
+    TangentArgs a, const TcgTile* tiles, int ntiles, int* tc_timeout) {
+  using O = Op<kBF16, kSplit>;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* opB = smem + O::kOffB;
   unsigned char* opA = smem + O::kOffA;
@@ -292,14 +364,14 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
     if (row < NN && k < kKLive) v = dnd[k * NN + row];   // k = gp*3 + r
     const float hi = round_in<kBF16>((float)v);
     put<kBF16>(opB, O::off(row, k), hi);
-    put<kBF16>(opB + O::kOpB, O::off(row, k), (float)(v - (double)hi));
+    if (kSplit) put<kBF16>(opB + O::kOpB, O::off(row, k), (float)(v - (double)hi));
   }
   // A rows 120..127 and the K padding stay zero (finite) for every element
   for (int idx = tid; idx < kM * O::kK; idx += kThreads) {
     const int row = idx / O::kK, k = idx % O::kK;
     if (row >= kRowsLive || k >= kKLive) {
       put<kBF16>(opA, O::off(row, k), 0.f);
-      put<kBF16>(opA + O::kOpA, O::off(row, k), 0.f);
+      if (kSplit) put<kBF16>(opA + O::kOpA, O::off(row, k), 0.f);
     }
   }
   // the first element's inputs
@@ -394,34 +466,7 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
         if (tid == 0) T.fail_n = n - 1;
         break;
       }
-      if (warp < 4) {   // warp w reads lane quadrant w
-        const int row = 32 * warp + lane;
-        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
-        uint32_t v[32];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
-            "tcgen05.wait::ld.sync.aligned;"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
-              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-              "=r"(v[30]), "=r"(v[31])
-            : "r"(taddr), "r"(taddr + 16)
-            : "memory");
-        if (row < kRowsLive) {
-          const int slot = row / NN, b = row % NN;
-          const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
-          const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
-          const int d2 = jj * NN + b;
-#pragma unroll
-          for (int an = 0; an < NN; ++an) {
-            if (ii == jj && an > b) continue;
-            const int d1 = ii * NN + an;
-            T.ke[d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[an]) * bf;
-          }
-        }
-      }
+      tc20_epilogue(tmem, warp, lane, tid, T, reinterpret_cast<float*>(opA), bf);
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       float* out = reinterpret_cast<float*>(a.estiff) + prev.estiff_off + (long long)prev.i * UT;
@@ -429,7 +474,9 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
     }
     // (4) Y of element n into the A operand (element n - 1's MMAs are
     // complete): 240 threads, one per row (pair, node b) and half of the
-    // Gauss points
+    // Gauss points; the second half also rewrites the row's K padding with
+    // zeros (the epilogue's scratch overwrote it in the first rows, and a
+    // bit pattern that decodes as Inf or NaN would turn 0 x pad into NaN)
     if (tid < 2 * kRowsLive) {
       const int row = tid % kRowsLive, half = tid / kRowsLive;
       const int slot = row / NN, b = row % NN;
@@ -441,8 +488,10 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
                     n2 = T.dn[(gp * 3 + 2) * NN + b];
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-          put_hilo<kBF16>(opA, O::kOpA, O::off(row, gp * 3 + r), h[3 * r] * n0 + h[3 * r + 1] * n1 + h[3 * r + 2] * n2);
+          put_split<kBF16, kSplit>(opA, O::kOpA, O::off(row, gp * 3 + r), h[3 * r] * n0 + h[3 * r + 1] * n1 + h[3 * r + 2] * n2);
       }
+      if (half)
+        for (int k = kKLive; k < O::kK; ++k) put_split<kBF16, kSplit>(opA, O::kOpA, O::off(row, k), 0.f);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
@@ -458,8 +507,10 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
       for (int ks = 0; ks < O::kSteps; ++ks) {
         const uint64_t o = (uint64_t)ks * (256 >> 4);   // one k-step = two core matrices along K
         mma20<kBF16>(tmem, da + o, db + o, ks > 0);
-        mma20<kBF16>(tmem, da + o, dbl + o, true);
-        mma20<kBF16>(tmem, dal + o, db + o, true);
+        if (kSplit) {
+          mma20<kBF16>(tmem, da + o, dbl + o, true);
+          mma20<kBF16>(tmem, dal + o, db + o, true);
+        }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           su32(&T.mma)) : "memory");
@@ -479,34 +530,7 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
     if (T.abort) {
       if (tid == 0) T.fail_n = n - 1;
     } else {
-      if (warp < 4) {
-        const int row = 32 * warp + lane;
-        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16);
-        uint32_t v[32];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
-            "tcgen05.wait::ld.sync.aligned;"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
-              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-              "=r"(v[30]), "=r"(v[31])
-            : "r"(taddr), "r"(taddr + 16)
-            : "memory");
-        if (row < kRowsLive) {
-          const int slot = row / NN, b = row % NN;
-          const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
-          const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
-          const int d2 = jj * NN + b;
-#pragma unroll
-          for (int an = 0; an < NN; ++an) {
-            if (ii == jj && an > b) continue;
-            const int d1 = ii * NN + an;
-            T.ke[d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[an]) * bf;
-          }
-        }
-      }
+      tc20_epilogue(tmem, warp, lane, tid, T, reinterpret_cast<float*>(opA), bf);
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       float* out = reinterpret_cast<float*>(a.estiff) + prev.estiff_off + (long long)prev.i * UT;
@@ -532,37 +556,50 @@ __global__ void __launch_bounds__(kThreads, kBF16 ? 2 : 1) k_tangent_tc_hex20(Ta
   }
 }
 
-template <bool kBF16>
+template <bool kBF16, bool kSplit>
 cudaError_t set_attr20() {
-  return cudaFuncSetAttribute(k_tangent_tc_hex20<kBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Op<kBF16>::kSmem);
+  return cudaFuncSetAttribute(k_tangent_tc_hex20<kBF16, kSplit>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Op<kBF16, kSplit>::kSmem);
 }
 
-static_assert(Op<false>::kSmem + sizeof(Tc20Static) <= 227 * 1024, "TF32 form exceeds shared memory");
-static_assert(Op<true>::kSmem + sizeof(Tc20Static) <= 227 * 1024, "BF16 form exceeds shared memory");
-static_assert(Op<false>::kOffA % 16 == 0 && Op<true>::kOffA % 16 == 0, "operands must be 16-byte aligned");
-static_assert(Op<false>::kOffIn % 16 == 0 && Op<true>::kOffIn % 16 == 0, "staging must be 16-byte aligned");
-static_assert(2 * (Op<true>::kSmem + sizeof(Tc20Static)) <= 226 * 1024, "two BF16 CTAs per SM");
+template <bool kBF16, bool kSplit>
+cudaError_t launch20(const DeviceModel& m, const TangentArgs& a, int* tc_timeout, cudaStream_t s) {
+  using O = Op<kBF16, kSplit>;
+  // as many CTAs as fit (1-2 per SM by shared memory), records taken in turn
+  const int grid = m.ntc20tiles < m.nsm * O::kPerSm ? m.ntc20tiles : m.nsm * O::kPerSm;
+  k_tangent_tc_hex20<kBF16, kSplit><<<grid, kThreads, O::kSmem, s>>>(a, m.tc20tiles, m.ntc20tiles, tc_timeout);
+  return cudaGetLastError();
+}
+
+template <bool kBF16, bool kSplit>
+constexpr bool fits() {
+  using O = Op<kBF16, kSplit>;
+  return O::kPerSm * (O::kSmem + (int)sizeof(Tc20Static)) <= 226 * 1024 && O::kOffA % 16 == 0 &&
+         O::kOffIn % 16 == 0 && (kRowsLive * (NN + 1) + 12 * NN) * 4 <= O::kOpA;
+}
+static_assert(fits<false, false>() && fits<false, true>() && fits<true, true>(),
+              "shared memory: operands, staging and CTAs per SM; the epilogue scratch in the A operand");
 static_assert(UT * 4 <= 8 * 1024, "Ke staging");
 
 }  // namespace
 
 cudaError_t init_tangent_tc20_kernels() {
-  cudaError_t e = set_attr20<false>();
-  return e == cudaSuccess ? set_attr20<true>() : e;
+  cudaError_t e = set_attr20<false, false>();
+  if (e == cudaSuccess) e = set_attr20<false, true>();
+  return e == cudaSuccess ? set_attr20<true, true>() : e;
 }
 
-cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, int* tc_timeout,
-                                    cudaStream_t s) {
+// BF16 requests always take split operands here: with one BF16 rounding of
+// the 27-point rule's operands (Ke error ~2e-3, the same operator error in
+// every element) the Newton solve of the mixed hex8/hex20/tet10 bars
+// diverged and met an indefinite K_ff in its first step, while the split
+// operands converge in the FP32 tangent's iterations. TF32 keeps its single
+// rounding (the FP32 tangent's iterations on the same problem).
+cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
+                                    int* tc_timeout, cudaStream_t s) {
   if (m.ntc20tiles == 0) return cudaSuccess;
-  // as many CTAs as fit (1-2 per SM by shared memory), records taken in turn
-  const int per_sm = bf16 ? 2 : 1;
-  const int grid = m.ntc20tiles < m.nsm * per_sm ? m.ntc20tiles : m.nsm * per_sm;
-  if (bf16)
-    k_tangent_tc_hex20<true><<<grid, kThreads, Op<true>::kSmem, s>>>(a, m.tc20tiles, m.ntc20tiles, tc_timeout);
-  else
-    k_tangent_tc_hex20<false><<<grid, kThreads, Op<false>::kSmem, s>>>(a, m.tc20tiles, m.ntc20tiles, tc_timeout);
-  return cudaGetLastError();
+  if (bf16) return launch20<true, true>(m, a, tc_timeout, s);
+  return split ? launch20<false, true>(m, a, tc_timeout, s) : launch20<false, false>(m, a, tc_timeout, s);
 }
 
 }  // namespace w3g

@@ -32,9 +32,10 @@
 // perturbs the material point values, which keeps that property too, as
 // long as the diagonal pairs' H^ii stay exactly symmetric after rounding
 // (only the upper triangle of Ke is stored, the lower one is its mirror):
-// they are formed for r <= s and written to both positions. What remains
-// is the FP32 accumulation (as in the FP32 CUDA-core kernel), so no
-// projection onto the translation-free matrices is needed.
+// they are formed for r <= s and written to both positions. The tensor
+// cores' FP32 accumulation does not keep it: its error has a mean along
+// the translations, the same in every element, so the epilogue projects
+// the translations out of every node-pair block.
 //
 // The kernel is persistent (one CTA per SM) and pipelined:
 //   warp 24 (producer) per tile, into a ring of shared-memory stages:
@@ -58,10 +59,11 @@
 //                      operand (K-major, no swizzle); thread 0 issues the
 //                      MMA chain (M is built once per CTA as the B
 //                      operand); warps 0-15 read the accumulator with
-//                      tcgen05.ld, each element's packed upper triangle
-//                      (utsz, span layout, setup.f:265-275) is staged in
-//                      shared memory and written with one bulk copy to
-//                      global memory (cp.async.bulk.global.shared::cta).
+//                      tcgen05.ld, project the translations out, and each
+//                      element's packed upper triangle (utsz, span layout,
+//                      setup.f:265-275) is staged in shared memory and
+//                      written with one bulk copy to global memory
+//                      (cp.async.bulk.global.shared::cta).
 //                      Six short threads per point instead of two long
 //                      ones: 24 warps hide the arithmetic and shared-
 //                      memory latencies that 8 warps at 168 registers
@@ -113,6 +115,10 @@ constexpr int kStage = kStXdu + kTile * TOT * 8;  // 49312
 static_assert(kStage % 128 == 0 || kStage % 16 == 0, "stage alignment");
 
 constexpr int kPtBytes = kPtN * kPoints * 4;
+// epilogue scratch inside the point scratch: per accumulator row, the four
+// column quarters' shares of 8 sums (row-fastest: a warp's 32 rows in
+// distinct banks)
+static_assert(4 * 8 * 128 * 4 <= kPtBytes, "epilogue scratch must fit the point scratch");
 
 template <bool kBF16, bool kSplit>
 struct Form {
@@ -261,6 +267,21 @@ __constant__ PairIdx c_pair = make_pair_idx();
 // {T}[r][q], into A operand row (slot, element e), k = (r*3 + s)*8 + gp.
 // One code path for the six pairs (indices from a table): specialised
 // copies let the compiler hoist the union of their loads and spill.
+// 16 accumulator columns of the warp's lane quadrant (the load and its wait
+// in one statement)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
+  uint32_t v[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int c = 0; c < 16; ++c) out[c] = __uint_as_float(v[c]);
+}
+
 template <bool kBF16, bool kSplit>
 __device__ __forceinline__ void tcg_phase3(float* pt, int p, int e, int gp, int slot, unsigned char* opA) {
   using F = Form<kBF16, kSplit>;
@@ -574,33 +595,79 @@ __global__ void __launch_bounds__(kThreads, 1) k_tangent_tcg_hex8(TangentArgs a,
       asm volatile("tcgen05.fence::after_thread_sync;");
       asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
       if (*cabort) break;
-      // accumulator -> packed Ke in the staging (the A region: the MMAs are
-      // done). Warp w < 16 reads TMEM lane quadrant w % 4 (the quadrant a
-      // warp may access), columns 16 (w / 4) .. + 15
+      // accumulator -> Ke. The tensor cores' FP32 accumulation is not
+      // sign-symmetric: its error has a mean, the same in every element,
+      // along the rigid translations, which a plastic mesh's softest modes
+      // do not tolerate (Newton stalls or K_ff turns indefinite). So each
+      // node-pair block leaves with the translations projected out,
+      // K' = P S P, P = I - 11^T / 8, S the block as stored (a diagonal
+      // block's upper triangle mirrored); the exact Ke has these null
+      // vectors, so the projection only removes error.
+      // Warp w < 16 reads TMEM lane quadrant w % 4 (the quadrant a warp may
+      // access), columns 16 (w / 4) .. + 15: rows x = 2 (w / 4), + 1 of its
+      // lane's block. (1) Each thread publishes its share q_b of the block's
+      // column sums (off-diagonal blocks) or of the row sums of S (diagonal
+      // blocks: the upper part of its rows, the mirrored part of the rows
+      // below), b = 0..7, in the point scratch (free until the next tile's
+      // phase 1); its own rows' sums stay in registers. (2) After one
+      // barrier it adds its lane's four shares, reloads its accumulator
+      // values and packs S_xb - (r_x + c_b) / 8 + (sum of S) / 64, times
+      // beta_fact, into the staging (the A region: the MMAs are done).
+      float* part = reinterpret_cast<float*>(smem + F::kOffPt);   // [4 column quarters][8][kM rows]
+      const int quad = warp & 3, cq = warp >> 2;
+      const int row = 32 * quad + lane, e = row & (kTile - 1), slot = row >> 4;
+      const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
+      const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
+      const bool diag = ii == jj;
+      const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(16 * cq);
+      float rs0 = 0.f, rs1 = 0.f;   // row sums of rows 2 cq, 2 cq + 1 (off-diagonal blocks)
       if (warp < 16) {
-        float* ke = reinterpret_cast<float*>(opA);
-        const int quad = warp & 3, cq = warp >> 2;
-        const int row = 32 * quad + lane, e = row & (kTile - 1), slot = row >> 4;
-        const uint32_t taddr = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(16 * cq);
-        const int ii = slot < 3 ? 0 : (slot < 5 ? 1 : 2);
-        const int jj = slot < 3 ? slot : (slot == 3 ? 1 : 2);
-        const bool keep = slot < 6 && e < tn;
-        const float bf = (float)a.beta_fact;
-        uint32_t v[16];   // the load and its wait in one statement
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-            "tcgen05.wait::ld.sync.aligned;"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-            : "r"(taddr)
-            : "memory");
-        if (keep) {
+        float v[16];
+        tmem_ld16(taddr, v);
+        float q[8];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+          const int x0 = 2 * cq, x1 = 2 * cq + 1;
+          // diagonal: S_xb = K_xb for b >= x contributes to r_x (below);
+          // for b > x it is also S_bx and contributes to r_b
+          q[b] = diag ? (b > x0 ? v[b] : 0.f) + (b > x1 ? v[8 + b] : 0.f) : v[b] + v[8 + b];
+          rs0 += diag && b < x0 ? 0.f : v[b];
+          rs1 += diag && b < x1 ? 0.f : v[8 + b];
+        }
+        if (diag) {   // the thread's own rows enter the shared sums
+#pragma unroll
+          for (int b = 0; b < 8; ++b) q[b] += b == 2 * cq ? rs0 : (b == 2 * cq + 1 ? rs1 : 0.f);
+        }
+#pragma unroll
+        for (int b = 0; b < 8; ++b) part[(cq * 8 + b) * kM + row] = q[b];
+      }
+      asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
+      if (warp < 16) {
+        // the load is warp-collective (.sync.aligned): every lane of the
+        // warp executes it, whatever its row
+        float v[16];
+        tmem_ld16(taddr, v);
+        if (slot < 6 && e < tn) {
+          float* ke = reinterpret_cast<float*>(opA);
+          const float bf = (float)a.beta_fact;
+          float sb[8], tot = 0.f;
+#pragma unroll
+          for (int b = 0; b < 8; ++b) {
+            sb[b] = part[b * kM + row] + part[(8 + b) * kM + row] + part[(16 + b) * kM + row] +
+                    part[(24 + b) * kM + row];
+            tot += sb[b];
+          }
+          // diagonal: sb = row sums of S (= its column sums); off-diagonal:
+          // sb = column sums, rs = the thread's row sums
+          const float r0 = diag ? sb[2 * cq] : rs0, r1 = diag ? sb[2 * cq + 1] : rs1;
+          const float t64 = 0.015625f * tot;
 #pragma unroll
           for (int c = 0; c < 16; ++c) {
-            const int ab = 16 * cq + c, an = ab >> 3, bn = ab & 7;
-            if (ii == jj && an > bn) continue;
+            const int an = 2 * cq + (c >> 3), bn = c & 7;
+            if (diag && an > bn) continue;
             const int d1 = ii * NN + an, d2 = jj * NN + bn;
-            ke[e * UT + d2 * (d2 + 1) / 2 + d1] = __uint_as_float(v[c]) * bf;
+            const float kp = v[c] - 0.125f * ((c < 8 ? r0 : r1) + sb[bn]) + t64;
+            ke[e * UT + d2 * (d2 + 1) / 2 + d1] = kp * bf;
           }
         }
       }
