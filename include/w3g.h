@@ -197,9 +197,8 @@ const char* w3g_last_error(void);
    widens to double only when host estiff pointers are given. The tensor-
    core forms (TF32, BF16, and their split X3 variants) cover 8-node and
    20-node bricks, each element matrix with the rigid translations
-   projected out after the accumulation (BF16 requests take the split
-   operands on 20-node bricks); tetrahedra take the FP32 kernel in the
-   same call. w3g_tanstf returns W3G_EFATAL if a tensor-core tile's
+   projected out after the accumulation; tetrahedra take the FP32 kernel
+   in the same call. w3g_tanstf returns W3G_EFATAL if a tensor-core tile's
    bounded wait for its MMAs gave up (that tile's Ke is then NaN). */
 int w3g_set_tangent_precision(w3g_context* ctx, int precision);
 

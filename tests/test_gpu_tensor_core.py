@@ -296,9 +296,10 @@ def test_tensor_core_tangent_in_a_graph_replay_equals_direct_launch(plastic_hex8
     eng.set_precision(abi.TANGENT_FP64)
 
 
-# the 20-node bricks' tensor-core kernel: TF32 rounds the operands once,
-# TF32X3 splits them, and both BF16 requests take the split operands
-TOL20 = {abi.TANGENT_TF32: 2e-3, abi.TANGENT_BF16: 1e-4, abi.TANGENT_TF32X3: 1e-5, abi.TANGENT_BF16X3: 1e-4}
+# the 20-node bricks' tensor-core kernel: the single forms round the
+# element's Y once (BF16 with the constant N_A split), the X3 forms split
+# both operands: the 8-node bricks' bounds
+TOL20 = dict(TOL)
 
 
 @pytest.fixture(scope="module")

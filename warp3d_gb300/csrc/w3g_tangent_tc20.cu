@@ -24,9 +24,10 @@
 // epilogue therefore projects the translations out of every node-pair
 // block, which leaves them at the FP32 rounding level whatever the operand
 // rounding. TF32 requests round both operands once (one MMA per k-step);
-// TF32x3 splits them, x = hi + lo in the input format, and accumulates
-// hi*hi + hi*lo + lo*hi (three MMAs); BF16 and BF16x3 requests both take
-// the split operands (see launch_tangent_tc_hex20).
+// BF16 requests round Y once and split the constant N_A, x = hi + lo in
+// the input format (Y*hi + Y*lo: two MMAs; see launch_tangent_tc_hex20);
+// the X3 forms split both and accumulate hi*hi + hi*lo + lo*hi (three
+// MMAs).
 //
 // One CTA of 8 warps per record of up to 8 elements of a block, elements in
 // turn, two CTAs per SM (one for TF32x3, by shared memory):
@@ -91,10 +92,12 @@ struct Op {
   static constexpr int kSBO = (kK / kPerCore) * 128 + 16;
   static constexpr int kOpA = (kM / 8) * kSBO;              // hi part; the lo part follows (split)
   static constexpr int kOpB = (kCols / 8) * kSBO;
-  static constexpr int kParts = kSplit ? 2 : 1;
+  static constexpr int kParts = kSplit ? 2 : 1;             // A operand parts
+  static constexpr bool kSplitB = kSplit || kBF16;          // N_A as hi + lo
+  static constexpr int kPartsB = kSplitB ? 2 : 1;
   static constexpr int kPerSm = (kBF16 || !kSplit) ? 2 : 1;   // CTAs per SM (shared memory)
   static constexpr int kOffB = 0;
-  static constexpr int kOffA = kOffB + kParts * kOpB;
+  static constexpr int kOffA = kOffB + kPartsB * kOpB;
   static constexpr int kOffIn = kOffA + kParts * kOpA;           // two Tc20Inputs: this and the next element
   static constexpr int kSmem = kOffIn + 2 * (int)sizeof(Tc20Inputs);
   // byte offset of (row, k) in a K-major no-swizzle operand
@@ -364,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, Op<kBF16, kSplit>::kPerSm) k_tangent
     if (row < NN && k < kKLive) v = dnd[k * NN + row];   // k = gp*3 + r
     const float hi = round_in<kBF16>((float)v);
     put<kBF16>(opB, O::off(row, k), hi);
-    if (kSplit) put<kBF16>(opB + O::kOpB, O::off(row, k), (float)(v - (double)hi));
+    if (O::kSplitB) put<kBF16>(opB + O::kOpB, O::off(row, k), (float)(v - (double)hi));
   }
   // A rows 120..127 and the K padding stay zero (finite) for every element
   for (int idx = tid; idx < kM * O::kK; idx += kThreads) {
@@ -507,10 +510,8 @@ __global__ void __launch_bounds__(kThreads, Op<kBF16, kSplit>::kPerSm) k_tangent
       for (int ks = 0; ks < O::kSteps; ++ks) {
         const uint64_t o = (uint64_t)ks * (256 >> 4);   // one k-step = two core matrices along K
         mma20<kBF16>(tmem, da + o, db + o, ks > 0);
-        if (kSplit) {
-          mma20<kBF16>(tmem, da + o, dbl + o, true);
-          mma20<kBF16>(tmem, dal + o, db + o, true);
-        }
+        if (O::kSplitB) mma20<kBF16>(tmem, da + o, dbl + o, true);
+        if (kSplit) mma20<kBF16>(tmem, dal + o, db + o, true);
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           su32(&T.mma)) : "memory");
@@ -577,7 +578,7 @@ constexpr bool fits() {
   return O::kPerSm * (O::kSmem + (int)sizeof(Tc20Static)) <= 226 * 1024 && O::kOffA % 16 == 0 &&
          O::kOffIn % 16 == 0 && (kRowsLive * (NN + 1) + 12 * NN) * 4 <= O::kOpA;
 }
-static_assert(fits<false, false>() && fits<false, true>() && fits<true, true>(),
+static_assert(fits<false, false>() && fits<false, true>() && fits<true, false>() && fits<true, true>(),
               "shared memory: operands, staging and CTAs per SM; the epilogue scratch in the A operand");
 static_assert(UT * 4 <= 8 * 1024, "Ke staging");
 
@@ -586,19 +587,20 @@ static_assert(UT * 4 <= 8 * 1024, "Ke staging");
 cudaError_t init_tangent_tc20_kernels() {
   cudaError_t e = set_attr20<false, false>();
   if (e == cudaSuccess) e = set_attr20<false, true>();
+  if (e == cudaSuccess) e = set_attr20<true, false>();
   return e == cudaSuccess ? set_attr20<true, true>() : e;
 }
 
-// BF16 requests always take split operands here: with one BF16 rounding of
-// the 27-point rule's operands (Ke error ~2e-3, the same operator error in
-// every element) the Newton solve of the mixed hex8/hex20/tet10 bars
-// diverged and met an indefinite K_ff in its first step, while the split
-// operands converge in the FP32 tangent's iterations. TF32 keeps its single
-// rounding (the FP32 tangent's iterations on the same problem).
+// BF16 requests split the constant N_A (hi + lo, two MMAs per k-step) and
+// round Y once: with N_A rounded once as well (Ke error ~2e-3, the same
+// operator error in every element) the Newton solve of the mixed
+// hex8/hex20/tet10 bars diverged and met an indefinite K_ff in its first
+// step. TF32 rounds both once (the FP32 tangent's iterations on the same
+// problem; a split N_A would leave room for one CTA per SM only).
 cudaError_t launch_tangent_tc_hex20(const DeviceModel& m, const TangentArgs& a, bool bf16, bool split,
                                     int* tc_timeout, cudaStream_t s) {
   if (m.ntc20tiles == 0) return cudaSuccess;
-  if (bf16) return launch20<true, true>(m, a, tc_timeout, s);
+  if (bf16) return split ? launch20<true, true>(m, a, tc_timeout, s) : launch20<true, false>(m, a, tc_timeout, s);
   return split ? launch20<false, true>(m, a, tc_timeout, s) : launch20<false, false>(m, a, tc_timeout, s);
 }
 
