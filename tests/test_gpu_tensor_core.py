@@ -348,6 +348,49 @@ def test_tensor_core_tangent_hex20(plastic_hex20, precision):
     assert worst <= 1e-6
 
 
+@pytest.fixture(scope="module")
+def plastic_hex20_many_records():
+    """14^3 20-node bricks in random blocks of 1..128: 361 records of up to
+    8 elements over 152-304 CTAs, so CTAs cross records (the small model
+    gives each CTA one). State: one recovery from the virgin state over an
+    affine increment with noise (plastic)."""
+    spans = random_spans(14 ** 3, np.random.Generator(np.random.PCG64(5)), lo=1, hi=128)
+    model, _ = make_model(n=14, jitter=0.05, spans=spans, etype=abi.ETYPE_Q3DISOP)
+    c = model.coords
+    du = np.zeros(model.nodof)
+    du[2::3] = 0.004 * c[:, 2]
+    du[0::3] = 0.0015 * c[:, 2]
+    du += np.random.Generator(np.random.PCG64(11)).normal(0.0, 2e-4, model.nodof)
+    u = np.zeros(model.nodof)
+    ora = oracle.Oracle(model)
+    eng = _engine(model)
+    ifv = np.zeros(model.nodof)
+    st, info = ora.recover(2, 2, False, model.c, u, du, ifv.copy())
+    assert st == 0 and info.plastic_work > 0.0
+    assert eng.recover(2, 2, False, model.c, u, du, ifv)[0] == 0
+    return model, eng, ora, u, du
+
+
+@pytest.mark.parametrize("precision", ALL)
+def test_tensor_core_tangent_hex20_several_records_per_cta(plastic_hex20_many_records, precision):
+    model, eng, ora, u, du = plastic_hex20_many_records
+    eng.set_precision(precision)
+    err = _tangent_err(model, eng, ora, 2, 2, u, du)
+    est = model.estiff_blocks()
+    eng.tanstf(2, 2, model.c, u, du, est)
+    eng.set_precision(abi.TANGENT_FP64)
+    worst = 0.0
+    for blk in est:
+        K = _unpack20(blk)
+        scale = np.max(np.abs(K), axis=(1, 2))
+        for d in range(3):
+            t = np.zeros(60)
+            t[20 * d:20 * d + 20] = 1.0
+            worst = max(worst, float(np.max(np.max(np.abs(K @ t), axis=1) / scale)))
+    print(f"hex20 {NAMES[precision]} 2,744 elements: rel err {err:.2e}, max |Ke t| / max |Ke| = {worst:.1e}")
+    assert err <= TOL20[precision] and worst <= 1e-6
+
+
 def test_tensor_core_hex20_wait_limit_zero_reports_efatal(plastic_hex20):
     model, eng, ora, u, du = plastic_hex20
     eng.set_precision(abi.TANGENT_TF32)
