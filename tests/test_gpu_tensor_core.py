@@ -2,12 +2,17 @@
 accumulation, tcgen05.mma) against the FP64 oracle.
 
 Element matrices: per element, max |Ke_gpu - Ke_oracle| / max |Ke_oracle|.
-The operands B and [D*]B are rounded once to the input format and the
-products accumulate in FP32, so the error scales with the format's unit
-roundoff: TF32 (10 stored mantissa bits, u = 2^-11) stays below 2e-3 and
-BF16 (7 bits, u = 2^-8) below 2e-2 of the element's largest entry. The
-split forms (x = hi + lo in the input format, three MMAs per product)
-carry about twice the bits: TF32X3 below 1e-5, BF16X3 below 2e-4.
+The operands (8-node displacement bricks: the material-point values H and
+the constant node-pair operator M; b-bar bricks: B and [D*]B; 20-node
+bricks: Y = H n_b and the constant N_A) are rounded once to the input
+format and the products accumulate in FP32, so the error scales with the
+format's unit roundoff: TF32 (10 stored mantissa bits, u = 2^-11) stays
+below 2e-3 and BF16 (7 bits, u = 2^-8) below 2e-2 of the element's
+largest entry. The split forms (x = hi + lo in the input format, three
+MMAs per product) carry about twice the bits: TF32X3 below 1e-5, BF16X3
+below 2e-4. Every kernel projects the rigid translations out of each
+element matrix after the accumulation, so Ke t stays at the FP32
+rounding level.
 
 Newton: the precision form changes only the tangent, never the residual,
 so the solution at the 1e-8 relative residual is the FP64 one; the cost is
