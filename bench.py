@@ -133,6 +133,8 @@ def parse():
     ap.add_argument("--batched-study", action="store_true",
                     help="instead of the bench line: Newton solves of the mixed-type bars, FP64 and FP32 tangent")
     ap.add_argument("--study-section", type=int, default=32, help="cells per side of the bars' section")
+    ap.add_argument("--crystal-study", action="store_true",
+                    help="instead of the bench line: Newton solves of the mm10 polycrystal per tangent form")
     return ap.parse_args()
 
 
@@ -976,6 +978,40 @@ def batched_study(args, dev):
             "forms": forms}
 
 
+def crystal_study(args, dev):
+    """The precision forms on the mm10 polycrystal of the crystal line
+    (crystal_n^3 8-node bricks, fcc, Euler angles uniform on SO(3), Voce)
+    under uniaxial tension, args.study_strain in args.study_steps equal
+    steps, every Newton iteration on the device (element path with the mm10
+    local solves, CSR assembly, Jacobi PCG, residual norms) to the 1e-8
+    relative residual; a step whose local solves fail is subdivided.
+    Per form: Newton iterations per step, PCG iterations, wall time and the
+    final displacements' error against the FP64 run."""
+    from warp3d_gb300.engine import Engine
+    from warp3d_gb300.model import Crystal, Model, cube_mesh, random_orientations
+    from warp3d_gb300.newton import uniaxial_bcs
+    from warp3d_gb300.solver import DeviceCsr
+    n = args.crystal_n
+    coords, incid = cube_mesh(n)
+    model = Model(coords, incid, materials=[Crystal()], angles=random_orientations(n ** 3, 4242), dt=1.0)
+    fixed, topz = uniaxial_bcs(model, (n, n, n))
+    t0 = time.perf_counter()
+    eng = Engine(model)
+    csr = DeviceCsr(eng)
+    setup_s = time.perf_counter() - t0
+    forms, _, _ = newton_forms(args, model, fixed, topz, n, args.study_forms.split(","), eng, csr)
+    out = {"workload": f"{n}^3 hex8 mm10 fcc polycrystal (random orientations, Voce), uniaxial "
+                       f"{100 * args.study_strain:g}% in {args.study_steps} steps",
+           "elements": model.noelem, "dofs": model.nodof, "csr_nnz": csr.nnz, "setup_s": setup_s,
+           "newton_tol": 1e-8,
+           "pcg_rtol": 1e-10 if args.study_forcing == "fixed" else
+           f"Eisenstat-Walker (gamma 0.9, eta_max {args.study_eta_max:g}, floor 1e-10)",
+           "forms": forms}
+    csr.close()
+    eng.close()
+    return out
+
+
 def precision_study(args, dev):
     """The precision forms on the n^3 cube (mm01, jitter 0.1h, blocks of
     128) under uniaxial tension, args.study_strain in args.study_steps
@@ -1128,6 +1164,9 @@ def main():
         return
     if args.type_study:
         print(json.dumps({"type_study": type_study(args, dev)}))
+        return
+    if args.crystal_study:
+        print(json.dumps({"crystal_study": crystal_study(args, dev)}))
         return
 
     from warp3d_gb300 import abi
