@@ -901,7 +901,7 @@ def newton_forms(args, model, fixed, topz, nz, names, eng, csr):
     initial = model.new_state()
     eng.set_precision(STUDY_FORMS["fp64"])
     eng.download(initial)
-    forms, u_ref, end_state = {}, None, None
+    forms, u_ref, end_state, steps_ref = {}, None, None, 0
     for name in names:
         eng.set_precision(STUDY_FORMS[name])
         eng.upload(initial)
@@ -940,10 +940,12 @@ def newton_forms(args, model, fixed, topz, nz, names, eng, csr):
             os.makedirs(args.study_save_u, exist_ok=True)
             np.save(os.path.join(args.study_save_u, f"u_{name}.npy"), u)
         if name == "fp64":
-            u_ref = u
+            u_ref, steps_ref = u, len(rec["steps"])
             end_state = model.new_state()
             eng.download(end_state)
-        elif u_ref is not None and rec["failed"] is None:
+        elif u_ref is not None and len(rec["steps"]) == steps_ref:
+            # the same number of converged steps as the FP64 run (all, or
+            # up to the step where both stopped)
             rec["u_rel_err_vs_fp64"] = float(np.max(np.abs(u - u_ref)) / np.max(np.abs(u_ref)))
         forms[name] = rec
         print(f"[study] {name}: newton {its} failed={rec['failed'] is not None} {rec['wall_s']:.1f}s",
