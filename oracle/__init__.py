@@ -2,8 +2,10 @@
 
 TEST INFRASTRUCTURE ONLY: the CPU restatement of WARP3D's element-block
 path that checks the CUDA engine and serves as the timed CPU baseline.
-Parity unpinned against executions of the reference (no Fortran compiler
-or MKL on these machines); pinned by the closed-form tests in tests/.
+No Fortran compiler or MKL on these machines to execute the reference;
+the mm01 finite-strain b-bar brick path is pinned end to end by WARP3D's
+own regression problem verification/test24 (tests/test_oracle_warp3d_test24.py,
+the checked stress to 3.6e-6), the rest by the closed-form tests in tests/.
 """
 from __future__ import annotations
 
