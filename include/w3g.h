@@ -93,12 +93,13 @@ extern "C" {
 /*
  * One crystal definition of mm10 crystal plasticity: c_array(cnum) of
  * module crystal_data (src/mod_crystals.f:140-230) as the crystal input
- * sets it (src/incrystal.f). Supported: slip_type 1 (fcc, 12 systems),
- * elastic_type 1 (isotropic), h_type 1 (Voce, one hardening variable),
- * one crystal per Gauss point, the default Newton solver.
+ * sets it (src/incrystal.f). Supported: slip_type 1 (fcc) and 2 (bcc,
+ * the 12 {110}<111> systems), elastic_type 1 (isotropic), h_type 1 (Voce,
+ * one hardening variable), one crystal per Gauss point, the default
+ * Newton solver.
  */
 typedef struct w3g_crystal {
-  int slip_type;                /* 1 = fcc                               */
+  int slip_type;                /* 1 = fcc, 2 = bcc (12 systems)         */
   int elastic_type;             /* 1 = isotropic                         */
   int h_type;                   /* 1 = Voce                              */
   int miter;                    /* local Newton iteration limit (30)     */

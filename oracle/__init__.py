@@ -3,9 +3,10 @@
 TEST INFRASTRUCTURE ONLY: the CPU restatement of WARP3D's element-block
 path that checks the CUDA engine and serves as the timed CPU baseline.
 No Fortran compiler or MKL on these machines to execute the reference;
-the mm01 finite-strain b-bar brick path is pinned end to end by WARP3D's
-own regression problem verification/test24 (tests/test_oracle_warp3d_test24.py,
-the checked stress to 3.6e-6), the rest by the closed-form tests in tests/.
+pinned end to end by two of WARP3D's own regression problems
+(verification/test24, mm01, to 3.6e-6; verification/test82/voche_model,
+mm10, to 4.0e-5 of the checked stress; tests/test_oracle_warp3d_*.py),
+the rest by the closed-form tests in tests/.
 """
 from __future__ import annotations
 

@@ -4,15 +4,16 @@
 //
 // Parity status: WARP3D is Fortran + Intel MKL and no Fortran compiler
 // exists on these machines, and the reference's own tests (verification/*)
-// are end-to-end decks with no element-level golden vectors. The mm01
-// finite-strain b-bar brick path is pinned end to end by one of them:
-// verification/test24 (hollow sphere, skew constraints, 21 load steps)
-// replayed through this oracle reproduces the element stress WARP3D's
-// checker compares to 3.6e-6 (its tolerance 1e-4;
-// tests/test_oracle_warp3d_test24.py). Everything else is pinned by
-// closed-form known answers (tests/test_oracle_*.py): patch tests,
-// rigid-body motions, the analytic bilinear uniaxial response and
-// finite-difference checks of the consistent tangent.
+// are end-to-end decks with no element-level golden vectors. Two of them
+// pin this oracle end to end, replayed from their data: verification/test24
+// (mm01, finite-strain b-bar bricks, skew constraints, 21 load steps) to
+// 3.6e-6 and verification/test82/voche_model (mm10, bcc, Voce, face
+// pressures) to 4.0e-5 of the element stress each checker compares (their
+// tolerance 1e-4; tests/test_oracle_warp3d_test24.py, _test82.py).
+// Everything else is pinned by closed-form known answers
+// (tests/test_oracle_*.py): patch tests, rigid-body motions, the analytic
+// bilinear uniaxial response and finite-difference checks of the
+// consistent tangent.
 //
 // Every routine follows the cited Fortran statement by statement,
 // including its literal constants and evaluation order, so that the

@@ -1,5 +1,5 @@
 // w3o_mm10.cpp -- the oracle's restatement of WARP3D's mm10 crystal
-// plasticity for one Gauss point with one fcc crystal, isotropic
+// plasticity for one Gauss point with one fcc or bcc (12-system) crystal, isotropic
 // elasticity and Voce hardening. TEST INFRASTRUCTURE ONLY.
 //
 // Follows, statement by statement:
@@ -15,8 +15,8 @@
 //   mm10_formR2 / formJ11 / formJ12 / formJ21 / formJ22 / formJ / formR /
 //     formR1 / form_dbarp / form_wbarp / form_wp / symsw / symswmat / iw /
 //     slipinc / rs and the Voce functions (src/mm10_b.f:63-2082);
-//   setup_mm10_rknstr (src/rknstr.f:1568-2027) and the fcc slip systems of
-//     finalize_new_crystal (src/mod_crystals.f:440-495).
+//   setup_mm10_rknstr (src/rknstr.f:1568-2027) and the fcc / bcc slip systems of
+//     finalize_new_crystal (src/mod_crystals.f:440-596).
 //
 // LAPACK/BLAS calls of the reference (MKL, not part of the sources) are
 // restated with the reference-BLAS/LAPACK algorithms: DGESV = unblocked
@@ -831,17 +831,19 @@ void output(const CrystalProps& p, State& np1, const State& n, double* p_strain_
   np1.u[7] = (double)numAct;
 }
 
-// fcc slip systems, finalize_new_crystal slip_type 1
-// (src/mod_crystals.f:440-495): directions b and normals n
-void fcc_systems(double bi[NS][3], double ni[NS][3]) {
+// slip systems of finalize_new_crystal: fcc, slip_type 1
+// (src/mod_crystals.f:440-518), directions b and normals n; bcc, slip_type
+// 2 (:519-596), the same two tables with the roles exchanged
+void slip_systems(int slip_type, double bi[NS][3], double ni[NS][3]) {
   const double f = 1.0 / std::sqrt(2.0);
-  const double b[NS][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f}, {f, 0, f}, {f, -f, 0},
-                           {0, -f, f}, {-f, 0, -f}, {f, f, 0}, {0, f, f}, {f, 0, -f}, {-f, -f, 0}};
+  const double v110[NS][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f}, {f, 0, f}, {f, -f, 0},
+                              {0, -f, f}, {-f, 0, -f}, {f, f, 0}, {0, f, f}, {f, 0, -f}, {-f, -f, 0}};
   const double g = 1.0 / std::sqrt(3.0);
-  const double nn[NS][3] = {{g, g, g}, {g, g, g}, {g, g, g}, {-g, -g, g}, {-g, -g, g}, {-g, -g, g},
-                            {-g, g, g}, {-g, g, g}, {-g, g, g}, {g, -g, g}, {g, -g, g}, {g, -g, g}};
-  std::memcpy(bi, b, sizeof(b));
-  std::memcpy(ni, nn, sizeof(nn));
+  const double v111[NS][3] = {{g, g, g}, {g, g, g}, {g, g, g}, {-g, -g, g}, {-g, -g, g}, {-g, -g, g},
+                              {-g, g, g}, {-g, g, g}, {-g, g, g}, {g, -g, g}, {g, -g, g}, {g, -g, g}};
+  const bool bcc = slip_type == 2;
+  std::memcpy(bi, bcc ? v111 : v110, sizeof(v110));
+  std::memcpy(ni, bcc ? v110 : v111, sizeof(v111));
 }
 
 }  // namespace
@@ -875,7 +877,7 @@ void mm10_element_props(const w3g_crystal& cr, const double* angles, CrystalProp
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) M3(trans_rot, i, j) = M3(r, j, i);
   double bi[NS][3], ni[NS][3];
-  fcc_systems(bi, ni);
+  slip_systems(cr.slip_type, bi, ni);
   for (int s = 0; s < NS; ++s) {
     double bs[3], ns[3], A[9];
     mult_type_3(bs, trans_rot, bi[s]);

@@ -1,7 +1,7 @@
 """Parity of the CUDA mm10 crystal-plasticity path with the oracle.
 
-A small polycrystal (8-node bricks, one fcc crystal per Gauss point,
-random orientations) is loaded with the oracle's Newton driver; the GPU
+A small polycrystal (8-node bricks, one fcc or bcc crystal per Gauss
+point, random orientations) is loaded with the oracle's Newton driver; the GPU
 then repeats one recovery and one tangent from the same state and every
 output array is compared: urcs_n1, eps_n1, rot_n1, the full 158-word
 mm10 history (tangent, slip totals, crystal stress, Euler angles, plastic
@@ -30,14 +30,14 @@ def _engine(model, **kw):
     return Engine(model, **kw)
 
 
-def _model(n=3, seed=7, spans=None, **kw):
+def _model(n=3, seed=7, spans=None, xtal=None, **kw):
     coords, incid = cube_mesh(n, jitter=0.05)
-    return Model(coords, incid, materials=[Crystal()], angles=random_orientations(n ** 3, seed),
+    return Model(coords, incid, materials=[xtal or Crystal()], angles=random_orientations(n ** 3, seed),
                  block_spans=spans, **kw), (n, n, n)
 
 
-def _loaded_case(**kw):
-    model, nxyz = _model(3, spans=[20, 7], **kw)
+def _loaded_case(xtal=None, **kw):
+    model, nxyz = _model(3, spans=[20, 7], xtal=xtal, **kw)
     ora = oracle.Oracle(model)
     fixed, topz = uniaxial_bcs(model, nxyz)
     drv = NewtonDriver(model, ora, fixed, tol=1e-8, maxit=60, extrapolate=True)
@@ -55,6 +55,12 @@ def _loaded_case(**kw):
 @pytest.fixture(scope="module")
 def crystal_case():
     return _loaded_case()
+
+
+@pytest.fixture(scope="module")
+def crystal_bcc_case():
+    # bcc: the 12 {110}<111> systems (slip_type 2)
+    return _loaded_case(xtal=Crystal(slip_type=2))
 
 
 @pytest.fixture(scope="module")
@@ -114,6 +120,12 @@ def test_mm10_recover_and_tangent_parity(crystal_case):
     _tangent(model, eng, ora, 4, 1, u, du)
     eng.set_precision(abi.TANGENT_FP32)
     _tangent(model, eng, ora, 4, 1, u, du, tol=TOL_FP32)
+
+
+def test_mm10_bcc_parity(crystal_bcc_case):
+    model, state, u, du = crystal_bcc_case
+    eng, ora = _compare(model, state, 4, 1, False, u, du)
+    _tangent(model, eng, ora, 4, 1, u, du)
 
 
 def test_mm10_bbar_parity(crystal_bbar_case):

@@ -474,10 +474,10 @@ int w3g_create(int device, const w3g_model_desc* md, w3g_context** out) {
           return fail(W3G_EARG, "element " + std::to_string(d.felem + i + 1) + ": bad crystal index");
         }
         const w3g_crystal& cr = md->crystals[cn];
-        if (cr.slip_type != 1 || cr.elastic_type != 1 || cr.h_type != 1) {
+        if ((cr.slip_type != 1 && cr.slip_type != 2) || cr.elastic_type != 1 || cr.h_type != 1) {
           delete c;
           return fail(W3G_EUNSUPPORTED, "crystal " + std::to_string(cn) +
-                                            ": only fcc slip, isotropic elasticity, Voce hardening");
+                                            ": only fcc or bcc (12-system) slip, isotropic elasticity, Voce hardening");
         }
       }
     }

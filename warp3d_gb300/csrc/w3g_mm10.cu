@@ -1191,12 +1191,18 @@ void build_crystal_elem(const w3g_crystal& cr, int type, const double* angles, C
   double tr[9];
   for (int r = 0; r < 3; ++r)
     for (int c = 0; c < 3; ++c) tr[r + 3 * c] = g[c + 3 * r];
-  // fcc {111}<110> systems: directions b, normals n (slip_type 1)
+  // the 12 systems of finalize_new_crystal (src/mod_crystals.f:440-596):
+  // fcc {111}<110> (slip_type 1) takes the <110> vectors as directions b
+  // and the <111> vectors as normals n; bcc {110}<111> (slip_type 2) the
+  // same two tables the other way round
   const double f = 1.0 / std::sqrt(2.0), h = 1.0 / std::sqrt(3.0);
-  const double b[kSlip][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f}, {f, 0, f}, {f, -f, 0},
-                              {0, -f, f}, {-f, 0, -f}, {f, f, 0}, {0, f, f}, {f, 0, -f}, {-f, -f, 0}};
-  const double nrm[kSlip][3] = {{h, h, h}, {h, h, h}, {h, h, h}, {-h, -h, h}, {-h, -h, h}, {-h, -h, h},
-                                {-h, h, h}, {-h, h, h}, {-h, h, h}, {h, -h, h}, {h, -h, h}, {h, -h, h}};
+  const double v110[kSlip][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f}, {f, 0, f}, {f, -f, 0},
+                                 {0, -f, f}, {-f, 0, -f}, {f, f, 0}, {0, f, f}, {f, 0, -f}, {-f, -f, 0}};
+  const double v111[kSlip][3] = {{h, h, h}, {h, h, h}, {h, h, h}, {-h, -h, h}, {-h, -h, h}, {-h, -h, h},
+                                 {-h, h, h}, {-h, h, h}, {-h, h, h}, {h, -h, h}, {h, -h, h}, {h, -h, h}};
+  const bool bcc = cr.slip_type == 2;
+  const double(*b)[3] = bcc ? v111 : v110;
+  const double(*nrm)[3] = bcc ? v110 : v111;
   for (int s = 0; s < kSlip; ++s) {
     double bs[3], ns[3], A[9], As[9], Aa[9];
     for (int r = 0; r < 3; ++r) bs[r] = tr[r] * b[s][0] + tr[r + 3] * b[s][1] + tr[r + 6] * b[s][2];

@@ -104,7 +104,7 @@ class Umat:
 @dataclass
 class Crystal:
     """mm10 crystal plasticity, WARP3D's crystal input (src/incrystal.f,
-    defaults of src/mod_crystals.f:250-416): fcc slip systems, isotropic
+    defaults of src/mod_crystals.f:250-416): fcc or bcc (12-system) slip, isotropic
     elasticity, Voce hardening tau_tilde' = theta_0 sum |1 - (tau_tilde -
     tau_y)/tau_v|^m |gamma_dot|, slip rate gamma = dg/tau |tau_s/tau|^(n-1)
     tau_s. One crystal per Gauss point."""
@@ -124,10 +124,11 @@ class Crystal:
     rtol: float = 5.0e-5
     rtol1: float = 1.0e-5
     miter: int = 30
+    slip_type: int = 1          # 1 fcc, 2 bcc (12 systems)
 
     def struct(self) -> abi.Crystal:
         c = abi.Crystal()
-        c.slip_type, c.elastic_type, c.h_type, c.miter = 1, 1, 1, self.miter
+        c.slip_type, c.elastic_type, c.h_type, c.miter = self.slip_type, 1, 1, self.miter
         for k in ("e", "nu", "harden_n", "tau_y", "tau_v", "theta_o", "voche_m", "iD_v", "k_o", "b", "atol",
                   "atol1", "rtol", "rtol1"):
             setattr(c, k, float(getattr(self, k)))
