@@ -34,7 +34,7 @@ UPDATE_COPY = 0
 UPDATE_SWAP = 1
 
 HIST_MM01 = 11
-HIST_MM10 = 158       # one fcc crystal, one hardening variable
+HIST_MM10 = 158       # one 12-system (fcc or bcc) crystal, one hardening variable
 HIST_UMAT = 20        # state variables of the UMAT compiled into the library (w3g_umat_features)
 
 TANGENT_FP64 = 0

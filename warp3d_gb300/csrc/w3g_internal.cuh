@@ -73,8 +73,8 @@ struct TcgTile {
 static_assert(sizeof(TcgTile) == 64, "TcgTile is one 64-byte record");
 
 // ---- mm10 crystal plasticity (w3g_mm10.cu) -----------------------------
-constexpr int kHistMM10 = 158;     // one fcc crystal, one hardening variable
-constexpr int kSlip = 12;          // fcc slip systems
+constexpr int kHistMM10 = 158;     // one 12-system crystal, one hardening variable
+constexpr int kSlip = 12;          // slip systems (fcc or bcc)
 constexpr int kMm10Scratch = 25;   // per GP: uddt 6, R(n+1) 9, F(n+1) 9, det F(n+1)
 // per-element crystal data, built on the host at model creation exactly as
 // setup_mm10_rknstr does (src/rknstr.f:1568-2027)
