@@ -3,7 +3,7 @@
 mm10's linear algebra is MKL in the reference and no execution of it is
 available, so these pins are physical and structural: the elastic limit,
 objectivity under a rotation of crystal and loading together, the cubic
-symmetry of the fcc slip systems, the symmetry of the stored tangent, and
+symmetry of the fcc and bcc slip systems, the symmetry of the stored tangent, and
 an equilibrium Newton solution of a small polycrystal.
 """
 import ctypes as C
@@ -128,18 +128,36 @@ def test_objectivity_rotating_crystal_and_loading():
         assert abs(s2[6] - s1[6]) < 1e3 * tol * abs(s1[6])   # work density is invariant
 
 
-def test_cube_orientation_uniaxial_symmetry():
+@pytest.mark.parametrize("slip_type", [1, 2], ids=["fcc", "bcc"])
+def test_cube_orientation_uniaxial_symmetry(slip_type):
     # identity lattice (psi = 90, theta = 0, phi = 90 gives g = I in Kocks):
-    # [001] tension activates 8 systems symmetrically -> sxx = syy, no shear
+    # [001] tension activates 8 systems symmetrically -> sxx = syy, no shear;
+    # fcc {111}<110> and bcc {110}<111> alike (bcc: the 8 systems whose
+    # {110} normal has a z component)
     g = _kocks([90.0, 0.0, 90.0])
     assert np.allclose(np.abs(g), np.eye(3), atol=1e-15)
     d = np.array([-0.0005, -0.0005, 0.001, 0.0, 0.0, 0.0])
-    s, h = _point([90.0, 0.0, 90.0], [d] * 6)
+    s, h = _point([90.0, 0.0, 90.0], [d] * 6, crystal=Crystal(slip_type=slip_type))
     assert abs(s[0] - s[1]) < 1e-9 * abs(s[2])
     assert np.abs(s[3:6]).max() < 1e-9 * abs(s[2])
     # resolved shear on the 8 active systems = szz-sxx times the Schmid factor 1/sqrt(6)
     tau = (s[2] - s[0]) / np.sqrt(6.0)
     assert 0.85 * h[TT] < tau < 1.0 * h[TT]
+
+
+def test_bcc_and_fcc_differ_at_a_general_orientation():
+    """The slip-system table is the only difference between the two
+    lattices: elastically identical, different once the crystal slips."""
+    ang = [20.0, 70.0, 110.0]
+    small = np.array([2.0, -1.0, 0.5, 1.0, -0.5, 0.25]) * 1e-7
+    s1, _ = _point(ang, [small, small], crystal=Crystal(slip_type=1))
+    s2, _ = _point(ang, [small, small], crystal=Crystal(slip_type=2))
+    assert np.allclose(s1[:6], s2[:6], rtol=1e-12, atol=1e-14)
+    d = np.array([-0.0005, -0.0005, 0.001, 0.0002, 0.0, 0.0])
+    s1, _ = _point(ang, [d] * 4, crystal=Crystal(slip_type=1))
+    s2, _ = _point(ang, [d] * 4, crystal=Crystal(slip_type=2))
+    # early plastic flow: ~1e-3 apart (equal tables would agree to ~1e-15)
+    assert np.abs(s1[:6] - s2[:6]).max() > 1e-4 * np.abs(s1[:6]).max()
 
 
 def test_polycrystal_newton_equilibrium():
