@@ -1106,7 +1106,31 @@ def compact_roofline(rf):
     return out
 
 
-def summarize_parity(p1, batched, crystal):
+def regression_pins():
+    """WARP3D's own regression problems replayed through the GPU engine
+    (the host-array C-ABI, FP64): verification/test24 (mm01, finite-strain
+    b-bar bricks) and verification/test82/voche_model (mm10, bcc, Voce),
+    from the committed fixtures; per deck the stress its checker compares,
+    WARP3D's value and the relative difference (the checker accepts 1e-4)."""
+    out = {}
+    try:
+        from tests import warp3d_test24 as t24
+        from tests import warp3d_test82 as t82
+        from warp3d_gb300.engine import Engine
+        for name, mod in (("test24_sphere_mm01", t24), ("test82_voce_mm10", t82)):
+            d = mod.load()
+            t0 = time.perf_counter()
+            sig, _, its = mod.solve(Engine, d)
+            expected = float(d["expected_answer"])
+            out[name] = {"computed": float(sig[0]), "warp3d": expected, "rel": abs(float(sig[0]) / expected - 1.0),
+                         "checker_rtol": mod.CHECKER_RTOL, "newton_iterations": int(sum(its)),
+                         "s": time.perf_counter() - t0}
+    except Exception as exc:   # reported, never fatal to the bench line
+        out["error"] = f"{type(exc).__name__}: {str(exc)[:200]}"
+    return out
+
+
+def summarize_parity(p1, batched, crystal, pins=None):
     """Max relative error of every FP64 output array against the oracle,
     per workload, and the precision forms' Ke error."""
     def one(p):
@@ -1117,8 +1141,11 @@ def summarize_parity(p1, batched, crystal):
         if "estiff_precision_forms" in p:
             d["ke_precision_forms"] = {k: _r(v, 3) for k, v in p["estiff_precision_forms"].items()}
         return d
-    return {"hex8_64cube": one(p1), "mixed_1m_batched": one((batched or {}).get("parity")),
-            "mm10_32cube": one((crystal or {}).get("parity")), "tolerance_fp64": 1e-12}
+    out = {"hex8_64cube": one(p1), "mixed_1m_batched": one((batched or {}).get("parity")),
+           "mm10_32cube": one((crystal or {}).get("parity")), "tolerance_fp64": 1e-12}
+    if pins:
+        out["warp3d_regression_rel"] = {k: (_r(v["rel"], 3) if isinstance(v, dict) else v) for k, v in pins.items()}
+    return out
 
 
 def summarize_leg(leg):
@@ -1264,6 +1291,7 @@ def main():
         parity1 = parity_sample(eng, model, spread_blocks(model, 64), 2, 1, False, model.c, u1, du,
                                 (tc.data_ptr(), tu.data_ptr(), tdu.data_ptr(), tifv.data_ptr()), stream,
                                 precisions=forms)
+    pins = regression_pins() if not args.no_parity and rank == 0 else None
 
     # ---- e2e through the host-array C-ABI ----
     e2e = None
@@ -1341,7 +1369,7 @@ def main():
         # the full record first, then the headline line (last line of the
         # output) with compact summaries of every leg
         details = {"details": {"mixed": mixed, "batched": batched, "crystal": crystal, "solver": solver,
-                               "formulations": formulations, "parity_hex8_64cube": parity1, "roofline": roofline,
+                               "formulations": formulations, "parity_hex8_64cube": parity1, "warp3d_regression": pins, "roofline": roofline,
                                "cpu_baseline": cb, "e2e": e2e}}
         print(json.dumps(details), flush=True)
         line = {
@@ -1355,7 +1383,7 @@ def main():
             "tangent_ms": tan64, "recovery_ms": rec64,
             "mixed": summarize_mixed(mixed), "e2e": e2e, "roofline": compact_roofline(roofline),
             "cpu_baseline": cb, "clocks": clocks, "gpu_launches": launches64,
-            "parity": summarize_parity(parity1, batched, crystal),
+            "parity": summarize_parity(parity1, batched, crystal, pins),
             "batched": summarize_leg(batched), "crystal": summarize_leg(crystal),
         }
         print(json.dumps(line), flush=True)
